@@ -1,0 +1,269 @@
+"""Seeded synthetic triangle meshes and the reference's input formats.
+
+A mesh here is the input half of the solver's drop-in interface: node
+coordinates, triangles, a region index per triangle and a list of boundary
+segments with a boundary index each. The same arrays can be written as a
+Salome UNV file plus an FVM_TVD ``task.xml`` (the formats the reference reads,
+src/mesh/MeshReaderSalomeUnv.cpp:267-447 and src/methods/fvm_tvd.cpp:26-128) or
+handed to the library directly.
+
+Generator: an n x n grid of squares on a rectangle, each square split into two
+counter-clockwise triangles by the same diagonal; interior nodes jittered by
+i.i.d. U(-a*h, +a*h) per coordinate from numpy's PCG64 with a stated seed;
+boundary nodes are not moved.
+"""
+from __future__ import annotations
+
+import io
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SIDE_BOTTOM, SIDE_RIGHT, SIDE_TOP, SIDE_LEFT = 0, 1, 2, 3
+
+
+@dataclass
+class Mesh:
+    nodes: np.ndarray            # (nn, 2) float64
+    tris: np.ndarray             # (nc, 3) int32, counter-clockwise, 0-based
+    cell_region: np.ndarray      # (nc,) int32, index into the task's region list
+    bsegs: np.ndarray            # (nb, 2) int32 node pairs on the boundary
+    bseg_bnd: np.ndarray         # (nb,) int32, index into the task's boundary list
+    bseg_side: np.ndarray = field(default=None)  # (nb,) int32 side tag of the square
+
+    @property
+    def n_cells(self) -> int:
+        return int(self.tris.shape[0])
+
+    def centroids(self) -> np.ndarray:
+        """Cell centres the way the reference forms them: (x0+x1+x2)/3."""
+        p = self.nodes[self.tris]
+        return np.stack([(p[:, 0, 0] + p[:, 1, 0] + p[:, 2, 0]) / 3.0,
+                         (p[:, 0, 1] + p[:, 1, 1] + p[:, 2, 1]) / 3.0], axis=1)
+
+
+def jittered_square(n: int, x0: float, x1: float, y0: float, y1: float,
+                    jitter: float, seed: int) -> Mesh:
+    """n x n squares x 2 triangles on [x0,x1]x[y0,y1], interior jitter a=jitter."""
+    hx = (x1 - x0) / n
+    hy = (y1 - y0) / n
+    i = np.arange(n + 1)
+    X, Y = np.meshgrid(x0 + i * hx, y0 + i * hy)        # row j = y index
+    nodes = np.stack([X.ravel(), Y.ravel()], axis=1).astype(np.float64)
+    nodes[n * (n + 1):, 1] = y1                         # exact top edge
+    nodes[n::n + 1, 0] = x1                             # exact right edge
+    if jitter > 0.0:
+        rng = np.random.Generator(np.random.PCG64(seed))
+        d = rng.uniform(-jitter, jitter, size=(n + 1, n + 1, 2))
+        inner = np.zeros((n + 1, n + 1), dtype=bool)
+        inner[1:n, 1:n] = True
+        inner = inner.ravel()
+        dd = d.reshape(-1, 2)
+        nodes[inner, 0] += dd[inner, 0] * hx
+        nodes[inner, 1] += dd[inner, 1] * hy
+    k = (np.arange(n)[None, :] + (n + 1) * np.arange(n)[:, None]).ravel()   # lower-left node
+    k00, k10, k01, k11 = k, k + 1, k + n + 1, k + n + 2
+    tris = np.empty((2 * n * n, 3), dtype=np.int32)
+    tris[0::2] = np.stack([k00, k10, k11], axis=1)
+    tris[1::2] = np.stack([k00, k11, k01], axis=1)
+    # boundary segments, side by side
+    s = np.arange(n)
+    bottom = np.stack([s, s + 1], axis=1)
+    right = np.stack([n + (n + 1) * s, n + (n + 1) * (s + 1)], axis=1)
+    top = np.stack([n * (n + 1) + s + 1, n * (n + 1) + s], axis=1)
+    left = np.stack([(n + 1) * (s + 1), (n + 1) * s], axis=1)
+    bsegs = np.concatenate([bottom, right, top, left]).astype(np.int32)
+    side = np.repeat(np.arange(4, dtype=np.int32), n)
+    return Mesh(nodes=nodes, tris=tris, cell_region=np.zeros(2 * n * n, np.int32),
+                bsegs=bsegs, bseg_bnd=np.zeros(4 * n, np.int32), bseg_side=side)
+
+
+# ---------------------------------------------------------------- initial data
+
+GAMMA = 1.4
+
+
+def cons_from_prim(r, u, v, p, gam=GAMMA):
+    """(rho, u, v, p) -> (rho, rho u, rho v, rho E) for a calorically perfect gas."""
+    r = np.asarray(r, np.float64)
+    e = p / (r * (gam - 1.0))
+    return np.stack([r, r * u, r * v, r * (e + 0.5 * (u * u + v * v))])
+
+
+def isentropic_vortex(xy: np.ndarray, beta: float, xc: float, yc: float,
+                      u_inf: float = 1.0, v_inf: float = 0.0, gam: float = GAMMA):
+    """Isentropic vortex of strength beta on a free stream rho=p=1 (R=1), at centroids.
+
+    du = -beta/(2 pi) (y-yc) exp((1-r^2)/2), dv = beta/(2 pi) (x-xc) exp((1-r^2)/2),
+    T = 1 - (gam-1) beta^2 / (8 gam pi^2) exp(1-r^2), rho = T^(1/(gam-1)), p = rho T.
+    """
+    dx = xy[:, 0] - xc
+    dy = xy[:, 1] - yc
+    r2 = dx * dx + dy * dy
+    ex = np.exp(0.5 * (1.0 - r2))
+    u = u_inf - beta / (2.0 * math.pi) * dy * ex
+    v = v_inf + beta / (2.0 * math.pi) * dx * ex
+    T = 1.0 - (gam - 1.0) * beta * beta / (8.0 * gam * math.pi * math.pi) * ex * ex
+    r = T ** (1.0 / (gam - 1.0))
+    p = r * T
+    return cons_from_prim(r, u, v, p, gam)
+
+
+FOUR_QUADRANT = {  # (rho, u, v, p) by quadrant of the unit square split at (1/2, 1/2)
+    "NE": (1.5, 0.0, 0.0, 1.5),
+    "NW": (0.5323, 1.206, 0.0, 0.3),
+    "SW": (0.138, 1.206, 1.206, 0.029),
+    "SE": (0.5323, 0.0, 1.206, 0.3),
+}
+QUADRANT_ORDER = ("NE", "NW", "SW", "SE")
+
+
+def quadrant_regions(xy: np.ndarray, xs: float = 0.5, ys: float = 0.5) -> np.ndarray:
+    """Region index per cell by centroid: 0 NE, 1 NW, 2 SW, 3 SE."""
+    east = xy[:, 0] > xs
+    north = xy[:, 1] > ys
+    reg = np.where(north, np.where(east, 0, 1), np.where(east, 3, 2))
+    return reg.astype(np.int32)
+
+
+# ---------------------------------------------------------------- UNV writer
+
+def write_unv(mesh: Mesh, region_names, bnd_names) -> str:
+    """Salome UNV text with blocks 2411 (nodes), 2412 (edges + triangles), 2467 (groups).
+
+    Coordinates use Python's shortest round-trip form, so the reader gets the
+    very same doubles back. Every cell goes into the group of its region and
+    every boundary segment into the group of its boundary, which is how the
+    reference binds regions and boundary conditions by name
+    (src/mesh/MeshReaderSalomeUnv.cpp:219-248).
+    """
+    out = io.StringIO()
+    w = out.write
+    w("    -1\n  2411\n")
+    for i, (x, y) in enumerate(mesh.nodes):
+        w(f"{i + 1:10d}{1:10d}{1:10d}{11:10d}\n")
+        w(f"  {repr(float(x))}  {repr(float(y))}  0.0\n")
+    w("    -1\n    -1\n  2412\n")
+    label = 0
+    edge_labels = []
+    for (a, b) in mesh.bsegs:
+        label += 1
+        edge_labels.append(label)
+        w(f"{label:10d}{11:10d}{2:10d}{1:10d}{7:10d}{2:10d}\n")
+        w(f"{0:10d}{1:10d}{1:10d}\n")
+        w(f"{a + 1:10d}{b + 1:10d}\n")
+    cell_labels = []
+    for (a, b, c) in mesh.tris:
+        label += 1
+        cell_labels.append(label)
+        w(f"{label:10d}{41:10d}{2:10d}{1:10d}{7:10d}{3:10d}\n")
+        w(f"{a + 1:10d}{b + 1:10d}{c + 1:10d}\n")
+    w("    -1\n    -1\n  2467\n")
+    groups = []
+    edge_labels = np.asarray(edge_labels)
+    cell_labels = np.asarray(cell_labels)
+    for k, name in enumerate(bnd_names):
+        groups.append((name, edge_labels[mesh.bseg_bnd == k]))
+    for k, name in enumerate(region_names):
+        groups.append((name, cell_labels[mesh.cell_region == k]))
+    for g, (name, labels) in enumerate(groups):
+        n = len(labels)
+        w(f"{g + 1:10d}{0:10d}{0:10d}{0:10d}{0:10d}{0:10d}{0:10d}{n:10d}\n")
+        w(f"{name}\n")
+        for j in range(0, n - 1, 2):
+            w(f"{8:10d}{labels[j]:10d}{0:10d}{0:10d}{8:10d}{labels[j + 1]:10d}{0:10d}{0:10d}\n")
+        if n % 2 == 1:
+            w(f"{8:10d}{labels[-1]:10d}{0:10d}{0:10d}\n")
+    w("    -1\n")
+    return out.getvalue()
+
+
+# ---------------------------------------------------------------- task.xml
+
+@dataclass
+class Region:
+    name: str
+    u: float
+    v: float
+    T: float
+    p: float
+    mat: int = 0
+
+
+@dataclass
+class Boundary:
+    name: str
+    kind: str                    # BOUND_INLET / BOUND_OUTLET / BOUND_WALL_SLIP / BOUND_WALL_NO_SLIP
+    edge_type: int = 1
+    u: float = 0.0
+    v: float = 0.0
+    T: float = 1.0
+    p: float = 1.0
+
+
+@dataclass
+class Task:
+    regions: list
+    boundaries: list
+    steady: int = 0
+    tau: float = 1.0e8
+    tmax: float = 1.0e8
+    cfl: float = 0.5
+    step_max: int = 10
+    file_output_step: int = 1000000
+    log_output_step: int = 1000000
+    limits: tuple = (1.0e-8, 1.0e8, 1.0e-8, 1.0e8, 1.0e8)   # ro min/max, p min/max, u max
+    # (name, M, Cp, K, ML); M = gR and Cp = 3.5 give gR/M = 1, Cv = 2.5, gamma = 1.4, T = p/rho
+    materials: list = field(default_factory=lambda: [("gas", 8.314472, 3.5, 0.0, 0.0)])
+    mesh_name: str = "mesh.unv"
+    mesh_type: str = "salome_unv"
+    # optional GPU method selections (absent -> reference behaviour)
+    flux: str | None = None
+    reconstruction: str | None = None
+    time_scheme: str | None = None
+    precision: str | None = None
+    method: str = "FVM_TVD"
+
+
+def _v(x) -> str:
+    return repr(float(x))
+
+
+def write_task_xml(t: Task) -> str:
+    rmin, rmax, pmin, pmax, umax = t.limits
+    L = ['<?xml version="1.0" encoding="UTF-8"?>', f'<task method="{t.method}">', "  <control>",
+         f'    <STEADY value="{int(t.steady)}" />', f'    <TAU value="{_v(t.tau)}" />',
+         f'    <TMAX value="{_v(t.tmax)}" />', f'    <CFL value="{_v(t.cfl)}" />',
+         f'    <STEP_MAX value="{int(t.step_max)}" />',
+         f'    <FILE_OUTPUT_STEP value="{int(t.file_output_step)}" />',
+         f'    <LOG_OUTPUT_STEP value="{int(t.log_output_step)}" />']
+    for tag, val in (("FLUX", t.flux), ("RECONSTRUCTION", t.reconstruction),
+                     ("TIME_SCHEME", t.time_scheme), ("PRECISION", t.precision)):
+        if val is not None:
+            L.append(f'    <{tag} value="{val}" />')
+    L += ["  </control>", "  <limits>", f'    <ro min="{_v(rmin)}" max="{_v(rmax)}" />',
+          f'    <p min="{_v(pmin)}" max="{_v(pmax)}" />', f'    <u max="{_v(umax)}" />', "  </limits>",
+          f'  <materials count="{len(t.materials)}">']
+    for k, (name, M, Cp, K, ML) in enumerate(t.materials):
+        L += [f'    <material id="{k}">', f"      <name>{name}</name>", "      <parameters>",
+              f'        <M value="{_v(M)}" />', f'        <Cp value="{_v(Cp)}" />',
+              f'        <K value="{_v(K)}" />', f'        <ML value="{_v(ML)}" />',
+              "      </parameters>", "    </material>"]
+    L += ["  </materials>", f'  <regions count="{len(t.regions)}">']
+    for k, r in enumerate(t.regions):
+        L += [f'    <region id="{k}">', f'      <material id="{r.mat}" />', '      <cell type="3" />',
+              f"      <name>{r.name}</name>", "      <parameters>", f'        <Vx value="{_v(r.u)}" />',
+              f'        <Vy value="{_v(r.v)}" />', f'        <T value="{_v(r.T)}" />',
+              f'        <P value="{_v(r.p)}" />', "      </parameters>", "    </region>"]
+    L += ["  </regions>", "  <boundaries>"]
+    for b in t.boundaries:
+        L += [f'    <boundCond edgeType="{b.edge_type}">', f"      <type>{b.kind}</type>",
+              f"      <name>{b.name}</name>"]
+        if b.kind == "BOUND_INLET":
+            L += ["      <parameters>", f'        <Vx value="{_v(b.u)}" />', f'        <Vy value="{_v(b.v)}" />',
+                  f'        <T value="{_v(b.T)}" />', f'        <P value="{_v(b.p)}" />', "      </parameters>"]
+        L.append("    </boundCond>")
+    L += ["  </boundaries>", "  <mesh>", f'    <name value="{t.mesh_name}" />',
+          f'    <filesType value="{t.mesh_type}" />', "  </mesh>", "</task>", ""]
+    return "\n".join(L)

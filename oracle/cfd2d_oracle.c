@@ -1,0 +1,809 @@
+/*
+ * cfd2d oracle: plain-C restatement of the reference FVM_TVD explicit solver.
+ * TEST INFRASTRUCTURE ONLY (see cfd2d_oracle.h): the checker, never the product.
+ *
+ * Structure mirrors the reference on purpose: array-of-edges loops that scatter
+ * into cells (src/methods/fvm_tvd.cpp:242-301, 329-365), the same conversions,
+ * the same ghost recipe and the same operation order, so that in reference mode
+ * the result equals the reference bit for bit.
+ */
+#include "cfd2d_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define GAS_R 8.314472 /* Material::gR, src/global.cpp:6 */
+
+/* Param, src/global.h:180-194 (viscosity unused on this path). */
+typedef struct { double r, p, e, E, u, v, cz, T; } Par;
+
+struct orc_mesh {
+    int nn, nc, ne;
+    int* cnodes;   /* nc x 3 */
+    int* cedges;   /* nc x 3, Cell::edgesInd: ascending edge numbers */
+    double *S, *cx, *cy;
+    int *n1, *n2, *c1, *c2, *bnd, *npts;
+    double *nx, *ny, *l;
+    double* pts;   /* ne x 3 x 2 */
+};
+
+struct orc_solver {
+    const orc_mesh* m;
+    orc_params p;
+    int nm;
+    double *matM, *matCp;
+    int* cell_mat;
+    int nbnd;
+    int* bkind;
+    double* bpar;
+    double *ro, *ru, *rv, *re;
+    double *ro_old, *ru_old, *rv_old, *re_old;
+    double *ro_int, *ru_int, *rv_int, *re_int;
+    double* grad; /* nc x 8: r.x r.y p.x p.y u.x u.y v.x v.y */
+    double* cTau;
+    unsigned* flag;
+    double TAU, t;
+    int newton_hit;
+};
+
+static double dmax(double a, double b) { return a > b ? a : b; } /* _max_, src/mesh/grid.h:102 */
+static double dmin(double a, double b) { return a < b ? a : b; }
+
+/* ------------------------------------------------------------------ mesh */
+
+static int* node_cells(int nn, int nc, const int* tri, int** off_out) {
+    int* off = (int*)calloc((size_t)nn + 1, sizeof(int));
+    for (int i = 0; i < 3 * nc; i++) off[tri[i] + 1]++;
+    for (int i = 0; i < nn; i++) off[i + 1] += off[i];
+    int* fill = (int*)malloc(sizeof(int) * (size_t)nn);
+    memcpy(fill, off, sizeof(int) * (size_t)nn);
+    int* lst = (int*)malloc(sizeof(int) * (size_t)(3 * nc > 0 ? 3 * nc : 1));
+    for (int i = 0; i < nc; i++)
+        for (int k = 0; k < 3; k++) lst[fill[tri[3 * i + k]]++] = i; /* ascending cell order */
+    free(fill);
+    *off_out = off;
+    return lst;
+}
+
+static long long pair_key(int a, int b) {
+    if (a > b) { int t = a; a = b; b = t; }
+    return ((long long)a << 32) | (unsigned)b;
+}
+
+typedef struct { long long key; int idx; } KeyIdx;
+static int cmp_keyidx(const void* x, const void* y) {
+    const KeyIdx* a = (const KeyIdx*)x; const KeyIdx* b = (const KeyIdx*)y;
+    if (a->key != b->key) return a->key < b->key ? -1 : 1;
+    return a->idx - b->idx;
+}
+
+int orc_mesh_build(int nn, const double* xy, int nc, const int* tri, const int* neigh_berkeley,
+                   int nb, const int* bseg, const int* bseg_bnd, int berkeley, orc_mesh** out) {
+    *out = NULL;
+    int* neigh = (int*)malloc(sizeof(int) * 3 * (size_t)nc);
+    orc_mesh* m = (orc_mesh*)calloc(1, sizeof(orc_mesh));
+    m->nn = nn; m->nc = nc;
+    m->cnodes = (int*)malloc(sizeof(int) * 3 * (size_t)nc);
+    memcpy(m->cnodes, tri, sizeof(int) * 3 * (size_t)nc);
+    m->cx = (double*)malloc(sizeof(double) * nc);
+    m->cy = (double*)malloc(sizeof(double) * nc);
+    for (int i = 0; i < nc; i++) { /* src/mesh/MeshReaderSalomeUnv.cpp:89-90 */
+        const int* t = tri + 3 * i;
+        m->cx[i] = (xy[2 * t[0]] + xy[2 * t[1]] + xy[2 * t[2]]) / 3.0;
+        m->cy[i] = (xy[2 * t[0] + 1] + xy[2 * t[1] + 1] + xy[2 * t[2] + 1]) / 3.0;
+    }
+    if (berkeley) {
+        memcpy(neigh, neigh_berkeley, sizeof(int) * 3 * (size_t)nc);
+    } else { /* neighbour across nodes (k, k+1): src/mesh/MeshReaderSalomeUnv.cpp:100-115 */
+        int* off; int* lst = node_cells(nn, nc, tri, &off);
+        for (int i = 0; i < nc; i++)
+            for (int k = 0; k < 3; k++) {
+                int a = tri[3 * i + k], b = tri[3 * i + (k + 1) % 3];
+                int ia = off[a], ib = off[b], nbh = -2;
+                while (ia < off[a + 1] && ib < off[b + 1]) {
+                    if (lst[ia] < lst[ib]) ia++;
+                    else if (lst[ia] > lst[ib]) ib++;
+                    else { if (lst[ia] != i) nbh = lst[ia]; ia++; ib++; }
+                }
+                neigh[3 * i + k] = nbh;
+            }
+        free(off); free(lst);
+    }
+    /* edge count, clearing the neighbour's back reference (:118-135) */
+    int ne = 0;
+    for (int i = 0; i < nc; i++)
+        for (int j = 0; j < 3; j++) {
+            int p = neigh[3 * i + j];
+            if (p > -1) {
+                for (int k = 0; k < 3; k++) if (neigh[3 * p + k] == i) neigh[3 * p + k] = -1;
+                ne++;
+            }
+            if (p == -2) ne++;
+        }
+    m->ne = ne;
+    m->cedges = (int*)malloc(sizeof(int) * 3 * (size_t)nc);
+    m->n1 = (int*)malloc(sizeof(int) * ne); m->n2 = (int*)malloc(sizeof(int) * ne);
+    m->c1 = (int*)malloc(sizeof(int) * ne); m->c2 = (int*)malloc(sizeof(int) * ne);
+    m->bnd = (int*)malloc(sizeof(int) * ne); m->npts = (int*)malloc(sizeof(int) * ne);
+    m->nx = (double*)malloc(sizeof(double) * ne); m->ny = (double*)malloc(sizeof(double) * ne);
+    m->l = (double*)malloc(sizeof(double) * ne);
+    m->pts = (double*)calloc((size_t)ne * 6, sizeof(double));
+    m->S = (double*)malloc(sizeof(double) * nc);
+    int* cfi = (int*)calloc((size_t)nc, sizeof(int));
+
+    KeyIdx* bk = (KeyIdx*)malloc(sizeof(KeyIdx) * (size_t)(nb > 0 ? nb : 1));
+    for (int s = 0; s < nb; s++) { bk[s].key = pair_key(bseg[2 * s], bseg[2 * s + 1]); bk[s].idx = s; }
+    qsort(bk, (size_t)nb, sizeof(KeyIdx), cmp_keyidx);
+
+    const double sq3 = 1.0 / sqrt(3.0);
+    int e = 0, err = 0;
+    for (int i = 0; i < nc && !err; i++)
+        for (int j = 0; j < 3; j++) {
+            int p = neigh[3 * i + j];
+            if (p == -1) continue;
+            const int* t = tri + 3 * i;
+            int a = berkeley ? t[(j + 1) % 3] : t[j];
+            int b = berkeley ? t[(j + 2) % 3] : t[(j + 1) % 3];
+            m->n1[e] = a; m->n2[e] = b;
+            double x1 = xy[2 * a], y1 = xy[2 * a + 1], x2 = xy[2 * b], y2 = xy[2 * b + 1];
+            double* P = m->pts + 6 * (size_t)e;
+            P[0] = (x1 + x2) / 2.0;
+            P[1] = (y1 + y2) / 2.0;
+            if (berkeley) {
+                m->npts[e] = 1; /* src/mesh/MeshReaderBerkleyTriangle.cpp:102-105 */
+            } else {            /* src/mesh/MeshReaderSalomeUnv.cpp:158-169 */
+                m->npts[e] = 3;
+                P[2] = (x1 + x2) / 2.0 - sq3 * (x2 - x1) / 2.0;
+                P[3] = (y1 + y2) / 2.0 - sq3 * (y2 - y1) / 2.0;
+                P[4] = (x1 + x2) / 2.0 + sq3 * (x2 - x1) / 2.0;
+                P[5] = (y1 + y2) / 2.0 + sq3 * (y2 - y1) / 2.0;
+            }
+            double nx = y2 - y1, ny = x1 - x2;
+            double l = sqrt(nx * nx + ny * ny);
+            nx /= l; ny /= l;
+            m->l[e] = l;
+            m->c1[e] = i;
+            m->cedges[3 * i + cfi[i]++] = e;
+            if (!berkeley) { /* outward from c1 (:181-187) */
+                double vx = m->cx[i] - P[0], vy = m->cy[i] - P[1];
+                if (vx * nx + vy * ny > 0) { nx *= -1; ny *= -1; }
+            }
+            m->nx[e] = nx; m->ny[e] = ny;
+            m->bnd[e] = -1;
+            if (p > -1) {
+                m->c2[e] = p;
+                m->cedges[3 * p + cfi[p]++] = e;
+            } else {
+                m->c2[e] = -1;
+                KeyIdx q; q.key = pair_key(a, b); q.idx = -1;
+                int lo = 0, hi = nb; /* first segment with this node pair */
+                while (lo < hi) { int mid = (lo + hi) / 2; if (bk[mid].key < q.key) lo = mid + 1; else hi = mid; }
+                if (lo < nb && bk[lo].key == q.key) m->bnd[e] = bseg_bnd[bk[lo].idx];
+                else { err = -222; break; } /* Exception TYPE_MESH_UNV_NOT_DEFINED_BND_EDGE */
+            }
+            e++;
+        }
+    free(bk); free(neigh);
+    if (!err)
+        for (int i = 0; i < nc; i++) {
+            if (cfi[i] != 3) { err = -221; break; }
+            double a = m->l[m->cedges[3 * i]], b = m->l[m->cedges[3 * i + 1]], c = m->l[m->cedges[3 * i + 2]];
+            double p = (a + b + c) / 2.0; /* Heron, src/mesh/MeshReaderSalomeUnv.cpp:250-255 */
+            m->S[i] = sqrt(p * (p - a) * (p - b) * (p - c));
+        }
+    free(cfi);
+    if (err) { orc_mesh_free(m); return err; }
+    *out = m;
+    return 0;
+}
+
+void orc_mesh_sizes(const orc_mesh* m, int* nc, int* ne) { *nc = m->nc; *ne = m->ne; }
+
+void orc_mesh_export(const orc_mesh* m, int* cell_edges, double* cell_S, double* cell_c,
+                     int* edge_n12, int* edge_c12, int* edge_bnd, int* edge_npts,
+                     double* edge_n, double* edge_l, double* edge_pts) {
+    for (int i = 0; i < m->nc; i++) {
+        for (int k = 0; k < 3; k++) cell_edges[3 * i + k] = m->cedges[3 * i + k];
+        cell_S[i] = m->S[i];
+        cell_c[2 * i] = m->cx[i]; cell_c[2 * i + 1] = m->cy[i];
+    }
+    for (int e = 0; e < m->ne; e++) {
+        edge_n12[2 * e] = m->n1[e]; edge_n12[2 * e + 1] = m->n2[e];
+        edge_c12[2 * e] = m->c1[e]; edge_c12[2 * e + 1] = m->c2[e];
+        edge_bnd[e] = m->bnd[e]; edge_npts[e] = m->npts[e];
+        edge_n[2 * e] = m->nx[e]; edge_n[2 * e + 1] = m->ny[e];
+        edge_l[e] = m->l[e];
+        for (int k = 0; k < 6; k++) edge_pts[6 * e + k] = m->pts[6 * e + k];
+    }
+}
+
+void orc_mesh_free(orc_mesh* m) {
+    if (!m) return;
+    free(m->cnodes); free(m->cedges); free(m->S); free(m->cx); free(m->cy);
+    free(m->n1); free(m->n2); free(m->c1); free(m->c2); free(m->bnd); free(m->npts);
+    free(m->nx); free(m->ny); free(m->l); free(m->pts);
+    free(m);
+}
+
+/* ------------------------------------------------------------------ physics */
+
+/* Material::URS, src/global.cpp:9-30 */
+static void urs(double M, double Cp, Par* par, int flag) {
+    double Cv = Cp - GAS_R / M;
+    double gam = Cp / Cv;
+    switch (flag) {
+    case 0: par->p = par->r * par->e * (gam - 1); par->cz = sqrt(gam * par->p / par->r); break;
+    case 1: par->e = par->p / (par->r * (gam - 1)); par->T = par->e / Cv; break;
+    case 2: par->r = par->p * M / (par->T * GAS_R); par->cz = sqrt(gam * par->p / par->r); break;
+    }
+}
+
+void orc_region_state(double M, double Cp, double u, double v, double T, double p, double* U4) {
+    Par par; memset(&par, 0, sizeof par);
+    par.u = u; par.v = v; par.T = T; par.p = p;
+    urs(M, Cp, &par, 2); /* src/methods/fvm_tvd.cpp:91-92 */
+    urs(M, Cp, &par, 1);
+    U4[0] = par.r;       /* convertParToCons, :795-801 */
+    U4[1] = par.r * par.u;
+    U4[2] = par.r * par.v;
+    U4[3] = par.r * (par.e + 0.5 * (par.u * par.u + par.v * par.v));
+}
+
+/* convertConsToPar, src/methods/fvm_tvd.cpp:803-813 */
+static void cons2par(const orc_solver* s, int i, Par* par) {
+    int mt = s->cell_mat[i];
+    par->r = s->ro[i];
+    par->u = s->ru[i] / s->ro[i];
+    par->v = s->rv[i] / s->ro[i];
+    par->E = s->re[i] / s->ro[i];
+    par->e = par->E - 0.5 * (par->u * par->u + par->v * par->v);
+    urs(s->matM[mt], s->matCp[mt], par, 0);
+    urs(s->matM[mt], s->matCp[mt], par, 1);
+}
+
+/* boundaryCond + CFDBnd*::run, src/methods/fvm_tvd.cpp:694-705, src/bnd_cond.cpp:75-110 */
+static void boundary_cond(const orc_solver* s, int e, const Par* pL, Par* pR) {
+    const orc_mesh* m = s->m;
+    int b = m->bnd[e];
+    int kind = s->bkind[b];
+    const double* bp = s->bpar + 4 * b;
+    if (kind == ORC_BND_INLET) {
+        pR->u = bp[0]; pR->v = bp[1]; pR->T = bp[2]; pR->p = bp[3];
+    } else if (kind == ORC_BND_OUTLET) {
+        *pR = *pL;
+    } else { /* BOUND_WALL_SLIP, and BOUND_WALL_NO_SLIP which the reference maps to the slip class */
+        *pR = *pL;
+        double Un = pL->u * m->nx[e] + pL->v * m->ny[e];
+        double Vx = m->nx[e] * Un * 2.0, Vy = m->ny[e] * Un * 2.0;
+        pR->u = pL->u - Vx;
+        pR->v = pL->v - Vy;
+    }
+    int mt = s->cell_mat[m->c1[e]];
+    urs(s->matM[mt], s->matCp[mt], pR, 2);
+    urs(s->matM[mt], s->matCp[mt], pR, 1);
+    pR->E = pR->e + 0.5 * (pR->u * pR->u + pR->v * pR->v);
+}
+
+/* Exact Riemann solver rim_orig, src/global.cpp:232-405, restated with structured
+ * control flow and an optional cap on its Newton loop. VB/VE are the tangential
+ * velocities carried through; the third component the reference passes is 0. */
+static int riemann_exact(double* RI_, double* EI_, double* PI_, double* UI_, double* VI_,
+                         double RB, double PB, double UB, double VB,
+                         double RE, double PE, double UE, double VE, double GAM, int cap) {
+    double AGAM = (GAM - 1.0);
+    double DGAM = (2.0 / AGAM);
+    double GGAM = (sqrt(GAM * AGAM));
+    double HGAM = (AGAM / 2.0);
+    double FGAM = (3.0 * GAM - 1.0);
+    double OGAM = (AGAM / (2.0 * GAM));
+    double QGAM = (GAM + 1.0);
+    double PGAM = (QGAM / (2.0 * GAM));
+    double RGAM = (4.0 * GAM);
+    double SGAM = (GAM * AGAM);
+    double TGAM = (QGAM / 2.0);
+    double US = 0.0, UF = 0.0;
+    double RF, RS, EF, ES, SBL, SFL, SSL, SEL, D, P;
+    double eps = 1.0e-5;
+    double CB = sqrt(GAM * PB / RB);
+    double CE = sqrt(GAM * PE / RE);
+    double EB = CB * CB / SGAM;
+    double EE = CE * CE / SGAM;
+    double RCB = RB * CB;
+    double RCE = RE * CE;
+    double DU = UB - UE;
+    double RI, EI, UI, VI;
+    int hit = 0;
+    if (DU < -2.0 * (CB + CE) / AGAM) { /* vacuum */
+        RF = 0.0; RS = 0.0; EF = 0.0; ES = 0.0;
+        SBL = UB - CB;
+        SFL = UB + 2.0 * CB / AGAM;
+        SSL = UE - 2.0 * CE / AGAM;
+        SEL = UE + CE;
+    } else {
+        P = (PB * RCE + PE * RCB + DU * RCB * RCE) / (RCB + RCE);
+        int it = 0;
+        for (;;) {
+            double PPB, PPE, F1, FS1, F2, FS2;
+            if (P < eps) P = eps;
+            PPB = P / PB;
+            if (PB > P) {
+                double ZFB = CB * exp(log(PPB) * OGAM);
+                F1 = DGAM * (ZFB - CB);
+                FS1 = ZFB / (GAM * P);
+            } else {
+                double PKB = PGAM * PPB + OGAM;
+                double ZNB = RCB * sqrt(PKB);
+                F1 = (P - PB) / ZNB;
+                FS1 = (QGAM * PPB + FGAM) / (RGAM * ZNB * PKB);
+            }
+            PPE = P / PE;
+            if (PE > P) {
+                double ZFE = CE * exp(log(PPE) * OGAM);
+                F2 = DGAM * (ZFE - CE);
+                FS2 = ZFE / (GAM * P);
+            } else {
+                double PKE = PGAM * PPE + OGAM;
+                double ZNE = RCE * sqrt(PKE);
+                F2 = (P - PE) / ZNE;
+                FS2 = (QGAM * PPE + FGAM) / (RGAM * ZNE * PKE);
+            }
+            double DP = (DU - F1 - F2) / (FS1 + FS2);
+            P = P + DP;
+            if (!(fabs(DU - F1 - F2) > eps)) break;
+            if (cap > 0 && ++it >= cap) { hit = 1; break; }
+        }
+        double PPB = P / PB, PPE = P / PE;
+        double ZFB = CB * exp(log(PPB) * OGAM);
+        double ZFE = CE * exp(log(PPE) * OGAM);
+        if (!(PB > P)) { /* left shock */
+            D = UB - sqrt((TGAM * P + HGAM * PB) / RB);
+            double UBD = UB - D, RUBD = RB * UBD;
+            RF = RUBD * RUBD / (PB - P + RUBD * UBD);
+            UF = D + RUBD / RF;
+            EF = P / (AGAM * RF);
+            SBL = D; SFL = D;
+        } else {         /* left rarefaction */
+            EF = ZFB * ZFB / SGAM;
+            UF = UB + DGAM * (CB - ZFB);
+            RF = P / (AGAM * EF);
+            SBL = UB - CB;
+            SFL = UF - ZFB;
+        }
+        if (!(PE > P)) { /* right shock */
+            D = UE + sqrt((TGAM * P + HGAM * PE) / RE);
+            double UED = UE - D, RUED = RE * UED;
+            RS = RUED * RUED / (PE - P + RUED * UED);
+            US = D + RUED / RS;
+            ES = P / (AGAM * RS);
+            SEL = D; SSL = D;
+        } else {         /* right rarefaction */
+            ES = ZFE * ZFE / SGAM;
+            US = UE - DGAM * (CE - ZFE);
+            RS = P / (AGAM * ES);
+            SSL = US + ZFE;
+            SEL = UE + CE;
+        }
+    }
+    /* sample at x/t = 0 */
+    if (SEL <= 0.0) { RI = RE; EI = EE; UI = UE; VI = VE; }
+    else if (SBL >= 0.0) { RI = RB; EI = EB; UI = UB; VI = VB; }
+    else if ((SSL >= 0.0) && (SFL <= 0.0)) {
+        if (US >= 0.0) { RI = RF; EI = EF; UI = UF; VI = VB; }
+        else { RI = RS; EI = ES; UI = US; VI = VE; }
+    } else if (SFL > 0.0) {
+        UI = (UB + DGAM * GGAM * sqrt(EB)) / (1 + DGAM);
+        VI = VB;
+        EI = (UI * UI) / SGAM;
+        RI = RB * exp(log(EI / EB) * (1 / AGAM));
+    } else {
+        UI = (UE - DGAM * GGAM * sqrt(EE)) / (1 + DGAM);
+        VI = VE;
+        EI = (UI * UI) / SGAM;
+        RI = RE * exp(log(EI / EE) * (1 / AGAM));
+    }
+    *RI_ = RI; *EI_ = EI; *UI_ = UI; *VI_ = VI;
+    *PI_ = AGAM * EI * RI;
+    return hit;
+}
+
+/* Godunov flux, FVM_TVD::calcFlux, src/methods/fvm_tvd.cpp:602-622 */
+static int flux_godunov(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM, int cap) {
+    double RI, EI, PI, UN, UT;
+    double unl = pL->u * nx + pL->v * ny;
+    double unr = pR->u * nx + pR->v * ny;
+    double utl = pL->u * ny - pL->v * nx;
+    double utr = pR->u * ny - pR->v * nx;
+    int hit = riemann_exact(&RI, &EI, &PI, &UN, &UT, pL->r, pL->p, unl, utl, pR->r, pR->p, unr, utr, GAM, cap);
+    double UI = UN * nx + UT * ny;
+    double VI = UN * ny - UT * nx;
+    f[0] = RI * UN;
+    f[1] = f[0] * UI + PI * nx;
+    f[2] = f[0] * VI + PI * ny;
+    f[3] = (RI * (EI + 0.5 * (UI * UI + VI * VI)) + PI) * UN;
+    return hit;
+}
+
+/* Lax-Friedrichs (Rusanov) flux, the reference's template in
+ * src/methods/fvm_tvd_implicit.cpp:939-960 (energy from p). */
+static void flux_lax(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
+    double unl = pL->u * nx + pL->v * ny;
+    double unr = pR->u * nx + pR->v * ny;
+    double alpha = dmax(fabs(unl) + sqrt(GAM * pL->p / pL->r), fabs(unr) + sqrt(GAM * pR->p / pR->r));
+    double rol = pL->r, rul = pL->r * pL->u, rvl = pL->r * pL->v;
+    double rel = pL->p / (GAM - 1.0) + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
+    double ror = pR->r, rur = pR->r * pR->u, rvr = pR->r * pR->v;
+    double rer = pR->p / (GAM - 1.0) + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
+    double frl = rol * unl, frr = ror * unr;
+    f[0] = 0.5 * (frr + frl - alpha * (ror - rol));
+    f[1] = 0.5 * (frr * pR->u + frl * pL->u + (pR->p + pL->p) * nx - alpha * (rur - rul));
+    f[2] = 0.5 * (frr * pR->v + frl * pL->v + (pR->p + pL->p) * ny - alpha * (rvr - rvl));
+    f[3] = 0.5 * ((rer + pR->p) * unr + (rel + pL->p) * unl - alpha * (rer - rel));
+}
+
+/* Physical flux through the unit normal n for a primitive state; E is the total
+ * energy per unit volume. */
+static void phys_flux(double* f, double r, double u, double v, double p, double E, double un, double nx, double ny) {
+    double m = r * un;
+    f[0] = m;
+    f[1] = m * u + p * nx;
+    f[2] = m * v + p * ny;
+    f[3] = (E + p) * un;
+}
+
+/* HLLC flux (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics,
+ * 3rd ed., sec. 10.4-10.5) with Davis wave-speed estimates
+ * S_L = min(un_L - c_L, un_R - c_R), S_R = max(un_L + c_L, un_R + c_R). */
+static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
+    double cL = sqrt(GAM * pL->p / pL->r), cR = sqrt(GAM * pR->p / pR->r);
+    double unL = pL->u * nx + pL->v * ny, unR = pR->u * nx + pR->v * ny;
+    double EL = pL->p / (GAM - 1.0) + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
+    double ER = pR->p / (GAM - 1.0) + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
+    double SL = dmin(unL - cL, unR - cR), SR = dmax(unL + cL, unR + cR);
+    if (SL >= 0.0) { phys_flux(f, pL->r, pL->u, pL->v, pL->p, EL, unL, nx, ny); return; }
+    if (SR <= 0.0) { phys_flux(f, pR->r, pR->u, pR->v, pR->p, ER, unR, nx, ny); return; }
+    double mL = pL->r * (SL - unL), mR = pR->r * (SR - unR);
+    double Ss = (pR->p - pL->p + mL * unL - mR * unR) / (mL - mR);
+    const Par* K; double SK, unK, EK, mK;
+    if (Ss >= 0.0) { K = pL; SK = SL; unK = unL; EK = EL; mK = mL; }
+    else { K = pR; SK = SR; unK = unR; EK = ER; mK = mR; }
+    double FK[4];
+    phys_flux(FK, K->r, K->u, K->v, K->p, EK, unK, nx, ny);
+    double fac = mK / (SK - Ss);
+    double ds = Ss - unK;
+    double U0 = fac;
+    double U1 = fac * (K->u + ds * nx);
+    double U2 = fac * (K->v + ds * ny);
+    double U3 = fac * (EK / K->r + ds * (Ss + K->p / mK));
+    f[0] = FK[0] + SK * (U0 - K->r);
+    f[1] = FK[1] + SK * (U1 - K->r * K->u);
+    f[2] = FK[2] + SK * (U2 - K->r * K->v);
+    f[3] = FK[3] + SK * (U3 - EK);
+}
+
+/* Roe flux (Roe, J. Comput. Phys. 43, 1981) in the face-normal frame with the
+ * Harten-Hyman entropy fix on the acoustic waves (Harten & Hyman, J. Comput.
+ * Phys. 50, 1983): delta = max(0, lam~ - lam_L, lam_R - lam~), |lam~| -> delta
+ * where |lam~| < delta. Roe averages as in the reference's roe_orig
+ * (src/global.cpp:407-441). */
+static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
+    double G1 = GAM - 1.0;
+    double unL = pL->u * nx + pL->v * ny, unR = pR->u * nx + pR->v * ny;
+    double EL = pL->p / G1 + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
+    double ER = pR->p / G1 + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
+    double HL = (EL + pL->p) / pL->r, HR = (ER + pR->p) / pR->r;
+    double sL = sqrt(pL->r), sR = sqrt(pR->r);
+    double w = 1.0 / (sL + sR);
+    double ut = (sL * pL->u + sR * pR->u) * w;
+    double vt = (sL * pL->v + sR * pR->v) * w;
+    double Ht = (sL * HL + sR * HR) * w;
+    double q2 = ut * ut + vt * vt;
+    double c2 = G1 * (Ht - 0.5 * q2);
+    double c = sqrt(c2);
+    double unt = ut * nx + vt * ny;
+    double rt = sL * sR;
+    double dr = pR->r - pL->r, dp = pR->p - pL->p, dun = unR - unL;
+    double dtx = (pR->u - pL->u) - dun * nx, dty = (pR->v - pL->v) - dun * ny;
+    double a1 = (dp - rt * c * dun) / (2.0 * c2);
+    double a2 = dr - dp / c2;
+    double a4 = (dp + rt * c * dun) / (2.0 * c2);
+    double l1 = unt - c, l4 = unt + c;
+    double cL = sqrt(GAM * pL->p / pL->r), cR = sqrt(GAM * pR->p / pR->r);
+    double d1 = dmax(0.0, dmax(l1 - (unL - cL), (unR - cR) - l1));
+    double d4 = dmax(0.0, dmax(l4 - (unL + cL), (unR + cR) - l4));
+    double al1 = fabs(l1); if (al1 < d1) al1 = d1;
+    double al4 = fabs(l4); if (al4 < d4) al4 = d4;
+    double al2 = fabs(unt);
+    double w1 = al1 * a1, w2 = al2 * a2, w4 = al4 * a4, ws = al2 * rt;
+    double D0 = w1 + w2 + w4;
+    double D1 = w1 * (ut - c * nx) + (w2 * ut + ws * dtx) + w4 * (ut + c * nx);
+    double D2 = w1 * (vt - c * ny) + (w2 * vt + ws * dty) + w4 * (vt + c * ny);
+    double D3 = w1 * (Ht - unt * c) + (w2 * (0.5 * q2) + ws * (ut * dtx + vt * dty)) + w4 * (Ht + unt * c);
+    double FL[4], FR[4];
+    phys_flux(FL, pL->r, pL->u, pL->v, pL->p, EL, unL, nx, ny);
+    phys_flux(FR, pR->r, pR->u, pR->v, pR->p, ER, unR, nx, ny);
+    f[0] = 0.5 * (FL[0] + FR[0] - D0);
+    f[1] = 0.5 * (FL[1] + FR[1] - D1);
+    f[2] = 0.5 * (FL[2] + FR[2] - D2);
+    f[3] = 0.5 * (FL[3] + FR[3] - D3);
+}
+
+/* MINMOD, src/methods/LimiterDGCockburn.cpp:110-123 */
+static double minmod(double a, double b) {
+    if (a * b > 0.0) return fabs(a) < fabs(b) ? a : b;
+    return 0;
+}
+
+/* ------------------------------------------------------------------ solver */
+
+static double* dalloc(int n) { return (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
+
+/* calcTimeStep, src/methods/fvm_tvd.cpp:216-240 */
+static void calc_time_step(orc_solver* s) {
+    const orc_mesh* m = s->m;
+    if (s->p.steady) {
+        for (int i = 0; i < m->nc; i++) {
+            Par p; cons2par(s, i, &p);
+            s->cTau[i] = s->p.cfl * m->S[i] / dmax(fabs(p.u) + p.cz, fabs(p.v) + p.cz);
+        }
+    } else {
+        for (int i = 0; i < m->nc; i++) {
+            Par p; cons2par(s, i, &p);
+            double t = s->p.cfl * m->S[i] / dmax(fabs(p.u) + p.cz, fabs(p.v) + p.cz);
+            if (s->TAU > t) s->TAU = t;
+        }
+        for (int i = 0; i < m->nc; i++) s->cTau[i] = s->TAU;
+    }
+}
+
+int orc_solver_create(const orc_mesh* m, const orc_params* prm, int nm, const double* mat,
+                      const int* cell_mat, int nbnd, const int* bnd_kind, const double* bnd_par,
+                      const double* U0, orc_solver** out) {
+    orc_solver* s = (orc_solver*)calloc(1, sizeof(orc_solver));
+    int nc = m->nc;
+    s->m = m; s->p = *prm; s->nm = nm; s->nbnd = nbnd;
+    s->matM = dalloc(nm); s->matCp = dalloc(nm);
+    for (int k = 0; k < nm; k++) { s->matM[k] = mat[2 * k]; s->matCp[k] = mat[2 * k + 1]; }
+    s->cell_mat = (int*)malloc(sizeof(int) * (size_t)nc);
+    memcpy(s->cell_mat, cell_mat, sizeof(int) * (size_t)nc);
+    s->bkind = (int*)malloc(sizeof(int) * (size_t)(nbnd > 0 ? nbnd : 1));
+    s->bpar = dalloc(4 * nbnd);
+    if (nbnd) { memcpy(s->bkind, bnd_kind, sizeof(int) * nbnd); memcpy(s->bpar, bnd_par, sizeof(double) * 4 * nbnd); }
+    s->ro = dalloc(nc); s->ru = dalloc(nc); s->rv = dalloc(nc); s->re = dalloc(nc);
+    s->ro_old = dalloc(nc); s->ru_old = dalloc(nc); s->rv_old = dalloc(nc); s->re_old = dalloc(nc);
+    s->ro_int = dalloc(nc); s->ru_int = dalloc(nc); s->rv_int = dalloc(nc); s->re_int = dalloc(nc);
+    s->grad = dalloc(8 * nc);
+    s->cTau = dalloc(nc);
+    s->flag = (unsigned*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(unsigned));
+    orc_set_state(s, U0);
+    s->TAU = prm->tau_xml;
+    calc_time_step(s); /* FVM_TVD::init, :211 */
+    *out = s;
+    return 0;
+}
+
+double orc_tau(const orc_solver* s) { return s->TAU; }
+
+void orc_set_state(orc_solver* s, const double* U) {
+    int nc = s->m->nc;
+    memcpy(s->ro, U, sizeof(double) * nc);
+    memcpy(s->ru, U + nc, sizeof(double) * nc);
+    memcpy(s->rv, U + 2 * (size_t)nc, sizeof(double) * nc);
+    memcpy(s->re, U + 3 * (size_t)nc, sizeof(double) * nc);
+}
+
+void orc_get_state(const orc_solver* s, double* U, double* ctau, unsigned* flags) {
+    int nc = s->m->nc;
+    if (U) {
+        memcpy(U, s->ro, sizeof(double) * nc);
+        memcpy(U + nc, s->ru, sizeof(double) * nc);
+        memcpy(U + 2 * (size_t)nc, s->rv, sizeof(double) * nc);
+        memcpy(U + 3 * (size_t)nc, s->re, sizeof(double) * nc);
+    }
+    if (ctau) memcpy(ctau, s->cTau, sizeof(double) * nc);
+    if (flags) memcpy(flags, s->flag, sizeof(unsigned) * nc);
+}
+
+/* calcGrad, src/methods/fvm_tvd.cpp:242-301 */
+static void calc_grad(orc_solver* s) {
+    const orc_mesh* m = s->m;
+    double* g = s->grad;
+    memset(g, 0, sizeof(double) * 8 * (size_t)m->nc);
+    for (int e = 0; e < m->ne; e++) {
+        int c1 = m->c1[e], c2 = m->c2[e];
+        Par pL, pR;
+        cons2par(s, c1, &pL);
+        if (c2 > -1) cons2par(s, c2, &pR);
+        else boundary_cond(s, e, &pL, &pR);
+        double nx = m->nx[e], ny = m->ny[e], l = m->l[e];
+        double v[8];
+        v[0] = (pL.r + pR.r) / 2 * nx * l; v[1] = (pL.r + pR.r) / 2 * ny * l;
+        v[2] = (pL.p + pR.p) / 2 * nx * l; v[3] = (pL.p + pR.p) / 2 * ny * l;
+        v[4] = (pL.u + pR.u) / 2 * nx * l; v[5] = (pL.u + pR.u) / 2 * ny * l;
+        v[6] = (pL.v + pR.v) / 2 * nx * l; v[7] = (pL.v + pR.v) / 2 * ny * l;
+        for (int k = 0; k < 8; k++) g[8 * (size_t)c1 + k] += v[k];
+        if (c2 > -1) for (int k = 0; k < 8; k++) g[8 * (size_t)c2 + k] -= v[k];
+    }
+    for (int i = 0; i < m->nc; i++) {
+        double si = m->S[i];
+        for (int k = 0; k < 8; k++) g[8 * (size_t)i + k] /= si;
+    }
+}
+
+/* One side's reconstruction at point (px, py): phi += grad(phi) . (P - C),
+ * src/methods/fvm_tvd.cpp:646-691; with MINMOD the increment is
+ * minmod(grad(phi) . (P - C), phi_neighbour - phi). */
+static void recon_side(const orc_solver* s, int c, double px, double py, Par* q, const Par* nb) {
+    const orc_mesh* m = s->m;
+    const double* g = s->grad + 8 * (size_t)c;
+    double dx = px - m->cx[c], dy = py - m->cy[c];
+    double dr = g[0] * dx + g[1] * dy;
+    double dp = g[2] * dx + g[3] * dy;
+    double du = g[4] * dx + g[5] * dy;
+    double dv = g[6] * dx + g[7] * dy;
+    if (s->p.recon == ORC_RECON_MINMOD) {
+        dr = minmod(dr, nb->r - q->r);
+        dp = minmod(dp, nb->p - q->p);
+        du = minmod(du, nb->u - q->u);
+        dv = minmod(dv, nb->v - q->v);
+    }
+    q->r += dr; q->p += dp; q->u += du; q->v += dv;
+}
+
+static void face_states(const orc_solver* s, int e, int gp, Par* pL, Par* pR) {
+    const orc_mesh* m = s->m;
+    int c1 = m->c1[e], c2 = m->c2[e];
+    double px = m->pts[6 * (size_t)e + 2 * gp], py = m->pts[6 * (size_t)e + 2 * gp + 1];
+    cons2par(s, c1, pL);
+    if (c2 > -1) {
+        cons2par(s, c2, pR);
+        if (s->p.recon != ORC_RECON_NONE) {
+            Par cL = *pL, cR = *pR;
+            recon_side(s, c1, px, py, pL, &cR);
+            recon_side(s, c2, px, py, pR, &cL);
+        }
+    } else {
+        if (s->p.recon != ORC_RECON_NONE) {
+            Par ghost;
+            if (s->p.recon == ORC_RECON_MINMOD) boundary_cond(s, e, pL, &ghost);
+            recon_side(s, c1, px, py, pL, &ghost);
+        }
+        boundary_cond(s, e, pL, pR);
+    }
+}
+
+static int calc_flux(const orc_solver* s, double* f, const Par* pL, const Par* pR, double nx, double ny) {
+    double GAM = s->p.gam_flux;
+    switch (s->p.flux) {
+    case ORC_FLUX_LAX: flux_lax(f, pL, pR, nx, ny, GAM); return 0;
+    case ORC_FLUX_ROE: flux_roe(f, pL, pR, nx, ny, GAM); return 0;
+    case ORC_FLUX_HLLC: flux_hllc(f, pL, pR, nx, ny, GAM); return 0;
+    default: return flux_godunov(f, pL, pR, nx, ny, GAM, s->p.newton_cap);
+    }
+}
+
+/* Edge loop of one Runge-Kutta stage, src/methods/fvm_tvd.cpp:324-365 */
+static void stage_residual(orc_solver* s) {
+    const orc_mesh* m = s->m;
+    int nc = m->nc;
+    memset(s->ro_int, 0, sizeof(double) * nc); memset(s->ru_int, 0, sizeof(double) * nc);
+    memset(s->rv_int, 0, sizeof(double) * nc); memset(s->re_int, 0, sizeof(double) * nc);
+    if (s->p.recon != ORC_RECON_NONE) calc_grad(s);
+    for (int e = 0; e < m->ne; e++) {
+        int c1 = m->c1[e], c2 = m->c2[e];
+        double nx = m->nx[e], ny = m->ny[e];
+        double l = m->l[e] * 0.5;
+        double fr = 0.0, fu = 0.0, fv = 0.0, fe = 0.0;
+        for (int gp = 1; gp < m->npts[e]; gp++) {
+            Par pL, pR; double f[4];
+            face_states(s, e, gp, &pL, &pR);
+            s->newton_hit |= calc_flux(s, f, &pL, &pR, nx, ny);
+            fr += f[0]; fu += f[1]; fv += f[2]; fe += f[3];
+        }
+        s->ro_int[c1] -= fr * l; s->ru_int[c1] -= fu * l;
+        s->rv_int[c1] -= fv * l; s->re_int[c1] -= fe * l;
+        if (c2 > -1) {
+            s->ro_int[c2] += fr * l; s->ru_int[c2] += fu * l;
+            s->rv_int[c2] += fv * l; s->re_int[c2] += fe * l;
+        }
+    }
+}
+
+void orc_residual(orc_solver* s, double* R) {
+    int nc = s->m->nc;
+    stage_residual(s);
+    memcpy(R, s->ro_int, sizeof(double) * nc);
+    memcpy(R + nc, s->ru_int, sizeof(double) * nc);
+    memcpy(R + 2 * (size_t)nc, s->rv_int, sizeof(double) * nc);
+    memcpy(R + 3 * (size_t)nc, s->re_int, sizeof(double) * nc);
+}
+
+static int is_lim(const orc_solver* s, int i) { return (s->flag[i] & 0x2u) > 0; }
+
+static void stage_update(orc_solver* s) { /* :366-374 */
+    const orc_mesh* m = s->m;
+    for (int i = 0; i < m->nc; i++) {
+        if (is_lim(s, i)) continue;
+        double cfl = s->cTau[i] / m->S[i];
+        s->ro[i] += cfl * s->ro_int[i]; s->ru[i] += cfl * s->ru_int[i];
+        s->rv[i] += cfl * s->rv_int[i]; s->re[i] += cfl * s->re_int[i];
+    }
+}
+
+static void check_limits(orc_solver* s, int i) { /* :439-446 */
+    Par par; cons2par(s, i, &par);
+    if (par.r < s->p.lim_rmin) s->flag[i] |= 0x2u;
+    if (par.r > s->p.lim_rmax) s->flag[i] |= 0x2u;
+    if (par.p < s->p.lim_pmin) s->flag[i] |= 0x2u;
+    if (par.p > s->p.lim_pmax) s->flag[i] |= 0x2u;
+    if (fabs(par.u) > s->p.lim_umax) s->flag[i] |= 0x2u;
+    if (fabs(par.v) > s->p.lim_umax) s->flag[i] |= 0x2u;
+}
+
+static void remediate(orc_solver* s) { /* remediateLimCells, :464-499 */
+    const orc_mesh* m = s->m;
+    for (int i = 0; i < m->nc; i++) {
+        if (!is_lim(s, i)) continue;
+        double sRO = 0.0, sRU = 0.0, sRV = 0.0, sRE = 0.0, S = 0.0;
+        for (int k = 0; k < 3; k++) {
+            int j = m->c2[m->cedges[3 * i + k]];
+            if (j >= 0) {
+                double sj = m->S[j];
+                S += sj;
+                sRO += s->ro[j] * sj; sRU += s->ru[j] * sj; sRV += s->rv[j] * sj; sRE += s->re[j] * sj;
+            }
+        }
+        s->ro[i] = sRO / S; s->ru[i] = sRU / S; s->rv[i] = sRV / S; s->re[i] = sRE / S;
+        s->flag[i] += 0x010000u;
+        if (s->flag[i] & 0x200000u) s->flag[i] &= 0x001110u;
+    }
+}
+
+int orc_step(orc_solver* s, int nsteps) {
+    const orc_mesh* m = s->m;
+    int nc = m->nc;
+    int nst = s->p.scheme == ORC_TIME_EULER ? 1 : (s->p.scheme == ORC_TIME_HEUN ? 2 : 3);
+    const double c13 = 1.0 / 3.0, c23 = 2.0 / 3.0;
+    s->newton_hit = 0;
+    for (int step = 0; step < nsteps; step++) {
+        if (!s->p.steady) s->t += s->TAU;
+        else calc_time_step(s);
+        memcpy(s->ro_old, s->ro, sizeof(double) * nc); memcpy(s->ru_old, s->ru, sizeof(double) * nc);
+        memcpy(s->rv_old, s->rv, sizeof(double) * nc); memcpy(s->re_old, s->re, sizeof(double) * nc);
+        for (int st = 0; st < nst; st++) {
+            stage_residual(s);
+            stage_update(s);
+            if (s->p.scheme == ORC_TIME_SSPRK3 && st == 1)
+                for (int i = 0; i < nc; i++) {
+                    if (is_lim(s, i)) continue;
+                    s->ro[i] = 0.75 * s->ro_old[i] + 0.25 * s->ro[i];
+                    s->ru[i] = 0.75 * s->ru_old[i] + 0.25 * s->ru[i];
+                    s->rv[i] = 0.75 * s->rv_old[i] + 0.25 * s->rv[i];
+                    s->re[i] = 0.75 * s->re_old[i] + 0.25 * s->re[i];
+                }
+        }
+        for (int i = 0; i < nc; i++) {
+            if (is_lim(s, i)) continue;
+            if (s->p.scheme == ORC_TIME_HEUN) { /* ICASE 97-65 eq. (4.10), :429-437 */
+                s->ro[i] = 0.5 * (s->ro_old[i] + s->ro[i]); s->ru[i] = 0.5 * (s->ru_old[i] + s->ru[i]);
+                s->rv[i] = 0.5 * (s->rv_old[i] + s->rv[i]); s->re[i] = 0.5 * (s->re_old[i] + s->re[i]);
+            } else if (s->p.scheme == ORC_TIME_SSPRK3) { /* Shu-Osher third stage */
+                s->ro[i] = c13 * s->ro_old[i] + c23 * s->ro[i]; s->ru[i] = c13 * s->ru_old[i] + c23 * s->ru[i];
+                s->rv[i] = c13 * s->rv_old[i] + c23 * s->rv[i]; s->re[i] = c13 * s->re_old[i] + c23 * s->re[i];
+            }
+            check_limits(s, i);
+        }
+        remediate(s);
+    }
+    return s->newton_hit;
+}
+
+void orc_solver_free(orc_solver* s) {
+    if (!s) return;
+    free(s->matM); free(s->matCp); free(s->cell_mat); free(s->bkind); free(s->bpar);
+    free(s->ro); free(s->ru); free(s->rv); free(s->re);
+    free(s->ro_old); free(s->ru_old); free(s->rv_old); free(s->re_old);
+    free(s->ro_int); free(s->ru_int); free(s->rv_int); free(s->re_int);
+    free(s->grad); free(s->cTau); free(s->flag);
+    free(s);
+}

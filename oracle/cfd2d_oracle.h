@@ -1,0 +1,78 @@
+/*
+ * cfd2d oracle: a plain-C restatement of the reference's explicit finite-volume
+ * solver FVM_TVD (src/methods/fvm_tvd.cpp) and of the pieces it calls.
+ *
+ * TEST INFRASTRUCTURE ONLY. The product (libcfd2d_gpu.so) never links, loads or
+ * calls this code; only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg use it, as the checker.
+ *
+ * Parity: pinned against the reference's own FVM_TVD compiled from its sources
+ * (oracle/Makefile, target "reference") on the fixtures in tests/golden/: in the
+ * reference's only mode (exact Godunov flux, unlimited linear reconstruction,
+ * Heun) this restatement reproduces the reference's state bit for bit.
+ * Options the reference does not have (Lax-Friedrichs, Roe, HLLC, minmod,
+ * explicit Euler, SSP-RK3) reuse the same structure, conventions and ghost
+ * states; their formulas are the published ones named at each function.
+ *
+ * Arithmetic order follows the reference expression by expression; build with
+ * -ffp-contract=off so no multiply-add is fused.
+ */
+#ifndef CFD2D_ORACLE_H
+#define CFD2D_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_FLUX_GODUNOV = 0, ORC_FLUX_LAX = 1, ORC_FLUX_ROE = 2, ORC_FLUX_HLLC = 3 };
+enum { ORC_RECON_NONE = 0, ORC_RECON_LINEAR = 1, ORC_RECON_MINMOD = 2 };
+enum { ORC_TIME_EULER = 0, ORC_TIME_HEUN = 1, ORC_TIME_SSPRK3 = 2 };
+enum { ORC_BND_INLET = 1, ORC_BND_OUTLET = 2, ORC_BND_WALL_SLIP = 3, ORC_BND_WALL_NO_SLIP = 4 };
+
+typedef struct orc_mesh orc_mesh;
+typedef struct orc_solver orc_solver;
+
+typedef struct {
+    int flux, recon, scheme, steady;
+    int newton_cap;          /* Godunov Newton iteration cap; 0 = none (the reference has none) */
+    int pad;
+    double tau_xml, cfl;
+    double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
+    double gam_flux;         /* the reference hard-codes 1.4 in FVM_TVD::run */
+} orc_params;
+
+/* Edge structure by the Salome-UNV reader's rules (3 points per edge: midpoint +
+ * 2 Gauss points; normals flipped outward from c1), or by the Berkeley-Triangle
+ * reader's rules when berkeley != 0 (1 point per edge, neighbour j opposite node j
+ * taken from neigh[], no flip). bseg: nb node pairs, bseg_bnd: their boundary
+ * index. Returns 0 or a negative error. */
+int orc_mesh_build(int nn, const double* xy, int nc, const int* tri, const int* neigh_berkeley,
+                   int nb, const int* bseg, const int* bseg_bnd, int berkeley, orc_mesh** out);
+void orc_mesh_sizes(const orc_mesh* m, int* nc, int* ne);
+void orc_mesh_export(const orc_mesh* m, int* cell_edges, double* cell_S, double* cell_c,
+                     int* edge_n12, int* edge_c12, int* edge_bnd, int* edge_npts,
+                     double* edge_n, double* edge_l, double* edge_pts);
+void orc_mesh_free(orc_mesh* m);
+
+/* Region state the way FVM_TVD::init forms it: URS(2), URS(1), convertParToCons. */
+void orc_region_state(double M, double Cp, double u, double v, double T, double p, double* U4);
+
+/* mat: nm x (M, Cp); cell_mat[nc]; bnd_kind[nbnd]; bnd_par: nbnd x (Vx, Vy, T, P);
+ * U0: 4 x nc (rho | rho u | rho v | rho E). Computes TAU as FVM_TVD::init does. */
+int orc_solver_create(const orc_mesh* m, const orc_params* prm, int nm, const double* mat,
+                      const int* cell_mat, int nbnd, const int* bnd_kind, const double* bnd_par,
+                      const double* U0, orc_solver** out);
+double orc_tau(const orc_solver* s);
+/* Advance nsteps steps of FVM_TVD::run's loop body. Returns 0, or 1 if the
+ * Newton cap was hit at least once. */
+int orc_step(orc_solver* s, int nsteps);
+void orc_get_state(const orc_solver* s, double* U4, double* ctau, unsigned* flags);
+void orc_set_state(orc_solver* s, const double* U4);
+/* R = residual of the current state (one stage's right-hand side, the
+ * reference's ro_int..re_int after the edge loop), 4 x nc. */
+void orc_residual(orc_solver* s, double* R4);
+void orc_solver_free(orc_solver* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

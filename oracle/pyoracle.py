@@ -1,0 +1,249 @@
+"""ctypes binding of the C oracle and a runner for the reference's own FVM_TVD.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker. The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "libcfd2d_oracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "ref_fvm_tvd")
+
+FLUX = {"GODUNOV": 0, "LAX": 1, "ROE": 2, "HLLC": 3}
+RECON = {"NONE": 0, "LINEAR": 1, "MINMOD": 2}
+TIME = {"EULER": 0, "HEUN": 1, "SSPRK3": 2}
+BND = {"BOUND_INLET": 1, "BOUND_OUTLET": 2, "BOUND_WALL_SLIP": 3, "BOUND_WALL_NO_SLIP": 4}
+
+
+class Params(C.Structure):
+    _fields_ = [("flux", C.c_int), ("recon", C.c_int), ("scheme", C.c_int), ("steady", C.c_int),
+                ("newton_cap", C.c_int), ("pad", C.c_int),
+                ("tau_xml", C.c_double), ("cfl", C.c_double),
+                ("lim_rmin", C.c_double), ("lim_rmax", C.c_double), ("lim_pmin", C.c_double),
+                ("lim_pmax", C.c_double), ("lim_umax", C.c_double), ("gam_flux", C.c_double)]
+
+
+def build(quiet: bool = True) -> str:
+    """Compile the restatement (make -C oracle restatement)."""
+    r = subprocess.run(["make", "-C", HERE, "restatement"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P, I, D, U = C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint)
+        IP = C.POINTER(C.c_int)
+        L.orc_mesh_build.argtypes = [I, D, I, IP, IP, I, IP, IP, I, C.POINTER(P)]
+        L.orc_mesh_sizes.argtypes = [P, IP, IP]
+        L.orc_mesh_export.argtypes = [P, IP, D, D, IP, IP, IP, IP, D, D, D]
+        L.orc_mesh_free.argtypes = [P]
+        L.orc_region_state.argtypes = [C.c_double] * 6 + [D]
+        L.orc_solver_create.argtypes = [P, C.POINTER(Params), I, D, IP, I, IP, D, D, C.POINTER(P)]
+        L.orc_tau.argtypes = [P]; L.orc_tau.restype = C.c_double
+        L.orc_step.argtypes = [P, I]
+        L.orc_get_state.argtypes = [P, D, D, U]
+        L.orc_set_state.argtypes = [P, D]
+        L.orc_residual.argtypes = [P, D]
+        L.orc_solver_free.argtypes = [P]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class OracleMesh:
+    """Edge structure built by the reference's reader rules (see cfd2d_oracle.h)."""
+
+    def __init__(self, nodes, tris, bsegs, bseg_bnd, berkeley_neigh=None):
+        L = lib()
+        self.nodes = np.ascontiguousarray(nodes, np.float64)
+        self.tris = np.ascontiguousarray(tris, np.int32)
+        bs = np.ascontiguousarray(bsegs, np.int32)
+        bb = np.ascontiguousarray(bseg_bnd, np.int32)
+        nb = np.ascontiguousarray(berkeley_neigh, np.int32) if berkeley_neigh is not None else None
+        h = C.c_void_p()
+        rc = L.orc_mesh_build(len(self.nodes), _d(self.nodes), len(self.tris), _i(self.tris),
+                              _i(nb) if nb is not None else None, len(bs), _i(bs), _i(bb),
+                              1 if nb is not None else 0, C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"oracle mesh build failed ({rc})")
+        self.h = h
+        nc, ne = C.c_int(), C.c_int()
+        L.orc_mesh_sizes(h, C.byref(nc), C.byref(ne))
+        self.nc, self.ne = nc.value, ne.value
+
+    @classmethod
+    def from_mesh(cls, mesh):
+        return cls(mesh.nodes, mesh.tris, mesh.bsegs, mesh.bseg_bnd)
+
+    def export(self) -> dict:
+        nc, ne = self.nc, self.ne
+        out = dict(cell_edges=np.zeros((nc, 3), np.int32), cell_S=np.zeros(nc), cell_c=np.zeros((nc, 2)),
+                   edge_n12=np.zeros((ne, 2), np.int32), edge_c12=np.zeros((ne, 2), np.int32),
+                   edge_bnd=np.zeros(ne, np.int32), edge_npts=np.zeros(ne, np.int32),
+                   edge_n=np.zeros((ne, 2)), edge_l=np.zeros(ne), edge_pts=np.zeros((ne, 3, 2)))
+        lib().orc_mesh_export(self.h, _i(out["cell_edges"]), _d(out["cell_S"]), _d(out["cell_c"]),
+                              _i(out["edge_n12"]), _i(out["edge_c12"]), _i(out["edge_bnd"]),
+                              _i(out["edge_npts"]), _d(out["edge_n"]), _d(out["edge_l"]), _d(out["edge_pts"]))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_mesh_free(self.h)
+            self.h = None
+
+
+def region_state(M, Cp, u, v, T, p) -> np.ndarray:
+    out = np.zeros(4)
+    lib().orc_region_state(M, Cp, u, v, T, p, _d(out))
+    return out
+
+
+class OracleSolver:
+    def __init__(self, mesh: OracleMesh, *, flux="GODUNOV", recon="LINEAR", scheme="HEUN", steady=0,
+                 tau=1e8, cfl=0.5, limits=(1e-8, 1e8, 1e-8, 1e8, 1e8), gam_flux=1.4, newton_cap=1000,
+                 materials=((8.314472, 3.5),), cell_mat=None, bnd_kind=(), bnd_par=None, U0=None):
+        L = lib()
+        self.mesh = mesh
+        p = Params(FLUX[flux], RECON[recon], TIME[scheme], int(steady), int(newton_cap), 0,
+                   float(tau), float(cfl), *[float(x) for x in limits], float(gam_flux))
+        mat = np.ascontiguousarray(np.asarray(materials, np.float64).reshape(-1, 2))
+        cm = np.ascontiguousarray(np.zeros(mesh.nc, np.int32) if cell_mat is None else cell_mat, np.int32)
+        bk = np.ascontiguousarray([BND[k] if isinstance(k, str) else int(k) for k in bnd_kind], np.int32)
+        bp = np.ascontiguousarray(np.zeros((len(bk), 4)) if bnd_par is None else bnd_par, np.float64)
+        U = np.ascontiguousarray(U0, np.float64).reshape(4, mesh.nc)
+        h = C.c_void_p()
+        rc = L.orc_solver_create(mesh.h, C.byref(p), len(mat), _d(mat), _i(cm), len(bk),
+                                 _i(bk) if len(bk) else None, _d(bp), _d(U), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"oracle solver create failed ({rc})")
+        self.h = h
+
+    @property
+    def tau(self) -> float:
+        return lib().orc_tau(self.h)
+
+    def step(self, n: int) -> int:
+        return lib().orc_step(self.h, int(n))
+
+    def state(self):
+        nc = self.mesh.nc
+        U = np.zeros((4, nc)); ct = np.zeros(nc); fl = np.zeros(nc, np.uint32)
+        lib().orc_get_state(self.h, _d(U), _d(ct), fl.ctypes.data_as(C.POINTER(C.c_uint)))
+        return U, ct, fl
+
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, np.float64)
+        lib().orc_set_state(self.h, _d(U))
+
+    def residual(self) -> np.ndarray:
+        R = np.zeros((4, self.mesh.nc))
+        lib().orc_residual(self.h, _d(R))
+        return R
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_solver_free(self.h)
+            self.h = None
+
+
+# ------------------------------------------------------------- task helpers
+
+def solver_from_task(task, mesh, omesh: OracleMesh | None = None, U0=None, **over) -> OracleSolver:
+    """Oracle solver configured like FVM_TVD::init configures itself from ``task``."""
+    omesh = omesh or OracleMesh.from_mesh(mesh)
+    mats = [(m[1], m[2]) for m in task.materials]
+    cell_mat = np.asarray([task.regions[r].mat for r in range(len(task.regions))], np.int32)[mesh.cell_region]
+    if U0 is None:
+        reg_U = np.stack([region_state(*mats[r.mat], r.u, r.v, r.T, r.p) for r in task.regions])
+        U0 = reg_U[mesh.cell_region].T.copy()
+    bk = [b.kind for b in task.boundaries]
+    bp = np.asarray([[b.u, b.v, b.T, b.p] for b in task.boundaries], np.float64)
+    kw = dict(flux=task.flux or "GODUNOV", recon=task.reconstruction or "LINEAR",
+              scheme=task.time_scheme or "HEUN", steady=task.steady, tau=task.tau, cfl=task.cfl,
+              limits=task.limits, materials=mats, cell_mat=cell_mat, bnd_kind=bk, bnd_par=bp, U0=U0)
+    kw.update(over)
+    return OracleSolver(omesh, **kw)
+
+
+# ------------------------------------------------------------- reference runs
+
+def read_ref_grid(path) -> dict:
+    raw = open(path, "rb").read()
+    nc, ne, nn, _ = np.frombuffer(raw[:16], np.int32)
+    off = 16
+    out = {}
+
+    def take(name, dtype, count, shape):
+        nonlocal off
+        a = np.frombuffer(raw, dtype, count, off).reshape(shape).copy()
+        off += a.nbytes
+        out[name] = a
+    take("nodes", np.float64, nn * 2, (nn, 2))
+    take("cell_nodes", np.int32, nc * 3, (nc, 3))
+    take("cell_edges", np.int32, nc * 3, (nc, 3))
+    take("cell_S", np.float64, nc, (nc,))
+    take("cell_c", np.float64, nc * 2, (nc, 2))
+    take("edge_n12", np.int32, ne * 2, (ne, 2))
+    take("edge_c12", np.int32, ne * 2, (ne, 2))
+    take("edge_type", np.int32, ne, (ne,))
+    take("edge_bnd", np.int32, ne, (ne,))
+    take("edge_npts", np.int32, ne, (ne,))
+    take("edge_n", np.float64, ne * 2, (ne, 2))
+    take("edge_l", np.float64, ne, (ne,))
+    take("edge_pts", np.float64, ne * 6, (ne, 3, 2))
+    assert off == len(raw)
+    return out
+
+
+def read_ref_state(path) -> dict:
+    raw = open(path, "rb").read()
+    nc = int(np.frombuffer(raw[:4], np.int32)[0])
+    tau, secs = np.frombuffer(raw, np.float64, 2, 16)
+    off = 32
+    U = np.frombuffer(raw, np.float64, 4 * nc, off).reshape(4, nc).copy(); off += 32 * nc
+    ct = np.frombuffer(raw, np.float64, nc, off).copy(); off += 8 * nc
+    fl = np.frombuffer(raw, np.uint32, nc, off).copy()
+    return dict(U=U, tau=float(tau), seconds=float(secs), cTau=ct, flags=fl)
+
+
+def run_reference(task_xml: str, unv_text: str, U0=None, timeout=120, workdir=None) -> dict:
+    """Run the reference's own FVM_TVD (oracle/_ref/ref_fvm_tvd) on one case."""
+    if not os.path.exists(REF_BIN):
+        raise FileNotFoundError(REF_BIN + " (build with: make -C oracle reference)")
+    with tempfile.TemporaryDirectory(dir=workdir) as d:
+        open(os.path.join(d, "task.xml"), "w").write(task_xml)
+        open(os.path.join(d, "mesh.unv"), "w").write(unv_text)
+        args = [REF_BIN, "task.xml", "out"]
+        if U0 is not None:
+            np.ascontiguousarray(U0, np.float64).tofile(os.path.join(d, "init.bin"))
+            args.append("init.bin")
+        r = subprocess.run(args, cwd=d, capture_output=True, text=True, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError("reference run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+        return dict(grid=read_ref_grid(os.path.join(d, "out.grid.bin")),
+                    init=read_ref_state(os.path.join(d, "out.init.bin")),
+                    final=read_ref_state(os.path.join(d, "out.state.bin")),
+                    stdout=r.stdout)
