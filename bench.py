@@ -1,0 +1,390 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FVM_TVD path: cell-updates/s at 2,097,152 triangles.
+
+Workload: the four-quadrant Riemann problem on [0,1]^2, 1024 x 1024 x 2 jittered
+triangles (seed 2, +-0.05h), HLLC flux, minmod reconstruction, SSP-RK3, CFL 0.4,
+transmissive boundaries. One step = one SSP-RK3 time step (3 stages) of every
+triangle. The headline value is the FP64 drop-in; the mixed form (FP32 faces,
+FP64 accumulation/update) is measured in the same run.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+For N > 1 launch with torch.distributed.run: each rank runs its own replica of
+the workload on its GPU (the path does not shard here; "replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cfd-2d_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s at 2.1M tris, FP64 vs mixed, %HBM peak; adjoint/forward ratio"
+UNIT = "cell-updates/s"
+N_SIDE = 1024
+WORKLOAD = ("four-quadrant Riemann problem on [0,1]^2, 1024x1024x2 = 2,097,152 jittered triangles (seed 2, "
+            "+-0.05h), HLLC + minmod + SSP-RK3, CFL 0.4, BOUND_OUTLET all round, STEADY=0")
+# algorithmic HBM bytes per cell-update of an ideal fused step (each cell's data
+# read once per stage, gradients on chip): FP64 SSP-RK3 and mixed SSP-RK3
+STEP_BYTES = {"fp64": 580.0, "mixed": 436.0}
+KINDS = ("grad", "flux", "update", "remediate")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def kernel_bytes(kind: str, nc: int, ne: int, fb: int) -> float:
+    """Compulsory bytes of one launch of a kernel kind (fb: bytes of a face real).
+
+    grad:   cells W(4) in, G(8) out, faces 12 B, S 8 B; edges nx,ny,l(3) + c1,c2 8 B
+    flux:   cells W(4) + G(8) in; edges c1,c2 8 B, nx,ny,l(3), Gauss offsets(8) in, F(4) out
+    update: cells faces 12 B, A 32 B in, B 32 B in (stages 2-3), result 32 B out, cfl 8 B,
+            flags 4 B, W(4) out; edges F(4) in  (stage 2/3 average: 2/3 of the B read)
+    """
+    if kind == "grad":
+        return nc * (12 * fb + 12 + 8) + ne * (3 * fb + 8)
+    if kind == "flux":
+        return nc * 12 * fb + ne * (8 + 15 * fb)
+    if kind == "update":
+        return nc * (12 + 32 + 32 * 2 / 3 + 32 + 8 + 4 + 4 * fb) + ne * 4 * fb
+    return 0.0
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each kernel kind from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "ncu_dram_traffic.txt")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch"):
+                _, key, val = line.split()[:3]
+                out[key] = float(val)
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.active = False
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            if self.active:
+                self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(ngpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+        dist = td
+    return world, rank, local, dist
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ reference arm
+
+def _ref_worker(args):
+    """One host process: the oracle (restatement of the reference FVM_TVD) on the workload."""
+    n, warm, steps, q = args
+    sys.path.insert(0, PKG); sys.path.insert(0, ROOT)
+    from cfd2d import cases
+    from oracle import pyoracle
+    t, m, _ = cases.four_quadrant(n, steps=1)
+    o = pyoracle.solver_from_task(t, m, flux="HLLC", recon="MINMOD", scheme="SSPRK3")
+    o.step(warm)
+    q.put(("ready", m.n_cells))
+    a = time.perf_counter()
+    o.step(steps)
+    q.put(("done", time.perf_counter() - a))
+
+
+def reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle import pyoracle
+    pyoracle.build()
+    ctx = mp.get_context("spawn")
+    procs = max(1, (os.cpu_count() or 1))
+    procs = min(procs, int(os.environ.get("CFD2D_REF_PROCS", 16)))
+    # bounded sample: the CPU step costs seconds, so time at most 3 steps per process
+    steps = max(1, min(args.steps, 3))
+    warm = 0 if args.warmup <= 0 else 1
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_ref_worker, args=((N_SIDE, warm, steps, q),)) for _ in range(procs)]
+    for p in ps:
+        p.start()
+    cells, times = 0, []
+    for _ in range(2 * procs):
+        kind, v = q.get()
+        if kind == "ready":
+            cells = v
+        else:
+            times.append(v)
+    for p in ps:
+        p.join()
+    T = max(times)
+    value = procs * cells * steps / T
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": steps, "warmup": warm, "ms_per_step": T / steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": cells, "parallelism": f"{procs} host processes, one "
+                       "independent instance each"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                             "sample": f"{steps} SSP-RK3 step(s) of the full 2,097,152-triangle workload per "
+                                       f"process, {procs} processes (the reference cannot run HLLC/minmod/SSP-RK3; "
+                                       "the oracle restates it and equals it bit for bit in its own mode)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ our arm
+
+def cpu_baseline_single(seconds: float = 12.0):
+    """The oracle on one host core on the same workload, for ~seconds of CPU work."""
+    from cfd2d import cases
+    from oracle import pyoracle
+    pyoracle.build()
+    t, m, _ = cases.four_quadrant(N_SIDE, steps=1)
+    o = pyoracle.solver_from_task(t, m, flux="HLLC", recon="MINMOD", scheme="SSPRK3")
+    a = time.perf_counter()
+    k = 0
+    while True:
+        o.step(1)
+        k += 1
+        if time.perf_counter() - a >= seconds or k >= 10:
+            break
+    dt = time.perf_counter() - a
+    return {"value": m.n_cells * k / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{k} SSP-RK3 step(s) of the full 2,097,152-triangle workload on one core"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", default="fp64,mixed", help="comma list of fp64, mixed (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--n", type=int, default=N_SIDE, help="squares per side (profiling runs only)")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup(args.gpus)
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+    W = max(3, args.warmup)
+    K = max(1, args.steps)
+
+    from cfd2d import capi, cases
+    capi.set_verbosity(0)
+    capi.set_device(local)
+    import torch
+
+    d = tempfile.mkdtemp(prefix="cfd2d_bench_")
+    forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    full = forms == ["fp64", "mixed"] and args.n == N_SIDE and not args.no_e2e and not args.no_profile
+    t, m, _ = cases.four_quadrant(args.n, steps=K)
+    solvers = {}
+    for f in forms:
+        t.precision = "MIXED" if f == "mixed" else None
+        solvers[f] = capi.Solver(cases.write_task(t, m, d), mesh=m)
+    nc, ne = m.n_cells, solvers[forms[0]].info.n_edges
+    for s in solvers.values():
+        s.step(W)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.5)
+
+    def timed(solver):
+        barrier(dist)
+        torch.cuda.synchronize()
+        sampler.active = True
+        ms = solver.timed_steps(K)
+        sampler.active = False
+        torch.cuda.synchronize()
+        barrier(dist)
+        return reduce_max(dist, ms)
+
+    ms_of = {f: timed(solvers[f]) for f in forms}
+    sampler.stop()
+    clocks = sampler.summary()
+    if not full:
+        if rank == 0:
+            print(json.dumps({"profiling_run": True, "forms": forms, "cells": nc, "steps": K, "warmup": W,
+                              "ms_per_step": {f: ms_of[f] / K for f in forms}}), flush=True)
+        return
+    s64, smx = solvers["fp64"], solvers["mixed"]
+    ms64, msmx = ms_of["fp64"], ms_of["mixed"]
+    # accuracy of the mixed form against the FP64 drop-in after the same W+K steps
+    U64, Umx = s64.state(), smx.state()
+    l1 = lambda a, b: float(np.sum(np.abs(a - b)) / np.sum(np.abs(b)))
+    linf = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    err = {"l1_rho": l1(Umx[0], U64[0]), "l1_rhoE": l1(Umx[3], U64[3]),
+           "linf_rho": linf(Umx[0], U64[0]), "linf_rhoE": linf(Umx[3], U64[3]), "steps": W + K}
+
+    # per-kernel device times (kernel-by-kernel launches with events, outside the timed region)
+    prof = {}
+    for name, s in (("fp64", s64), ("mixed", smx)):
+        ms, cnt = s.profile_steps(3)
+        prof[name] = {k: {"ms_per_launch": float(ms[i] / max(cnt[i], 1)), "launches": int(cnt[i]),
+                          "share": float(ms[i] / max(ms.sum(), 1e-30))} for i, k in enumerate(KINDS)}
+
+    # end to end through the C ABI: H2D of the step's input state from pinned memory,
+    # one step, D2H of the result into pinned memory, every step
+    Ke = min(K, 20)
+    pin_in = torch.empty((4, nc), dtype=torch.float64).pin_memory()
+    pin_out = torch.empty((4, nc), dtype=torch.float64).pin_memory()
+    pin_in.copy_(torch.from_numpy(s64.state()))
+    ptr_in = [pin_in[k].data_ptr() for k in range(4)]
+    ptr_out = [pin_out[k].data_ptr() for k in range(4)]
+    barrier(dist)
+    a = time.perf_counter()
+    for _ in range(Ke):
+        s64.set_state_from(ptr_in)
+        s64.step(1)
+        s64.state_into(ptr_out)
+    e2e_s = reduce_max(dist, (time.perf_counter() - a) / Ke)
+
+    hbm, peak_kind = measured_peaks()
+    traffic = ncu_traffic()
+    # dominant kernel of the FP64 drop-in
+    dom = max(KINDS, key=lambda k: prof["fp64"][k]["ms_per_launch"] * prof["fp64"][k]["launches"])
+    dom_bytes = kernel_bytes(dom, nc, ne, 8)
+    dom_ms = prof["fp64"][dom]["ms_per_launch"]
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    value = world * nc * K / (ms64 * 1e-3)
+    value_mx = world * nc * K / (msmx * 1e-3)
+    step_gbs = nc / (ms64 / K * 1e-3) * STEP_BYTES["fp64"] / 1e9
+    step_gbs_mx = nc / (msmx / K * 1e-3) * STEP_BYTES["mixed"] / 1e9
+    mx_dom = max(KINDS, key=lambda k: prof["mixed"][k]["ms_per_launch"] * prof["mixed"][k]["launches"])
+    mx_bytes = kernel_bytes(mx_dom, nc, ne, 4)
+    mx_ach = mx_bytes / (prof["mixed"][mx_dom]["ms_per_launch"] * 1e-3) / 1e9
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms64 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": nc, "edges": ne, "form": "FP64 drop-in (headline); mixed below",
+                   "l2": "no flush: the step's working set (~0.9 GB FP64, ~0.6 GB mixed) exceeds the 129 MB L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": f"k_flux" if dom == "flux" else f"k_{dom}",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic.get(f"{dom}_fp64"), "algorithmic_bytes_per_launch": dom_bytes,
+                     "peak_kind": peak_kind,
+                     "note": "FP64 kernels are bound by GB300's FP64 issue rate, not HBM"},
+        "roofline_step": {"fp64": {"achieved": step_gbs, "frac": step_gbs / hbm, "bytes_per_cell_update": 580},
+                          "mixed": {"achieved": step_gbs_mx, "frac": step_gbs_mx / hbm, "bytes_per_cell_update": 436,
+                                    "dominant_kernel": f"k_{mx_dom}", "dominant_achieved": mx_ach,
+                                    "dominant_frac": mx_ach / hbm,
+                                    "dominant_traffic": traffic.get(f"{mx_dom}_mixed")},
+                          "peak": hbm, "unit": "GB/s", "peak_kind": peak_kind},
+        "mixed": {"value": value_mx, "unit": UNIT, "ms_per_step": msmx / K, "speedup_vs_fp64": ms64 / msmx,
+                  "dtype": "f32 faces / f64 accumulate", "error_vs_fp64": err},
+        "adjoint_forward_ratio": None,
+        "kernels": prof,
+        "e2e": {"value": world * nc / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 32 * nc,
+                "d2h_bytes_per_step": 32 * nc,
+                "path": "cfd2d_set_state (pinned H2D) + cfd2d_step(1) + cfd2d_get_state (pinned D2H), FP64",
+                "steps": Ke},
+        "gpu_launches": K * (3 * 3 + 1),
+        "clocks": clocks,
+    }
+    if world == 1 and rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_single()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s64.close()
+    smx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

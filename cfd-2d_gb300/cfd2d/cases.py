@@ -1,0 +1,68 @@
+"""Seeded synthetic workloads (the configurations the solver is measured on).
+
+Each builder returns (task, mesh, U0): a task description, the mesh arrays
+and the per-cell initial conserved state (None = the task's regions).
+"""
+from __future__ import annotations
+
+import math
+import os
+import tempfile
+
+import numpy as np
+
+from . import meshgen as mg
+
+GAMMA = 1.4
+FREE = (1.0, 1.0, 0.0, 1.0)  # rho, u, v, p of the vortex free stream
+
+
+def vortex(n: int, *, beta=5.0, mach=None, seed=1, jitter=0.1, flux="LAX", recon="NONE", scheme="EULER",
+           cfl=0.5, steps=200, steady=0, precision=None, bnd_kinds=None):
+    """Isentropic vortex on [0,10]^2 (n x n x 2 triangles), free stream rho=p=1.
+
+    mach=None gives u=1 (the 20,000-triangle plain case); otherwise u = mach*sqrt(gamma).
+    Far field: BOUND_INLET with the free stream on all sides (or the kinds given per side).
+    """
+    m = mg.jittered_square(n, 0.0, 10.0, 0.0, 10.0, jitter, seed)
+    u_inf = 1.0 if mach is None else mach * math.sqrt(GAMMA)
+    kinds = bnd_kinds or ("BOUND_INLET",) * 4
+    bnds = [mg.Boundary(f"side{k}", kind, k + 1, u_inf, 0.0, 1.0, 1.0) for k, kind in enumerate(kinds)]
+    m.bseg_bnd = m.bseg_side.copy()
+    t = mg.Task(regions=[mg.Region("fluid", u_inf, 0.0, 1.0, 1.0)], boundaries=bnds, steady=steady, cfl=cfl,
+                step_max=steps, flux=flux, reconstruction=recon, time_scheme=scheme, precision=precision)
+    U0 = mg.isentropic_vortex(m.centroids(), beta, 5.0, 5.0, u_inf=u_inf)
+    return t, m, U0
+
+
+def four_quadrant(n: int, *, seed=2, jitter=0.05, flux="HLLC", recon="MINMOD", scheme="SSPRK3", cfl=0.4,
+                  steps=1000, precision=None, steady=0):
+    """Four-quadrant Riemann problem on [0,1]^2 (n x n x 2 triangles), outlets all round.
+
+    Quadrant states (rho, u, v, p): NE (1.5, 0, 0, 1.5), NW (0.5323, 1.206, 0, 0.3),
+    SW (0.138, 1.206, 1.206, 0.029), SE (0.5323, 0, 1.206, 0.3); a cell's quadrant
+    is the one holding its centroid. Four XML regions, so the reference's own
+    region initialisation sets the state.
+    """
+    m = mg.jittered_square(n, 0.0, 1.0, 0.0, 1.0, jitter, seed)
+    m.cell_region = mg.quadrant_regions(m.centroids())
+    regs = []
+    for q in mg.QUADRANT_ORDER:
+        r, u, v, p = mg.FOUR_QUADRANT[q]
+        regs.append(mg.Region(q, u, v, p / r, p))  # T = p / rho with gR/M = 1
+    t = mg.Task(regions=regs, boundaries=[mg.Boundary("outlet", "BOUND_OUTLET", 1)], steady=steady, cfl=cfl,
+                step_max=steps, flux=flux, reconstruction=recon, time_scheme=scheme, precision=precision)
+    m.bseg_bnd = np.zeros(len(m.bsegs), np.int32)
+    return t, m, None
+
+
+def write_task(task, mesh, directory=None, with_unv=False) -> str:
+    """task.xml (and optionally mesh.unv) in a directory; returns the task path."""
+    d = directory or tempfile.mkdtemp(prefix="cfd2d_")
+    if with_unv:
+        with open(os.path.join(d, "mesh.unv"), "w") as f:
+            f.write(mg.write_unv(mesh, [r.name for r in task.regions], [b.name for b in task.boundaries]))
+    path = os.path.join(d, "task.xml")
+    with open(path, "w") as f:
+        f.write(mg.write_task_xml(task))
+    return path

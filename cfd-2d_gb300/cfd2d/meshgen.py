@@ -179,6 +179,42 @@ def write_unv(mesh: Mesh, region_names, bnd_names) -> str:
     return out.getvalue()
 
 
+def triangle_neighbours(tris: np.ndarray) -> np.ndarray:
+    """Berkeley-Triangle .neigh convention: neighbour j is across the edge opposite node j; -1 if none."""
+    nc = len(tris)
+    a = np.concatenate([tris[:, 1], tris[:, 2], tris[:, 0]])
+    b = np.concatenate([tris[:, 2], tris[:, 0], tris[:, 1]])
+    cell = np.tile(np.arange(nc), 3)
+    slot = np.repeat(np.arange(3), nc)
+    key = np.minimum(a, b).astype(np.int64) * (1 << 32) + np.maximum(a, b)
+    order = np.argsort(key, kind="stable")
+    ks = key[order]
+    nb = -np.ones((nc, 3), np.int64)
+    same = np.nonzero(ks[1:] == ks[:-1])[0]
+    i0, i1 = order[same], order[same + 1]
+    nb[cell[i0], slot[i0]] = cell[i1]
+    nb[cell[i1], slot[i1]] = cell[i0]
+    return nb.astype(np.int32)
+
+
+def write_triangle(mesh: Mesh, bnd_markers) -> dict:
+    """Berkeley-Triangle files (.node .ele .neigh .poly), 1-based, as the reference reads them
+    (src/mesh/MeshReaderBerkleyTriangle.cpp:3-170). The .ele attribute is the region index,
+    which becomes the cell's region name ("0", "1", ...); the .poly marker of a boundary
+    segment is ``bnd_markers[bseg_bnd]`` and binds to a boundCond by its edgeType."""
+    nn, nc = len(mesh.nodes), len(mesh.tris)
+    node = [f"{nn} 2 0 1"] + [f"{i + 1} {repr(float(x))} {repr(float(y))} 0" for i, (x, y) in enumerate(mesh.nodes)]
+    ele = [f"{nc} 3 1"] + [f"{i + 1} {a + 1} {b + 1} {c + 1} {int(r)}"
+                           for i, ((a, b, c), r) in enumerate(zip(mesh.tris, mesh.cell_region))]
+    nb = triangle_neighbours(mesh.tris)
+    neigh = [f"{nc} 3"] + [f"{i + 1} {x + 1 if x >= 0 else -1} {y + 1 if y >= 0 else -1} {z + 1 if z >= 0 else -1}"
+                           for i, (x, y, z) in enumerate(nb)]
+    poly = ["0 2 0 1", f"{len(mesh.bsegs)} 1"] + [f"{k + 1} {a + 1} {b + 1} {int(bnd_markers[int(s)])}"
+                                                for k, ((a, b), s) in enumerate(zip(mesh.bsegs, mesh.bseg_bnd))]
+    return {ext: "\n".join(lines) + "\n" for ext, lines in
+            ((".node", node), (".ele", ele), (".neigh", neigh), (".poly", poly))}
+
+
 # ---------------------------------------------------------------- task.xml
 
 @dataclass

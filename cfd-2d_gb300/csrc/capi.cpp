@@ -1,0 +1,375 @@
+// extern "C" entry points (include/cfd2d.h). Every call catches everything and
+// returns a status code; the message of the last failure is kept per thread.
+#include <sys/stat.h>
+
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "cfd2d.h"
+#include "mesh.hpp"
+#include "solver.hpp"
+#include "task.hpp"
+
+struct cfd2d_solver {
+    std::unique_ptr<cfd2d::Solver> s;
+};
+
+struct cfd2d_mesh {
+    cfd2d::Topo topo;
+    std::vector<int> edge_bnd;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        g_err.clear();
+        return f();
+    } catch (const cfd2d::Error& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(CFD2D_ERR_CAPACITY, "host memory exhausted");
+    } catch (const std::exception& e) {
+        return fail(CFD2D_ERR_INVALID_ARG, e.what());
+    } catch (...) {
+        return fail(CFD2D_ERR_INVALID_ARG, "unknown error");
+    }
+}
+
+bool file_exists(const std::string& p) {
+    struct stat st;
+    return ::stat(p.c_str(), &st) == 0;
+}
+
+std::string resolve(const cfd2d::TaskConfig& t, const std::string& name, const char* probe_ext) {
+    if (name.empty() || name[0] == '/') return name;
+    if (file_exists(name + probe_ext)) return name;
+    std::string alt = t.dir + "/" + name;
+    if (file_exists(alt + probe_ext)) return alt;
+    return name;
+}
+
+// Read the task's mesh and bind it (MeshReader::create + the binding in FVM_TVD::init).
+void load_task_mesh(const cfd2d::TaskConfig& t, cfd2d::Topo& topo, std::vector<int>& cell_region,
+                    std::vector<int>& edge_bnd, int& gauss_points) {
+    cfd2d::RawMesh raw;
+    if (t.mesh_type == "salome_unv") {
+        raw = cfd2d::read_unv(resolve(t, t.mesh_name, ""));
+        gauss_points = 2;
+    } else {
+        raw = cfd2d::read_triangle(resolve(t, t.mesh_name, ".node"));
+        // the reference's Triangle reader gives every edge one point, so its
+        // Gauss-point loop never runs (src/mesh/MeshReaderBerkleyTriangle.cpp:102)
+        gauss_points = t.gauss_points == 2 ? 2 : 0;
+        if (gauss_points == 0)
+            cfd2d::log_line("WARNING: berkeley_triangle mesh: edges carry one point as in the reference, "
+                            "so no flux is computed; set <mesh><gaussPoints value=\"2\"/> for two Gauss points\n");
+    }
+    topo = cfd2d::build_topology(raw.nn(), raw.xy.data(), raw.nc(), raw.tri.data(),
+                                 raw.berkeley ? raw.neigh.data() : nullptr, (int)raw.bseg.size() / 2,
+                                 raw.bseg.data(), !raw.berkeley, gauss_points);
+    cfd2d::bind_mesh(t, raw, topo, cell_region, edge_bnd);
+}
+
+void check_desc(const cfd2d_mesh_desc* m) {
+    if (!m || m->n_nodes <= 0 || m->n_cells <= 0 || !m->xy || !m->tri || m->n_bsegs < 0 ||
+        (m->n_bsegs > 0 && (!m->bseg || !m->bseg_bnd)))
+        throw cfd2d::Error(CFD2D_ERR_INVALID_ARG, "mesh description is incomplete");
+}
+
+cfd2d::Topo topo_from_desc(const cfd2d_mesh_desc* m, const int* berkeley_neigh, int gauss_points) {
+    return cfd2d::build_topology(m->n_nodes, m->xy, m->n_cells, m->tri, berkeley_neigh, m->n_bsegs, m->bseg,
+                                 berkeley_neigh == nullptr, gauss_points);
+}
+
+std::vector<int> edge_bnd_from_desc(const cfd2d_mesh_desc* m, const cfd2d::Topo& t, int nbnd) {
+    std::vector<int> eb(t.ne, -1);
+    for (int e = 0; e < t.ne; e++) {
+        if (t.c2[e] >= 0) continue;
+        int s = t.bseg_of_edge[e];
+        int b = s >= 0 ? m->bseg_bnd[s] : -1;
+        if (b < 0 || (nbnd >= 0 && b >= nbnd))
+            throw cfd2d::Error(CFD2D_ERR_EDGE_UNKNOWN,
+                               "ERROR (boundary condition): unknown edge type of edge " + std::to_string(e) + "...");
+        eb[e] = b;
+    }
+    return eb;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cfd2d_create(const char* task_xml_path, cfd2d_t** out) {
+    return guarded([&] {
+        if (!task_xml_path || !out) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        *out = nullptr;
+        cfd2d::TaskConfig t = cfd2d::parse_task(task_xml_path);
+        cfd2d::Topo topo;
+        std::vector<int> cr, eb;
+        int gp = 2;
+        load_task_mesh(t, topo, cr, eb, gp);
+        auto h = std::make_unique<cfd2d_solver>();
+        h->s = std::make_unique<cfd2d::Solver>(t, std::move(topo), cr, eb, gp);
+        *out = h.release();
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_create_with_mesh(const char* task_xml_path, const cfd2d_mesh_desc* mesh, cfd2d_t** out) {
+    return guarded([&] {
+        if (!task_xml_path || !out) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        *out = nullptr;
+        check_desc(mesh);
+        if (!mesh->cell_region) return fail(CFD2D_ERR_INVALID_ARG, "cell_region is required");
+        cfd2d::TaskConfig t = cfd2d::parse_task(task_xml_path);
+        cfd2d::Topo topo = topo_from_desc(mesh, nullptr, 2);
+        std::vector<int> cr(mesh->cell_region, mesh->cell_region + mesh->n_cells);
+        for (int r : cr)
+            if (r < 0 || r >= (int)t.regions.size())
+                return fail(CFD2D_ERR_REGION_UNKNOWN, "cell_region refers to a missing region");
+        std::vector<int> eb = edge_bnd_from_desc(mesh, topo, (int)t.bnds.size());
+        auto h = std::make_unique<cfd2d_solver>();
+        h->s = std::make_unique<cfd2d::Solver>(t, std::move(topo), cr, eb, 2);
+        *out = h.release();
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_step(cfd2d_t* h, int nsteps) {
+    return guarded([&] {
+        if (!h || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
+        int s = h->s->step(nsteps);
+        if (s != CFD2D_OK) g_err = s == CFD2D_ERR_NEWTON_CAP ? "exact Riemann solver hit its iteration cap"
+                                                            : "non-positive or NaN density/pressure";
+        return s;
+    });
+}
+
+int cfd2d_run(cfd2d_t* h) {
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        return h->s->run();
+    });
+}
+
+int cfd2d_destroy(cfd2d_t* h) {
+    return guarded([&] {
+        delete h;
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_get_info(const cfd2d_t* h, cfd2d_info_t* info) {
+    return guarded([&] {
+        if (!h || !info) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        const cfd2d::Solver& s = *h->s;
+        std::memset(info, 0, sizeof *info);
+        info->n_cells = s.topo().nc;
+        info->n_edges = s.topo().ne;
+        info->n_boundary_edges = s.layout().ne - s.layout().n_int;
+        info->n_nodes = s.topo().nn;
+        info->step = s.n_steps();
+        info->flux = s.task().flux;
+        info->recon = s.task().recon;
+        info->scheme = s.task().scheme;
+        info->precision = s.task().precision;
+        info->steady = s.task().steady;
+        info->time = s.time();
+        info->tau = s.tau();
+        info->device_bytes = s.device_bytes();
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_get_state(cfd2d_t* h, double* ro, double* ru, double* rv, double* re) {
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        h->s->get_state(ro, ru, rv, re);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_set_state(cfd2d_t* h, const double* ro, const double* ru, const double* rv, const double* re,
+                    int reset_time_step) {
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        h->s->set_state(ro, ru, rv, re, reset_time_step != 0);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_get_time_step(cfd2d_t* h, double* ctau) {
+    return guarded([&] {
+        if (!h || !ctau) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->get_ctau(ctau);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_get_flags(cfd2d_t* h, unsigned* flags) {
+    return guarded([&] {
+        if (!h || !flags) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->get_flags(flags);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_residual(cfd2d_t* h, double* R) {
+    return guarded([&] {
+        if (!h || !R) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->residual(R);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_conservation(cfd2d_t* h, double sums[4]) {
+    return guarded([&] {
+        if (!h || !sums) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->conservation(sums);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_save_vtk(cfd2d_t* h, int step) {
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        h->s->save_vtk(step);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms) {
+    return guarded([&] {
+        if (!h || !device_ms || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
+        *device_ms = h->s->timed_steps(nsteps);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_launches[4]) {
+    return guarded([&] {
+        if (!h || !kernel_ms || !kernel_launches || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
+        h->s->profile_steps(nsteps, kernel_ms, kernel_launches);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_set_device(int device) {
+    return guarded([&] {
+        cudaError_t e = cudaSetDevice(device);
+        if (e != cudaSuccess) return fail(e == cudaErrorNoDevice ? CFD2D_ERR_NO_DEVICE : CFD2D_ERR_CUDA,
+                                          std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_last_error(char* buf, size_t n) {
+    if (!buf || n == 0) return CFD2D_ERR_INVALID_ARG;
+    std::strncpy(buf, g_err.c_str(), n - 1);
+    buf[n - 1] = 0;
+    return CFD2D_OK;
+}
+
+int cfd2d_set_verbosity(int level) {
+    cfd2d::set_verbosity(level);
+    return CFD2D_OK;
+}
+
+int cfd2d_set_log_file(const char* path) {
+    return guarded([&] {
+        cfd2d::set_log_file(path);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_mesh_load(const char* task_xml_path, cfd2d_mesh_t** out) {
+    return guarded([&] {
+        if (!task_xml_path || !out) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        *out = nullptr;
+        cfd2d::TaskConfig t = cfd2d::parse_task(task_xml_path);
+        auto m = std::make_unique<cfd2d_mesh>();
+        std::vector<int> cr;
+        int gp = 2;
+        load_task_mesh(t, m->topo, cr, m->edge_bnd, gp);
+        *out = m.release();
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_mesh_build(const cfd2d_mesh_desc* mesh, const int* berkeley_neigh, cfd2d_mesh_t** out) {
+    return guarded([&] {
+        if (!out) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        *out = nullptr;
+        check_desc(mesh);
+        auto m = std::make_unique<cfd2d_mesh>();
+        m->topo = topo_from_desc(mesh, berkeley_neigh, berkeley_neigh ? 0 : 2);
+        m->edge_bnd.assign(m->topo.ne, -1);
+        for (int e = 0; e < m->topo.ne; e++) {
+            int s = m->topo.bseg_of_edge[e];
+            if (m->topo.c2[e] < 0 && s >= 0) m->edge_bnd[e] = mesh->bseg_bnd[s];
+        }
+        *out = m.release();
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_mesh_sizes(const cfd2d_mesh_t* m, int* n_cells, int* n_edges) {
+    if (!m) return fail(CFD2D_ERR_INVALID_ARG, "null mesh");
+    if (n_cells) *n_cells = m->topo.nc;
+    if (n_edges) *n_edges = m->topo.ne;
+    return CFD2D_OK;
+}
+
+int cfd2d_mesh_export(const cfd2d_mesh_t* m, int* cell_edges, double* cell_S, double* cell_c, int* edge_n12,
+                      int* edge_c12, int* edge_bnd, int* edge_npts, double* edge_n, double* edge_l,
+                      double* edge_pts) {
+    return guarded([&] {
+        if (!m) return fail(CFD2D_ERR_INVALID_ARG, "null mesh");
+        const cfd2d::Topo& t = m->topo;
+        for (int i = 0; i < t.nc; i++) {
+            for (int k = 0; k < 3; k++)
+                if (cell_edges) cell_edges[3 * i + k] = t.cedges[3 * i + k];
+            if (cell_S) cell_S[i] = t.S[i];
+            if (cell_c) { cell_c[2 * i] = t.cx[i]; cell_c[2 * i + 1] = t.cy[i]; }
+        }
+        for (int e = 0; e < t.ne; e++) {
+            if (edge_n12) { edge_n12[2 * e] = t.n1[e]; edge_n12[2 * e + 1] = t.n2[e]; }
+            if (edge_c12) { edge_c12[2 * e] = t.c1[e]; edge_c12[2 * e + 1] = t.c2[e]; }
+            if (edge_bnd) edge_bnd[e] = m->edge_bnd[e];
+            if (edge_npts) edge_npts[e] = t.npts[e];
+            if (edge_n) { edge_n[2 * e] = t.nx[e]; edge_n[2 * e + 1] = t.ny[e]; }
+            if (edge_l) edge_l[e] = t.l[e];
+            if (edge_pts)
+                for (int k = 0; k < 6; k++) edge_pts[6 * e + k] = t.pts[6 * (size_t)e + k];
+        }
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_mesh_order(const cfd2d_mesh_t* m, int rcm, int* perm) {
+    return guarded([&] {
+        if (!m || !perm) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        std::vector<int> p;
+        if (rcm) p = cfd2d::rcm_order(m->topo);
+        else for (int i = 0; i < m->topo.nc; i++) p.push_back(i);
+        std::copy(p.begin(), p.end(), perm);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_mesh_free(cfd2d_mesh_t* m) {
+    delete m;
+    return CFD2D_OK;
+}
+
+}  // extern "C"

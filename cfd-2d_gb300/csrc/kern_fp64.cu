@@ -1,0 +1,5 @@
+// FP64 face precision: the drop-in. Built with -fmad=false so that, as in the
+// reference, no product is fused into a following sum.
+#define KT double
+#define KFN(name) launch_##name##_fp64
+#include "kern_inst.cuh"

@@ -1,0 +1,109 @@
+// Device data layout and kernel launchers of the GB300 FVM_TVD path.
+//
+// Layout in HBM (all structure-of-arrays, cells and edges in the locality order
+// chosen on the host; "original" numbers are the reference's cell and edge
+// numbers, src/mesh/MeshReaderSalomeUnv.cpp:118-217):
+//   cells (nc):  conserved state A[4][nc] and stage state B[4][nc] (FP64),
+//                primitives W[4][nc] (r, u, v, p) and Green-Gauss gradients
+//                G[8][nc] in the face precision, cfl[nc] = cTau/S, cTau[nc],
+//                flags[nc], faces face[3][nc] = (edge << 1) | side ordered by
+//                ascending original edge number, S[nc], rem_nb[3][nc].
+//   edges (ne):  c1/c2[ne] (c2 = -1 for boundary edges, which are stored last),
+//                nx, ny, l[ne], Gauss-point offsets dl[8][ne] from each side's
+//                centroid (gp0: dxL dyL dxR dyR, gp1: ...), edge flux F[4][ne]
+//                (already multiplied by l/2), boundary index bnd[ne].
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cfd2d {
+
+enum FluxKind { FLUX_GODUNOV = 0, FLUX_LAX = 1, FLUX_ROE = 2, FLUX_HLLC = 3 };
+enum ReconKind { RECON_NONE = 0, RECON_LINEAR = 1, RECON_MINMOD = 2 };
+enum SchemeKind { TIME_EULER = 0, TIME_HEUN = 1, TIME_SSPRK3 = 2 };
+enum PrecisionKind { PREC_FP64 = 0, PREC_MIXED = 1 };
+enum BndKind { BND_INLET = 1, BND_OUTLET = 2, BND_WALL_SLIP = 3, BND_WALL_NO_SLIP = 4 };
+
+// error word bits (device -> host)
+enum : unsigned { ERRBIT_NEWTON_CAP = 1u, ERRBIT_NONPHYSICAL = 2u };
+
+constexpr double GAS_R = 8.314472;  // Material::gR, src/global.cpp:6
+
+struct DevMat {     // Material (src/global.h:208-222) with its derived constants
+    double M, Cp, Cv, gam, gm1;
+};
+
+struct DevBnd {     // one <boundCond>: kind and (Vx, Vy, T, P)
+    int kind, pad;
+    double u, v, T, p;
+};
+
+// Everything a kernel needs; passed by value.
+struct DevCase {
+    int nc, ne, n_int;
+    // geometry
+    const int* face;       // 3*nc
+    const int* ec1;        // ne
+    const int* ec2;        // ne
+    const int* ebnd;       // ne (boundary index, -1 inside)
+    const double* nx;      // ne
+    const double* ny;
+    const double* l;
+    const double* dl;      // 8*ne
+    const float* nx32;
+    const float* ny32;
+    const float* l32;
+    const float* dl32;
+    const double* S;       // nc
+    const int* rem_nb;     // 3*nc
+    const int* iperm;      // original cell -> storage cell
+    const uint8_t* cmat;   // nc, nullptr when one material
+    // tables
+    const DevMat* mats;
+    const DevBnd* bnds;
+    DevMat mat0;
+    double gam_flux;
+    double cfl_number;
+    double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
+    int steady;
+    int newton_cap;
+    // state
+    double* A;             // 4*nc conserved state U^n (and result)
+    double* B;             // 4*nc stage state
+    double* cfl;           // nc   cTau/S of the step about to run
+    double* ctau;          // nc   cTau of the last step (the reference's cTau array)
+    double* ctau_next;     // nc   cTau of the next step (local time step)
+    unsigned* flags;       // nc
+    int* n_lim;            // 1
+    unsigned* err;         // 1
+    double* W64;           // 4*nc
+    double* G64;           // 8*nc
+    double* F64;           // 4*ne
+    float* W32;
+    float* G32;
+    float* F32;
+};
+
+// ---- launchers (kern_fp64.cu / kern_mixed.cu / kern_common.cu)
+void launch_grad(const DevCase& c, int precision, cudaStream_t s);
+void launch_flux(const DevCase& c, int precision, int flux, int recon, cudaStream_t s);
+// stage update; reads A (and B for later stages), writes B or A and the next primitives
+void launch_update(const DevCase& c, int precision, int scheme, int stage, cudaStream_t s);
+void launch_remediate(const DevCase& c, int precision, cudaStream_t s);
+// primitives (+ local time step when steady) from A, for every cell
+void launch_prims(const DevCase& c, int precision, cudaStream_t s);
+// min over cells of CFL*S/max(|u|+c,|v|+c) into *out (as ordered bits of a positive double)
+void launch_dt_min(const DevCase& c, unsigned long long* out, cudaStream_t s);
+// cfl[i] = tau / S[i]
+void launch_fill_cfl(const DevCase& c, double tau, cudaStream_t s);
+// state permutation between caller order (original cells) and storage order
+void launch_gather_state(const DevCase& c, const double* src_orig, double* dst_store, cudaStream_t s);
+void launch_scatter_state(const DevCase& c, const double* src_store, double* dst_orig, cudaStream_t s);
+void launch_permute_scalar(const DevCase& c, const double* src_store, double* dst_orig, cudaStream_t s);
+void launch_permute_flags(const DevCase& c, const unsigned* src_store, unsigned* dst_orig, cudaStream_t s);
+// residual of one stage (the reference's ro_int..re_int) in storage order
+void launch_residual(const DevCase& c, int precision, double* R, cudaStream_t s);
+// deterministic FP64 sums of S*U over cells (mass, x/y momentum, energy)
+void launch_conservation(const DevCase& c, double* partial, int nblocks, cudaStream_t s);
+
+}  // namespace cfd2d

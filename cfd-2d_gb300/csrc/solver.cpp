@@ -1,0 +1,498 @@
+#include "solver.hpp"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "cfd2d.h"
+
+namespace cfd2d {
+
+// ------------------------------------------------------------------ logging
+
+namespace {
+std::mutex g_log_mu;
+int g_verbosity = 1;
+FILE* g_log_file = nullptr;
+constexpr int kConservationBlocks = 512;
+}  // namespace
+
+void log_line(const char* fmt, ...) {  // log(), src/global.cpp:32-46
+    std::lock_guard<std::mutex> lk(g_log_mu);
+    if (g_verbosity > 0) {
+        va_list a;
+        va_start(a, fmt);
+        std::vprintf(fmt, a);
+        va_end(a);
+        std::fflush(stdout);
+    }
+    if (g_log_file) {
+        va_list a;
+        va_start(a, fmt);
+        std::vfprintf(g_log_file, fmt, a);
+        va_end(a);
+        std::fflush(g_log_file);
+    }
+}
+
+void set_verbosity(int v) {
+    std::lock_guard<std::mutex> lk(g_log_mu);
+    g_verbosity = v;
+}
+
+void set_log_file(const char* path) {
+    std::lock_guard<std::mutex> lk(g_log_mu);
+    if (g_log_file) std::fclose(g_log_file);
+    g_log_file = path ? std::fopen(path, "a") : nullptr;
+    if (path && !g_log_file) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' opening error.");
+}
+
+// ------------------------------------------------------------------ solver
+
+template <typename T>
+T* Solver::dalloc(size_t n) {
+    void* p = nullptr;
+    size_t b = std::max<size_t>(n, 1) * sizeof(T);
+    CUDA_CHECK(cudaMalloc(&p, b));
+    allocs_.push_back(p);
+    bytes_ += b;
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+T* Solver::upload(const std::vector<T>& v) {
+    T* p = dalloc<T>(v.size());
+    if (!v.empty()) CUDA_CHECK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+    return p;
+}
+
+template <typename T>
+static std::vector<float> to_f32(const std::vector<T>& v) {
+    return std::vector<float>(v.begin(), v.end());
+}
+
+Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_region,
+               const std::vector<int>& edge_bnd, int gauss_points)
+    : task_(t), topo_(std::move(topo)), gauss_points_(gauss_points) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(CFD2D_ERR_NO_DEVICE, "no CUDA device");
+    CUDA_CHECK(cudaGetDevice(&dev_));
+    const int nc = topo_.nc;
+    cell_mat_.resize(nc);
+    for (int i = 0; i < nc; i++) cell_mat_[i] = task_.regions[cell_region[i]].matId;
+    lay_ = make_layout(topo_, cell_mat_, edge_bnd, task_.reorder != 0);
+    const int ne = lay_.ne;
+    CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    try {
+        DevCase& c = dc_;
+        c.nc = nc; c.ne = ne; c.n_int = lay_.n_int;
+        c.face = upload(lay_.face);
+        c.ec1 = upload(lay_.ec1);
+        c.ec2 = upload(lay_.ec2);
+        c.ebnd = upload(lay_.ebnd);
+        c.S = upload(lay_.S);
+        c.rem_nb = upload(lay_.rem_nb);
+        c.iperm = upload(lay_.iperm);
+        const bool mixed = task_.precision == PREC_MIXED;
+        if (mixed) {
+            c.nx32 = upload(to_f32(lay_.nx));
+            c.ny32 = upload(to_f32(lay_.ny));
+            c.l32 = upload(to_f32(lay_.l));
+            c.dl32 = upload(to_f32(lay_.dl));
+        } else {
+            c.nx = upload(lay_.nx);
+            c.ny = upload(lay_.ny);
+            c.l = upload(lay_.l);
+            c.dl = upload(lay_.dl);
+        }
+        std::vector<DevMat> mats;
+        for (auto& m : task_.mats) {
+            DevMat d;
+            d.M = m.M; d.Cp = m.Cp;
+            d.Cv = m.Cp - GAS_R / m.M;  // Material::URS, src/global.cpp:11-12
+            d.gam = m.Cp / d.Cv;
+            d.gm1 = d.gam - 1;
+            mats.push_back(d);
+        }
+        c.mats = upload(mats);
+        c.mat0 = mats[0];
+        if (mats.size() > 1) c.cmat = upload(lay_.cmat);
+        std::vector<DevBnd> bnds;
+        for (auto& b : task_.bnds) {
+            DevBnd d{};
+            d.kind = b.kind;
+            d.u = b.par[0]; d.v = b.par[1]; d.T = b.par[2]; d.p = b.par[3];
+            bnds.push_back(d);
+        }
+        if (bnds.empty()) bnds.push_back(DevBnd{});
+        c.bnds = upload(bnds);
+        c.gam_flux = 1.4;  // hard-coded in FVM_TVD::run, src/methods/fvm_tvd.cpp:345,398
+        c.cfl_number = task_.cfl;
+        c.lim_rmin = task_.lim_rmin; c.lim_rmax = task_.lim_rmax;
+        c.lim_pmin = task_.lim_pmin; c.lim_pmax = task_.lim_pmax; c.lim_umax = task_.lim_umax;
+        c.steady = task_.steady;
+        c.newton_cap = task_.newton_cap;
+        c.A = dalloc<double>(4 * (size_t)nc);
+        c.B = dalloc<double>(4 * (size_t)nc);
+        c.cfl = dalloc<double>(nc);
+        c.ctau = dalloc<double>(nc);
+        c.ctau_next = task_.steady ? dalloc<double>(nc) : c.ctau;
+        c.flags = dalloc<unsigned>(nc);
+        c.n_lim = dalloc<int>(1);
+        c.err = dalloc<unsigned>(1);
+        if (mixed) {
+            c.W32 = dalloc<float>(4 * (size_t)nc);
+            c.G32 = dalloc<float>(8 * (size_t)nc);
+            c.F32 = dalloc<float>(4 * (size_t)ne);
+        } else {
+            c.W64 = dalloc<double>(4 * (size_t)nc);
+            c.G64 = dalloc<double>(8 * (size_t)nc);
+            c.F64 = dalloc<double>(4 * (size_t)ne);
+        }
+        stage_ = dalloc<double>(4 * (size_t)nc);
+        dtmin_ = dalloc<unsigned long long>(1);
+        partial_ = dalloc<double>(4 * kConservationBlocks);
+        CUDA_CHECK(cudaMemsetAsync(c.flags, 0, sizeof(unsigned) * nc, stream_));
+        CUDA_CHECK(cudaMemsetAsync(c.n_lim, 0, sizeof(int), stream_));
+        CUDA_CHECK(cudaMemsetAsync(c.err, 0, sizeof(unsigned), stream_));
+        // initial state from the regions (src/methods/fvm_tvd.cpp:199-204), storage order
+        std::vector<double> U(4 * (size_t)nc);
+        std::vector<std::array<double, 4>> reg(task_.regions.size());
+        for (size_t r = 0; r < reg.size(); r++)
+            region_state(task_.mats[task_.regions[r].matId], task_.regions[r], reg[r].data());
+        for (int i = 0; i < nc; i++) {
+            const auto& u = reg[cell_region[lay_.perm[i]]];
+            for (int k = 0; k < 4; k++) U[(size_t)k * nc + i] = u[k];
+        }
+        CUDA_CHECK(cudaMemcpyAsync(c.A, U.data(), U.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
+        tau_ = task_.tau;
+        launch_prims(c, task_.precision, stream_);
+        compute_tau();
+        CUDA_CHECK(cudaStreamSynchronize(stream_));
+        if (!task_.steady) log_line("time step: %25.16E\n", tau_);  // calcTimeStep, :238
+        build_graph();
+    } catch (...) {
+        for (void* p : allocs_) cudaFree(p);
+        allocs_.clear();
+        if (stream_) cudaStreamDestroy(stream_);
+        stream_ = nullptr;
+        throw;
+    }
+}
+
+Solver::~Solver() {
+    use_device();
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (void* p : allocs_) cudaFree(p);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+// calcTimeStep at init (src/methods/fvm_tvd.cpp:216-240): STEADY=1 leaves the
+// per-cell cTau from launch_prims; STEADY=0 takes TAU = min(TAU, min_i ...).
+void Solver::compute_tau() {
+    if (task_.steady) return;
+    unsigned long long init;
+    double t0 = tau_;
+    std::memcpy(&init, &t0, sizeof init);
+    if (!(t0 > 0)) init = 0x7ff0000000000000ull;
+    CUDA_CHECK(cudaMemcpyAsync(dtmin_, &init, sizeof init, cudaMemcpyHostToDevice, stream_));
+    launch_dt_min(dc_, dtmin_, stream_);
+    unsigned long long bits;
+    CUDA_CHECK(cudaMemcpyAsync(&bits, dtmin_, sizeof bits, cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+    double m;
+    std::memcpy(&m, &bits, sizeof m);
+    if (!(t0 > m)) m = t0;
+    tau_ = m;
+    launch_fill_cfl(dc_, tau_, stream_);
+}
+
+// One time step. With ev/kinds/nev, an event pair brackets each kernel launch
+// (profiling); the captured graph has no events.
+void Solver::enqueue_step(cudaEvent_t* ev, int* kinds, int* nev) {
+    const int nst = task_.scheme == TIME_EULER ? 1 : (task_.scheme == TIME_HEUN ? 2 : 3);
+    const int p = task_.precision;
+    auto mark = [&](int kind, bool begin) {
+        if (!ev) return;
+        if (begin) kinds[*nev / 2] = kind;
+        CUDA_CHECK(cudaEventRecord(ev[(*nev)++], stream_));
+    };
+    for (int st = 0; st < nst; st++) {
+        if (gauss_points_ == 0) {  // 1-point edges: the Gauss-point loop is empty, no flux
+            size_t b = 4 * (size_t)dc_.ne * (p == PREC_MIXED ? sizeof(float) : sizeof(double));
+            CUDA_CHECK(cudaMemsetAsync(p == PREC_MIXED ? (void*)dc_.F32 : (void*)dc_.F64, 0, b, stream_));
+        } else {
+            if (task_.recon != RECON_NONE) {
+                mark(0, true);
+                launch_grad(dc_, p, stream_);
+                mark(0, false);
+            }
+            mark(1, true);
+            launch_flux(dc_, p, task_.flux, task_.recon, stream_);
+            mark(1, false);
+        }
+        mark(2, true);
+        launch_update(dc_, p, task_.scheme, st, stream_);
+        mark(2, false);
+    }
+    mark(3, true);
+    launch_remediate(dc_, p, stream_);
+    mark(3, false);
+}
+
+double Solver::timed_steps(int n) {
+    use_device();
+    cudaEvent_t a, b;
+    CUDA_CHECK(cudaEventCreate(&a));
+    CUDA_CHECK(cudaEventCreate(&b));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+    CUDA_CHECK(cudaEventRecord(a, stream_));
+    for (int k = 0; k < n; k++) {
+        if (!task_.steady) t_ += tau_;
+        CUDA_CHECK(cudaGraphLaunch(gexec_, stream_));
+        steps_++;
+    }
+    CUDA_CHECK(cudaEventRecord(b, stream_));
+    CUDA_CHECK(cudaEventSynchronize(b));
+    float ms = 0;
+    CUDA_CHECK(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ms;
+}
+
+void Solver::profile_steps(int n, double ms[4], int launches[4]) {
+    use_device();
+    for (int k = 0; k < 4; k++) { ms[k] = 0; launches[k] = 0; }
+    std::vector<cudaEvent_t> ev(32);
+    for (auto& e : ev) CUDA_CHECK(cudaEventCreate(&e));
+    int kinds[16];
+    for (int s = 0; s < n; s++) {
+        int nev = 0;
+        if (!task_.steady) t_ += tau_;
+        enqueue_step(ev.data(), kinds, &nev);
+        steps_++;
+        CUDA_CHECK(cudaStreamSynchronize(stream_));
+        for (int j = 0; j + 1 < nev; j += 2) {
+            float t = 0;
+            CUDA_CHECK(cudaEventElapsedTime(&t, ev[j], ev[j + 1]));
+            ms[kinds[j / 2]] += t;
+            launches[kinds[j / 2]]++;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+}
+
+void Solver::build_graph() {
+    CUDA_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    try {
+        enqueue_step();
+    } catch (...) {
+        cudaGraph_t g;
+        cudaStreamEndCapture(stream_, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    CUDA_CHECK(cudaStreamEndCapture(stream_, &graph_));
+    CUDA_CHECK(cudaGraphInstantiate(&gexec_, graph_, 0));
+}
+
+int Solver::read_status() {
+    unsigned e = 0;
+    CUDA_CHECK(cudaMemcpyAsync(&e, dc_.err, sizeof e, cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaMemsetAsync(dc_.err, 0, sizeof(unsigned), stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+    if (e & ERRBIT_NEWTON_CAP) return CFD2D_ERR_NEWTON_CAP;
+    if (e & ERRBIT_NONPHYSICAL) return CFD2D_ERR_NONPHYSICAL;
+    return CFD2D_OK;
+}
+
+int Solver::step(int n) {
+    use_device();
+    for (int k = 0; k < n; k++) {
+        if (!task_.steady) t_ += tau_;  // src/methods/fvm_tvd.cpp:312-316
+        CUDA_CHECK(cudaGraphLaunch(gexec_, stream_));
+        steps_++;
+    }
+    return read_status();
+}
+
+int Solver::run() {  // FVM_TVD::run, src/methods/fvm_tvd.cpp:303-462
+    use_device();
+    if (steps_ == 0) save_vtk(0);
+    int status = CFD2D_OK;
+    const unsigned smax = (unsigned)task_.step_max;
+    while (t_ < task_.tmax && (unsigned)steps_ < smax) {
+        if (!task_.steady) t_ += tau_;
+        CUDA_CHECK(cudaGraphLaunch(gexec_, stream_));
+        steps_++;
+        const bool save = task_.file_step != 0 && steps_ % task_.file_step == 0;
+        const bool print = task_.print_step != 0 && steps_ % task_.print_step == 0;
+        if (save || print) {
+            int s = read_status();
+            if (s != CFD2D_OK) status = s;
+            if (save) save_vtk(steps_);
+            if (print) log_line("step: %d\t\ttime step: %.16f\n", steps_, t_);
+        }
+    }
+    int s = read_status();
+    return s != CFD2D_OK ? s : status;
+}
+
+void Solver::get_state(double* ro, double* ru, double* rv, double* re) {
+    use_device();
+    const int nc = dc_.nc;
+    launch_scatter_state(dc_, dc_.A, stage_, stream_);
+    double* dst[4] = {ro, ru, rv, re};
+    for (int k = 0; k < 4; k++)
+        if (dst[k])
+            CUDA_CHECK(cudaMemcpyAsync(dst[k], stage_ + (size_t)k * nc, sizeof(double) * nc, cudaMemcpyDeviceToHost,
+                                       stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
+void Solver::set_state(const double* ro, const double* ru, const double* rv, const double* re, bool reset_tau) {
+    use_device();
+    const int nc = dc_.nc;
+    const double* src[4] = {ro, ru, rv, re};
+    for (int k = 0; k < 4; k++) {
+        if (!src[k]) throw Error(CFD2D_ERR_INVALID_ARG, "set_state: all four arrays are required");
+        CUDA_CHECK(cudaMemcpyAsync(stage_ + (size_t)k * nc, src[k], sizeof(double) * nc, cudaMemcpyHostToDevice,
+                                   stream_));
+    }
+    launch_gather_state(dc_, stage_, dc_.A, stream_);
+    launch_prims(dc_, task_.precision, stream_);
+    if (reset_tau) {
+        tau_ = task_.tau;
+        compute_tau();
+    }
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
+void Solver::get_ctau(double* out) {
+    use_device();
+    launch_permute_scalar(dc_, dc_.ctau, stage_, stream_);
+    CUDA_CHECK(cudaMemcpyAsync(out, stage_, sizeof(double) * dc_.nc, cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
+void Solver::get_flags(unsigned* out) {
+    use_device();
+    unsigned* tmp = reinterpret_cast<unsigned*>(stage_);
+    launch_permute_flags(dc_, dc_.flags, tmp, stream_);
+    CUDA_CHECK(cudaMemcpyAsync(out, tmp, sizeof(unsigned) * dc_.nc, cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
+void Solver::residual(double* R) {
+    use_device();
+    const int p = task_.precision;
+    if (gauss_points_ == 0) {
+        size_t b = 4 * (size_t)dc_.ne * (p == PREC_MIXED ? sizeof(float) : sizeof(double));
+        CUDA_CHECK(cudaMemsetAsync(p == PREC_MIXED ? (void*)dc_.F32 : (void*)dc_.F64, 0, b, stream_));
+    } else {
+        if (task_.recon != RECON_NONE) launch_grad(dc_, p, stream_);
+        launch_flux(dc_, p, task_.flux, task_.recon, stream_);
+    }
+    launch_residual(dc_, p, dc_.B, stream_);  // B is scratch between steps
+    launch_scatter_state(dc_, dc_.B, stage_, stream_);
+    CUDA_CHECK(cudaMemcpyAsync(R, stage_, sizeof(double) * 4 * dc_.nc, cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
+void Solver::conservation(double sums[4]) {
+    use_device();
+    launch_conservation(dc_, partial_, kConservationBlocks, stream_);
+    std::vector<double> h(4 * kConservationBlocks);
+    CUDA_CHECK(cudaMemcpyAsync(h.data(), partial_, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+    for (int k = 0; k < 4; k++) {
+        double s = 0.0;
+        for (int b = 0; b < kConservationBlocks; b++) s += h[4 * b + k];
+        sums[k] = s;
+    }
+}
+
+// FVM_TVD::save, src/methods/fvm_tvd.cpp:501-600 (same fields, formats and quirks).
+void Solver::save_vtk(int step) {
+    const int nc = topo_.nc, nn = topo_.nn;
+    std::vector<double> U(4 * (size_t)nc), ct(nc);
+    get_state(U.data(), U.data() + nc, U.data() + 2 * (size_t)nc, U.data() + 3 * (size_t)nc);
+    get_ctau(ct.data());
+    char name[64];
+    std::snprintf(name, sizeof name, "res_%010d.vtk", step);
+    FILE* fp = std::fopen(name, "w");
+    if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + name + "' opening error.");
+    struct P { double r, u, v, p, cz, T, gam; };
+    auto par = [&](int i) {
+        const TaskMaterial& m = task_.mats[cell_mat_[i]];
+        double Cv = m.Cp - GAS_R / m.M, gam = m.Cp / Cv;
+        P q;
+        q.r = U[i];
+        q.u = U[nc + i] / U[i];
+        q.v = U[2 * (size_t)nc + i] / U[i];
+        double E = U[3 * (size_t)nc + i] / U[i];
+        double e = E - 0.5 * (q.u * q.u + q.v * q.v);
+        q.p = q.r * e * (gam - 1);
+        q.cz = std::sqrt(gam * q.p / q.r);
+        double e2 = q.p / (q.r * (gam - 1));
+        q.T = e2 / Cv;
+        q.gam = gam;
+        return q;
+    };
+    std::fprintf(fp, "# vtk DataFile Version 2.0\nGASDIN data file\nASCII\nDATASET UNSTRUCTURED_GRID\n");
+    std::fprintf(fp, "POINTS %d float\n", nn);
+    for (int i = 0; i < nn; i++) std::fprintf(fp, "%f %f %f  ", topo_.xy[2 * i], topo_.xy[2 * i + 1], 0.0);
+    std::fprintf(fp, "\n");
+    std::fprintf(fp, "CELLS %d %d\n", nc, 4 * nc);
+    for (int i = 0; i < nc; i++)
+        std::fprintf(fp, "3 %d %d %d\n", topo_.tri[3 * i], topo_.tri[3 * i + 1], topo_.tri[3 * i + 2]);
+    std::fprintf(fp, "\n");
+    std::fprintf(fp, "CELL_TYPES %d\n", nc);
+    for (int i = 0; i < nc; i++) std::fprintf(fp, "5\n");
+    std::fprintf(fp, "\n");
+    // the reference's "i+1 % 8 == 0" is i+1 == 0: one newline at the end of each field
+    auto field = [&](const char* head, auto val) {
+        std::fputs(head, fp);
+        for (int i = 0; i < nc; i++) {
+            std::fprintf(fp, "%25.16f ", val(i));
+            if (i + 1 == nc) std::fprintf(fp, "\n");
+        }
+    };
+    std::fprintf(fp, "CELL_DATA %d\n", nc);
+    field("SCALARS Density float 1\nLOOKUP_TABLE default\n", [&](int i) { return par(i).r; });
+    field("SCALARS Pressure float 1\nLOOKUP_TABLE default\n", [&](int i) { return par(i).p; });
+    field("SCALARS Temperature float 1\nLOOKUP_TABLE default\n", [&](int i) { return par(i).T; });
+    field("SCALARS MachNumber float 1\nLOOKUP_TABLE default\n", [&](int i) {
+        P q = par(i);
+        return (q.u * q.u + q.v * q.v) / q.cz;
+    });
+    std::fprintf(fp, "VECTORS Velosity float\n");
+    for (int i = 0; i < nc; i++) {
+        P q = par(i);
+        std::fprintf(fp, "%25.16f %25.16f %25.16f ", q.u, q.v, 0.0);
+        if (i + 1 == nc) std::fprintf(fp, "\n");
+    }
+    std::fprintf(fp, "SCALARS Total_pressure float 1\nLOOKUP_TABLE default\n");
+    for (int i = 0; i < nc; i++) {
+        P q = par(i);
+        double agam = q.gam - 1.0;
+        double M2 = (q.u * q.u + q.v * q.v) / (q.gam * q.p / q.r);
+        std::fprintf(fp, "%f ", q.p * std::pow(1.0 + 0.5 * M2 * agam, q.gam / (q.gam - 1.0)));
+        if ((i + 1) % 8 == 0 || i + 1 == nc) std::fprintf(fp, "\n");
+    }
+    field("SCALARS TAU float 1\nLOOKUP_TABLE default\n", [&](int i) { return ct[i]; });
+    std::fclose(fp);
+    if (g_verbosity > 0) {
+        std::printf("File '%s' saved...\n", name);
+        std::fflush(stdout);
+    }
+}
+
+}  // namespace cfd2d

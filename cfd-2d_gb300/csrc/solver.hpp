@@ -1,0 +1,88 @@
+// Host driver of one FVM_TVD instance on the GPU: owns the device arrays, the
+// stream and the CUDA graph of one time step.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.hpp"
+#include "mesh.hpp"
+#include "task.hpp"
+
+namespace cfd2d {
+
+void log_line(const char* fmt, ...);
+void set_verbosity(int v);
+void set_log_file(const char* path);
+
+#define CUDA_CHECK(x)                                                                                    \
+    do {                                                                                                 \
+        cudaError_t e_ = (x);                                                                            \
+        if (e_ != cudaSuccess)                                                                           \
+            throw ::cfd2d::Error(CFD2D_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));       \
+    } while (0)
+
+class Solver {
+public:
+    Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_region, const std::vector<int>& edge_bnd,
+           int gauss_points);
+    ~Solver();
+    Solver(const Solver&) = delete;
+    Solver& operator=(const Solver&) = delete;
+
+    int step(int n);  // CFD2D_OK, or a warning code from the device error word
+    int run();
+    void get_state(double* ro, double* ru, double* rv, double* re);
+    void set_state(const double* ro, const double* ru, const double* rv, const double* re, bool reset_tau);
+    void get_ctau(double* out);
+    void get_flags(unsigned* out);
+    void residual(double* R);
+    void conservation(double sums[4]);
+    void save_vtk(int step);
+    // device time of n steps (CUDA events around the graph launches on the solver's stream)
+    double timed_steps(int n);
+    // n steps launched one kernel at a time with events around each launch;
+    // per kind (0 grad, 1 flux, 2 update, 3 remediate): total ms and launch count
+    void profile_steps(int n, double ms[4], int launches[4]);
+
+    const TaskConfig& task() const { return task_; }
+    const Topo& topo() const { return topo_; }
+    const Layout& layout() const { return lay_; }
+    int n_steps() const { return steps_; }
+    double time() const { return t_; }
+    double tau() const { return tau_; }
+    size_t device_bytes() const { return bytes_; }
+    cudaStream_t stream() const { return stream_; }
+    const DevCase& dev() const { return dc_; }
+    int precision() const { return task_.precision; }
+
+private:
+    template <typename T> T* dalloc(size_t n);
+    template <typename T> T* upload(const std::vector<T>& v);
+    void compute_tau();
+    void enqueue_step(cudaEvent_t* ev = nullptr, int* kinds = nullptr, int* nev = nullptr);
+    void build_graph();
+    int read_status();
+    void use_device() const { cudaSetDevice(dev_); }
+
+    TaskConfig task_;
+    Topo topo_;
+    Layout lay_;
+    std::vector<int> cell_mat_;
+    int gauss_points_;
+    int dev_ = 0;
+    DevCase dc_{};
+    cudaStream_t stream_ = nullptr;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t gexec_ = nullptr;
+    std::vector<void*> allocs_;
+    size_t bytes_ = 0;
+    double* stage_ = nullptr;     // 4*nc staging for permutations and residuals
+    unsigned long long* dtmin_ = nullptr;
+    double* partial_ = nullptr;
+    double tau_ = 0, t_ = 0;
+    int steps_ = 0;
+};
+
+}  // namespace cfd2d

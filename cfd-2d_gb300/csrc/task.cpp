@@ -1,0 +1,216 @@
+#include "task.hpp"
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+
+#include "cfd2d.h"
+#include "xml.hpp"
+
+namespace cfd2d {
+
+namespace {
+
+const XmlNode* need(const XmlNode* n, const char* name, const char* where) {
+    const XmlNode* c = n ? n->child(name) : nullptr;
+    if (!c) throw Error(CFD2D_ERR_TASK, std::string("task.xml: missing <") + name + "> in <" + where + ">");
+    return c;
+}
+
+// TiXmlElement::Attribute(name, double*) / (name, int*): atof / atoi of the value.
+double attr_d(const XmlNode* n, const char* a) {
+    const char* v = n->attr(a);
+    if (!v) throw Error(CFD2D_ERR_TASK, "task.xml: <" + n->name + "> has no attribute '" + a + "'");
+    return std::atof(v);
+}
+int attr_i(const XmlNode* n, const char* a) {
+    const char* v = n->attr(a);
+    if (!v) throw Error(CFD2D_ERR_TASK, "task.xml: <" + n->name + "> has no attribute '" + a + "'");
+    return std::atoi(v);
+}
+
+int pick(const XmlNode* ctl, const char* tag, std::initializer_list<std::pair<const char*, int>> opts, int dflt) {
+    const XmlNode* n = ctl->child(tag);
+    if (!n) return dflt;
+    const char* v = n->attr("value");
+    if (!v) throw Error(CFD2D_ERR_TASK, std::string("task.xml: <") + tag + "> has no value");
+    for (auto& o : opts)
+        if (std::strcmp(v, o.first) == 0) return o.second;
+    throw Error(CFD2D_ERR_TASK, std::string("task.xml: unknown ") + tag + " '" + v + "'");
+}
+
+}  // namespace
+
+TaskConfig parse_task(const std::string& path) {
+    TaskConfig t;
+    t.path = path;
+    size_t slash = path.find_last_of('/');
+    t.dir = slash == std::string::npos ? std::string(".") : path.substr(0, slash);
+    std::unique_ptr<XmlNode> doc;
+    try {
+        doc = xml_load(path);
+    } catch (const std::exception& e) {
+        throw Error(CFD2D_ERR_XML, std::string("ERROR: ") + e.what());
+    }
+    const XmlNode* task = doc->child("task");
+    if (!task) throw Error(CFD2D_ERR_TASK, "task.xml: no <task> element");
+    const char* method = task->attr("method");
+    if (method && std::strcmp(method, "FVM_TVD") != 0 && std::strcmp(method, "FVM_TVD_GPU") != 0)
+        throw Error(CFD2D_ERR_TASK, std::string("ERROR: method '") + method + "' is not served by this library.");
+
+    const XmlNode* ctl = need(task, "control", "task");
+    t.steady = attr_i(need(ctl, "STEADY", "control"), "value") == 0 ? 0 : 1;
+    t.tau = attr_d(need(ctl, "TAU", "control"), "value");
+    t.tmax = attr_d(need(ctl, "TMAX", "control"), "value");
+    t.cfl = attr_d(need(ctl, "CFL", "control"), "value");
+    t.step_max = attr_i(need(ctl, "STEP_MAX", "control"), "value");
+    t.file_step = attr_i(need(ctl, "FILE_OUTPUT_STEP", "control"), "value");
+    t.print_step = attr_i(need(ctl, "LOG_OUTPUT_STEP", "control"), "value");
+    t.flux = pick(ctl, "FLUX", {{"GODUNOV", FLUX_GODUNOV}, {"LAX", FLUX_LAX}, {"ROE", FLUX_ROE}, {"HLLC", FLUX_HLLC}},
+                  FLUX_GODUNOV);
+    t.recon = pick(ctl, "RECONSTRUCTION",
+                   {{"NONE", RECON_NONE}, {"FIRST_ORDER", RECON_NONE}, {"LINEAR", RECON_LINEAR}, {"MINMOD", RECON_MINMOD}},
+                   RECON_LINEAR);
+    t.scheme = pick(ctl, "TIME_SCHEME", {{"EULER", TIME_EULER}, {"HEUN", TIME_HEUN}, {"SSPRK3", TIME_SSPRK3}}, TIME_HEUN);
+    t.precision = pick(ctl, "PRECISION", {{"FP64", PREC_FP64}, {"MIXED", PREC_MIXED}}, PREC_FP64);
+    t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}}, 1);
+    if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = attr_i(n, "value");
+    if (t.newton_cap < 1) t.newton_cap = 1;
+
+    const XmlNode* lim = need(task, "limits", "task");
+    t.lim_rmin = attr_d(need(lim, "ro", "limits"), "min");
+    t.lim_rmax = attr_d(need(lim, "ro", "limits"), "max");
+    t.lim_pmin = attr_d(need(lim, "p", "limits"), "min");
+    t.lim_pmax = attr_d(need(lim, "p", "limits"), "max");
+    t.lim_umax = attr_d(need(lim, "u", "limits"), "max");
+
+    const XmlNode* mats = need(task, "materials", "task");
+    int nm = attr_i(mats, "count");
+    auto mlist = mats->children_named("material");
+    if (nm < 1 || nm > (int)mlist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <materials count> does not match");
+    if (nm > 255) throw Error(CFD2D_ERR_TASK, "task.xml: more than 255 materials");
+    for (int i = 0; i < nm; i++) {
+        TaskMaterial m;
+        m.id = attr_i(mlist[i], "id");
+        m.name = need(mlist[i], "name", "material")->text;
+        const XmlNode* p = need(mlist[i], "parameters", "material");
+        m.M = attr_d(need(p, "M", "parameters"), "value");
+        m.Cp = attr_d(need(p, "Cp", "parameters"), "value");
+        m.K = attr_d(need(p, "K", "parameters"), "value");
+        m.ML = attr_d(need(p, "ML", "parameters"), "value");
+        t.mats.push_back(m);
+    }
+
+    const XmlNode* regs = need(task, "regions", "task");
+    int nr = attr_i(regs, "count");
+    auto rlist = regs->children_named("region");
+    if (nr < 1 || nr > (int)rlist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <regions count> does not match");
+    for (int i = 0; i < nr; i++) {
+        TaskRegion r;
+        r.id = attr_i(rlist[i], "id");
+        r.matId = attr_i(need(rlist[i], "material", "region"), "id");
+        r.cellType = attr_i(need(rlist[i], "cell", "region"), "type");
+        r.name = need(rlist[i], "name", "region")->text;
+        const XmlNode* p = need(rlist[i], "parameters", "region");
+        r.u = attr_d(need(p, "Vx", "parameters"), "value");
+        r.v = attr_d(need(p, "Vy", "parameters"), "value");
+        r.T = attr_d(need(p, "T", "parameters"), "value");
+        r.p = attr_d(need(p, "P", "parameters"), "value");
+        if (r.matId < 0 || r.matId >= nm) throw Error(CFD2D_ERR_TASK, "task.xml: region refers to a missing material");
+        t.regions.push_back(r);
+    }
+
+    const XmlNode* bnds = need(task, "boundaries", "task");
+    for (const XmlNode* b : bnds->children_named("boundCond")) {  // CFDBoundary::create, src/bnd_cond.cpp:10-72
+        TaskBound tb;
+        const char* type = need(b, "type", "boundCond")->text.c_str();
+        if (std::strcmp(type, "BOUND_INLET") == 0) {
+            tb.kind = BND_INLET;
+            const XmlNode* p = b->child("parameters");
+            const char* names[4] = {"Vx", "Vy", "T", "P"};
+            for (int k = 0; k < 4; k++) {
+                const XmlNode* n = p ? p->child(names[k]) : nullptr;
+                if (!n) throw Error(CFD2D_ERR_BOUND_NOPAR, std::string("Parameter '") + names[k] +
+                                                               "' isn't specified  for BOUND_INLET.");
+                tb.par[k] = attr_d(n, "value");
+            }
+        } else if (std::strcmp(type, "BOUND_OUTLET") == 0) {
+            tb.kind = BND_OUTLET;
+        } else if (std::strcmp(type, "BOUND_WALL_NO_SLIP") == 0) {
+            tb.kind = BND_WALL_NO_SLIP;
+        } else if (std::strcmp(type, "BOUND_WALL_SLIP") == 0) {
+            tb.kind = BND_WALL_SLIP;
+        } else {
+            throw Error(CFD2D_ERR_BOUND_UNKNOWN, std::string("Unknown boundary type '") + type + "' specified.");
+        }
+        tb.edgeType = attr_i(b, "edgeType");
+        tb.name = need(b, "name", "boundCond")->text;
+        t.bnds.push_back(tb);
+    }
+
+    const XmlNode* mesh = need(task, "mesh", "task");
+    const char* mn = need(mesh, "name", "mesh")->attr("value");
+    const char* mt = need(mesh, "filesType", "mesh")->attr("value");
+    if (!mn || !mt) throw Error(CFD2D_ERR_TASK, "task.xml: <mesh> needs name and filesType values");
+    t.mesh_name = mn;
+    t.mesh_type = mt;
+    if (t.mesh_type != "berkeley_triangle" && t.mesh_type != "salome_unv")
+        throw Error(CFD2D_ERR_MESH_WRONG_NAME, "Wrong mesh type.");
+    if (const XmlNode* g = mesh->child("gaussPoints")) t.gauss_points = attr_i(g, "value");
+    return t;
+}
+
+void region_state(const TaskMaterial& m, const TaskRegion& r, double U[4]) {
+    double Cv = m.Cp - GAS_R / m.M;     // Material::URS, src/global.cpp:9-30
+    double gam = m.Cp / Cv;
+    double p = r.p, T = r.T, u = r.u, v = r.v;
+    double ro = p * m.M / (T * GAS_R);  // URS(2)
+    double e = p / (ro * (gam - 1));     // URS(1)
+    U[0] = ro;                           // convertParToCons, src/methods/fvm_tvd.cpp:795-801
+    U[1] = ro * u;
+    U[2] = ro * v;
+    U[3] = ro * (e + 0.5 * (u * u + v * v));
+}
+
+void bind_mesh(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::vector<int>& cell_region,
+               std::vector<int>& edge_bnd) {
+    const int nc = topo.nc, ne = topo.ne;
+    cell_region.assign(nc, -1);
+    for (int i = 0; i < nc; i++) {  // getRegion(typeName), src/methods/fvm_tvd.cpp:773-786
+        const std::string& nm = raw.cell_name[i];
+        for (size_t r = 0; r < t.regions.size(); r++)
+            if (t.regions[r].name == nm) { cell_region[i] = (int)r; break; }
+        if (cell_region[i] < 0)
+            throw Error(CFD2D_ERR_REGION_UNKNOWN, "ERROR: unknown cell name '" + nm + "' of cell " + std::to_string(i));
+    }
+    edge_bnd.assign(ne, -1);
+    std::map<long long, int> marker;  // Triangle: a later .poly line for the same edge wins (findEdge, src/mesh/grid.cpp:38-48)
+    if (raw.berkeley)
+        for (size_t s = 0; s < raw.bseg_marker.size(); s++) {
+            long long a = raw.bseg[2 * s], b = raw.bseg[2 * s + 1];
+            marker[std::min(a, b) * (1ll << 32) + std::max(a, b)] = raw.bseg_marker[s];
+        }
+    for (int e = 0; e < ne; e++) {  // boundary binding, src/methods/fvm_tvd.cpp:131-174
+        if (topo.c2[e] >= 0) continue;
+        int s = topo.bseg_of_edge[e];
+        int b = -1;
+        if (!raw.berkeley) {
+            const std::string nm = s >= 0 ? raw.bseg_name[s] : std::string();
+            for (size_t k = 0; k < t.bnds.size(); k++)
+                if (!nm.empty() && t.bnds[k].name == nm) { b = (int)k; break; }
+        } else {
+            long long a = topo.n1[e], c = topo.n2[e];
+            auto it = marker.find(std::min(a, c) * (1ll << 32) + std::max(a, c));
+            int type = it != marker.end() ? it->second : -1;
+            for (size_t k = 0; k < t.bnds.size(); k++)
+                if (type != 0 && t.bnds[k].edgeType == type) { b = (int)k; break; }
+        }
+        if (b < 0)
+            throw Error(CFD2D_ERR_EDGE_UNKNOWN,
+                        "ERROR (boundary condition): unknown edge type of edge " + std::to_string(e) + "...");
+        edge_bnd[e] = b;
+    }
+}
+
+}  // namespace cfd2d

@@ -1,0 +1,159 @@
+/*
+ * cfd2d_gb300 — C ABI of the GB300 drop-in for the reference's explicit
+ * finite-volume method FVM_TVD (zhrv/cfd-2d).
+ *
+ * The reference selects the method through its C++ plugin interface
+ *   class Method { virtual void init(char* xml); virtual void run(); virtual void done(); }
+ *   (src/methods/method.h:6-11), instantiated by name in Solver::initMethod
+ *   (src/methods/solver.cpp:13-61) from <task method="FVM_TVD">.
+ * These entry points replace FVM_TVD::init / run / done
+ * (src/methods/fvm_tvd.cpp:7-213, 303-462, 731-752) one for one, and add the
+ * state access a caller outside the reference's process needs. Plain C types
+ * only; every entry point returns 0 or an error code and never exits the
+ * process (the reference calls exit()/EXIT() on errors, src/global.cpp:48-53).
+ *
+ * State arrays are in the reference's cell order (the order of the triangles in
+ * the mesh file); the library reorders cells internally for locality.
+ */
+#ifndef CFD2D_H
+#define CFD2D_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define CFD2D_OK 0
+/* the reference's Exception / EXIT codes (src/global.h:241-248) */
+#define CFD2D_ERR_BOUND_NOPAR 101                   /* BOUND_INLET without Vx/Vy/T/P */
+#define CFD2D_ERR_BOUND_UNKNOWN 102                 /* unknown <boundCond><type> */
+#define CFD2D_ERR_MESH_WRONG_NAME 201               /* unknown <mesh><filesType> */
+#define CFD2D_ERR_MESH_UNV_UNKNOWN_ELEMENT 221      /* UNV element type other than 11/41 */
+#define CFD2D_ERR_MESH_UNV_NOT_DEFINED_BND_EDGE 222 /* boundary edge without a UNV edge element */
+#define CFD2D_ERR_FILE_OPENING 301
+/* conditions the reference ends with EXIT(1) or undefined behaviour */
+#define CFD2D_ERR_XML 1              /* task file cannot be read or parsed (reference: exit(ErrorId)) */
+#define CFD2D_ERR_TASK 2             /* a required task element/attribute is missing */
+#define CFD2D_ERR_REGION_UNKNOWN 3   /* a cell's region name is not in <regions> (fvm_tvd.cpp:773-781) */
+#define CFD2D_ERR_EDGE_UNKNOWN 4     /* a boundary edge matches no <boundCond> (fvm_tvd.cpp:148-170) */
+#define CFD2D_ERR_MESH_FORMAT 5      /* malformed mesh file or arrays */
+#define CFD2D_ERR_INVALID_ARG 6
+/* GPU-side conditions */
+#define CFD2D_ERR_CUDA 501           /* a CUDA call failed; see cfd2d_last_error */
+#define CFD2D_ERR_NO_DEVICE 502
+#define CFD2D_ERR_NEWTON_CAP 503     /* the exact Riemann solver hit its iteration cap (state still advanced) */
+#define CFD2D_ERR_NONPHYSICAL 504    /* non-positive or NaN density/pressure appeared (state still advanced) */
+#define CFD2D_ERR_CAPACITY 505       /* a size exceeds a fixed capacity of the entry point */
+
+/* ---- method selections (task.xml <control> extensions) ------------------ */
+enum { CFD2D_FLUX_GODUNOV = 0, CFD2D_FLUX_LAX = 1, CFD2D_FLUX_ROE = 2, CFD2D_FLUX_HLLC = 3 };
+enum { CFD2D_RECON_NONE = 0, CFD2D_RECON_LINEAR = 1, CFD2D_RECON_MINMOD = 2 };
+enum { CFD2D_TIME_EULER = 0, CFD2D_TIME_HEUN = 1, CFD2D_TIME_SSPRK3 = 2 };
+enum { CFD2D_PREC_FP64 = 0, CFD2D_PREC_MIXED = 1 };
+
+typedef struct cfd2d_solver cfd2d_t;
+typedef struct cfd2d_mesh cfd2d_mesh_t;
+
+/* A mesh handed over as arrays instead of a mesh file. Regions and boundary
+ * conditions are referred to by position in the task's <regions> and
+ * <boundaries> lists (document order). */
+typedef struct {
+    int n_nodes;
+    const double* xy;        /* 2*n_nodes */
+    int n_cells;
+    const int* tri;          /* 3*n_cells, 0-based node numbers */
+    const int* cell_region;  /* n_cells */
+    int n_bsegs;
+    const int* bseg;         /* 2*n_bsegs boundary node pairs */
+    const int* bseg_bnd;     /* n_bsegs */
+} cfd2d_mesh_desc;
+
+typedef struct {
+    int n_cells, n_edges, n_boundary_edges, n_nodes;
+    int step;                /* steps taken */
+    int flux, recon, scheme, precision, steady;
+    double time;             /* t as the reference accumulates it (t += TAU per unsteady step) */
+    double tau;              /* global time step TAU (unsteady) */
+    size_t device_bytes;     /* device memory held by the handle */
+} cfd2d_info_t;
+
+/* FVM_TVD::init (src/methods/fvm_tvd.cpp:7-213): read task.xml and its mesh,
+ * set the initial state from the regions and compute TAU. A relative mesh name
+ * is opened relative to the working directory, else to task.xml's directory. */
+int cfd2d_create(const char* task_xml_path, cfd2d_t** out);
+
+/* FVM_TVD::init with the mesh given as arrays (the task's <mesh> is ignored). */
+int cfd2d_create_with_mesh(const char* task_xml_path, const cfd2d_mesh_desc* mesh, cfd2d_t** out);
+
+/* nsteps iterations of FVM_TVD::run's loop body (src/methods/fvm_tvd.cpp:310-460)
+ * without file output; blocks until done. */
+int cfd2d_step(cfd2d_t* h, int nsteps);
+
+/* FVM_TVD::run: the whole loop while t < TMAX and step < STEP_MAX, writing
+ * res_%010d.vtk every FILE_OUTPUT_STEP (and res_0000000000.vtk first when
+ * starting from step 0, which the reference writes at the end of init) and the
+ * log line every LOG_OUTPUT_STEP. */
+int cfd2d_run(cfd2d_t* h);
+
+/* FVM_TVD::done: free everything the handle owns. */
+int cfd2d_destroy(cfd2d_t* h);
+
+int cfd2d_get_info(const cfd2d_t* h, cfd2d_info_t* info);
+
+/* Conserved state ro, ru, rv, re (FVM_TVD's arrays, src/methods/fvm_tvd.h:86-89). */
+int cfd2d_get_state(cfd2d_t* h, double* ro, double* ru, double* rv, double* re);
+/* Replace the conserved state. reset_time_step != 0 redoes init's time step
+ * (TAU = min(TAU from task.xml, CFL pass), src/methods/fvm_tvd.cpp:211). */
+int cfd2d_set_state(cfd2d_t* h, const double* ro, const double* ru, const double* rv, const double* re,
+                    int reset_time_step);
+/* Per-cell time step cTau and cell flag words (CELL_FLAG_LIM = 2, src/mesh/grid.h:12-14). */
+int cfd2d_get_time_step(cfd2d_t* h, double* ctau);
+int cfd2d_get_flags(cfd2d_t* h, unsigned* flags);
+/* One stage's right-hand side for the current state: the reference's
+ * ro_int..re_int after the edge loop (src/methods/fvm_tvd.cpp:324-365), 4 x n_cells. */
+int cfd2d_residual(cfd2d_t* h, double* R);
+/* Sums over cells of S*(ro, ru, rv, re) in FP64, summed in a fixed order. */
+int cfd2d_conservation(cfd2d_t* h, double sums[4]);
+/* FVM_TVD::save (src/methods/fvm_tvd.cpp:501-600): res_%010d.vtk in the working directory. */
+int cfd2d_save_vtk(cfd2d_t* h, int step);
+
+/* Device time in milliseconds of nsteps steps, from CUDA events recorded on the
+ * handle's stream around the step graph launches (the steps are taken). */
+int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms);
+/* nsteps steps launched kernel by kernel with CUDA events around each launch:
+ * per kernel kind (0 gradients, 1 edge fluxes, 2 stage updates, 3 remediation)
+ * the total device ms and the number of launches (the steps are taken). */
+int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_launches[4]);
+
+/* Select the CUDA device that cfd2d_create* places new solvers on (default: the
+ * calling thread's current device). A solver keeps its device for life. */
+int cfd2d_set_device(int device);
+
+/* Message of the last failed call on this thread. */
+int cfd2d_last_error(char* buf, size_t n);
+/* Log lines (the reference's log(), src/global.cpp:32-46) go to stdout unless
+ * verbosity is 0, and are appended to path when a log file is set (NULL closes). */
+int cfd2d_set_verbosity(int level);
+int cfd2d_set_log_file(const char* path);
+
+/* ---- host-only mesh inspection (no GPU needed) -------------------------- */
+/* Read the mesh a task names and build its edges exactly as the reference's
+ * reader does (MeshReader::create, src/mesh/MeshReader.cpp:7-23). */
+int cfd2d_mesh_load(const char* task_xml_path, cfd2d_mesh_t** out);
+/* Same from arrays (berkeley_neigh != NULL selects the Triangle reader's rules). */
+int cfd2d_mesh_build(const cfd2d_mesh_desc* mesh, const int* berkeley_neigh, cfd2d_mesh_t** out);
+int cfd2d_mesh_sizes(const cfd2d_mesh_t* m, int* n_cells, int* n_edges);
+/* Cell::edgesInd/S/c and Edge n1,n2/c1,c2/boundary index/point count/n/l/points
+ * (src/mesh/grid.h:18-67); any pointer may be NULL. */
+int cfd2d_mesh_export(const cfd2d_mesh_t* m, int* cell_edges, double* cell_S, double* cell_c,
+                      int* edge_n12, int* edge_c12, int* edge_bnd, int* edge_npts,
+                      double* edge_n, double* edge_l, double* edge_pts);
+/* The locality order the solver would use: storage cell -> reference cell. */
+int cfd2d_mesh_order(const cfd2d_mesh_t* m, int rcm, int* perm);
+int cfd2d_mesh_free(cfd2d_mesh_t* m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
