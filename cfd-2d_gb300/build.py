@@ -38,7 +38,8 @@ def cuda_home() -> str:
 
 
 HOST_SOURCES = ["xml.cpp", "mesh.cpp", "task.cpp", "solver.cpp", "capi.cpp"]
-DEVICE_SOURCES = {"kern_fp64.cu": "false", "kern_common.cu": "false", "kern_mixed.cu": "true"}
+DEVICE_SOURCES = {"kern_fp64.cu": "false", "kern_common.cu": "false", "kern_mixed.cu": "true",
+                  "noalloc.cu": "false"}
 HEADERS = ["xml.hpp", "mesh.hpp", "task.hpp", "solver.hpp", "kernels.hpp", "kernels.cuh", "kern_inst.cuh"]
 
 

@@ -58,6 +58,8 @@ SIGNATURES = {
     "cfd2d_save_vtk": [_P, _I],
     "cfd2d_timed_steps": [_P, _I, _D],
     "cfd2d_profile_steps": [_P, _I, _D, _IP],
+    "cfd2d_residual_first_order_static": [_I, _I, _P, _P, _P, _P, _P, _I, _IP, _D, C.c_double, C.c_double, _I,
+                                          _P, _P, _P],
     "cfd2d_set_device": [_I],
     "cfd2d_last_error": [C.c_char_p, C.c_size_t],
     "cfd2d_set_verbosity": [_I],

@@ -130,6 +130,35 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
  * calling thread's current device). A solver keeps its device for life. */
 int cfd2d_set_device(int device);
 
+/* ---- fixed-scratch residual (allocates nothing) ------------------------- */
+/* No counterpart in the reference. For callers that cannot allocate device
+ * memory when they call in (recording a CUDA graph, where cudaMalloc is not
+ * allowed during capture; a host framework whose memory pool owns the device;
+ * a real-time loop that forbids allocation after start-up): the first-order
+ * residual R (the reference's ro_int..re_int with the cell-centre states, as
+ * cfd2d_residual returns for RECONSTRUCTION NONE) of the state U, computed with
+ * no cudaMalloc/cudaFree and no allocating library call. Its only scratch, one
+ * FP64 flux per edge, is a fixed device array of CFD2D_STATIC_MAX_EDGES x 4
+ * doubles (8 MiB) in the library, held by every GPU that loads the library
+ * until exit. All pointers except bnd_kind/bnd_par (host, n_bnd <= 16 entries)
+ * are device memory, in the reference's numbering as cfd2d_mesh_export writes
+ * it: cell_edges 3*n_cells (ascending), edge_c12 2*n_edges, edge_n 2*n_edges,
+ * edge_l and edge_bnd n_edges, U and R 4*n_cells. One material (M, Cp); flux
+ * is CFD2D_FLUX_*. Runs asynchronously on stream (a cudaStream_t, NULL = the
+ * default stream). The first call on a device looks up the array's device
+ * address (make it before any stream capture). All calls share the array:
+ * calls that overlap on the GPU race, so order them on one stream. Returns
+ * CFD2D_ERR_CAPACITY when n_edges > CFD2D_STATIC_MAX_EDGES or n_bnd > 16,
+ * CFD2D_ERR_INVALID_ARG for a null pointer, a non-positive size or an unknown
+ * flux, CFD2D_ERR_CUDA when the array lookup or a launch fails; it leaves the
+ * cfd2d_last_error message untouched (setting it could allocate). An index
+ * outside the mesh gives NaN in R, never an out-of-bounds access. */
+#define CFD2D_STATIC_MAX_EDGES 262144
+int cfd2d_residual_first_order_static(int n_cells, int n_edges, const int* cell_edges, const int* edge_c12,
+                                      const double* edge_n, const double* edge_l, const int* edge_bnd, int n_bnd,
+                                      const int* bnd_kind, const double* bnd_par, double M, double Cp, int flux,
+                                      const double* U, double* R, void* stream);
+
 /* Message of the last failed call on this thread. */
 int cfd2d_last_error(char* buf, size_t n);
 /* Log lines (the reference's log(), src/global.cpp:32-46) go to stdout unless
