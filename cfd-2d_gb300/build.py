@@ -79,7 +79,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         out = os.path.join(OBJ, s + ".o")
         objs.append(out)
         if force or _stale(out, [src] + hdrs):
-            jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", f"-fmad={fmad}", "-Xptxas", "-v",
+            extra = ["-use_fast_math"] if fmad == "true" else []
+            jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", f"-fmad={fmad}", *extra, "-Xptxas", "-v",
                          "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INC, "-I", CSRC,
                          "-c", src, "-o", out])
     logs = []

@@ -60,6 +60,7 @@ SIGNATURES = {
     "cfd2d_profile_steps": [_P, _I, _D, _IP],
     "cfd2d_residual_first_order_static": [_I, _I, _P, _P, _P, _P, _P, _I, _IP, _D, C.c_double, C.c_double, _I,
                                           _P, _P, _P],
+    "cfd2d_selftest": [_I, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
     "cfd2d_set_device": [_I],
     "cfd2d_last_error": [C.c_char_p, C.c_size_t],
     "cfd2d_set_verbosity": [_I],
@@ -118,6 +119,13 @@ def mesh_desc(nodes, tris, cell_region, bsegs, bseg_bnd):
     d = MeshDesc(len(keep[0]), _d(keep[0]), len(keep[1]), _i(keep[1]), _i(keep[2]), len(keep[3]), _i(keep[3]),
                  _i(keep[4]))
     return d, keep
+
+
+def selftest(which: int, n: int, seed: int = 1) -> int:
+    """Mismatch count of a device arithmetic helper against the hardware operation."""
+    out = C.c_longlong(-1)
+    check(lib().cfd2d_selftest(int(which), int(n), int(seed), C.byref(out)))
+    return out.value
 
 
 def set_device(device: int):

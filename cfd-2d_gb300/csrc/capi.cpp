@@ -264,6 +264,16 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
     });
 }
 
+int cfd2d_selftest(int which, long long n, unsigned long long seed, long long* mismatches) {
+    return guarded([&] {
+        if (!mismatches || which < 0 || which > 2 || n < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
+        long long r = cfd2d::selftest_arith(which, n, seed);
+        if (r < 0) return fail(CFD2D_ERR_CUDA, "self-test launch failed");
+        *mismatches = r;
+        return CFD2D_OK;
+    });
+}
+
 int cfd2d_set_device(int device) {
     return guarded([&] {
         cudaError_t e = cudaSetDevice(device);

@@ -122,7 +122,48 @@ __global__ void __launch_bounds__(256) k_conservation(const DevCase c, double* _
     if (threadIdx.x == 0)
         for (int k = 0; k < 4; k++) partial[4 * blockIdx.x + k] = sh[k][0];
 }
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {  // splitmix64 finaliser
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+__global__ void k_selftest(int which, long long n, unsigned long long seed, unsigned long long* bad) {
+    unsigned long long local = 0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long r1 = mix64(seed ^ (2 * k)), r2 = mix64(seed ^ (2 * k + 1));
+        if (which == 0) {  // quotients of random doubles over a wide exponent range, by the reciprocal form
+            const double a = __longlong_as_double((long long)(((r1 % 1400) + 324ull) << 52 | (r2 & 0xfffffffffffffull) |
+                                                              (r1 & 0x8000000000000000ull)));
+            const double b = __longlong_as_double((long long)((((r2 >> 52) % 1400) + 324ull) << 52 |
+                                                              (mix64(r1) & 0xfffffffffffffull)));
+            const double y = 1.0 / b;
+            const double q1 = div_rn(a, b, y), q2 = a / b;
+            local += __double_as_longlong(q1) != __double_as_longlong(q2);
+        } else if (which == 1) {  // widening of random normal floats
+            const float f = __uint_as_float((unsigned)(((r1 % 254) + 1) << 23) | (unsigned)(r2 & 0x807fffffu));
+            local += __double_as_longlong(widen(f)) != __double_as_longlong((double)f);
+        } else {  // narrowing of random doubles in float range: within 1 ulp of the hardware's
+            const double d = __longlong_as_double((long long)(((r1 % 250) + 1023 - 124) << 52 | (r2 & 0x800fffffffffffffull)));
+            const int u1 = __float_as_int(narrow(d)), u2 = __float_as_int((float)d);
+            local += (u1 - u2 > 1 || u2 - u1 > 1);
+        }
+    }
+    if (local) atomicAdd(bad, local);
+}
 }  // namespace
+
+long long selftest_arith(int which, long long n, unsigned long long seed) {
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof *d) != cudaSuccess) return -1;
+    cudaMemset(d, 0, sizeof *d);
+    k_selftest<<<1216, 256>>>(which, n, seed, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? (long long)h : -1;
+}
 
 void launch_dt_min(const DevCase& c, unsigned long long* out, cudaStream_t s) {
     k_dt_min<<<nblk(c.nc, 256), 256, 0, s>>>(c, out);

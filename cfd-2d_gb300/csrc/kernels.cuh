@@ -59,16 +59,84 @@ __device__ __forceinline__ DevMat mat_of(const DevCase& c, int cell) {
     return c.cmat ? c.mats[c.cmat[cell]] : c.mat0;
 }
 
+// Records gathered by index are stored as array-of-structures so a neighbour's
+// data arrives in 16-byte vector loads: W (r, u, v, p) and F (4 fluxes) are one
+// 4-vector per cell / edge, G (8 gradient components) two.
+__device__ __forceinline__ void ld4(const float* __restrict__ p, int i, float* v) {
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p) + i);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ld4(const double* __restrict__ p, int i, double* v) {
+    const double2* q = reinterpret_cast<const double2*>(p) + 2 * (size_t)i;
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float* __restrict__ p, int i, float a0, float a1, float a2, float a3) {
+    reinterpret_cast<float4*>(p)[i] = make_float4(a0, a1, a2, a3);
+}
+__device__ __forceinline__ void st4(double* __restrict__ p, int i, double a0, double a1, double a2, double a3) {
+    double2* q = reinterpret_cast<double2*>(p) + 2 * (size_t)i;
+    q[0] = make_double2(a0, a1);
+    q[1] = make_double2(a2, a3);
+}
 template <typename T>
-__device__ __forceinline__ Prim<T> load_prim(const T* __restrict__ W, int n, int i) {
+__device__ __forceinline__ void ld8(const T* __restrict__ p, int i, T* v) {
+    ld4(p, 2 * i, v);
+    ld4(p, 2 * i + 1, v + 4);
+}
+template <typename T>
+__device__ __forceinline__ void st8(T* __restrict__ p, int i, const T* v) {
+    st4(p, 2 * i, v[0], v[1], v[2], v[3]);
+    st4(p, 2 * i + 1, v[4], v[5], v[6], v[7]);
+}
+
+template <typename T>
+__device__ __forceinline__ Prim<T> load_prim(const T* __restrict__ W, int i) {
+    T v[4];
+    ld4(W, i, v);
     Prim<T> q;
-    q.r = W[i]; q.u = W[n + i]; q.v = W[2 * n + i]; q.p = W[3 * n + i];
+    q.r = v[0]; q.u = v[1]; q.v = v[2]; q.p = v[3];
     return q;
 }
 
 template <typename T>
-__device__ __forceinline__ void store_prim(T* __restrict__ W, int n, int i, const Prim<T>& q) {
-    W[i] = q.r; W[n + i] = q.u; W[2 * n + i] = q.v; W[3 * n + i] = q.p;
+__device__ __forceinline__ void store_prim(T* __restrict__ W, int i, const Prim<T>& q) {
+    st4(W, i, q.r, q.u, q.v, q.p);
+}
+
+// Material constants in the face precision (the mixed form keeps FP32 copies so
+// its face kernels issue no FP64 instruction).
+template <typename T> struct MatT { T M, Cv, gm1; };
+template <typename T> __device__ __forceinline__ MatT<T> matT_of(const DevCase& c, int cell);
+template <> __device__ __forceinline__ MatT<double> matT_of<double>(const DevCase& c, int cell) {
+    const DevMat m = c.cmat ? c.mats[c.cmat[cell]] : c.mat0;
+    return MatT<double>{m.M, m.Cv, m.gm1};
+}
+template <> __device__ __forceinline__ MatT<float> matT_of<float>(const DevCase& c, int cell) {
+    if (!c.cmat) return MatT<float>{c.mat0_f[0], c.mat0_f[1], c.mat0_f[2]};
+    const DevMat m = c.mats[c.cmat[cell]];
+    return MatT<float>{float(m.M), float(m.Cv), float(m.gm1)};
+}
+template <typename T> __device__ __forceinline__ T gam_of(const DevCase& c);
+template <> __device__ __forceinline__ double gam_of<double>(const DevCase& c) { return c.gam_flux; }
+template <> __device__ __forceinline__ float gam_of<float>(const DevCase& c) { return c.gam_flux_f; }
+
+// a / b correctly rounded from y = RN(1/b): q = RN(a y), r = a - b q exactly
+// (one FMA), result RN(q + r y) (Markstein, "IA-64 and Elementary Functions",
+// 2000, the division theorem). Three FP64 instructions instead of a full
+// division; the exponent guard keeps a, y and the quotient far from underflow
+// and overflow, where the theorem needs no extra conditions, and divides
+// outright otherwise (zero, subnormal, huge, inf, NaN).
+__device__ __forceinline__ double div_rn(double a, double b, double y) {
+    const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+    const int ey = (int)((__double_as_longlong(y) >> 52) & 0x7ff);
+    const int eq = ea + ey - 1023;
+    if (ea > 0x100 && ea < 0x700 && ey > 0x100 && ey < 0x700 && eq > 0x100 && eq < 0x700) {
+        const double q = a * y;
+        const double r = fma(-q, b, a);
+        return fma(r, y, q);
+    }
+    return a / b;
 }
 
 // convertConsToPar + Material::URS(0), src/methods/fvm_tvd.cpp:803-813, src/global.cpp:15-18
@@ -76,9 +144,17 @@ template <typename T>
 __device__ __forceinline__ Prim<T> cons2prim(T ro, T ru, T rv, T re, T gm1) {
     Prim<T> q;
     q.r = ro;
-    q.u = ru / ro;
-    q.v = rv / ro;
-    T E = re / ro;
+    T E;
+    if constexpr (sizeof(T) == 8) {  // the three quotients by ro share one reciprocal
+        const double y = 1.0 / ro;
+        q.u = div_rn(ru, ro, y);
+        q.v = div_rn(rv, ro, y);
+        E = div_rn(re, ro, y);
+    } else {
+        q.u = ru / ro;
+        q.v = rv / ro;
+        E = re / ro;
+    }
     T e = E - T(0.5) * (q.u * q.u + q.v * q.v);
     q.p = q.r * e * gm1;
     return q;
@@ -111,11 +187,23 @@ __device__ __forceinline__ Prim<T> ghost_state(const DevBnd& b, const Prim<T>& q
     return g;
 }
 
-// MINMOD, src/methods/LimiterDGCockburn.cpp:110-123
-template <typename T>
-__device__ __forceinline__ T minmod(T a, T b) {
-    if (a * b > T(0)) return t_abs(a) < t_abs(b) ? a : b;
-    return T(0);
+// MINMOD, src/methods/LimiterDGCockburn.cpp:110-123: a*b > 0 ? (|a| < |b| ? a : b) : 0.
+// The sign test reads the bits of the rounded product a*b (positive, non-NaN
+// doubles are exactly the patterns in (0, 0x7ff0...0]) and |a| < |b| compares
+// magnitude bits, which orders non-NaN values like fabs does; the result is the
+// reference's bit for bit with one FP64 multiply instead of three FP64 compares.
+__device__ __forceinline__ double minmod(double a, double b) {
+    const long long pb = __double_as_longlong(a * b);
+    if (pb <= 0 || pb > 0x7ff0000000000000ll) return 0.0;
+    const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffll;
+    const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffll;
+    return ma < mb ? a : b;
+}
+__device__ __forceinline__ float minmod(float a, float b) {
+    const int pb = __float_as_int(a * b);
+    if (pb <= 0 || pb > 0x7f800000) return 0.0f;
+    const int ma = __float_as_int(a) & 0x7fffffff, mb = __float_as_int(b) & 0x7fffffff;
+    return ma < mb ? a : b;
 }
 
 // ------------------------------------------------------------------ fluxes
@@ -282,14 +370,17 @@ __device__ __forceinline__ void phys_flux(T* f, T r, T u, T v, T p, T E, T un, T
     f[3] = (E + p) * un;
 }
 
-// HLLC (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, sec. 10.4-10.5),
-// Davis wave speeds S_L = min(unL-cL, unR-cR), S_R = max(unL+cL, unR+cR).
+// HLLC (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, sec. 10.4-10.6),
+// Davis wave speeds S_L = min(unL-cL, unR-cR), S_R = max(unL+cL, unR+cR), star flux
+// F*_K = [S*(S_K U_K - F_K) + S_K p* D*] / (S_K - S*), D* = (0, nx, ny, S*),
+// p* = p_K + rho_K (S_K - un_K)(S* - un_K): one division instead of Toro's star state.
 template <typename T>
 __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM) {
+    const T IG1 = T(1.0) / (GAM - T(1.0));
     T cL = t_sqrt(GAM * L.p / L.r), cR = t_sqrt(GAM * R.p / R.r);
     T unL = L.u * nx + L.v * ny, unR = R.u * nx + R.v * ny;
-    T EL = L.p / (GAM - T(1.0)) + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
-    T ER = R.p / (GAM - T(1.0)) + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    T EL = L.p * IG1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
+    T ER = R.p * IG1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
     T SL = t_min(unL - cL, unR - cR), SR = t_max(unL + cL, unR + cR);
     if (SL >= T(0.0)) { phys_flux(f, L.r, L.u, L.v, L.p, EL, unL, nx, ny); return; }
     if (SR <= T(0.0)) { phys_flux(f, R.r, R.u, R.v, R.p, ER, unR, nx, ny); return; }
@@ -300,16 +391,13 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
     T SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
     T FK[4];
     phys_flux(FK, K.r, K.u, K.v, K.p, EK, unK, nx, ny);
-    T fac = mK / (SK - Ss);
-    T ds = Ss - unK;
-    T U0 = fac;
-    T U1 = fac * (K.u + ds * nx);
-    T U2 = fac * (K.v + ds * ny);
-    T U3 = fac * (EK / K.r + ds * (Ss + K.p / mK));
-    f[0] = FK[0] + SK * (U0 - K.r);
-    f[1] = FK[1] + SK * (U1 - K.r * K.u);
-    f[2] = FK[2] + SK * (U2 - K.r * K.v);
-    f[3] = FK[3] + SK * (U3 - EK);
+    T ps = K.p + mK * (Ss - unK);
+    T inv = T(1.0) / (SK - Ss);
+    T sp = SK * ps;
+    f[0] = (Ss * (SK * K.r - FK[0])) * inv;
+    f[1] = (Ss * (SK * (K.r * K.u) - FK[1]) + sp * nx) * inv;
+    f[2] = (Ss * (SK * (K.r * K.v) - FK[2]) + sp * ny) * inv;
+    f[3] = (Ss * (SK * EK - FK[3]) + sp * Ss) * inv;
 }
 
 // Roe flux (Roe 1981) in the face-normal frame with the Harten-Hyman entropy fix
@@ -317,10 +405,10 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
 // where |lam~| < delta. Roe averages as in roe_orig (src/global.cpp:407-441).
 template <typename T>
 __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM) {
-    T G1 = GAM - T(1.0);
+    T G1 = GAM - T(1.0), IG1 = T(1.0) / (GAM - T(1.0));
     T unL = L.u * nx + L.v * ny, unR = R.u * nx + R.v * ny;
-    T EL = L.p / G1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
-    T ER = R.p / G1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    T EL = L.p * IG1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
+    T ER = R.p * IG1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
     T HL = (EL + L.p) / L.r, HR = (ER + R.p) / R.r;
     T sL = t_sqrt(L.r), sR = t_sqrt(R.r);
     T w = T(1.0) / (sL + sR);
@@ -330,13 +418,14 @@ __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& 
     T q2 = ut * ut + vt * vt;
     T c2 = G1 * (Ht - T(0.5) * q2);
     T c = t_sqrt(c2);
+    T ic2 = T(1.0) / c2;
     T unt = ut * nx + vt * ny;
     T rt = sL * sR;
     T dr = R.r - L.r, dp = R.p - L.p, dun = unR - unL;
     T dtx = (R.u - L.u) - dun * nx, dty = (R.v - L.v) - dun * ny;
-    T a1 = (dp - rt * c * dun) / (T(2.0) * c2);
-    T a2 = dr - dp / c2;
-    T a4 = (dp + rt * c * dun) / (T(2.0) * c2);
+    T a1 = (dp - rt * c * dun) * (T(0.5) * ic2);
+    T a2 = dr - dp * ic2;
+    T a4 = (dp + rt * c * dun) * (T(0.5) * ic2);
     T l1 = unt - c, l4 = unt + c;
     T cL = t_sqrt(GAM * L.p / L.r), cR = t_sqrt(GAM * R.p / R.r);
     T d1 = t_max(T(0.0), t_max(l1 - (unL - cL), (unR - cR) - l1));
@@ -369,15 +458,16 @@ __device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& 
 // ------------------------------------------------------------------ kernels
 
 // Green-Gauss gradients of r, p, u, v (calcGrad, src/methods/fvm_tvd.cpp:242-301),
-// gathered per cell over its faces in ascending original edge order.
+// gathered per cell over its faces in ascending original edge order. FP64 divides
+// by S like the reference; the mixed form multiplies by 1/S in FP32.
 template <typename T>
 __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
     const int nc = c.nc;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     const T* __restrict__ W = W_of<T>(c);
-    const Prim<T> q = load_prim(W, nc, i);
-    T g0 = T(0.0), g1 = T(0.0), g2 = T(0.0), g3 = T(0.0), g4 = T(0.0), g5 = T(0.0), g6 = T(0.0), g7 = T(0.0);
+    const Prim<T> q = load_prim(W, i);
+    T g[8] = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const int f = c.face[k * nc + i];
@@ -387,28 +477,29 @@ __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
         Prim<T> o;
         const int j = side2 ? c.ec1[e] : c.ec2[e];
         if (j >= 0) {
-            o = load_prim(W, nc, j);
+            o = load_prim(W, j);
         } else {
-            const DevMat mt = mat_of(c, i);
-            const T Tc = temperature(q, T(mt.gm1), T(mt.Cv));
-            o = ghost_state(c.bnds[c.ebnd[e]], q, Tc, nx, ny, T(mt.M));
+            const MatT<T> mt = matT_of<T>(c, i);
+            const T Tc = temperature(q, mt.gm1, mt.Cv);
+            o = ghost_state(c.bnds[c.ebnd[e]], q, Tc, nx, ny, mt.M);
         }
         const T hr = (q.r + o.r) / T(2), hp = (q.p + o.p) / T(2);
         const T hu = (q.u + o.u) / T(2), hv = (q.v + o.v) / T(2);
-        const T ax = hr * nx * l, ay = hr * ny * l, bx = hp * nx * l, by = hp * ny * l;
-        const T cx = hu * nx * l, cy = hu * ny * l, dx = hv * nx * l, dy = hv * ny * l;
-        if (side2) {
-            g0 = g0 - ax; g1 = g1 - ay; g2 = g2 - bx; g3 = g3 - by;
-            g4 = g4 - cx; g5 = g5 - cy; g6 = g6 - dx; g7 = g7 - dy;
-        } else {
-            g0 = g0 + ax; g1 = g1 + ay; g2 = g2 + bx; g3 = g3 + by;
-            g4 = g4 + cx; g5 = g5 + cy; g6 = g6 + dx; g7 = g7 + dy;
-        }
+        const T v[8] = {hr * nx * l, hr * ny * l, hp * nx * l, hp * ny * l,
+                        hu * nx * l, hu * ny * l, hv * nx * l, hv * ny * l};
+#pragma unroll
+        for (int m = 0; m < 8; m++) g[m] = side2 ? g[m] - v[m] : g[m] + v[m];
     }
-    const T s = T(c.S[i]);
-    T* __restrict__ G = G_of<T>(c);
-    G[i] = g0 / s; G[nc + i] = g1 / s; G[2 * nc + i] = g2 / s; G[3 * nc + i] = g3 / s;
-    G[4 * nc + i] = g4 / s; G[5 * nc + i] = g5 / s; G[6 * nc + i] = g6 / s; G[7 * nc + i] = g7 / s;
+    if constexpr (sizeof(T) == 8) {
+        const double s = c.S[i], y = c.invS[i];  // y = RN(1/S), computed on the host
+#pragma unroll
+        for (int m = 0; m < 8; m++) g[m] = div_rn(g[m], s, y);
+    } else {
+        const float is = c.invS32[i];
+#pragma unroll
+        for (int m = 0; m < 8; m++) g[m] = g[m] * is;
+    }
+    st8(G_of<T>(c), i, g);
 }
 
 template <typename T, int RECON>
@@ -429,35 +520,31 @@ __device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, 
 // Edge flux over the edge's two Gauss points, times l/2 (src/methods/fvm_tvd.cpp:329-352).
 template <typename T, int FLUX, int RECON>
 __global__ void __launch_bounds__(256) k_flux(const DevCase c) {
-    const int ne = c.ne, nc = c.nc;
+    const int ne = c.ne;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;
     const T* __restrict__ W = W_of<T>(c);
     const T* __restrict__ G = G_of<T>(c);
     const T* __restrict__ DL = DL_of<T>(c);
     const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
-    const T GAM = T(c.gam_flux);
+    const T GAM = gam_of<T>(c);
     const int c1 = c.ec1[e];
     const bool inner = e < c.n_int;
-    const Prim<T> qL = load_prim(W, nc, c1);
+    const Prim<T> qL = load_prim(W, c1);
     T gL[8], gR[8];
-    if (RECON != RECON_NONE)
-#pragma unroll
-        for (int k = 0; k < 8; k++) gL[k] = G[k * nc + c1];
+    if (RECON != RECON_NONE) ld8(G, c1, gL);
     Prim<T> qR = qL, gc = qL;
     DevBnd b{};
     T Tc = T(0), M = T(0);
     if (inner) {
         const int c2 = c.ec2[e];
-        qR = load_prim(W, nc, c2);
-        if (RECON != RECON_NONE)
-#pragma unroll
-            for (int k = 0; k < 8; k++) gR[k] = G[k * nc + c2];
+        qR = load_prim(W, c2);
+        if (RECON != RECON_NONE) ld8(G, c2, gR);
     } else {
         b = c.bnds[c.ebnd[e]];
-        const DevMat mt = mat_of(c, c1);
-        Tc = temperature(qL, T(mt.gm1), T(mt.Cv));
-        M = T(mt.M);
+        const MatT<T> mt = matT_of<T>(c, c1);
+        Tc = temperature(qL, mt.gm1, mt.Cv);
+        M = mt.M;
         if (RECON == RECON_MINMOD) gc = ghost_state(b, qL, Tc, nx, ny, M);
     }
     T fs[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
@@ -484,19 +571,93 @@ __global__ void __launch_bounds__(256) k_flux(const DevCase c) {
     }
     if (hit) atomicOr(c.err, ERRBIT_NEWTON_CAP);
     const T lh = l * T(0.5);
-    T* __restrict__ F = F_of<T>(c);
-    F[e] = fs[0] * lh; F[ne + e] = fs[1] * lh; F[2 * ne + e] = fs[2] * lh; F[3 * ne + e] = fs[3] * lh;
+    st4(F_of<T>(c), e, fs[0] * lh, fs[1] * lh, fs[2] * lh, fs[3] * lh);
+}
+
+// FP32 <-> FP64 conversions on the integer pipe. GB300's FP64 unit issues ~2
+// instructions per clock and SM, and the hardware conversions run there; these
+// bit-level versions keep the mixed form's update kernel off that unit.
+// Widening is exact for zero, normal, infinite and NaN floats (the mixed kernels
+// run with FTZ, so no subnormal float reaches it; one would read as zero).
+__device__ __forceinline__ double widen(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned ex = (b >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
+    if (ex == 0) return __longlong_as_double((long long)sgn);
+    const unsigned long long e64 = ex == 0xffu ? 0x7ffull : (unsigned long long)(ex + (1023 - 127));
+    return __longlong_as_double((long long)(sgn | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// Narrowing rounds to nearest (ties away from zero), flushes below FLT_MIN to
+// zero, saturates to infinity and keeps NaN a NaN.
+__device__ __forceinline__ float narrow(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ffull);
+    if (e == 0x7ff) return __uint_as_float(sgn | ((b & 0xfffffffffffffull) ? 0x7fc00000u : 0x7f800000u));
+    const int ef = e - 1023 + 127;
+    if (ef <= 0) return __uint_as_float(sgn);
+    if (ef >= 0xff) return __uint_as_float(sgn | 0x7f800000u);
+    const unsigned m = (unsigned)(b >> 29) & 0x7fffffu;
+    const unsigned rnd = (unsigned)(b >> 28) & 1u;
+    return __uint_as_float((sgn | ((unsigned)ef << 23) | m) + rnd);  // a carry moves into the exponent
+}
+
+// Knuth's TwoSum: s + e == a + b exactly (round to nearest, no reassociation).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Residual of cell i: the reference's ro_int..re_int (src/methods/fvm_tvd.cpp:353-363).
+// FP64 faces: 0 -/+ F in ascending original edge order, the reference's own sums.
+// FP32 faces: the three signed fluxes summed exactly as an FP32 pair, then rounded
+// once into FP64 (as accurate as an FP64 sum of the same three values).
+template <typename T>
+__device__ __forceinline__ void gather_residual(const DevCase& c, int i, double* R) {
+    const int nc = c.nc;
+    const T* __restrict__ F = F_of<T>(c);
+    if constexpr (sizeof(T) == 8) {
+        R[0] = 0.0; R[1] = 0.0; R[2] = 0.0; R[3] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int f = c.face[k * nc + i];
+            double v[4];
+            ld4(F, f >> 1, v);
+#pragma unroll
+            for (int q = 0; q < 4; q++) R[q] = (f & 1) ? R[q] + v[q] : R[q] - v[q];
+        }
+    } else {
+        float t[3][4];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const int f = c.face[k * nc + i];
+            float v[4];
+            ld4(F, f >> 1, v);
+#pragma unroll
+            for (int q = 0; q < 4; q++) t[k][q] = (f & 1) ? v[q] : -v[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float s1, e1, s2, e2;
+            two_sum(t[0][q], t[1][q], s1, e1);
+            two_sum(s1, t[2][q], s2, e2);
+            R[q] = widen(s2) + widen(e1 + e2);
+        }
+    }
 }
 
 template <typename T>
-__device__ __forceinline__ Prim<T> prim_face_of(double ro, double ru, double rv, double re, double gm1);
+__device__ __forceinline__ Prim<T> prim_face_of(double ro, double ru, double rv, double re, const DevCase& c, int i);
 template <>
-__device__ __forceinline__ Prim<double> prim_face_of<double>(double ro, double ru, double rv, double re, double gm1) {
-    return cons2prim<double>(ro, ru, rv, re, gm1);
+__device__ __forceinline__ Prim<double> prim_face_of<double>(double ro, double ru, double rv, double re,
+                                                             const DevCase& c, int i) {
+    return cons2prim<double>(ro, ru, rv, re, mat_of(c, i).gm1);
 }
 template <>
-__device__ __forceinline__ Prim<float> prim_face_of<float>(double ro, double ru, double rv, double re, double gm1) {
-    return cons2prim<float>(float(ro), float(ru), float(rv), float(re), float(gm1));
+__device__ __forceinline__ Prim<float> prim_face_of<float>(double ro, double ru, double rv, double re,
+                                                           const DevCase& c, int i) {
+    return cons2prim<float>(narrow(ro), narrow(ru), narrow(rv), narrow(re), matT_of<float>(c, i).gm1);
 }
 
 // local time step of one cell (calcTimeStep STEADY branch, src/methods/fvm_tvd.cpp:218-224)
@@ -507,18 +668,25 @@ __device__ __forceinline__ void local_dt(const DevCase& c, int i, const Prim<dou
     c.cfl[i] = t / c.S[i];
 }
 
-__device__ __forceinline__ bool outside_limits(const DevCase& c, const Prim<double>& q) {  // :439-446
-    return q.r < c.lim_rmin || q.r > c.lim_rmax || q.p < c.lim_pmin || q.p > c.lim_pmax ||
-           fabs(q.u) > c.lim_umax || fabs(q.v) > c.lim_umax;
+template <typename T>
+__device__ __forceinline__ bool outside_limits(const DevCase& c, const Prim<T>& q) {  // :439-446
+    if constexpr (sizeof(T) == 8)
+        return q.r < c.lim_rmin || q.r > c.lim_rmax || q.p < c.lim_pmin || q.p > c.lim_pmax ||
+               fabs(q.u) > c.lim_umax || fabs(q.v) > c.lim_umax;
+    else
+        return q.r < c.lim_f[0] || q.r > c.lim_f[1] || q.p < c.lim_f[2] || q.p > c.lim_f[3] ||
+               fabsf(q.u) > c.lim_f[4] || fabsf(q.v) > c.lim_f[4];
 }
 
 // One Runge-Kutta stage update with the residual gathered from the edge fluxes.
 // SCHEME/STAGE: Euler (0), Heun (0,1; src/methods/fvm_tvd.cpp:366-447), SSP-RK3 Shu-Osher (0,1,2).
+// The last stage checks the limits (in the face precision) and, for a local time
+// step, computes the next step's cTau in FP64.
 template <typename T, int SCHEME, int STAGE>
 __global__ void __launch_bounds__(256) k_update(const DevCase c) {
     constexpr bool FINAL = (SCHEME == TIME_EULER && STAGE == 0) || (SCHEME == TIME_HEUN && STAGE == 1) ||
                            (SCHEME == TIME_SSPRK3 && STAGE == 2);
-    const int nc = c.nc, ne = c.ne;
+    const int nc = c.nc;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     if (STAGE == 0 && c.steady) c.ctau[i] = c.ctau_next[i];  // the step now running uses ctau_next
@@ -529,20 +697,12 @@ __global__ void __launch_bounds__(256) k_update(const DevCase c) {
         if (FINAL) atomicAdd(c.n_lim, 1);
         return;
     }
-    const T* __restrict__ F = F_of<T>(c);
-    double R0 = 0.0, R1 = 0.0, R2 = 0.0, R3 = 0.0;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const int f = c.face[k * nc + i];
-        const int e = f >> 1;
-        const double f0 = double(F[e]), f1 = double(F[ne + e]), f2 = double(F[2 * ne + e]), f3 = double(F[3 * ne + e]);
-        if (f & 1) { R0 = R0 + f0; R1 = R1 + f1; R2 = R2 + f2; R3 = R3 + f3; }
-        else { R0 = R0 - f0; R1 = R1 - f1; R2 = R2 - f2; R3 = R3 - f3; }
-    }
+    double R[4];
+    gather_residual<T>(c, i, R);
     const double cf = c.cfl[i];
     const double* __restrict__ src = STAGE == 0 ? c.A : c.B;
-    double u0 = src[i] + cf * R0, u1 = src[nc + i] + cf * R1, u2 = src[2 * nc + i] + cf * R2,
-           u3 = src[3 * nc + i] + cf * R3;
+    double u0 = src[i] + cf * R[0], u1 = src[nc + i] + cf * R[1], u2 = src[2 * nc + i] + cf * R[2],
+           u3 = src[3 * nc + i] + cf * R[3];
     double* dst = FINAL ? c.A : c.B;
     if (SCHEME == TIME_HEUN && STAGE == 1) {
         u0 = 0.5 * (c.A[i] + u0); u1 = 0.5 * (c.A[nc + i] + u1);
@@ -556,20 +716,18 @@ __global__ void __launch_bounds__(256) k_update(const DevCase c) {
         u2 = c13 * c.A[2 * nc + i] + c23 * u2; u3 = c13 * c.A[3 * nc + i] + c23 * u3;
     }
     dst[i] = u0; dst[nc + i] = u1; dst[2 * nc + i] = u2; dst[3 * nc + i] = u3;
-    const DevMat mt = mat_of(c, i);
+    const Prim<T> w = prim_face_of<T>(u0, u1, u2, u3, c, i);
+    store_prim(Wm_of<T>(c), i, w);
     if (FINAL) {
-        const Prim<double> q = cons2prim<double>(u0, u1, u2, u3, mt.gm1);
-        if (outside_limits(c, q)) {
+        if (outside_limits(c, w)) {
             c.flags[i] |= 0x2u;
             atomicAdd(c.n_lim, 1);
         }
-        if (!(q.r > 0.0) || !(q.p > 0.0)) atomicOr(c.err, ERRBIT_NONPHYSICAL);
-        if (c.steady) local_dt(c, i, q, mt);
-        Prim<T> w;
-        w.r = T(q.r); w.u = T(q.u); w.v = T(q.v); w.p = T(q.p);
-        store_prim(Wm_of<T>(c), nc, i, w);
-    } else {
-        store_prim(Wm_of<T>(c), nc, i, prim_face_of<T>(u0, u1, u2, u3, mt.gm1));
+        if (!(w.r > T(0)) || !(w.p > T(0))) atomicOr(c.err, ERRBIT_NONPHYSICAL);
+        if (c.steady) {
+            const DevMat mt = mat_of(c, i);
+            local_dt(c, i, cons2prim<double>(u0, u1, u2, u3, mt.gm1), mt);
+        }
     }
 }
 
@@ -580,6 +738,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) k_remediate(const DevCase c) {
     __shared__ int list[1024];
     __shared__ int cnt;
+    __shared__ int wsum[32];
     const int nc = c.nc;
     if (*c.n_lim == 0) return;
     for (int base = 0; base < nc; base += blockDim.x) {
@@ -587,7 +746,6 @@ __global__ void __launch_bounds__(1024) k_remediate(const DevCase c) {
         const int i = o < nc ? c.iperm[o] : -1;
         const bool fl = o < nc && (c.flags[i] & 0x2u);
         const unsigned ball = __ballot_sync(0xffffffffu, fl);
-        __shared__ int wsum[32];
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         if (lane == 0) wsum[warp] = __popc(ball);
         __syncthreads();
@@ -617,11 +775,8 @@ __global__ void __launch_bounds__(1024) k_remediate(const DevCase c) {
                 if (f & 0x200000u) f &= 0x001110u;
                 c.flags[ci] = f;
                 const DevMat mt = mat_of(c, ci);
-                const Prim<double> q = cons2prim<double>(u0, u1, u2, u3, mt.gm1);
-                if (c.steady) local_dt(c, ci, q, mt);
-                Prim<T> w;
-                w.r = T(q.r); w.u = T(q.u); w.v = T(q.v); w.p = T(q.p);
-                store_prim(Wm_of<T>(c), nc, ci, w);
+                if (c.steady) local_dt(c, ci, cons2prim<double>(u0, u1, u2, u3, mt.gm1), mt);
+                store_prim(Wm_of<T>(c), ci, prim_face_of<T>(u0, u1, u2, u3, c, ci));
             }
         }
         __syncthreads();
@@ -635,33 +790,23 @@ __global__ void __launch_bounds__(256) k_prims(const DevCase c) {
     const int nc = c.nc;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
-    const DevMat mt = mat_of(c, i);
-    const Prim<double> q = cons2prim<double>(c.A[i], c.A[nc + i], c.A[2 * nc + i], c.A[3 * nc + i], mt.gm1);
+    const double u0 = c.A[i], u1 = c.A[nc + i], u2 = c.A[2 * nc + i], u3 = c.A[3 * nc + i];
     if (c.steady) {
-        local_dt(c, i, q, mt);
+        const DevMat mt = mat_of(c, i);
+        local_dt(c, i, cons2prim<double>(u0, u1, u2, u3, mt.gm1), mt);
         c.ctau[i] = c.ctau_next[i];
     }
-    Prim<T> w;
-    w.r = T(q.r); w.u = T(q.u); w.v = T(q.v); w.p = T(q.p);
-    store_prim(Wm_of<T>(c), nc, i, w);
+    store_prim(Wm_of<T>(c), i, prim_face_of<T>(u0, u1, u2, u3, c, i));
 }
 
 // Residual of the current edge fluxes (the reference's *_int arrays) for every cell.
 template <typename T>
 __global__ void __launch_bounds__(256) k_residual(const DevCase c, double* __restrict__ R) {
-    const int nc = c.nc, ne = c.ne;
+    const int nc = c.nc;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
-    const T* __restrict__ F = F_of<T>(c);
-    double r[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int k = 0; k < 3; k++) {
-        const int f = c.face[k * nc + i];
-        const int e = f >> 1;
-        for (int q = 0; q < 4; q++) {
-            const double v = double(F[q * ne + e]);
-            r[q] = (f & 1) ? r[q] + v : r[q] - v;
-        }
-    }
+    double r[4];
+    gather_residual<T>(c, i, r);
     for (int q = 0; q < 4; q++) R[q * nc + i] = r[q];
 }
 

@@ -4,13 +4,13 @@
 // chosen on the host; "original" numbers are the reference's cell and edge
 // numbers, src/mesh/MeshReaderSalomeUnv.cpp:118-217):
 //   cells (nc):  conserved state A[4][nc] and stage state B[4][nc] (FP64),
-//                primitives W[4][nc] (r, u, v, p) and Green-Gauss gradients
-//                G[8][nc] in the face precision, cfl[nc] = cTau/S, cTau[nc],
+//                primitives W[nc][4] (r, u, v, p) and Green-Gauss gradients
+//                G[nc][8] in the face precision (records, gathered by index), cfl[nc] = cTau/S, cTau[nc],
 //                flags[nc], faces face[3][nc] = (edge << 1) | side ordered by
 //                ascending original edge number, S[nc], rem_nb[3][nc].
 //   edges (ne):  c1/c2[ne] (c2 = -1 for boundary edges, which are stored last),
 //                nx, ny, l[ne], Gauss-point offsets dl[8][ne] from each side's
-//                centroid (gp0: dxL dyL dxR dyR, gp1: ...), edge flux F[4][ne]
+//                centroid (gp0: dxL dyL dxR dyR, gp1: ...), edge flux F[ne][4]
 //                (already multiplied by l/2), boundary index bnd[ne].
 #pragma once
 #include <cstdint>
@@ -55,6 +55,7 @@ struct DevCase {
     const float* l32;
     const float* dl32;
     const double* S;       // nc
+    const double* invS;    // nc, RN(1/S) (FP64 form)
     const int* rem_nb;     // 3*nc
     const int* iperm;      // original cell -> storage cell
     const uint8_t* cmat;   // nc, nullptr when one material
@@ -62,6 +63,10 @@ struct DevCase {
     const DevMat* mats;
     const DevBnd* bnds;
     DevMat mat0;
+    float mat0_f[3];       // M, Cv, gam-1 of material 0 in FP32 (mixed form)
+    float gam_flux_f;
+    float lim_f[5];        // limits in FP32 (mixed form)
+    const float* invS32;   // nc, 1/S in FP32 (mixed form)
     double gam_flux;
     double cfl_number;
     double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
@@ -103,6 +108,9 @@ void launch_permute_scalar(const DevCase& c, const double* src_store, double* ds
 void launch_permute_flags(const DevCase& c, const unsigned* src_store, unsigned* dst_orig, cudaStream_t s);
 // residual of one stage (the reference's ro_int..re_int) in storage order
 void launch_residual(const DevCase& c, int precision, double* R, cudaStream_t s);
+// built-in checks of the arithmetic helpers against the hardware operations
+// (which: 0 div_rn vs '/', 1 widen vs (double), 2 narrow vs (float) within 1 ulp)
+long long selftest_arith(int which, long long n, unsigned long long seed);
 // deterministic FP64 sums of S*U over cells (mass, x/y momentum, energy)
 void launch_conservation(const DevCase& c, double* partial, int nblocks, cudaStream_t s);
 

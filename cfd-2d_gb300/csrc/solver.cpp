@@ -103,7 +103,13 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
             c.ny32 = upload(to_f32(lay_.ny));
             c.l32 = upload(to_f32(lay_.l));
             c.dl32 = upload(to_f32(lay_.dl));
+            std::vector<float> is(nc);
+            for (int i = 0; i < nc; i++) is[i] = (float)(1.0 / lay_.S[i]);
+            c.invS32 = upload(is);
         } else {
+            std::vector<double> is(nc);
+            for (int i = 0; i < nc; i++) is[i] = 1.0 / lay_.S[i];
+            c.invS = upload(is);
             c.nx = upload(lay_.nx);
             c.ny = upload(lay_.ny);
             c.l = upload(lay_.l);
@@ -120,6 +126,7 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
         }
         c.mats = upload(mats);
         c.mat0 = mats[0];
+        c.mat0_f[0] = (float)mats[0].M; c.mat0_f[1] = (float)mats[0].Cv; c.mat0_f[2] = (float)mats[0].gm1;
         if (mats.size() > 1) c.cmat = upload(lay_.cmat);
         std::vector<DevBnd> bnds;
         for (auto& b : task_.bnds) {
@@ -131,6 +138,9 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
         if (bnds.empty()) bnds.push_back(DevBnd{});
         c.bnds = upload(bnds);
         c.gam_flux = 1.4;  // hard-coded in FVM_TVD::run, src/methods/fvm_tvd.cpp:345,398
+        c.gam_flux_f = 1.4f;
+        c.lim_f[0] = (float)task_.lim_rmin; c.lim_f[1] = (float)task_.lim_rmax;
+        c.lim_f[2] = (float)task_.lim_pmin; c.lim_f[3] = (float)task_.lim_pmax; c.lim_f[4] = (float)task_.lim_umax;
         c.cfl_number = task_.cfl;
         c.lim_rmin = task_.lim_rmin; c.lim_rmax = task_.lim_rmax;
         c.lim_pmin = task_.lim_pmin; c.lim_pmax = task_.lim_pmax; c.lim_umax = task_.lim_umax;

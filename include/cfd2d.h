@@ -126,6 +126,13 @@ int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms);
  * the total device ms and the number of launches (the steps are taken). */
 int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_launches[4]);
 
+/* Built-in check of the device arithmetic helpers on n seeded random operands,
+ * against the hardware operation on the current device: which = 0 FP64 division
+ * through a precomputed reciprocal (must equal '/' bit for bit), 1 FP32->FP64
+ * widening on the integer pipe (must equal the conversion), 2 FP64->FP32
+ * narrowing on the integer pipe (within 1 ulp). *mismatches receives the count. */
+int cfd2d_selftest(int which, long long n, unsigned long long seed, long long* mismatches);
+
 /* Select the CUDA device that cfd2d_create* places new solvers on (default: the
  * calling thread's current device). A solver keeps its device for life. */
 int cfd2d_set_device(int device);

@@ -452,13 +452,19 @@ static void phys_flux(double* f, double r, double u, double v, double p, double 
 }
 
 /* HLLC flux (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics,
- * 3rd ed., sec. 10.4-10.5) with Davis wave-speed estimates
- * S_L = min(un_L - c_L, un_R - c_R), S_R = max(un_L + c_L, un_R + c_R). */
+ * 3rd ed., sec. 10.4-10.6) with Davis wave-speed estimates
+ * S_L = min(un_L - c_L, un_R - c_R), S_R = max(un_L + c_L, un_R + c_R), and the
+ * star flux in the form with a single division,
+ *   F*_K = [S*(S_K U_K - F_K) + S_K p* D*] / (S_K - S*),  D* = (0, nx, ny, S*),
+ *   p* = p_K + rho_K (S_K - un_K)(S* - un_K),
+ * which equals F_K + S_K (U*_K - U_K) for Toro's star state U*_K. Energies use
+ * p/(gamma-1) as p * (1/(gamma-1)). */
 static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
+    double IG1 = 1.0 / (GAM - 1.0);
     double cL = sqrt(GAM * pL->p / pL->r), cR = sqrt(GAM * pR->p / pR->r);
     double unL = pL->u * nx + pL->v * ny, unR = pR->u * nx + pR->v * ny;
-    double EL = pL->p / (GAM - 1.0) + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
-    double ER = pR->p / (GAM - 1.0) + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
+    double EL = pL->p * IG1 + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
+    double ER = pR->p * IG1 + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
     double SL = dmin(unL - cL, unR - cR), SR = dmax(unL + cL, unR + cR);
     if (SL >= 0.0) { phys_flux(f, pL->r, pL->u, pL->v, pL->p, EL, unL, nx, ny); return; }
     if (SR <= 0.0) { phys_flux(f, pR->r, pR->u, pR->v, pR->p, ER, unR, nx, ny); return; }
@@ -469,16 +475,13 @@ static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double
     else { K = pR; SK = SR; unK = unR; EK = ER; mK = mR; }
     double FK[4];
     phys_flux(FK, K->r, K->u, K->v, K->p, EK, unK, nx, ny);
-    double fac = mK / (SK - Ss);
-    double ds = Ss - unK;
-    double U0 = fac;
-    double U1 = fac * (K->u + ds * nx);
-    double U2 = fac * (K->v + ds * ny);
-    double U3 = fac * (EK / K->r + ds * (Ss + K->p / mK));
-    f[0] = FK[0] + SK * (U0 - K->r);
-    f[1] = FK[1] + SK * (U1 - K->r * K->u);
-    f[2] = FK[2] + SK * (U2 - K->r * K->v);
-    f[3] = FK[3] + SK * (U3 - EK);
+    double ps = K->p + mK * (Ss - unK);
+    double inv = 1.0 / (SK - Ss);
+    double sp = SK * ps;
+    f[0] = (Ss * (SK * K->r - FK[0])) * inv;
+    f[1] = (Ss * (SK * (K->r * K->u) - FK[1]) + sp * nx) * inv;
+    f[2] = (Ss * (SK * (K->r * K->v) - FK[2]) + sp * ny) * inv;
+    f[3] = (Ss * (SK * EK - FK[3]) + sp * Ss) * inv;
 }
 
 /* Roe flux (Roe, J. Comput. Phys. 43, 1981) in the face-normal frame with the
@@ -487,10 +490,10 @@ static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double
  * where |lam~| < delta. Roe averages as in the reference's roe_orig
  * (src/global.cpp:407-441). */
 static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
-    double G1 = GAM - 1.0;
+    double G1 = GAM - 1.0, IG1 = 1.0 / (GAM - 1.0);
     double unL = pL->u * nx + pL->v * ny, unR = pR->u * nx + pR->v * ny;
-    double EL = pL->p / G1 + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
-    double ER = pR->p / G1 + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
+    double EL = pL->p * IG1 + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
+    double ER = pR->p * IG1 + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
     double HL = (EL + pL->p) / pL->r, HR = (ER + pR->p) / pR->r;
     double sL = sqrt(pL->r), sR = sqrt(pR->r);
     double w = 1.0 / (sL + sR);
@@ -500,13 +503,14 @@ static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double 
     double q2 = ut * ut + vt * vt;
     double c2 = G1 * (Ht - 0.5 * q2);
     double c = sqrt(c2);
+    double ic2 = 1.0 / c2;
     double unt = ut * nx + vt * ny;
     double rt = sL * sR;
     double dr = pR->r - pL->r, dp = pR->p - pL->p, dun = unR - unL;
     double dtx = (pR->u - pL->u) - dun * nx, dty = (pR->v - pL->v) - dun * ny;
-    double a1 = (dp - rt * c * dun) / (2.0 * c2);
-    double a2 = dr - dp / c2;
-    double a4 = (dp + rt * c * dun) / (2.0 * c2);
+    double a1 = (dp - rt * c * dun) * (0.5 * ic2);
+    double a2 = dr - dp * ic2;
+    double a4 = (dp + rt * c * dun) * (0.5 * ic2);
     double l1 = unt - c, l4 = unt + c;
     double cL = sqrt(GAM * pL->p / pL->r), cR = sqrt(GAM * pR->p / pR->r);
     double d1 = dmax(0.0, dmax(l1 - (unL - cL), (unR - cR) - l1));
