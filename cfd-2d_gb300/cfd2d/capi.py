@@ -56,6 +56,10 @@ SIGNATURES = {
     "cfd2d_residual": [_P, _D],
     "cfd2d_conservation": [_P, _D],
     "cfd2d_save_vtk": [_P, _I],
+    "cfd2d_set_objective": [_P, _I, _D, C.c_double],
+    "cfd2d_forward": [_P, _I, _I, _D],
+    "cfd2d_backward": [_P, _D, _D],
+    "cfd2d_set_boundary": [_P, _I, _D],
     "cfd2d_timed_steps": [_P, _I, _D],
     "cfd2d_profile_steps": [_P, _I, _D, _IP],
     "cfd2d_residual_first_order_static": [_I, _I, _P, _P, _P, _P, _P, _I, _IP, _D, C.c_double, C.c_double, _I,
@@ -136,6 +140,14 @@ def set_verbosity(level: int):
     lib().cfd2d_set_verbosity(int(level))
 
 
+def _count_boundaries(task_xml: str) -> int:
+    import xml.etree.ElementTree as ET
+    try:
+        return len(ET.parse(task_xml).getroot().find("boundaries").findall("boundCond"))
+    except Exception:
+        return 0
+
+
 class Solver:
     """One FVM_TVD instance on the GPU."""
 
@@ -150,6 +162,7 @@ class Solver:
         self.h = h
         self.info = self.get_info()
         self.n = self.info.n_cells
+        self._nbnd = _count_boundaries(task_xml)
 
     def get_info(self) -> Info:
         inf = Info()
@@ -194,6 +207,28 @@ class Solver:
 
     def save_vtk(self, step: int):
         check(lib().cfd2d_save_vtk(self.h, int(step)))
+
+    # ---- discrete adjoint
+    def set_objective(self, kind: int, weights, p_ref: float = 0.0):
+        w = np.ascontiguousarray(weights, np.float64)
+        check(lib().cfd2d_set_objective(self.h, int(kind), _d(w), float(p_ref)))
+
+    def forward(self, nsteps: int, checkpoint_every: int) -> float:
+        J = np.zeros(1)
+        check(lib().cfd2d_forward(self.h, int(nsteps), int(checkpoint_every), _d(J)))
+        return float(J[0])
+
+    def backward(self):
+        """(dJ/dU0 as 4 x n_cells, dJ/d(Vx, Vy, T, P) per boundary as n_bnd x 4)."""
+        g = np.empty((4, self.n))
+        nb = max(self._nbnd, 1)
+        gb = np.zeros((nb, 4))
+        check(lib().cfd2d_backward(self.h, _d(g), _d(gb)))
+        return g, gb[:self._nbnd]
+
+    def set_boundary(self, b: int, par):
+        p = np.ascontiguousarray(par, np.float64)
+        check(lib().cfd2d_set_boundary(self.h, int(b), _d(p)))
 
     def timed_steps(self, n: int) -> float:
         """Device milliseconds for n steps (CUDA events on the solver's stream)."""

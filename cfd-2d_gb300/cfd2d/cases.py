@@ -66,3 +66,34 @@ def write_task(task, mesh, directory=None, with_unv=False) -> str:
     with open(path, "w") as f:
         f.write(mg.write_task_xml(task))
     return path
+
+
+def vortex_adjoint(n: int, *, steps=200, mach=None, beta=5.0, seed=4, jitter=0.1, flux="HLLC", recon="MINMOD",
+                   scheme="SSPRK3", cfl=0.5, bnd_kinds=None, box=((6.0, 8.0), (4.0, 6.0))):
+    """Differentiation workload: the isentropic vortex with the objective
+    J = sum over cells whose centroid lies in box of S * (p - 1)^2.
+
+    The global time step is pinned by TAU in the task (0.99 of the CFL value of
+    the unperturbed state), so it does not move with the state being
+    differentiated. Returns (task, mesh, U0, weights, u0_of_mach) where
+    u0_of_mach(M) gives the initial state for another free-stream Mach number.
+    """
+    t, m, U0 = vortex(n, beta=beta, mach=mach, seed=seed, jitter=jitter, flux=flux, recon=recon, scheme=scheme,
+                      cfl=cfl, steps=steps, bnd_kinds=bnd_kinds)
+    xy = m.centroids()
+    p = m.nodes[m.tris]
+    S = 0.5 * np.abs((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) -
+                     (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
+    (x0, x1), (y0, y1) = box
+    inside = (xy[:, 0] >= x0) & (xy[:, 0] <= x1) & (xy[:, 1] >= y0) & (xy[:, 1] <= y1)
+    w = np.where(inside, S, 0.0)
+    # CFL time step of the unperturbed state (the reference's area-based formula)
+    r, ru, rv, rE = U0
+    u, v = ru / r, rv / r
+    pr = (GAMMA - 1.0) * (rE - 0.5 * r * (u * u + v * v))
+    c = np.sqrt(GAMMA * pr / r)
+    t.tau = 0.99 * float(np.min(cfl * S / np.maximum(np.abs(u) + c, np.abs(v) + c)))
+
+    def u0_of_mach(M):
+        return mg.isentropic_vortex(xy, beta, 5.0, 5.0, u_inf=M * math.sqrt(GAMMA))
+    return t, m, U0, w, u0_of_mach

@@ -248,6 +248,39 @@ int cfd2d_save_vtk(cfd2d_t* h, int step) {
     });
 }
 
+int cfd2d_set_objective(cfd2d_t* h, int kind, const double* weights, double p_ref) {
+    return guarded([&] {
+        if (!h || !weights) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->set_objective(kind, weights, p_ref);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_forward(cfd2d_t* h, int nsteps, int checkpoint_every, double* J) {
+    return guarded([&] {
+        if (!h || !J) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        int st = CFD2D_OK;
+        *J = h->s->forward(nsteps, checkpoint_every, &st);
+        return st;
+    });
+}
+
+int cfd2d_backward(cfd2d_t* h, double* dJdU0, double* dJdbnd) {
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        h->s->backward(dJdU0, dJdbnd);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_set_boundary(cfd2d_t* h, int b, const double par[4]) {
+    return guarded([&] {
+        if (!h || !par) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->set_boundary_params(b, par);
+        return CFD2D_OK;
+    });
+}
+
 int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms) {
     return guarded([&] {
         if (!h || !device_ms || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");

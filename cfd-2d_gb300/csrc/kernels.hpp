@@ -108,6 +108,34 @@ void launch_permute_scalar(const DevCase& c, const double* src_store, double* ds
 void launch_permute_flags(const DevCase& c, const unsigned* src_store, unsigned* dst_orig, cudaStream_t s);
 // residual of one stage (the reference's ro_int..re_int) in storage order
 void launch_residual(const DevCase& c, int precision, double* R, cudaStream_t s);
+// ---- discrete adjoint (adjoint.cu)
+// Adjoint work arrays of one backward stage.
+struct AdjCase {
+    const double* X;   // 4*nc stage input state (SoA)
+    const double* mu;  // nc x 4 (AoS) cfl * t_bar
+    double* eq;        // ne x 24: q1_bar(4) g1_bar(8) q2_bar(4) g2_bar(8)
+    double* eb;        // (ne - n_int) x 4 boundary-parameter adjoints, flux path
+    double* eb2;       // (ne - n_int) x 4 boundary-parameter adjoints, gradient path
+    double* qbar;      // nc x 4
+    double* gbar;      // nc x 8
+    double* tb;        // 4*nc (SoA) t_bar of the current stage
+    double* acc;       // 4*nc adjoint accumulated for the step's input U^n
+    double* lam;       // 4*nc adjoint of the step's output / input
+    double* mu_out;    // nc x 4
+    double* dbnd;      // n_bnd x 4 accumulated boundary-parameter adjoints
+    int n_bnd;
+};
+
+void launch_adj_flux(const DevCase& c, const AdjCase& a, int flux, int recon, cudaStream_t s);
+void launch_adj_gather(const DevCase& c, const AdjCase& a, cudaStream_t s);
+void launch_adj_cell(const DevCase& c, const AdjCase& a, double coef_t, double coef_acc, int first, cudaStream_t s);
+void launch_adj_step_start(const DevCase& c, const AdjCase& a, double coef_t, double coef_acc, cudaStream_t s);
+void launch_adj_bnd_reduce(const DevCase& c, const AdjCase& a, cudaStream_t s);
+void launch_objective(const DevCase& c, const double* w, int kind, double p_ref, double* partial, int nblocks,
+                      cudaStream_t s);
+void launch_objective_grad(const DevCase& c, const AdjCase& a, const double* w, int kind, double p_ref,
+                           cudaStream_t s);
+
 // built-in checks of the arithmetic helpers against the hardware operations
 // (which: 0 div_rn vs '/', 1 widen vs (double), 2 narrow vs (float) within 1 ulp)
 long long selftest_arith(int which, long long n, unsigned long long seed);

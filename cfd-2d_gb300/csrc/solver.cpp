@@ -54,23 +54,6 @@ void set_log_file(const char* path) {
 // ------------------------------------------------------------------ solver
 
 template <typename T>
-T* Solver::dalloc(size_t n) {
-    void* p = nullptr;
-    size_t b = std::max<size_t>(n, 1) * sizeof(T);
-    CUDA_CHECK(cudaMalloc(&p, b));
-    allocs_.push_back(p);
-    bytes_ += b;
-    return static_cast<T*>(p);
-}
-
-template <typename T>
-T* Solver::upload(const std::vector<T>& v) {
-    T* p = dalloc<T>(v.size());
-    if (!v.empty()) CUDA_CHECK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
-    return p;
-}
-
-template <typename T>
 static std::vector<float> to_f32(const std::vector<T>& v) {
     return std::vector<float>(v.begin(), v.end());
 }

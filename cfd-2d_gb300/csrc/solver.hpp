@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "cfd2d.h"
 #include "kernels.hpp"
 #include "mesh.hpp"
 #include "task.hpp"
@@ -57,8 +58,40 @@ public:
     const DevCase& dev() const { return dc_; }
     int precision() const { return task_.precision; }
 
+    // ---- discrete adjoint (solver_adjoint.cpp)
+    // objective J = sum_i w_i (p_i - p_ref)^2 (kind 0) or sum_i w_i rho_i^2 (kind 1), w in reference cell order
+    void set_objective(int kind, const double* w, double p_ref);
+    // nsteps steps from the current state, keeping a checkpoint every k steps; returns J of the final state
+    double forward(int nsteps, int k, int* status);
+    // dJ/dU of the state forward() started from (4 x nc, reference order) and dJ/d(Vx, Vy, T, P) per boundary
+    void backward(double* dJdU0, double* dJdbnd);
+    void set_boundary_params(int b, const double par[4]);
+
 private:
     template <typename T> T* dalloc(size_t n);
+    void adjoint_setup();
+    void record_step(double* store);
+    DevCase adj_dc_{};
+    bool adj_ready_ = false;
+    int obj_kind_ = -1;
+    double obj_pref_ = 0;
+    double* obj_w_ = nullptr;
+    double* obj_partial_ = nullptr;
+    double* adj_eq_ = nullptr;
+    double* adj_eb_ = nullptr;
+    double* adj_eb2_ = nullptr;
+    double* adj_qbar_ = nullptr;
+    double* adj_gbar_ = nullptr;
+    double* adj_tb_ = nullptr;
+    double* adj_acc_ = nullptr;
+    double* adj_lam_ = nullptr;
+    double* adj_mu_ = nullptr;
+    double* adj_dbnd_ = nullptr;
+    double* adj_final_ = nullptr;
+    double* ckpt_ = nullptr;
+    double* segstore_ = nullptr;
+    size_t ckpt_slots_ = 0, seg_slots_ = 0;
+    int fw_steps_ = 0, fw_k_ = 0;
     template <typename T> T* upload(const std::vector<T>& v);
     void compute_tau();
     void enqueue_step(cudaEvent_t* ev = nullptr, int* kinds = nullptr, int* nev = nullptr);
@@ -84,5 +117,23 @@ private:
     double tau_ = 0, t_ = 0;
     int steps_ = 0;
 };
+
+// device allocations owned (and freed) by the solver
+template <typename T>
+inline T* Solver::dalloc(size_t n) {
+    void* p = nullptr;
+    size_t b = std::max<size_t>(n, 1) * sizeof(T);
+    CUDA_CHECK(cudaMalloc(&p, b));
+    allocs_.push_back(p);
+    bytes_ += b;
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+inline T* Solver::upload(const std::vector<T>& v) {
+    T* p = dalloc<T>(v.size());
+    if (!v.empty()) CUDA_CHECK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+    return p;
+}
 
 }  // namespace cfd2d

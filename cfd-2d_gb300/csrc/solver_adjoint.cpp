@@ -1,0 +1,214 @@
+// Discrete adjoint driver: checkpointed forward, backward sweep with segment
+// recompute (the forward's own kernels re-run from each checkpoint, so the
+// recomputed stage states are the forward's bit for bit), objective and its
+// gradient, boundary-parameter sensitivities.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "cfd2d.h"
+#include "solver.hpp"
+
+namespace cfd2d {
+
+namespace {
+constexpr int kObjBlocks = 512;
+
+int n_stages(int scheme) { return scheme == TIME_EULER ? 1 : (scheme == TIME_HEUN ? 2 : 3); }
+
+// (coef_t, coef_acc) of the step's last combination, U^{n+1} = coef_acc U^n + coef_t t_last
+void final_coefs(int scheme, double& ct, double& ca) {
+    if (scheme == TIME_SSPRK3) { ct = 2.0 / 3.0; ca = 1.0 / 3.0; }
+    else if (scheme == TIME_HEUN) { ct = 0.5; ca = 0.5; }
+    else { ct = 1.0; ca = 0.0; }
+}
+
+// the input X_s of stage s > 0 as a combination of the previous stage's output and U^n
+void stage_coefs(int scheme, int s, double& ct, double& ca) {
+    if (scheme == TIME_SSPRK3 && s == 2) { ct = 0.25; ca = 0.75; }
+    else { ct = 1.0; ca = 0.0; }
+}
+}  // namespace
+
+void Solver::adjoint_setup() {
+    if (adj_ready_) return;
+    const int nc = dc_.nc, ne = dc_.ne, nb = dc_.ne - dc_.n_int;
+    if (task_.steady) throw Error(CFD2D_ERR_INVALID_ARG, "the adjoint needs a global time step (STEADY=0)");
+    if (task_.flux != FLUX_HLLC && task_.flux != FLUX_LAX)
+        throw Error(CFD2D_ERR_INVALID_ARG, "the adjoint differentiates the HLLC and LAX fluxes");
+    if (gauss_points_ == 0) throw Error(CFD2D_ERR_INVALID_ARG, "the adjoint needs two-point edges");
+    adj_dc_ = dc_;
+    if (task_.precision == PREC_MIXED) {  // the FP64 adjoint of the mixed forward needs FP64 geometry
+        std::vector<double> is(nc);
+        for (int i = 0; i < nc; i++) is[i] = 1.0 / lay_.S[i];
+        adj_dc_.invS = upload(is);
+        adj_dc_.nx = upload(lay_.nx);
+        adj_dc_.ny = upload(lay_.ny);
+        adj_dc_.l = upload(lay_.l);
+        adj_dc_.dl = upload(lay_.dl);
+        adj_dc_.W64 = dalloc<double>(4 * (size_t)nc);
+        adj_dc_.G64 = dalloc<double>(8 * (size_t)nc);
+    }
+    adj_eq_ = dalloc<double>(24 * (size_t)ne);
+    adj_eb_ = dalloc<double>(4 * (size_t)std::max(nb, 1));
+    adj_eb2_ = dalloc<double>(4 * (size_t)std::max(nb, 1));
+    adj_qbar_ = dalloc<double>(4 * (size_t)nc);
+    adj_gbar_ = dalloc<double>(8 * (size_t)nc);
+    adj_tb_ = dalloc<double>(4 * (size_t)nc);
+    adj_acc_ = dalloc<double>(4 * (size_t)nc);
+    adj_lam_ = dalloc<double>(4 * (size_t)nc);
+    adj_mu_ = dalloc<double>(4 * (size_t)nc);
+    adj_dbnd_ = dalloc<double>(4 * std::max<size_t>(task_.bnds.size(), 1));
+    adj_final_ = dalloc<double>(4 * (size_t)nc);
+    obj_partial_ = dalloc<double>(kObjBlocks);
+    CUDA_CHECK(cudaMemsetAsync(adj_eb_, 0, sizeof(double) * 4 * std::max(nb, 1), stream_));
+    CUDA_CHECK(cudaMemsetAsync(adj_eb2_, 0, sizeof(double) * 4 * std::max(nb, 1), stream_));
+    adj_ready_ = true;
+}
+
+void Solver::set_objective(int kind, const double* w, double p_ref) {
+    use_device();
+    if (kind != 0 && kind != 1) throw Error(CFD2D_ERR_INVALID_ARG, "objective kind is 0 (pressure) or 1 (density)");
+    adjoint_setup();
+    const int nc = dc_.nc;
+    std::vector<double> ws(nc);
+    for (int i = 0; i < nc; i++) ws[i] = w[lay_.perm[i]];
+    if (!obj_w_) obj_w_ = dalloc<double>(nc);
+    CUDA_CHECK(cudaMemcpyAsync(obj_w_, ws.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+    obj_kind_ = kind;
+    obj_pref_ = p_ref;
+}
+
+void Solver::set_boundary_params(int b, const double par[4]) {
+    use_device();
+    if (b < 0 || b >= (int)task_.bnds.size()) throw Error(CFD2D_ERR_INVALID_ARG, "boundary index out of range");
+    for (int k = 0; k < 4; k++) task_.bnds[b].par[k] = par[k];
+    DevBnd d{};
+    d.kind = task_.bnds[b].kind;
+    d.u = par[0]; d.v = par[1]; d.T = par[2]; d.p = par[3];
+    CUDA_CHECK(cudaMemcpyAsync(const_cast<DevBnd*>(dc_.bnds) + b, &d, sizeof d, cudaMemcpyHostToDevice, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
+double Solver::forward(int nsteps, int k, int* status) {
+    use_device();
+    if (obj_kind_ < 0) throw Error(CFD2D_ERR_INVALID_ARG, "set an objective first");
+    if (nsteps < 1 || k < 1) throw Error(CFD2D_ERR_INVALID_ARG, "nsteps and the checkpoint interval must be >= 1");
+    adjoint_setup();
+    const size_t nc = dc_.nc;
+    const size_t nseg = (nsteps + k - 1) / k;
+    if (nseg > ckpt_slots_) {
+        ckpt_ = dalloc<double>(nseg * 4 * nc);
+        ckpt_slots_ = nseg;
+    }
+    const int nst = n_stages(task_.scheme);
+    if ((size_t)k * nst > seg_slots_) {
+        segstore_ = dalloc<double>((size_t)k * nst * 4 * nc);
+        seg_slots_ = (size_t)k * nst;
+    }
+    CUDA_CHECK(cudaMemsetAsync(dc_.flags, 0, sizeof(unsigned) * nc, stream_));
+    for (size_t s = 0; s < nseg; s++) {
+        CUDA_CHECK(cudaMemcpyAsync(ckpt_ + s * 4 * nc, dc_.A, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice,
+                                   stream_));
+        const int n = std::min<int>(k, nsteps - (int)s * k);
+        for (int j = 0; j < n; j++) {
+            if (!task_.steady) t_ += tau_;
+            CUDA_CHECK(cudaGraphLaunch(gexec_, stream_));
+            steps_++;
+        }
+    }
+    fw_steps_ = nsteps;
+    fw_k_ = k;
+    CUDA_CHECK(cudaMemcpyAsync(adj_final_, dc_.A, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice, stream_));
+    launch_objective(dc_, obj_w_, obj_kind_, obj_pref_, obj_partial_, kObjBlocks, stream_);
+    std::vector<double> h(kObjBlocks);
+    CUDA_CHECK(cudaMemcpyAsync(h.data(), obj_partial_, sizeof(double) * kObjBlocks, cudaMemcpyDeviceToHost, stream_));
+    *status = read_status();  // synchronises
+    double J = 0.0;
+    for (double v : h) J += v;
+    return J;
+}
+
+// One forward step that keeps every stage's input state in store[stage].
+void Solver::record_step(double* store) {
+    const size_t nc = dc_.nc;
+    const int nst = n_stages(task_.scheme);
+    const int p = task_.precision;
+    for (int st = 0; st < nst; st++) {
+        CUDA_CHECK(cudaMemcpyAsync(store + st * 4 * nc, st == 0 ? dc_.A : dc_.B, sizeof(double) * 4 * nc,
+                                   cudaMemcpyDeviceToDevice, stream_));
+        if (task_.recon != RECON_NONE) launch_grad(dc_, p, stream_);
+        launch_flux(dc_, p, task_.flux, task_.recon, stream_);
+        launch_update(dc_, p, task_.scheme, st, stream_);
+    }
+    launch_remediate(dc_, p, stream_);
+}
+
+void Solver::backward(double* dJdU0, double* dJdbnd) {
+    use_device();
+    if (fw_steps_ < 1) throw Error(CFD2D_ERR_INVALID_ARG, "run forward() first");
+    const size_t nc = dc_.nc;
+    {  // the adjoint does not differentiate limiter remediation
+        std::vector<unsigned> fl(nc);
+        CUDA_CHECK(cudaMemcpyAsync(fl.data(), dc_.flags, sizeof(unsigned) * nc, cudaMemcpyDeviceToHost, stream_));
+        CUDA_CHECK(cudaStreamSynchronize(stream_));
+        for (unsigned f : fl)
+            if (f & 0x2u)
+                throw Error(CFD2D_ERR_INVALID_ARG, "limiter flags were raised in the forward run; the adjoint "
+                                                   "does not differentiate remediation");
+    }
+    const int nst = n_stages(task_.scheme);
+    AdjCase a{};
+    a.eq = adj_eq_; a.eb = adj_eb_; a.eb2 = adj_eb2_; a.qbar = adj_qbar_; a.gbar = adj_gbar_;
+    a.tb = adj_tb_; a.acc = adj_acc_; a.lam = adj_lam_; a.mu = adj_mu_; a.mu_out = adj_mu_;
+    a.dbnd = adj_dbnd_; a.n_bnd = (int)task_.bnds.size();
+    CUDA_CHECK(cudaMemsetAsync(adj_dbnd_, 0, sizeof(double) * 4 * std::max<size_t>(task_.bnds.size(), 1), stream_));
+    // lambda = dJ/dU of the final state
+    {
+        DevCase cf = dc_;
+        cf.A = adj_final_;
+        launch_objective_grad(cf, a, obj_w_, obj_kind_, obj_pref_, stream_);
+    }
+    double ct_f, ca_f;
+    final_coefs(task_.scheme, ct_f, ca_f);
+    const int nseg = (fw_steps_ + fw_k_ - 1) / fw_k_;
+    for (int seg = nseg - 1; seg >= 0; seg--) {
+        const int n = std::min(fw_k_, fw_steps_ - seg * fw_k_);
+        CUDA_CHECK(cudaMemcpyAsync(dc_.A, ckpt_ + (size_t)seg * 4 * nc, sizeof(double) * 4 * nc,
+                                   cudaMemcpyDeviceToDevice, stream_));
+        launch_prims(dc_, task_.precision, stream_);
+        for (int j = 0; j < n; j++) record_step(segstore_ + (size_t)j * nst * 4 * nc);
+        for (int j = n - 1; j >= 0; j--) {
+            launch_adj_step_start(adj_dc_, a, ct_f, ca_f, stream_);
+            for (int st = nst - 1; st >= 0; st--) {
+                DevCase cx = adj_dc_;
+                cx.A = segstore_ + ((size_t)j * nst + st) * 4 * nc;
+                a.X = cx.A;
+                launch_prims(cx, PREC_FP64, stream_);
+                if (task_.recon != RECON_NONE) launch_grad(cx, PREC_FP64, stream_);
+                launch_adj_flux(cx, a, task_.flux, task_.recon, stream_);
+                launch_adj_gather(cx, a, stream_);
+                double ct = 1.0, ca = 0.0;
+                if (st > 0) stage_coefs(task_.scheme, st, ct, ca);
+                launch_adj_cell(cx, a, ct, ca, st == 0 ? 1 : 0, stream_);
+                launch_adj_bnd_reduce(cx, a, stream_);
+            }
+        }
+    }
+    // the solver's state is the forward's final state again
+    CUDA_CHECK(cudaMemcpyAsync(dc_.A, adj_final_, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice, stream_));
+    launch_prims(dc_, task_.precision, stream_);
+    if (dJdU0) {
+        launch_scatter_state(dc_, adj_lam_, stage_, stream_);
+        for (int k = 0; k < 4; k++)
+            CUDA_CHECK(cudaMemcpyAsync(dJdU0 + k * nc, stage_ + k * nc, sizeof(double) * nc, cudaMemcpyDeviceToHost,
+                                       stream_));
+    }
+    if (dJdbnd && !task_.bnds.empty())
+        CUDA_CHECK(cudaMemcpyAsync(dJdbnd, adj_dbnd_, sizeof(double) * 4 * task_.bnds.size(), cudaMemcpyDeviceToHost,
+                                   stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
+}  // namespace cfd2d

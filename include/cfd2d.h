@@ -118,6 +118,24 @@ int cfd2d_conservation(cfd2d_t* h, double sums[4]);
 /* FVM_TVD::save (src/methods/fvm_tvd.cpp:501-600): res_%010d.vtk in the working directory. */
 int cfd2d_save_vtk(cfd2d_t* h, int step);
 
+/* ---- discrete adjoint (forward/backward pair) ---------------------------- */
+/* Objective of the final state: J = sum_i w_i (p_i - p_ref)^2 (kind 0) or
+ * J = sum_i w_i rho_i^2 (kind 1); weights per cell in the reference's order. */
+int cfd2d_set_objective(cfd2d_t* h, int kind, const double* weights, double p_ref);
+/* nsteps steps from the current state keeping a checkpoint of the state every
+ * checkpoint_every steps; *J receives the objective of the final state. The
+ * state ends at step nsteps as with cfd2d_step. Needs STEADY=0 (TAU held
+ * fixed), the HLLC or LAX flux and no active limiter. */
+int cfd2d_forward(cfd2d_t* h, int nsteps, int checkpoint_every, double* J);
+/* Gradient of that J by the hand-written discrete adjoint of the forward's
+ * steps (recomputed segment by segment from the checkpoints): dJdU0 (4 x
+ * n_cells, ro|ru|rv|re) with respect to the state cfd2d_forward started from,
+ * and dJdbnd (4 per <boundCond>: Vx, Vy, T, P) with respect to the boundary
+ * parameters; either pointer may be NULL. */
+int cfd2d_backward(cfd2d_t* h, double* dJdU0, double* dJdbnd);
+/* Replace the parameters (Vx, Vy, T, P) of the b-th <boundCond>. */
+int cfd2d_set_boundary(cfd2d_t* h, int b, const double par[4]);
+
 /* Device time in milliseconds of nsteps steps, from CUDA events recorded on the
  * handle's stream around the step graph launches (the steps are taken). */
 int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms);
