@@ -36,7 +36,7 @@ class Info(C.Structure):
     _fields_ = [("n_cells", C.c_int), ("n_edges", C.c_int), ("n_boundary_edges", C.c_int), ("n_nodes", C.c_int),
                 ("step", C.c_int), ("flux", C.c_int), ("recon", C.c_int), ("scheme", C.c_int),
                 ("precision", C.c_int), ("steady", C.c_int), ("time", C.c_double), ("tau", C.c_double),
-                ("device_bytes", C.c_size_t)]
+                ("device_bytes", C.c_size_t), ("n_instances", C.c_int)]
 
 
 # every symbol include/cfd2d.h declares, with its ctypes signature
@@ -56,6 +56,10 @@ SIGNATURES = {
     "cfd2d_residual": [_P, _D],
     "cfd2d_conservation": [_P, _D],
     "cfd2d_save_vtk": [_P, _I],
+    "cfd2d_batch_create": [_I, C.POINTER(C.c_char_p), C.POINTER(MeshDesc), C.POINTER(_P)],
+    "cfd2d_batch_instance": [_P, _I, _IP, _IP, _D, _D],
+    "cfd2d_autotune": [_P, C.c_char_p],
+    "cfd2d_load_tuning": [_P, C.c_char_p],
     "cfd2d_set_objective": [_P, _I, _D, C.c_double],
     "cfd2d_forward": [_P, _I, _I, _D],
     "cfd2d_backward": [_P, _D, _D],
@@ -230,6 +234,12 @@ class Solver:
         p = np.ascontiguousarray(par, np.float64)
         check(lib().cfd2d_set_boundary(self.h, int(b), _d(p)))
 
+    def autotune(self, json_path: str | None = None):
+        check(lib().cfd2d_autotune(self.h, json_path.encode() if json_path else None))
+
+    def load_tuning(self, json_path: str):
+        check(lib().cfd2d_load_tuning(self.h, json_path.encode()))
+
     def timed_steps(self, n: int) -> float:
         """Device milliseconds for n steps (CUDA events on the solver's stream)."""
         ms = np.zeros(1)
@@ -265,6 +275,38 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+class Batch(Solver):
+    """Many independent instances solved together (cfd2d_batch_create)."""
+
+    def __init__(self, task_xmls, meshes=None):
+        L = lib()
+        n = len(task_xmls)
+        paths = (C.c_char_p * n)(*[p.encode() for p in task_xmls])
+        h = C.c_void_p()
+        if meshes is None:
+            check(L.cfd2d_batch_create(n, paths, None, C.byref(h)))
+        else:
+            descs = (MeshDesc * n)()
+            self._keep = []
+            for k, m in enumerate(meshes):
+                d, keep = mesh_desc(m.nodes, m.tris, m.cell_region, m.bsegs, m.bseg_bnd)
+                descs[k] = d
+                self._keep.append(keep)
+            check(L.cfd2d_batch_create(n, paths, descs, C.byref(h)))
+        self.h = h
+        self.info = self.get_info()
+        self.n = self.info.n_cells
+        self._nbnd = sum(_count_boundaries(p) for p in task_xmls)
+        self.count = n
+
+    def instance(self, k: int):
+        """(cell_offset, n_cells, tau, time) of instance k."""
+        off, nc = C.c_int(), C.c_int()
+        tau, t = np.zeros(1), np.zeros(1)
+        check(lib().cfd2d_batch_instance(self.h, int(k), C.byref(off), C.byref(nc), _d(tau), _d(t)))
+        return off.value, nc.value, float(tau[0]), float(t[0])
 
 
 class Mesh:

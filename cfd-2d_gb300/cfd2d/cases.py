@@ -97,3 +97,26 @@ def vortex_adjoint(n: int, *, steps=200, mach=None, beta=5.0, seed=4, jitter=0.1
     def u0_of_mach(M):
         return mg.isentropic_vortex(xy, beta, 5.0, 5.0, u_inf=M * math.sqrt(GAMMA))
     return t, m, U0, w, u0_of_mach
+
+
+def batched_vortices(count: int = 256, *, seed=3, min_cells=10_000, max_cells=400_000, flux="ROE", recon="MINMOD",
+                     scheme="SSPRK3", cfl=0.5, steps=500, precision=None):
+    """Batch of isentropic vortices on [0,10]^2 with uneven sizes.
+
+    Triangle counts N_k are drawn log-uniform in [min_cells, max_cells]
+    (n_k = round(sqrt(N_k / 2)) squares per side), free-stream Mach uniform in
+    [0.1, 0.8] (u = M sqrt(gamma), rho = p = 1), vortex strength uniform in
+    [1, 5]; instance k's mesh jitter seed is seed * 1000 + k. Returns a list of
+    (task, mesh, U0).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    N = np.exp(rng.uniform(np.log(min_cells), np.log(max_cells), count))
+    mach = rng.uniform(0.1, 0.8, count)
+    beta = rng.uniform(1.0, 5.0, count)
+    out = []
+    for k in range(count):
+        n = max(2, int(round(math.sqrt(N[k] / 2.0))))
+        t, m, U0 = vortex(n, beta=float(beta[k]), mach=float(mach[k]), seed=seed * 1000 + k, flux=flux, recon=recon,
+                          scheme=scheme, cfl=cfl, steps=steps, precision=precision)
+        out.append((t, m, U0))
+    return out

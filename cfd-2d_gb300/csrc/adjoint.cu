@@ -49,17 +49,20 @@ __global__ void __launch_bounds__(256) k_adj_flux(const DevCase c, const AdjCase
     const bool inner = e < c.n_int;
     const int c2 = inner ? c.ec2[e] : -1;
     const Prim<double> qL = load_prim(W, c1);
-    double gL[8] = {0}, gR[8] = {0};
-    if (RECON != RECON_NONE) ld8(G, c1, gL);
     Prim<double> qR = qL, gc = qL;
     DevBnd b{};
     double Tc = 0, M = 0, gm1 = 0, Cv = 0;
-    double m1[4], m2[4] = {0, 0, 0, 0};
-    ld4(a.mu, c1, m1);
+    double fb[4];
+    {
+        double m1[4], m2[4] = {0, 0, 0, 0};
+        ld4(a.mu, c1, m1);
+        if (inner) ld4(a.mu, c2, m2);
+        // F = (sum over Gauss points of f) * l/2; R_c1 -= F, R_c2 += F
+        const double lh = l * 0.5 * (RECON == RECON_NONE ? 2.0 : 1.0);
+        for (int k = 0; k < 4; k++) fb[k] = (m2[k] - m1[k]) * lh;
+    }
     if (inner) {
         qR = load_prim(W, c2);
-        if (RECON != RECON_NONE) ld8(G, c2, gR);
-        ld4(a.mu, c2, m2);
     } else {
         b = c.bnds[c.ebnd[e]];
         const DevMat mt = mat_of(c, c1);
@@ -67,29 +70,28 @@ __global__ void __launch_bounds__(256) k_adj_flux(const DevCase c, const AdjCase
         Tc = temperature(qL, gm1, Cv);
         if (RECON == RECON_MINMOD) gc = ghost_state(b, qL, Tc, nx, ny, M);
     }
-    // F = (sum over Gauss points of f) * l/2; R_c1 -= F, R_c2 += F
-    const double lh = l * 0.5;
-    double fb[4];
-    for (int k = 0; k < 4; k++) fb[k] = (m2[k] - m1[k]) * lh * (RECON == RECON_NONE ? 2.0 : 1.0);
     Prim<double> q1b = zero_prim(), q2b = zero_prim(), gcb = zero_prim();
     double g1b[8] = {0}, g2b[8] = {0}, bp[4] = {0, 0, 0, 0}, Tcb = 0;
     const int ngp = RECON == RECON_NONE ? 1 : 2;
+#pragma unroll 1
     for (int gp = 0; gp < ngp; gp++) {
-        Prim<double> pL = qL, pR;
+        Prim<double> pL = qL, pR = qR;
+        double aL[4] = {0, 0, 0, 0}, aR[4] = {0, 0, 0, 0};
         double dxL = 0, dyL = 0, dxR = 0, dyR = 0;
         if (RECON != RECON_NONE) {
+            double g[8];
             dxL = DL[(4 * gp) * ne + e]; dyL = DL[(4 * gp + 1) * ne + e];
-            reconstruct<double, RECON>(pL, gL, dxL, dyL, inner ? qR : gc);
-        }
-        if (inner) {
-            pR = qR;
-            if (RECON != RECON_NONE) {
+            ld8(G, c1, g);
+            project(g, dxL, dyL, aL);
+            pL = recon_a<RECON>(qL, aL, inner ? qR : gc);
+            if (inner) {
                 dxR = DL[(4 * gp + 2) * ne + e]; dyR = DL[(4 * gp + 3) * ne + e];
-                reconstruct<double, RECON>(pR, gR, dxR, dyR, qL);
+                ld8(G, c2, g);
+                project(g, dxR, dyR, aR);
+                pR = recon_a<RECON>(qR, aR, qL);
             }
-        } else {
-            pR = ghost_state(b, pL, Tc, nx, ny, M);
         }
+        if (!inner) pR = ghost_state(b, pL, Tc, nx, ny, M);
         Prim<double> pLb = zero_prim(), pRb = zero_prim();
         vjp_flux<FLUX>(pL, pR, nx, ny, GAM, fb, pLb, pRb);
         if (!inner) vjp_ghost(b, pL, Tc, nx, ny, M, pRb, pLb, Tcb, bp);
@@ -97,17 +99,17 @@ __global__ void __launch_bounds__(256) k_adj_flux(const DevCase c, const AdjCase
             q1b.r += pLb.r; q1b.u += pLb.u; q1b.v += pLb.v; q1b.p += pLb.p;
             if (inner) { q2b.r += pRb.r; q2b.u += pRb.u; q2b.v += pRb.v; q2b.p += pRb.p; }
         } else if (inner) {
-            vjp_reconstruct<RECON>(qL, gL, dxL, dyL, qR, pLb, q1b, g1b, q2b);
-            vjp_reconstruct<RECON>(qR, gR, dxR, dyR, qL, pRb, q2b, g2b, q1b);
+            vjp_reconstruct_a<RECON>(qL, aL, dxL, dyL, qR, pLb, q1b, g1b, q2b);
+            vjp_reconstruct_a<RECON>(qR, aR, dxR, dyR, qL, pRb, q2b, g2b, q1b);
         } else {
-            vjp_reconstruct<RECON>(qL, gL, dxL, dyL, gc, pLb, q1b, g1b, gcb);
+            vjp_reconstruct_a<RECON>(qL, aL, dxL, dyL, gc, pLb, q1b, g1b, gcb);
         }
     }
     if (!inner) {
         if (RECON == RECON_MINMOD) vjp_ghost(b, qL, Tc, nx, ny, M, gcb, q1b, Tcb, bp);
         vjp_temperature(qL, gm1, Cv, Tcb, q1b);
-        double* o = a.eb + 4 * (size_t)(e - c.n_int);
-        o[0] = bp[0]; o[1] = bp[1]; o[2] = bp[2]; o[3] = bp[3];
+        double* o = a.eb + 4 * (size_t)(e - c.n_int);  // this edge's own running sum over stages and steps
+        o[0] += bp[0]; o[1] += bp[1]; o[2] += bp[2]; o[3] += bp[3];
     }
     double* o = a.eq + 24 * (size_t)e;
     o[0] = q1b.r; o[1] = q1b.u; o[2] = q1b.v; o[3] = q1b.p;
@@ -147,14 +149,14 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
     qb.r = qbv[0]; qb.u = qbv[1]; qb.v = qbv[2]; qb.p = qbv[3];
     double gi[8];
     ld8(a.gbar, i, gi);
-    const double Si = c.S[i];
+    const double iSi = c.invS[i];
     double Tcb = 0;
     for (int k = 0; k < 3; k++) {
         const int f = c.face[k * nc + i];
         const int e = f >> 1;
         const bool side2 = f & 1;
         const double nx = c.nx[e], ny = c.ny[e], l = c.l[e];
-        const double wi = (side2 ? -0.5 : 0.5) * l / Si;
+        const double wi = (side2 ? -0.5 : 0.5) * l * iSi;
         // d g_i / d q_i and d g_i / d (neighbour or ghost): the same weight
         const double s0 = wi * (nx * gi[0] + ny * gi[1]), s1 = wi * (nx * gi[2] + ny * gi[3]);
         const double s2 = wi * (nx * gi[4] + ny * gi[5]), s3 = wi * (nx * gi[6] + ny * gi[7]);
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
         if (j >= 0) {  // the neighbour's gradient uses this cell's value with the opposite orientation
             double gj[8];
             ld8(a.gbar, j, gj);
-            const double wj = (side2 ? 0.5 : -0.5) * l / c.S[j];
+            const double wj = (side2 ? 0.5 : -0.5) * l * c.invS[j];
             qb.r += wj * (nx * gj[0] + ny * gj[1]);
             qb.p += wj * (nx * gj[2] + ny * gj[3]);
             qb.u += wj * (nx * gj[4] + ny * gj[5]);
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
             double bp[4] = {0, 0, 0, 0};
             vjp_ghost(b, q, Tc, nx, ny, mt.M, ob, qb, Tcb, bp);
             double* o = a.eb2 + 4 * (size_t)(e - c.n_int);
-            o[0] = bp[0]; o[1] = bp[1]; o[2] = bp[2]; o[3] = bp[3];
+            o[0] += bp[0]; o[1] += bp[1]; o[2] += bp[2]; o[3] += bp[3];
         }
     }
     if (Tcb != 0.0) vjp_temperature(q, mt.gm1, mt.Cv, Tcb, qb);
@@ -215,7 +217,8 @@ __global__ void __launch_bounds__(256) k_adj_step_start(const DevCase c, const A
     st4(a.mu_out, i, cf * t[0], cf * t[1], cf * t[2], cf * t[3]);
 }
 
-// dbnd[b] += sum over boundary edges of boundary b (flux and gradient paths), in a fixed order.
+// dbnd[b] = sum over boundary edges of boundary b of their running sums (flux and
+// gradient paths, all stages and steps), in a fixed order.
 __global__ void __launch_bounds__(256) k_adj_bnd_reduce(const DevCase c, const AdjCase a) {
     __shared__ double sh[4][256];
     const int nb = c.ne - c.n_int;
@@ -233,7 +236,7 @@ __global__ void __launch_bounds__(256) k_adj_bnd_reduce(const DevCase c, const A
             __syncthreads();
         }
         if (threadIdx.x == 0)
-            for (int m = 0; m < 4; m++) a.dbnd[4 * bi + m] += sh[m][0];
+            for (int m = 0; m < 4; m++) a.dbnd[4 * bi + m] = sh[m][0];
         __syncthreads();
     }
 }

@@ -11,8 +11,8 @@ namespace cfd2d {
 
 // convertConsToPar: (rho, rho u, rho v, rho E) -> (r, u, v, p)
 __device__ __forceinline__ void vjp_cons2prim(const double* U, double gm1, const Prim<double>& pb, double* Ub) {
-    const double ro = U[0];
-    const double u = U[1] / ro, v = U[2] / ro, E = U[3] / ro;
+    const double ro = U[0], iro = 1.0 / ro;  // the reverse sweep needs no bit parity: one reciprocal
+    const double u = U[1] * iro, v = U[2] * iro, E = U[3] * iro;
     const double e = E - 0.5 * (u * u + v * v);
     // p = r e gm1
     double rb = pb.r + pb.p * e * gm1;
@@ -20,19 +20,19 @@ __device__ __forceinline__ void vjp_cons2prim(const double* U, double gm1, const
     // e = E - (u^2 + v^2)/2
     const double Eb = eb;
     const double ub = pb.u - eb * u, vb = pb.v - eb * v;
-    Ub[1] += ub / ro;
-    Ub[2] += vb / ro;
-    Ub[3] += Eb / ro;
-    rb -= (ub * u + vb * v + Eb * E) / ro;
+    Ub[1] += ub * iro;
+    Ub[2] += vb * iro;
+    Ub[3] += Eb * iro;
+    rb -= (ub * u + vb * v + Eb * E) * iro;
     Ub[0] += rb;
 }
 
 // Tc = (p / (r gm1)) / Cv
 __device__ __forceinline__ void vjp_temperature(const Prim<double>& q, double gm1, double Cv, double Tb,
                                                 Prim<double>& qb) {
-    const double T = (q.p / (q.r * gm1)) / Cv;
-    qb.p += Tb / (q.r * gm1 * Cv);
-    qb.r -= Tb * T / q.r;
+    const double k = 1.0 / (q.r * gm1 * Cv);
+    qb.p += Tb * k;
+    qb.r -= Tb * (q.p * k) / q.r;
 }
 
 // ghost_state(b, q, Tc, n, M): the reference's CFDBnd*::run + URS(2) for the density.
@@ -41,16 +41,16 @@ __device__ __forceinline__ void vjp_ghost(const DevBnd& b, const Prim<double>& q
                                           double M, const Prim<double>& gb, Prim<double>& qb, double& Tcb,
                                           double* bp_bar) {
     if (b.kind == BND_INLET) {
-        const double rg = b.p * M / (b.T * GAS_R);
+        const double k = M / (b.T * GAS_R);
         bp_bar[0] += gb.u;
         bp_bar[1] += gb.v;
-        bp_bar[3] += gb.p + gb.r * M / (b.T * GAS_R);
-        bp_bar[2] -= gb.r * rg / b.T;
+        bp_bar[3] += gb.p + gb.r * k;
+        bp_bar[2] -= gb.r * (b.p * k) / b.T;
         return;
     }
-    const double rg = q.p * M / (Tc * GAS_R);
-    qb.p += gb.p + gb.r * M / (Tc * GAS_R);
-    Tcb -= gb.r * rg / Tc;
+    const double k = M / (Tc * GAS_R);
+    qb.p += gb.p + gb.r * k;
+    Tcb -= gb.r * (q.p * k) / Tc;
     if (b.kind == BND_OUTLET) {
         qb.u += gb.u;
         qb.v += gb.v;
@@ -112,8 +112,8 @@ __device__ __forceinline__ void vjp_lax(const Prim<double>& L, const Prim<double
     rolb += rulb * L.u + rvlb * L.v; Lb.u += rulb * L.r; Lb.v += rvlb * L.r;
     Rb.r += rorb; Lb.r += rolb;
     // alpha = max(|unl| + cL, |unr| + cR)
-    if (first) { unlb += alphab * (unl >= 0 ? 1.0 : -1.0); const double ab = alphab / (2.0 * cL); Lb.p += ab * GAM / L.r; Lb.r -= ab * aL / L.r; }
-    else { unrb += alphab * (unr >= 0 ? 1.0 : -1.0); const double ab = alphab / (2.0 * cR); Rb.p += ab * GAM / R.r; Rb.r -= ab * aR / R.r; }
+    if (first) { unlb += alphab * (unl >= 0 ? 1.0 : -1.0); const double ab = 0.5 * alphab / (cL * L.r); Lb.p += ab * GAM; Lb.r -= ab * aL; }
+    else { unrb += alphab * (unr >= 0 ? 1.0 : -1.0); const double ab = 0.5 * alphab / (cR * R.r); Rb.p += ab * GAM; Rb.r -= ab * aR; }
     Lb.u += unlb * nx; Lb.v += unlb * ny; Rb.u += unrb * nx; Rb.v += unrb * ny;
 }
 
@@ -179,7 +179,8 @@ __device__ __forceinline__ void vjp_hllc(const Prim<double>& L, const Prim<doubl
             Rb.r += Krb; Rb.u += Kub; Rb.v += Kvb; Rb.p += Kpb; ERb += EKb; unRb += unKb; SRb += SKb; mRb += mKb;
         }
         // Ss = num / den
-        const double numb = Ssb / den, denb = -Ssb * Ss / den;
+        const double iden = 1.0 / den;
+        const double numb = Ssb * iden, denb = -Ssb * Ss * iden;
         Rb.p += numb; Lb.p -= numb;
         mLb += numb * unL + denb; unLb += numb * mL;
         mRb += -numb * unR - denb; unRb -= numb * mR;
@@ -195,9 +196,61 @@ __device__ __forceinline__ void vjp_hllc(const Prim<double>& L, const Prim<doubl
     Rb.p += ERb * IG1; Rb.r += ERb * 0.5 * (R.u * R.u + R.v * R.v); Rb.u += ERb * R.r * R.u; Rb.v += ERb * R.r * R.v;
     // un = u nx + v ny
     Lb.u += unLb * nx; Lb.v += unLb * ny; Rb.u += unRb * nx; Rb.v += unRb * ny;
-    // c = sqrt(GAM p / r)
-    if (cLb != 0.0) { const double ab = cLb / (2.0 * cL); Lb.p += ab * GAM / L.r; Lb.r -= ab * aL / L.r; }
-    if (cRb != 0.0) { const double ab = cRb / (2.0 * cR); Rb.p += ab * GAM / R.r; Rb.r -= ab * aR / R.r; }
+    // c = sqrt(GAM p / r): dc = (GAM dp - a dr) / (2 c r)
+    if (cLb != 0.0) { const double ab = 0.5 * cLb / (cL * L.r); Lb.p += ab * GAM; Lb.r -= ab * aL; }
+    if (cRb != 0.0) { const double ab = 0.5 * cRb / (cR * R.r); Rb.p += ab * GAM; Rb.r -= ab * aR; }
+}
+
+// One side's reconstruction p = q + delta(a, nb - q) with the projections
+// a = g . dl already formed (in the forward's operation order): pb -> qb, gb
+// (8: r, p, u, v gradients, through a) and nbb (the minmod neighbour values).
+template <int RECON>
+__device__ __forceinline__ void vjp_reconstruct_a(const Prim<double>& q, const double* a, double dx, double dy,
+                                                  const Prim<double>& nb, const Prim<double>& pb, Prim<double>& qb,
+                                                  double* gb, Prim<double>& nbb) {
+    const double qv[4] = {q.r, q.p, q.u, q.v}, nv[4] = {nb.r, nb.p, nb.u, nb.v};
+    const double pv[4] = {pb.r, pb.p, pb.u, pb.v};
+    double qbv[4] = {0, 0, 0, 0}, nbv[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double db = pv[k];
+        qbv[k] += db;
+        if (RECON == RECON_LINEAR) {
+            gb[2 * k] += db * dx;
+            gb[2 * k + 1] += db * dy;
+            continue;
+        }
+        const double b = nv[k] - qv[k];  // minmod(a, b): a*b > 0 ? (|a| < |b| ? a : b) : 0
+        if (a[k] * b > 0.0) {
+            if (fabs(a[k]) < fabs(b)) { gb[2 * k] += db * dx; gb[2 * k + 1] += db * dy; }
+            else { nbv[k] += db; qbv[k] -= db; }
+        }
+    }
+    qb.r += qbv[0]; qb.p += qbv[1]; qb.u += qbv[2]; qb.v += qbv[3];
+    nbb.r += nbv[0]; nbb.p += nbv[1]; nbb.u += nbv[2]; nbb.v += nbv[3];
+}
+
+// Projections a = g . dl of one side's four gradients, as reconstruct() forms them.
+__device__ __forceinline__ void project(const double* g, double dx, double dy, double* a) {
+    a[0] = g[0] * dx + g[1] * dy;
+    a[1] = g[2] * dx + g[3] * dy;
+    a[2] = g[4] * dx + g[5] * dy;
+    a[3] = g[6] * dx + g[7] * dy;
+}
+
+// The forward reconstruction from the projections (kernels.cuh reconstruct).
+template <int RECON>
+__device__ __forceinline__ Prim<double> recon_a(const Prim<double>& q, const double* a, const Prim<double>& nb) {
+    Prim<double> p = q;
+    double d0 = a[0], d1 = a[1], d2 = a[2], d3 = a[3];
+    if (RECON == RECON_MINMOD) {
+        d0 = minmod(d0, nb.r - q.r);
+        d1 = minmod(d1, nb.p - q.p);
+        d2 = minmod(d2, nb.u - q.u);
+        d3 = minmod(d3, nb.v - q.v);
+    }
+    p.r += d0; p.p += d1; p.u += d2; p.v += d3;
+    return p;
 }
 
 // One side's reconstruction p = q + delta(g . dl, nb - q) (kernels.cuh reconstruct):

@@ -145,6 +145,77 @@ int cfd2d_create_with_mesh(const char* task_xml_path, const cfd2d_mesh_desc* mes
     });
 }
 
+int cfd2d_batch_create(int n, const char* const* task_xml_paths, const cfd2d_mesh_desc* meshes, cfd2d_t** out) {
+    return guarded([&] {
+        if (n < 1 || !task_xml_paths || !out) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
+        *out = nullptr;
+        std::vector<cfd2d::TaskConfig> tasks;
+        std::vector<cfd2d::Topo> topos(n);
+        std::vector<std::vector<int>> cregs(n), ebnds(n);
+        for (int k = 0; k < n; k++) {
+            if (!task_xml_paths[k]) return fail(CFD2D_ERR_INVALID_ARG, "null task path");
+            tasks.push_back(cfd2d::parse_task(task_xml_paths[k]));
+            if (meshes) {
+                const cfd2d_mesh_desc* m = meshes + k;
+                check_desc(m);
+                if (!m->cell_region) return fail(CFD2D_ERR_INVALID_ARG, "cell_region is required");
+                topos[k] = topo_from_desc(m, nullptr, 2);
+                cregs[k].assign(m->cell_region, m->cell_region + m->n_cells);
+                for (int r : cregs[k])
+                    if (r < 0 || r >= (int)tasks[k].regions.size())
+                        return fail(CFD2D_ERR_REGION_UNKNOWN, "cell_region refers to a missing region");
+                ebnds[k] = edge_bnd_from_desc(m, topos[k], (int)tasks[k].bnds.size());
+            } else {
+                int gp = 2;
+                load_task_mesh(tasks[k], topos[k], cregs[k], ebnds[k], gp);
+                if (gp != 2) return fail(CFD2D_ERR_INVALID_ARG, "batch instances need two-point edges");
+            }
+        }
+        cfd2d::Batch b = cfd2d::merge_batch(tasks, topos, cregs, ebnds);
+        auto h = std::make_unique<cfd2d_solver>();
+        h->s = std::make_unique<cfd2d::Solver>(b.task, std::move(b.topo), b.cell_region, b.edge_bnd, 2, b.inst);
+        *out = h.release();
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_batch_instance(const cfd2d_t* h, int k, int* cell_offset, int* n_cells, double* tau, double* time) {
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        const cfd2d::Solver& s = *h->s;
+        if (k < 0 || k >= s.n_instances()) return fail(CFD2D_ERR_INVALID_ARG, "instance out of range");
+        if (!s.is_batch()) {
+            if (cell_offset) *cell_offset = 0;
+            if (n_cells) *n_cells = s.topo().nc;
+            if (tau) *tau = s.tau();
+            if (time) *time = s.time();
+            return CFD2D_OK;
+        }
+        const cfd2d::Instance& in = s.instance(k);
+        if (cell_offset) *cell_offset = in.cell_off;
+        if (n_cells) *n_cells = in.nc;
+        if (tau) *tau = in.tau;
+        if (time) *time = in.t;
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_autotune(cfd2d_t* h, const char* json_path) {
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        h->s->autotune(json_path, 5);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_load_tuning(cfd2d_t* h, const char* json_path) {
+    return guarded([&] {
+        if (!h || !json_path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->load_tuning(json_path);
+        return CFD2D_OK;
+    });
+}
+
 int cfd2d_step(cfd2d_t* h, int nsteps) {
     return guarded([&] {
         if (!h || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
@@ -187,6 +258,7 @@ int cfd2d_get_info(const cfd2d_t* h, cfd2d_info_t* info) {
         info->time = s.time();
         info->tau = s.tau();
         info->device_bytes = s.device_bytes();
+        info->n_instances = s.n_instances();
         return CFD2D_OK;
     });
 }

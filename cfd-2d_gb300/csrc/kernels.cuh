@@ -461,10 +461,8 @@ __device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& 
 // gathered per cell over its faces in ascending original edge order. FP64 divides
 // by S like the reference; the mixed form multiplies by 1/S in FP32.
 template <typename T>
-__global__ void __launch_bounds__(256) k_grad(const DevCase c) {
+__device__ __forceinline__ void grad_one(const DevCase& c, int i) {
     const int nc = c.nc;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nc) return;
     const T* __restrict__ W = W_of<T>(c);
     const Prim<T> q = load_prim(W, i);
     T g[8] = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
@@ -488,7 +486,7 @@ __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
         const T v[8] = {hr * nx * l, hr * ny * l, hp * nx * l, hp * ny * l,
                         hu * nx * l, hu * ny * l, hv * nx * l, hv * ny * l};
 #pragma unroll
-        for (int m = 0; m < 8; m++) g[m] = side2 ? g[m] - v[m] : g[m] + v[m];
+        for (int m = 0; m < 8; m++) g[m] = g[m] + (side2 ? -v[m] : v[m]);  // x - y is x + (-y) in IEEE
     }
     if constexpr (sizeof(T) == 8) {
         const double s = c.S[i], y = c.invS[i];  // y = RN(1/S), computed on the host
@@ -500,6 +498,16 @@ __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
         for (int m = 0; m < 8; m++) g[m] = g[m] * is;
     }
     st8(G_of<T>(c), i, g);
+}
+
+template <typename T, bool STRIDE>
+__global__ void __launch_bounds__(256) k_grad(const DevCase c) {
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!STRIDE) {  // one thread per item
+        if (i0 < c.nc) grad_one<T>(c, i0);
+        return;
+    }
+    for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) grad_one<T>(c, i);  // persistent grid
 }
 
 template <typename T, int RECON>
@@ -519,10 +527,8 @@ __device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, 
 
 // Edge flux over the edge's two Gauss points, times l/2 (src/methods/fvm_tvd.cpp:329-352).
 template <typename T, int FLUX, int RECON>
-__global__ void __launch_bounds__(256) k_flux(const DevCase c) {
+__device__ __forceinline__ void flux_one(const DevCase& c, int e) {
     const int ne = c.ne;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
     const T* __restrict__ W = W_of<T>(c);
     const T* __restrict__ G = G_of<T>(c);
     const T* __restrict__ DL = DL_of<T>(c);
@@ -572,6 +578,16 @@ __global__ void __launch_bounds__(256) k_flux(const DevCase c) {
     if (hit) atomicOr(c.err, ERRBIT_NEWTON_CAP);
     const T lh = l * T(0.5);
     st4(F_of<T>(c), e, fs[0] * lh, fs[1] * lh, fs[2] * lh, fs[3] * lh);
+}
+
+template <typename T, int FLUX, int RECON, bool STRIDE>
+__global__ void __launch_bounds__(256) k_flux(const DevCase c) {
+    const int e0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!STRIDE) {  // one thread per item
+        if (e0 < c.ne) flux_one<T, FLUX, RECON>(c, e0);
+        return;
+    }
+    for (int e = e0; e < c.ne; e += gridDim.x * blockDim.x) flux_one<T, FLUX, RECON>(c, e);  // persistent grid
 }
 
 // FP32 <-> FP64 conversions on the integer pipe. GB300's FP64 unit issues ~2
@@ -625,7 +641,7 @@ __device__ __forceinline__ void gather_residual(const DevCase& c, int i, double*
             double v[4];
             ld4(F, f >> 1, v);
 #pragma unroll
-            for (int q = 0; q < 4; q++) R[q] = (f & 1) ? R[q] + v[q] : R[q] - v[q];
+            for (int q = 0; q < 4; q++) R[q] = R[q] + ((f & 1) ? v[q] : -v[q]);
         }
     } else {
         float t[3][4];
@@ -683,12 +699,10 @@ __device__ __forceinline__ bool outside_limits(const DevCase& c, const Prim<T>& 
 // The last stage checks the limits (in the face precision) and, for a local time
 // step, computes the next step's cTau in FP64.
 template <typename T, int SCHEME, int STAGE>
-__global__ void __launch_bounds__(256) k_update(const DevCase c) {
+__device__ __forceinline__ void update_one(const DevCase& c, int i) {
     constexpr bool FINAL = (SCHEME == TIME_EULER && STAGE == 0) || (SCHEME == TIME_HEUN && STAGE == 1) ||
                            (SCHEME == TIME_SSPRK3 && STAGE == 2);
     const int nc = c.nc;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nc) return;
     if (STAGE == 0 && c.steady) c.ctau[i] = c.ctau_next[i];  // the step now running uses ctau_next
     if (c.flags[i] & 0x2u) {  // cellIsLim: no update; later stages read B
         if (STAGE == 0 && !FINAL)
@@ -729,6 +743,16 @@ __global__ void __launch_bounds__(256) k_update(const DevCase c) {
             local_dt(c, i, cons2prim<double>(u0, u1, u2, u3, mt.gm1), mt);
         }
     }
+}
+
+template <typename T, int SCHEME, int STAGE, bool STRIDE>
+__global__ void __launch_bounds__(256) k_update(const DevCase c) {
+    const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!STRIDE) {  // one thread per item
+        if (i0 < c.nc) update_one<T, SCHEME, STAGE>(c, i0);
+        return;
+    }
+    for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) update_one<T, SCHEME, STAGE>(c, i);  // persistent grid
 }
 
 // remediateLimCells, src/methods/fvm_tvd.cpp:464-499: flagged cells, in original

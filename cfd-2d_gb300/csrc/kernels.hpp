@@ -38,9 +38,15 @@ struct DevBnd {     // one <boundCond>: kind and (Vx, Vy, T, P)
     double u, v, T, p;
 };
 
+// Launch shape of one kernel kind: threads per block and blocks (0 = one
+// thread per item; otherwise a persistent grid that strides over the items).
+struct LaunchShape { int block = 256, grid = 0; };
+enum { KIND_GRAD = 0, KIND_FLUX = 1, KIND_UPDATE = 2, N_TUNED_KINDS = 3 };
+
 // Everything a kernel needs; passed by value.
 struct DevCase {
     int nc, ne, n_int;
+    LaunchShape shape[N_TUNED_KINDS];
     // geometry
     const int* face;       // 3*nc
     const int* ec1;        // ne

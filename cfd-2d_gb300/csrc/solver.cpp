@@ -59,8 +59,8 @@ static std::vector<float> to_f32(const std::vector<T>& v) {
 }
 
 Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_region,
-               const std::vector<int>& edge_bnd, int gauss_points)
-    : task_(t), topo_(std::move(topo)), gauss_points_(gauss_points) {
+               const std::vector<int>& edge_bnd, int gauss_points, std::vector<Instance> instances)
+    : task_(t), topo_(std::move(topo)), gauss_points_(gauss_points), inst_(std::move(instances)) {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(CFD2D_ERR_NO_DEVICE, "no CUDA device");
     CUDA_CHECK(cudaGetDevice(&dev_));
@@ -166,7 +166,7 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
         launch_prims(c, task_.precision, stream_);
         compute_tau();
         CUDA_CHECK(cudaStreamSynchronize(stream_));
-        if (!task_.steady) log_line("time step: %25.16E\n", tau_);  // calcTimeStep, :238
+        if (!task_.steady && inst_.empty()) log_line("time step: %25.16E\n", tau_);  // calcTimeStep, :238
         build_graph();
     } catch (...) {
         for (void* p : allocs_) cudaFree(p);
@@ -190,6 +190,10 @@ Solver::~Solver() {
 // per-cell cTau from launch_prims; STEADY=0 takes TAU = min(TAU, min_i ...).
 void Solver::compute_tau() {
     if (task_.steady) return;
+    if (!inst_.empty()) {
+        compute_tau_batch();
+        return;
+    }
     unsigned long long init;
     double t0 = tau_;
     std::memcpy(&init, &t0, sizeof init);
@@ -310,6 +314,8 @@ int Solver::step(int n) {
     use_device();
     for (int k = 0; k < n; k++) {
         if (!task_.steady) t_ += tau_;  // src/methods/fvm_tvd.cpp:312-316
+        if (!task_.steady)
+            for (auto& in : inst_) in.t += in.tau;
         CUDA_CHECK(cudaGraphLaunch(gexec_, stream_));
         steps_++;
     }

@@ -24,10 +24,27 @@ void set_log_file(const char* path);
             throw ::cfd2d::Error(CFD2D_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));       \
     } while (0)
 
+// One member of a batch: its cells are [cell_off, cell_off + nc) of the union
+// mesh (reference order), with its own CFL number and XML time step.
+struct Instance {
+    int cell_off = 0, nc = 0;
+    double tau_xml = 0, cfl = 0, tau = 0, t = 0;
+};
+
+// A batch merged into one union mesh and task (solver_batch.cpp).
+struct Batch {
+    TaskConfig task;
+    Topo topo;
+    std::vector<int> cell_region, edge_bnd;
+    std::vector<Instance> inst;
+};
+Batch merge_batch(std::vector<TaskConfig>& tasks, std::vector<Topo>& topos, std::vector<std::vector<int>>& cregs,
+                  std::vector<std::vector<int>>& ebnds);
+
 class Solver {
 public:
     Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_region, const std::vector<int>& edge_bnd,
-           int gauss_points);
+           int gauss_points, std::vector<Instance> instances = {});
     ~Solver();
     Solver(const Solver&) = delete;
     Solver& operator=(const Solver&) = delete;
@@ -58,6 +75,15 @@ public:
     const DevCase& dev() const { return dc_; }
     int precision() const { return task_.precision; }
 
+    // ---- batches and launch shapes (solver_batch.cpp)
+    int n_instances() const { return (int)std::max<size_t>(inst_.size(), 1); }
+    const Instance& instance(int k) const { return inst_[k]; }
+    bool is_batch() const { return !inst_.empty(); }
+    // sweep block size x persistent-grid factor per kernel kind; keep the fastest; write JSON when path given
+    void autotune(const char* json_path, int reps);
+    void load_tuning(const char* json_path);
+    const LaunchShape& shape(int kind) const { return dc_.shape[kind]; }
+
     // ---- discrete adjoint (solver_adjoint.cpp)
     // objective J = sum_i w_i (p_i - p_ref)^2 (kind 0) or sum_i w_i rho_i^2 (kind 1), w in reference cell order
     void set_objective(int kind, const double* w, double p_ref);
@@ -70,7 +96,7 @@ public:
 private:
     template <typename T> T* dalloc(size_t n);
     void adjoint_setup();
-    void record_step(double* store);
+    void record_step(double* store, double* wg);
     DevCase adj_dc_{};
     bool adj_ready_ = false;
     int obj_kind_ = -1;
@@ -90,6 +116,9 @@ private:
     double* adj_final_ = nullptr;
     double* ckpt_ = nullptr;
     double* segstore_ = nullptr;
+    double* wgstore_ = nullptr;   // per recorded stage: W (4 nc) then G (8 nc), FP64 form only
+    size_t wg_slots_ = 0;
+    bool store_wg_ = false;
     size_t ckpt_slots_ = 0, seg_slots_ = 0;
     int fw_steps_ = 0, fw_k_ = 0;
     template <typename T> T* upload(const std::vector<T>& v);
@@ -109,6 +138,9 @@ private:
     cudaStream_t stream_ = nullptr;
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t gexec_ = nullptr;
+    std::vector<Instance> inst_;
+    void compute_tau_batch();
+    void rebuild_graph();
     std::vector<void*> allocs_;
     size_t bytes_ = 0;
     double* stage_ = nullptr;     // 4*nc staging for permutations and residuals

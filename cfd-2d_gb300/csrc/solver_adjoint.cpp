@@ -107,6 +107,23 @@ double Solver::forward(int nsteps, int k, int* status) {
         segstore_ = dalloc<double>((size_t)k * nst * 4 * nc);
         seg_slots_ = (size_t)k * nst;
     }
+    // keep each recorded stage's primitives and gradients when the segment's worth fits in a
+    // quarter of the free device memory (FP64 form; the mixed form's are FP32 and get re-derived)
+    store_wg_ = false;
+    if (task_.precision == PREC_FP64) {
+        const size_t need = (size_t)k * nst * 12 * nc;
+        if (need <= wg_slots_) {
+            store_wg_ = true;
+        } else {
+            size_t free_b = 0, total_b = 0;
+            CUDA_CHECK(cudaMemGetInfo(&free_b, &total_b));
+            if (need * sizeof(double) <= free_b / 4) {
+                wgstore_ = dalloc<double>(need);
+                wg_slots_ = need;
+                store_wg_ = true;
+            }
+        }
+    }
     CUDA_CHECK(cudaMemsetAsync(dc_.flags, 0, sizeof(unsigned) * nc, stream_));
     for (size_t s = 0; s < nseg; s++) {
         CUDA_CHECK(cudaMemcpyAsync(ckpt_ + s * 4 * nc, dc_.A, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice,
@@ -130,8 +147,9 @@ double Solver::forward(int nsteps, int k, int* status) {
     return J;
 }
 
-// One forward step that keeps every stage's input state in store[stage].
-void Solver::record_step(double* store) {
+// One forward step that keeps every stage's input state in store[stage] and,
+// when wg is given, the stage's primitives and gradients in wg[stage].
+void Solver::record_step(double* store, double* wg) {
     const size_t nc = dc_.nc;
     const int nst = n_stages(task_.scheme);
     const int p = task_.precision;
@@ -139,6 +157,13 @@ void Solver::record_step(double* store) {
         CUDA_CHECK(cudaMemcpyAsync(store + st * 4 * nc, st == 0 ? dc_.A : dc_.B, sizeof(double) * 4 * nc,
                                    cudaMemcpyDeviceToDevice, stream_));
         if (task_.recon != RECON_NONE) launch_grad(dc_, p, stream_);
+        if (wg) {
+            double* w = wg + (size_t)st * 12 * nc;
+            CUDA_CHECK(cudaMemcpyAsync(w, dc_.W64, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice, stream_));
+            if (task_.recon != RECON_NONE)
+                CUDA_CHECK(cudaMemcpyAsync(w + 4 * nc, dc_.G64, sizeof(double) * 8 * nc, cudaMemcpyDeviceToDevice,
+                                           stream_));
+        }
         launch_flux(dc_, p, task_.flux, task_.recon, stream_);
         launch_update(dc_, p, task_.scheme, st, stream_);
     }
@@ -163,7 +188,9 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
     a.eq = adj_eq_; a.eb = adj_eb_; a.eb2 = adj_eb2_; a.qbar = adj_qbar_; a.gbar = adj_gbar_;
     a.tb = adj_tb_; a.acc = adj_acc_; a.lam = adj_lam_; a.mu = adj_mu_; a.mu_out = adj_mu_;
     a.dbnd = adj_dbnd_; a.n_bnd = (int)task_.bnds.size();
-    CUDA_CHECK(cudaMemsetAsync(adj_dbnd_, 0, sizeof(double) * 4 * std::max<size_t>(task_.bnds.size(), 1), stream_));
+    const size_t nbe = 4 * (size_t)std::max(dc_.ne - dc_.n_int, 1);
+    CUDA_CHECK(cudaMemsetAsync(adj_eb_, 0, sizeof(double) * nbe, stream_));
+    CUDA_CHECK(cudaMemsetAsync(adj_eb2_, 0, sizeof(double) * nbe, stream_));
     // lambda = dJ/dU of the final state
     {
         DevCase cf = dc_;
@@ -178,24 +205,30 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
         CUDA_CHECK(cudaMemcpyAsync(dc_.A, ckpt_ + (size_t)seg * 4 * nc, sizeof(double) * 4 * nc,
                                    cudaMemcpyDeviceToDevice, stream_));
         launch_prims(dc_, task_.precision, stream_);
-        for (int j = 0; j < n; j++) record_step(segstore_ + (size_t)j * nst * 4 * nc);
+        for (int j = 0; j < n; j++)
+            record_step(segstore_ + (size_t)j * nst * 4 * nc, store_wg_ ? wgstore_ + (size_t)j * nst * 12 * nc : nullptr);
         for (int j = n - 1; j >= 0; j--) {
             launch_adj_step_start(adj_dc_, a, ct_f, ca_f, stream_);
             for (int st = nst - 1; st >= 0; st--) {
                 DevCase cx = adj_dc_;
                 cx.A = segstore_ + ((size_t)j * nst + st) * 4 * nc;
                 a.X = cx.A;
-                launch_prims(cx, PREC_FP64, stream_);
-                if (task_.recon != RECON_NONE) launch_grad(cx, PREC_FP64, stream_);
+                if (store_wg_) {  // the recorded stage's own W and G
+                    cx.W64 = wgstore_ + ((size_t)j * nst + st) * 12 * nc;
+                    cx.G64 = cx.W64 + 4 * nc;
+                } else {
+                    launch_prims(cx, PREC_FP64, stream_);
+                    if (task_.recon != RECON_NONE) launch_grad(cx, PREC_FP64, stream_);
+                }
                 launch_adj_flux(cx, a, task_.flux, task_.recon, stream_);
                 launch_adj_gather(cx, a, stream_);
                 double ct = 1.0, ca = 0.0;
                 if (st > 0) stage_coefs(task_.scheme, st, ct, ca);
                 launch_adj_cell(cx, a, ct, ca, st == 0 ? 1 : 0, stream_);
-                launch_adj_bnd_reduce(cx, a, stream_);
             }
         }
     }
+    launch_adj_bnd_reduce(adj_dc_, a, stream_);
     // the solver's state is the forward's final state again
     CUDA_CHECK(cudaMemcpyAsync(dc_.A, adj_final_, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice, stream_));
     launch_prims(dc_, task_.precision, stream_);

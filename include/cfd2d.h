@@ -76,6 +76,7 @@ typedef struct {
     double time;             /* t as the reference accumulates it (t += TAU per unsteady step) */
     double tau;              /* global time step TAU (unsteady) */
     size_t device_bytes;     /* device memory held by the handle */
+    int n_instances;         /* 1, or the number of instances of a batch */
 } cfd2d_info_t;
 
 /* FVM_TVD::init (src/methods/fvm_tvd.cpp:7-213): read task.xml and its mesh,
@@ -117,6 +118,27 @@ int cfd2d_residual(cfd2d_t* h, double* R);
 int cfd2d_conservation(cfd2d_t* h, double sums[4]);
 /* FVM_TVD::save (src/methods/fvm_tvd.cpp:501-600): res_%010d.vtk in the working directory. */
 int cfd2d_save_vtk(cfd2d_t* h, int step);
+
+/* ---- batches -------------------------------------------------------------- */
+/* No counterpart in the reference (one FVM_TVD per process there): n
+ * independent instances, each a task file and (meshes != NULL) its mesh as
+ * arrays, else the task's own mesh file, solved together by one set of kernels
+ * per stage over the union of their meshes. Instances share FLUX,
+ * RECONSTRUCTION, TIME_SCHEME, PRECISION, STEADY and the limits of the first
+ * task; each keeps its own mesh, regions, materials, boundary conditions, CFL
+ * and time step, and its results equal its single-instance solve bit for bit.
+ * The handle works with every entry point above; the state arrays hold the
+ * instances one after another (see cfd2d_batch_instance). */
+int cfd2d_batch_create(int n, const char* const* task_xml_paths, const cfd2d_mesh_desc* meshes, cfd2d_t** out);
+/* Instance k of a batch: first cell in the state arrays, cell count, its TAU and time. */
+int cfd2d_batch_instance(const cfd2d_t* h, int k, int* cell_offset, int* n_cells, double* tau, double* time);
+/* Time each kernel kind over block sizes {64,128,256} x grids {one thread per
+ * item, 1/2/4/8 persistent blocks per SM} on this handle's mesh, keep the
+ * fastest, re-capture the step graph, and write the choice as JSON to
+ * json_path (NULL: do not write). Results do not depend on the shapes. */
+int cfd2d_autotune(cfd2d_t* h, const char* json_path);
+/* Apply launch shapes saved by cfd2d_autotune. */
+int cfd2d_load_tuning(cfd2d_t* h, const char* json_path);
 
 /* ---- discrete adjoint (forward/backward pair) ---------------------------- */
 /* Objective of the final state: J = sum_i w_i (p_i - p_ref)^2 (kind 0) or
