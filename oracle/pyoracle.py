@@ -243,7 +243,8 @@ def run_reference(task_xml: str, unv_text: str, U0=None, timeout=120, workdir=No
         r = subprocess.run(args, cwd=d, capture_output=True, text=True, timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError("reference run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+        vtk = {f: open(os.path.join(d, f)).read() for f in sorted(os.listdir(d)) if f.endswith(".vtk")}
         return dict(grid=read_ref_grid(os.path.join(d, "out.grid.bin")),
                     init=read_ref_state(os.path.join(d, "out.init.bin")),
                     final=read_ref_state(os.path.join(d, "out.state.bin")),
-                    stdout=r.stdout)
+                    stdout=r.stdout, vtk=vtk)

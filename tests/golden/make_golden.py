@@ -48,7 +48,7 @@ def two_region_case(n, steps, seed, pr=0.5, bkinds=BK4, steady=0, shuffle=False)
     m.bseg_bnd = m.bseg_side.copy()
     t = mg.Task(regions=[mg.Region("left", 0.0, 0.0, 1.0, 1.0), mg.Region("right", 0.0, 0.0, 1.0, pr)],
                 boundaries=[mg.Boundary(f"bnd{k}", bk, k + 1, 0.1, 0.0, 1.0, 1.0) for k, bk in enumerate(bkinds)],
-                step_max=steps, steady=steady)
+                step_max=steps, steady=steady, file_output_step=steps, log_output_step=max(1, steps // 2))
     return m, t, None
 
 
@@ -88,9 +88,12 @@ def main():
         unv = mg.write_unv(m, region_names, bnd_names)
         ref = po.run_reference(xml, unv, U0)
         g, fi, ff = ref["grid"], ref["init"], ref["final"]
+        solver_lines = [ln for ln in ref["stdout"].splitlines() if ln.startswith(("time step:", "step:", "File '"))]
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"),
             task_xml=np.array(xml), mesh_unv=np.array(unv),
+            ref_vtk_names=np.array(list(ref["vtk"].keys())), ref_vtk=np.array(list(ref["vtk"].values())),
+            ref_log=np.array("\n".join(solver_lines)),
             nodes=m.nodes, tris=m.tris, cell_region=m.cell_region, bsegs=m.bsegs, bseg_bnd=m.bseg_bnd,
             region_names=np.array(region_names), bnd_names=np.array(bnd_names),
             U0=np.zeros((0,)) if U0 is None else U0, steps=np.int32(t.step_max),
