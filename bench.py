@@ -403,7 +403,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--n", type=int, default=N_SIDE, help="squares per side (profiling runs only)")
-    ap.add_argument("--workload", default="four_quadrant", choices=["four_quadrant", "batched", "combined"],
+    ap.add_argument("--workload", default="four_quadrant", choices=["four_quadrant", "batched", "combined", "adjoint"],
                     help="four_quadrant: the headline 2.1M-triangle line; batched: 256 uneven vortex instances")
     ap.add_argument("--instances", type=int, default=256)
     args = ap.parse_args()
@@ -424,6 +424,17 @@ def main():
         return
     if args.workload == "combined":
         combined_workload(args, capi, cases, world, rank, dist, W, K)
+        return
+    if args.workload == "adjoint":  # one checkpointed forward + backward of K steps (profiling runs)
+        t, m, U0, w, _ = cases.vortex_adjoint(256, steps=K)
+        s = capi.Solver(cases.write_task(t, m, tempfile.mkdtemp()), mesh=m)
+        s.set_objective(0, w, 1.0)
+        s.set_state(U0)
+        J = s.forward(K, max(1, K // 2))
+        g, _ = s.backward()
+        if rank == 0:
+            print(json.dumps({"profiling_run": True, "workload": "adjoint", "steps": K, "J": J,
+                              "grad_norm": float(np.linalg.norm(g))}), flush=True)
         return
 
     d = tempfile.mkdtemp(prefix="cfd2d_bench_")

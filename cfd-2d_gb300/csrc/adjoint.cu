@@ -82,12 +82,12 @@ __global__ void __launch_bounds__(256) k_adj_flux(const DevCase c, const AdjCase
             double g[8];
             dxL = DL[(4 * gp) * ne + e]; dyL = DL[(4 * gp + 1) * ne + e];
             ld8(G, c1, g);
-            project(g, dxL, dyL, aL);
+            project<RECON>(g, dxL, dyL, aL);
             pL = recon_a<RECON>(qL, aL, inner ? qR : gc);
             if (inner) {
                 dxR = DL[(4 * gp + 2) * ne + e]; dyR = DL[(4 * gp + 3) * ne + e];
                 ld8(G, c2, g);
-                project(g, dxR, dyR, aR);
+                project<RECON>(g, dxR, dyR, aR);
                 pR = recon_a<RECON>(qR, aR, qL);
             }
         }

@@ -123,9 +123,9 @@ __device__ __forceinline__ void vjp_hllc(const Prim<double>& L, const Prim<doubl
     const double IG1 = 1.0 / (GAM - 1.0);
     const double aL = GAM * L.p / L.r, aR = GAM * R.p / R.r;
     const double cL = sqrt(aL), cR = sqrt(aR);
-    const double unL = L.u * nx + L.v * ny, unR = R.u * nx + R.v * ny;
-    const double EL = L.p * IG1 + 0.5 * L.r * (L.u * L.u + L.v * L.v);
-    const double ER = R.p * IG1 + 0.5 * R.r * (R.u * R.u + R.v * R.v);
+    const double unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
+    const double EL = energy(L.r, L.u, L.v, L.p, IG1);
+    const double ER = energy(R.r, R.u, R.v, R.p, IG1);
     const double sl1 = unL - cL, sl2 = unR - cR, sr1 = unL + cL, sr2 = unR + cR;
     const bool l1 = sl1 < sl2, r1 = sr1 > sr2;
     const double SL = l1 ? sl1 : sl2, SR = r1 ? sr1 : sr2;
@@ -135,14 +135,14 @@ __device__ __forceinline__ void vjp_hllc(const Prim<double>& L, const Prim<doubl
         else vjp_phys(R.r, R.u, R.v, R.p, ER, unR, nx, ny, fb, Rb.r, Rb.u, Rb.v, Rb.p, ERb, unRb);
     } else {
         const double mL = L.r * (SL - unL), mR = R.r * (SR - unR);
-        const double num = R.p - L.p + mL * unL - mR * unR, den = mL - mR;
+        const double num = fma(-mR, unR, fma(mL, unL, R.p - L.p)), den = mL - mR;
         const double Ss = num / den;
         const bool left = Ss >= 0.0;
         const Prim<double>& K = left ? L : R;
         const double SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
         const double m = K.r * unK;
         const double FK0 = m, FK1 = m * K.u + K.p * nx, FK2 = m * K.v + K.p * ny, FK3 = (EK + K.p) * unK;
-        const double ps = K.p + mK * (Ss - unK);
+        const double ps = fma(mK, Ss - unK, K.p);
         const double inv = 1.0 / (SK - Ss);
         const double sp = SK * ps;
         const double A0 = SK * K.r - FK0, A1 = SK * (K.r * K.u) - FK1, A2 = SK * (K.r * K.v) - FK2,
@@ -231,11 +231,12 @@ __device__ __forceinline__ void vjp_reconstruct_a(const Prim<double>& q, const d
 }
 
 // Projections a = g . dl of one side's four gradients, as reconstruct() forms them.
+template <int RECON>
 __device__ __forceinline__ void project(const double* g, double dx, double dy, double* a) {
-    a[0] = g[0] * dx + g[1] * dy;
-    a[1] = g[2] * dx + g[3] * dy;
-    a[2] = g[4] * dx + g[5] * dy;
-    a[3] = g[6] * dx + g[7] * dy;
+    a[0] = proj<double, RECON>(g[0], g[1], dx, dy);
+    a[1] = proj<double, RECON>(g[2], g[3], dx, dy);
+    a[2] = proj<double, RECON>(g[4], g[5], dx, dy);
+    a[3] = proj<double, RECON>(g[6], g[7], dx, dy);
 }
 
 // The forward reconstruction from the projections (kernels.cuh reconstruct).

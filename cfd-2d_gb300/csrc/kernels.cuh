@@ -27,6 +27,8 @@ __device__ __forceinline__ double t_log(double x) { return log(x); }
 __device__ __forceinline__ float t_log(float x) { return logf(x); }
 __device__ __forceinline__ double t_abs(double x) { return fabs(x); }
 __device__ __forceinline__ float t_abs(float x) { return fabsf(x); }
+__device__ __forceinline__ double t_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float t_fma(float a, float b, float c) { return fmaf(a, b, c); }
 template <typename T> __device__ __forceinline__ T t_max(T a, T b) { return a > b ? a : b; }  // _max_, src/mesh/grid.h:102
 template <typename T> __device__ __forceinline__ T t_min(T a, T b) { return a < b ? a : b; }
 
@@ -361,13 +363,19 @@ __device__ __forceinline__ void flux_lax(T* f, const Prim<T>& L, const Prim<T>& 
     f[3] = T(0.5) * ((rer + R.p) * unr + (rel + L.p) * unl - alpha * (rer - rel));
 }
 
+// The fluxes below (HLLC, Roe, the minmod increment) have no counterpart in the
+// reference; their multiply-adds are fused, exactly as the oracle defines them.
 template <typename T>
 __device__ __forceinline__ void phys_flux(T* f, T r, T u, T v, T p, T E, T un, T nx, T ny) {
     T m = r * un;
     f[0] = m;
-    f[1] = m * u + p * nx;
-    f[2] = m * v + p * ny;
+    f[1] = t_fma(m, u, p * nx);
+    f[2] = t_fma(m, v, p * ny);
     f[3] = (E + p) * un;
+}
+template <typename T> __device__ __forceinline__ T dot2(T a, T x, T b, T y) { return t_fma(a, x, b * y); }
+template <typename T> __device__ __forceinline__ T energy(T r, T u, T v, T p, T IG1) {
+    return t_fma(p, IG1, (T(0.5) * r) * t_fma(u, u, v * v));
 }
 
 // HLLC (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, sec. 10.4-10.6),
@@ -378,26 +386,26 @@ template <typename T>
 __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM) {
     const T IG1 = T(1.0) / (GAM - T(1.0));
     T cL = t_sqrt(GAM * L.p / L.r), cR = t_sqrt(GAM * R.p / R.r);
-    T unL = L.u * nx + L.v * ny, unR = R.u * nx + R.v * ny;
-    T EL = L.p * IG1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
-    T ER = R.p * IG1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
+    T EL = energy(L.r, L.u, L.v, L.p, IG1);
+    T ER = energy(R.r, R.u, R.v, R.p, IG1);
     T SL = t_min(unL - cL, unR - cR), SR = t_max(unL + cL, unR + cR);
     if (SL >= T(0.0)) { phys_flux(f, L.r, L.u, L.v, L.p, EL, unL, nx, ny); return; }
     if (SR <= T(0.0)) { phys_flux(f, R.r, R.u, R.v, R.p, ER, unR, nx, ny); return; }
     T mL = L.r * (SL - unL), mR = R.r * (SR - unR);
-    T Ss = (R.p - L.p + mL * unL - mR * unR) / (mL - mR);
+    T Ss = t_fma(-mR, unR, t_fma(mL, unL, R.p - L.p)) / (mL - mR);
     const bool left = Ss >= T(0.0);
     const Prim<T>& K = left ? L : R;
     T SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
     T FK[4];
     phys_flux(FK, K.r, K.u, K.v, K.p, EK, unK, nx, ny);
-    T ps = K.p + mK * (Ss - unK);
+    T ps = t_fma(mK, Ss - unK, K.p);
     T inv = T(1.0) / (SK - Ss);
     T sp = SK * ps;
-    f[0] = (Ss * (SK * K.r - FK[0])) * inv;
-    f[1] = (Ss * (SK * (K.r * K.u) - FK[1]) + sp * nx) * inv;
-    f[2] = (Ss * (SK * (K.r * K.v) - FK[2]) + sp * ny) * inv;
-    f[3] = (Ss * (SK * EK - FK[3]) + sp * Ss) * inv;
+    f[0] = (Ss * t_fma(SK, K.r, -FK[0])) * inv;
+    f[1] = t_fma(Ss, t_fma(SK, K.r * K.u, -FK[1]), sp * nx) * inv;
+    f[2] = t_fma(Ss, t_fma(SK, K.r * K.v, -FK[2]), sp * ny) * inv;
+    f[3] = t_fma(Ss, t_fma(SK, EK, -FK[3]), sp * Ss) * inv;
 }
 
 // Roe flux (Roe 1981) in the face-normal frame with the Harten-Hyman entropy fix
@@ -406,9 +414,9 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
 template <typename T>
 __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM) {
     T G1 = GAM - T(1.0), IG1 = T(1.0) / (GAM - T(1.0));
-    T unL = L.u * nx + L.v * ny, unR = R.u * nx + R.v * ny;
-    T EL = L.p * IG1 + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
-    T ER = R.p * IG1 + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
+    T EL = energy(L.r, L.u, L.v, L.p, IG1);
+    T ER = energy(R.r, R.u, R.v, R.p, IG1);
     T HL = (EL + L.p) / L.r, HR = (ER + R.p) / R.r;
     T sL = t_sqrt(L.r), sR = t_sqrt(R.r);
     T w = T(1.0) / (sL + sR);
@@ -510,12 +518,20 @@ __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
     for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) grad_one<T>(c, i);  // persistent grid
 }
 
+// Projection g . dl of one gradient: the reference's reconstruction (LINEAR)
+// unfused, this project's minmod increment fused.
+template <typename T, int RECON>
+__device__ __forceinline__ T proj(T gx, T gy, T dx, T dy) {
+    if (RECON == RECON_MINMOD) return dot2(gx, dx, gy, dy);
+    return gx * dx + gy * dy;
+}
+
 template <typename T, int RECON>
 __device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, const Prim<T>& nb) {
-    T dr = g[0] * dx + g[1] * dy;
-    T dp = g[2] * dx + g[3] * dy;
-    T du = g[4] * dx + g[5] * dy;
-    T dv = g[6] * dx + g[7] * dy;
+    T dr = proj<T, RECON>(g[0], g[1], dx, dy);
+    T dp = proj<T, RECON>(g[2], g[3], dx, dy);
+    T du = proj<T, RECON>(g[4], g[5], dx, dy);
+    T dv = proj<T, RECON>(g[6], g[7], dx, dy);
     if (RECON == RECON_MINMOD) {
         dr = minmod(dr, nb.r - q.r);
         dp = minmod(dp, nb.p - q.p);

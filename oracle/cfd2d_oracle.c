@@ -442,13 +442,22 @@ static void flux_lax(double* f, const Par* pL, const Par* pR, double nx, double 
 }
 
 /* Physical flux through the unit normal n for a primitive state; E is the total
- * energy per unit volume. */
+ * energy per unit volume. The fluxes defined here (HLLC, Roe, the minmod
+ * increment) have no counterpart in the reference; their multiply-adds are
+ * fused (C99 fma), exactly as the GPU evaluates them. */
 static void phys_flux(double* f, double r, double u, double v, double p, double E, double un, double nx, double ny) {
     double m = r * un;
     f[0] = m;
-    f[1] = m * u + p * nx;
-    f[2] = m * v + p * ny;
+    f[1] = fma(m, u, p * nx);
+    f[2] = fma(m, v, p * ny);
     f[3] = (E + p) * un;
+}
+
+/* a x + b y with one rounding less */
+static double dot2(double a, double x, double b, double y) { return fma(a, x, b * y); }
+/* kinetic part p*IG1 + (0.5 r)(u^2 + v^2) of the total energy */
+static double energy(double r, double u, double v, double p, double IG1) {
+    return fma(p, IG1, (0.5 * r) * fma(u, u, v * v));
 }
 
 /* HLLC flux (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics,
@@ -462,26 +471,26 @@ static void phys_flux(double* f, double r, double u, double v, double p, double 
 static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
     double IG1 = 1.0 / (GAM - 1.0);
     double cL = sqrt(GAM * pL->p / pL->r), cR = sqrt(GAM * pR->p / pR->r);
-    double unL = pL->u * nx + pL->v * ny, unR = pR->u * nx + pR->v * ny;
-    double EL = pL->p * IG1 + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
-    double ER = pR->p * IG1 + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
+    double unL = dot2(pL->u, nx, pL->v, ny), unR = dot2(pR->u, nx, pR->v, ny);
+    double EL = energy(pL->r, pL->u, pL->v, pL->p, IG1);
+    double ER = energy(pR->r, pR->u, pR->v, pR->p, IG1);
     double SL = dmin(unL - cL, unR - cR), SR = dmax(unL + cL, unR + cR);
     if (SL >= 0.0) { phys_flux(f, pL->r, pL->u, pL->v, pL->p, EL, unL, nx, ny); return; }
     if (SR <= 0.0) { phys_flux(f, pR->r, pR->u, pR->v, pR->p, ER, unR, nx, ny); return; }
     double mL = pL->r * (SL - unL), mR = pR->r * (SR - unR);
-    double Ss = (pR->p - pL->p + mL * unL - mR * unR) / (mL - mR);
+    double Ss = fma(-mR, unR, fma(mL, unL, pR->p - pL->p)) / (mL - mR);
     const Par* K; double SK, unK, EK, mK;
     if (Ss >= 0.0) { K = pL; SK = SL; unK = unL; EK = EL; mK = mL; }
     else { K = pR; SK = SR; unK = unR; EK = ER; mK = mR; }
     double FK[4];
     phys_flux(FK, K->r, K->u, K->v, K->p, EK, unK, nx, ny);
-    double ps = K->p + mK * (Ss - unK);
+    double ps = fma(mK, Ss - unK, K->p);
     double inv = 1.0 / (SK - Ss);
     double sp = SK * ps;
-    f[0] = (Ss * (SK * K->r - FK[0])) * inv;
-    f[1] = (Ss * (SK * (K->r * K->u) - FK[1]) + sp * nx) * inv;
-    f[2] = (Ss * (SK * (K->r * K->v) - FK[2]) + sp * ny) * inv;
-    f[3] = (Ss * (SK * EK - FK[3]) + sp * Ss) * inv;
+    f[0] = (Ss * fma(SK, K->r, -FK[0])) * inv;
+    f[1] = fma(Ss, fma(SK, K->r * K->u, -FK[1]), sp * nx) * inv;
+    f[2] = fma(Ss, fma(SK, K->r * K->v, -FK[2]), sp * ny) * inv;
+    f[3] = fma(Ss, fma(SK, EK, -FK[3]), sp * Ss) * inv;
 }
 
 /* Roe flux (Roe, J. Comput. Phys. 43, 1981) in the face-normal frame with the
@@ -491,9 +500,9 @@ static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double
  * (src/global.cpp:407-441). */
 static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
     double G1 = GAM - 1.0, IG1 = 1.0 / (GAM - 1.0);
-    double unL = pL->u * nx + pL->v * ny, unR = pR->u * nx + pR->v * ny;
-    double EL = pL->p * IG1 + 0.5 * pL->r * (pL->u * pL->u + pL->v * pL->v);
-    double ER = pR->p * IG1 + 0.5 * pR->r * (pR->u * pR->u + pR->v * pR->v);
+    double unL = dot2(pL->u, nx, pL->v, ny), unR = dot2(pR->u, nx, pR->v, ny);
+    double EL = energy(pL->r, pL->u, pL->v, pL->p, IG1);
+    double ER = energy(pR->r, pR->u, pR->v, pR->p, IG1);
     double HL = (EL + pL->p) / pL->r, HR = (ER + pR->p) / pR->r;
     double sL = sqrt(pL->r), sR = sqrt(pR->r);
     double w = 1.0 / (sL + sR);
@@ -641,10 +650,14 @@ static void recon_side(const orc_solver* s, int c, double px, double py, Par* q,
     const orc_mesh* m = s->m;
     const double* g = s->grad + 8 * (size_t)c;
     double dx = px - m->cx[c], dy = py - m->cy[c];
-    double dr = g[0] * dx + g[1] * dy;
-    double dp = g[2] * dx + g[3] * dy;
-    double du = g[4] * dx + g[5] * dy;
-    double dv = g[6] * dx + g[7] * dy;
+    double dr, dp, du, dv;
+    if (s->p.recon == ORC_RECON_MINMOD) { /* this project's limiter: fused projections */
+        dr = dot2(g[0], dx, g[1], dy); dp = dot2(g[2], dx, g[3], dy);
+        du = dot2(g[4], dx, g[5], dy); dv = dot2(g[6], dx, g[7], dy);
+    } else {                              /* the reference's reconstruction, unfused */
+        dr = g[0] * dx + g[1] * dy; dp = g[2] * dx + g[3] * dy;
+        du = g[4] * dx + g[5] * dy; dv = g[6] * dx + g[7] * dy;
+    }
     if (s->p.recon == ORC_RECON_MINMOD) {
         dr = minmod(dr, nb->r - q->r);
         dp = minmod(dp, nb->p - q->p);
