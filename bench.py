@@ -466,9 +466,15 @@ def main():
     sampler.stop()
     clocks = sampler.summary()
     if not full:
+        line = {"profiling_run": True, "forms": forms, "cells": nc, "steps": K, "warmup": W,
+                "ms_per_step": {f: ms_of[f] / K for f in forms}}
+        if not args.no_profile:  # per-kernel device ms per launch, launched kernel by kernel with events
+            line["ms_per_launch"] = {}
+            for f in forms:
+                ms, cnt = solvers[f].profile_steps(3)
+                line["ms_per_launch"][f] = {k: round(float(ms[i] / max(cnt[i], 1)), 5) for i, k in enumerate(KINDS)}
         if rank == 0:
-            print(json.dumps({"profiling_run": True, "forms": forms, "cells": nc, "steps": K, "warmup": W,
-                              "ms_per_step": {f: ms_of[f] / K for f in forms}}), flush=True)
+            print(json.dumps(line), flush=True)
         return
     s64, smx = solvers["fp64"], solvers["mixed"]
     ms64, msmx = ms_of["fp64"], ms_of["mixed"]

@@ -371,7 +371,7 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
 
 int cfd2d_selftest(int which, long long n, unsigned long long seed, long long* mismatches) {
     return guarded([&] {
-        if (!mismatches || which < 0 || which > 2 || n < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
+        if (!mismatches || which < 0 || which > 3 || n < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
         long long r = cfd2d::selftest_arith(which, n, seed);
         if (r < 0) return fail(CFD2D_ERR_CUDA, "self-test launch failed");
         *mismatches = r;

@@ -138,12 +138,26 @@ __global__ void k_selftest(int which, long long n, unsigned long long seed, unsi
                                                               (r1 & 0x8000000000000000ull)));
             const double b = __longlong_as_double((long long)((((r2 >> 52) % 1400) + 324ull) << 52 |
                                                               (mix64(r1) & 0xfffffffffffffull)));
-            const double y = 1.0 / b;
-            const double q1 = div_rn(a, b, y), q2 = a / b;
+            double a2 = a, b2 = b;
+            if ((r1 & 0xf0) == 0) a2 = (r1 & 0x100) ? -0.0 : 0.0;      // zero dividends, both signs
+            if ((r2 & 0xf00) == 0) b2 = __longlong_as_double((long long)(r2 & 0xfff0000000000000ull));  // any exponent
+            const double y = 1.0 / b2;
+            const double q1 = div_rn(a2, b2, y), q2 = a2 / b2;
             local += __double_as_longlong(q1) != __double_as_longlong(q2);
         } else if (which == 1) {  // widening of random normal floats
             const float f = __uint_as_float((unsigned)(((r1 % 254) + 1) << 23) | (unsigned)(r2 & 0x807fffffu));
             local += __double_as_longlong(widen(f)) != __double_as_longlong((double)f);
+        } else if (which == 3) {  // minmod against the reference's a*b > 0 ? (|a|<|b| ? a : b) : 0
+            // exponent fields over the whole range (zero, subnormal, normal, inf/NaN), with extra
+            // weight near the product's underflow threshold (sum of fields ~ 972)
+            const unsigned long long ex1 = (r1 & 3) == 0 ? (r1 >> 8) % 2048 : 300 + (r1 >> 8) % 400;
+            const unsigned long long ex2 = (r2 & 3) == 0 ? (r2 >> 8) % 2048 : 972 - ex1 + (long long)((r2 >> 8) % 9) - 4;
+            const unsigned long long m1 = (r1 & 12) == 0 ? 0 : mix64(r2) & 0xfffffffffffffull;
+            const unsigned long long m2 = (r2 & 12) == 0 ? 0 : mix64(r1) & 0xfffffffffffffull;
+            const double a = __longlong_as_double((long long)((r1 & 0x8000000000000000ull) | (ex1 & 0x7ff) << 52 | m1));
+            const double b = __longlong_as_double((long long)(((r2 << 1) & 0x8000000000000000ull) | (ex2 & 0x7ff) << 52 | m2));
+            const double ref = a * b > 0.0 ? (fabs(a) < fabs(b) ? a : b) : 0.0;
+            local += __double_as_longlong(minmod(a, b)) != __double_as_longlong(ref);
         } else {  // narrowing of random doubles in float range: within 1 ulp of the hardware's
             const double d = __longlong_as_double((long long)(((r1 % 250) + 1023 - 124) << 52 | (r2 & 0x800fffffffffffffull)));
             const int u1 = __float_as_int(narrow(d)), u2 = __float_as_int((float)d);

@@ -122,24 +122,43 @@ template <> __device__ __forceinline__ MatT<float> matT_of<float>(const DevCase&
 template <typename T> __device__ __forceinline__ T gam_of(const DevCase& c);
 template <> __device__ __forceinline__ double gam_of<double>(const DevCase& c) { return c.gam_flux; }
 template <> __device__ __forceinline__ float gam_of<float>(const DevCase& c) { return c.gam_flux_f; }
+template <typename T> __device__ __forceinline__ T ig1_of(const DevCase& c);
+template <> __device__ __forceinline__ double ig1_of<double>(const DevCase& c) { return c.ig1_flux; }
+template <> __device__ __forceinline__ float ig1_of<float>(const DevCase& c) { return c.ig1_flux_f; }
 
 // a / b correctly rounded from y = RN(1/b): q = RN(a y), r = a - b q exactly
 // (one FMA), result RN(q + r y) (Markstein, "IA-64 and Elementary Functions",
 // 2000, the division theorem). Three FP64 instructions instead of a full
 // division; the exponent guard keeps a, y and the quotient far from underflow
-// and overflow, where the theorem needs no extra conditions, and divides
-// outright otherwise (zero, subnormal, huge, inf, NaN).
+// and overflow, where the theorem needs no extra conditions. A zero dividend
+// over a finite y (b nonzero, not NaN) gives the zero with the sign of a XOR b,
+// built on the integer pipe (zero gradients and velocities are common). Other
+// operands (subnormal, huge, inf, NaN, b zero) divide outright.
+// The outright division sits in a function of its own so that the compiler
+// branches to it instead of evaluating it beside the common path.
+static __device__ __noinline__ double div_outright(double a, double b) { return a / b; }
 __device__ __forceinline__ double div_rn(double a, double b, double y) {
-    const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
-    const int ey = (int)((__double_as_longlong(y) >> 52) & 0x7ff);
+    const long long ia = __double_as_longlong(a), iy = __double_as_longlong(y);
+    const int ea = (int)((ia >> 52) & 0x7ff);
+    const int ey = (int)((iy >> 52) & 0x7ff);
     const int eq = ea + ey - 1023;
-    if (ea > 0x100 && ea < 0x700 && ey > 0x100 && ey < 0x700 && eq > 0x100 && eq < 0x700) {
+    if (__builtin_expect(ea > 0x100 && ea < 0x700 && ey > 0x100 && ey < 0x700 && eq > 0x100 && eq < 0x700, 1)) {
         const double q = a * y;
         const double r = fma(-q, b, a);
         return fma(r, y, q);
     }
-    return a / b;
+    if ((ia & 0x7fffffffffffffffll) == 0 && ey < 0x7ff)
+        return __longlong_as_double((ia ^ iy) & (long long)0x8000000000000000ull);
+    return div_outright(a, b);
 }
+// -x when s, else x: a sign-bit flip on the integer pipe (x - y is x + (-y) in IEEE).
+__device__ __forceinline__ double neg_if(double x, bool s) {
+    return __hiloint2double(__double2hiint(x) ^ (s ? (int)0x80000000 : 0), __double2loint(x));
+}
+__device__ __forceinline__ float neg_if(float x, bool s) { return __int_as_float(__float_as_int(x) ^ (s ? (int)0x80000000 : 0)); }
+// a / b given y = RN(1/b): the correctly rounded quotient in FP64, a * y in the FP32 faces.
+__device__ __forceinline__ double div_by(double a, double b, double y) { return div_rn(a, b, y); }
+__device__ __forceinline__ float div_by(float a, float, float y) { return a * y; }
 
 // convertConsToPar + Material::URS(0), src/methods/fvm_tvd.cpp:803-813, src/global.cpp:15-18
 template <typename T>
@@ -190,15 +209,25 @@ __device__ __forceinline__ Prim<T> ghost_state(const DevBnd& b, const Prim<T>& q
 }
 
 // MINMOD, src/methods/LimiterDGCockburn.cpp:110-123: a*b > 0 ? (|a| < |b| ? a : b) : 0.
-// The sign test reads the bits of the rounded product a*b (positive, non-NaN
-// doubles are exactly the patterns in (0, 0x7ff0...0]) and |a| < |b| compares
-// magnitude bits, which orders non-NaN values like fabs does; the result is the
-// reference's bit for bit with one FP64 multiply instead of three FP64 compares.
+// |a| < |b| compares magnitude bits, which orders non-NaN values like fabs does.
+// The sign test runs on the integer pipe: a zero operand gives a product of +-0
+// or NaN (0 * inf), never > 0; for normal or infinite operands of one sign whose
+// exponent fields sum to at least 972, |a b| >= 2^(ea+eb-2046) >= 2^-1074, so the
+// rounded product is > 0 (or +inf); NaN or opposite signs fail the test.
+// Subnormal operands and products near the underflow threshold take the FP64
+// multiply and read the sign of its bits (positive, non-NaN doubles are exactly
+// the patterns in (0, 0x7ff0...0]). Bit for bit the reference's result.
 __device__ __forceinline__ double minmod(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7fffffffffffffffll, mb = ib & 0x7fffffffffffffffll;
+    if (ma == 0 || mb == 0) return 0.0;
+    const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
+    if (ea >= 1 && eb >= 1 && ea + eb >= 972) {
+        if ((ia ^ ib) < 0 || ma > 0x7ff0000000000000ll || mb > 0x7ff0000000000000ll) return 0.0;
+        return ma < mb ? a : b;
+    }
     const long long pb = __double_as_longlong(a * b);
     if (pb <= 0 || pb > 0x7ff0000000000000ll) return 0.0;
-    const long long ma = __double_as_longlong(a) & 0x7fffffffffffffffll;
-    const long long mb = __double_as_longlong(b) & 0x7fffffffffffffffll;
     return ma < mb ? a : b;
 }
 __device__ __forceinline__ float minmod(float a, float b) {
@@ -348,14 +377,14 @@ __device__ __forceinline__ bool flux_godunov(T* f, const Prim<T>& L, const Prim<
 
 // Lax-Friedrichs (Rusanov), the reference's template src/methods/fvm_tvd_implicit.cpp:939-960
 template <typename T>
-__device__ __forceinline__ void flux_lax(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM) {
+__device__ __forceinline__ void flux_lax(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
     T unl = L.u * nx + L.v * ny;
     T unr = R.u * nx + R.v * ny;
     T alpha = t_max(t_abs(unl) + t_sqrt(GAM * L.p / L.r), t_abs(unr) + t_sqrt(GAM * R.p / R.r));
     T rol = L.r, rul = L.r * L.u, rvl = L.r * L.v;
-    T rel = L.p / (GAM - T(1.0)) + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
+    T rel = div_by(L.p, GAM - T(1.0), IG1) + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
     T ror = R.r, rur = R.r * R.u, rvr = R.r * R.v;
-    T rer = R.p / (GAM - T(1.0)) + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    T rer = div_by(R.p, GAM - T(1.0), IG1) + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
     T frl = rol * unl, frr = ror * unr;
     f[0] = T(0.5) * (frr + frl - alpha * (ror - rol));
     f[1] = T(0.5) * (frr * R.u + frl * L.u + (R.p + L.p) * nx - alpha * (rur - rul));
@@ -383,8 +412,7 @@ template <typename T> __device__ __forceinline__ T energy(T r, T u, T v, T p, T 
 // F*_K = [S*(S_K U_K - F_K) + S_K p* D*] / (S_K - S*), D* = (0, nx, ny, S*),
 // p* = p_K + rho_K (S_K - un_K)(S* - un_K): one division instead of Toro's star state.
 template <typename T>
-__device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM) {
-    const T IG1 = T(1.0) / (GAM - T(1.0));
+__device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
     T cL = t_sqrt(GAM * L.p / L.r), cR = t_sqrt(GAM * R.p / R.r);
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     T EL = energy(L.r, L.u, L.v, L.p, IG1);
@@ -412,12 +440,13 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
 // on the acoustic waves: delta = max(0, lam~ - lam_L, lam_R - lam~), |lam~| -> delta
 // where |lam~| < delta. Roe averages as in roe_orig (src/global.cpp:407-441).
 template <typename T>
-__device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM) {
-    T G1 = GAM - T(1.0), IG1 = T(1.0) / (GAM - T(1.0));
+__device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
+    T G1 = GAM - T(1.0);
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     T EL = energy(L.r, L.u, L.v, L.p, IG1);
     T ER = energy(R.r, R.u, R.v, R.p, IG1);
-    T HL = (EL + L.p) / L.r, HR = (ER + R.p) / R.r;
+    const T yL = T(1.0) / L.r, yR = T(1.0) / R.r;  // each shared by two quotients below
+    T HL = div_by(EL + L.p, L.r, yL), HR = div_by(ER + R.p, R.r, yR);
     T sL = t_sqrt(L.r), sR = t_sqrt(R.r);
     T w = T(1.0) / (sL + sR);
     T ut = (sL * L.u + sR * R.u) * w;
@@ -435,7 +464,7 @@ __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& 
     T a2 = dr - dp * ic2;
     T a4 = (dp + rt * c * dun) * (T(0.5) * ic2);
     T l1 = unt - c, l4 = unt + c;
-    T cL = t_sqrt(GAM * L.p / L.r), cR = t_sqrt(GAM * R.p / R.r);
+    T cL = t_sqrt(div_by(GAM * L.p, L.r, yL)), cR = t_sqrt(div_by(GAM * R.p, R.r, yR));
     T d1 = t_max(T(0.0), t_max(l1 - (unL - cL), (unR - cR) - l1));
     T d4 = t_max(T(0.0), t_max(l4 - (unL + cL), (unR + cR) - l4));
     T al1 = t_abs(l1); if (al1 < d1) al1 = d1;
@@ -456,10 +485,11 @@ __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& 
 }
 
 template <typename T, int FLUX>
-__device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, int cap) {
-    if (FLUX == FLUX_LAX) { flux_lax(f, L, R, nx, ny, GAM); return false; }
-    if (FLUX == FLUX_ROE) { flux_roe(f, L, R, nx, ny, GAM); return false; }
-    if (FLUX == FLUX_HLLC) { flux_hllc(f, L, R, nx, ny, GAM); return false; }
+__device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1,
+                                         int cap) {
+    if (FLUX == FLUX_LAX) { flux_lax(f, L, R, nx, ny, GAM, IG1); return false; }
+    if (FLUX == FLUX_ROE) { flux_roe(f, L, R, nx, ny, GAM, IG1); return false; }
+    if (FLUX == FLUX_HLLC) { flux_hllc(f, L, R, nx, ny, GAM, IG1); return false; }
     return flux_godunov(f, L, R, nx, ny, GAM, cap);
 }
 
@@ -489,12 +519,13 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
             const T Tc = temperature(q, mt.gm1, mt.Cv);
             o = ghost_state(c.bnds[c.ebnd[e]], q, Tc, nx, ny, mt.M);
         }
-        const T hr = (q.r + o.r) / T(2), hp = (q.p + o.p) / T(2);
-        const T hu = (q.u + o.u) / T(2), hv = (q.v + o.v) / T(2);
+        // x * 0.5 is the correctly rounded x / 2 (exact halving), without a division
+        const T hr = (q.r + o.r) * T(0.5), hp = (q.p + o.p) * T(0.5);
+        const T hu = (q.u + o.u) * T(0.5), hv = (q.v + o.v) * T(0.5);
         const T v[8] = {hr * nx * l, hr * ny * l, hp * nx * l, hp * ny * l,
                         hu * nx * l, hu * ny * l, hv * nx * l, hv * ny * l};
 #pragma unroll
-        for (int m = 0; m < 8; m++) g[m] = g[m] + (side2 ? -v[m] : v[m]);  // x - y is x + (-y) in IEEE
+        for (int m = 0; m < 8; m++) g[m] = g[m] + neg_if(v[m], side2);  // c2 subtracts, c1 adds
     }
     if constexpr (sizeof(T) == 8) {
         const double s = c.S[i], y = c.invS[i];  // y = RN(1/S), computed on the host
@@ -549,7 +580,7 @@ __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
     const T* __restrict__ G = G_of<T>(c);
     const T* __restrict__ DL = DL_of<T>(c);
     const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
-    const T GAM = gam_of<T>(c);
+    const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
     const int c1 = c.ec1[e];
     const bool inner = e < c.n_int;
     const Prim<T> qL = load_prim(W, c1);
@@ -584,7 +615,7 @@ __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
             pR = ghost_state(b, pL, Tc, nx, ny, M);
         }
         T f[4];
-        hit |= num_flux<T, FLUX>(f, pL, pR, nx, ny, GAM, c.newton_cap);
+        hit |= num_flux<T, FLUX>(f, pL, pR, nx, ny, GAM, IG1, c.newton_cap);
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
         if (RECON == RECON_NONE) {  // both Gauss points see the cell-centre states
             fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
@@ -657,7 +688,7 @@ __device__ __forceinline__ void gather_residual(const DevCase& c, int i, double*
             double v[4];
             ld4(F, f >> 1, v);
 #pragma unroll
-            for (int q = 0; q < 4; q++) R[q] = R[q] + ((f & 1) ? v[q] : -v[q]);
+            for (int q = 0; q < 4; q++) R[q] = R[q] + neg_if(v[q], !(f & 1));
         }
     } else {
         float t[3][4];
@@ -667,7 +698,7 @@ __device__ __forceinline__ void gather_residual(const DevCase& c, int i, double*
             float v[4];
             ld4(F, f >> 1, v);
 #pragma unroll
-            for (int q = 0; q < 4; q++) t[k][q] = (f & 1) ? v[q] : -v[q];
+            for (int q = 0; q < 4; q++) t[k][q] = neg_if(v[q], !(f & 1));
         }
 #pragma unroll
         for (int q = 0; q < 4; q++) {

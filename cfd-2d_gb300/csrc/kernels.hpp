@@ -40,7 +40,9 @@ struct DevBnd {     // one <boundCond>: kind and (Vx, Vy, T, P)
 
 // Launch shape of one kernel kind: threads per block and blocks (0 = one
 // thread per item; otherwise a persistent grid that strides over the items).
-struct LaunchShape { int block = 256, grid = 0; };
+// Default: 64-thread blocks, one thread per item (measured best for the single
+// four-quadrant workload in both precisions; the autotuner can override it).
+struct LaunchShape { int block = 64, grid = 0; };
 enum { KIND_GRAD = 0, KIND_FLUX = 1, KIND_UPDATE = 2, N_TUNED_KINDS = 3 };
 
 // Everything a kernel needs; passed by value.
@@ -71,9 +73,11 @@ struct DevCase {
     DevMat mat0;
     float mat0_f[3];       // M, Cv, gam-1 of material 0 in FP32 (mixed form)
     float gam_flux_f;
+    float ig1_flux_f;      // 1/(gam_flux - 1) in FP32
     float lim_f[5];        // limits in FP32 (mixed form)
     const float* invS32;   // nc, 1/S in FP32 (mixed form)
     double gam_flux;
+    double ig1_flux;       // RN(1/(gam_flux - 1)), computed on the host
     double cfl_number;
     double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
     int steady;

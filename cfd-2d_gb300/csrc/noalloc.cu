@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256) k_static_edge_flux(const StaticArgs a) {
         qR = ghost_state(a.b[bi], qL, Tc, nx, ny, a.mat.M);
     }
     double f[4];
-    num_flux<double, FLUX>(f, qL, qR, nx, ny, a.gam, 100);
+    num_flux<double, FLUX>(f, qL, qR, nx, ny, a.gam, 1.0 / (a.gam - 1.0), 100);
     const double lh = l * 0.5;
     for (int k = 0; k < 4; k++) {  // both Gauss points see the same states
         double s = 0.0;

@@ -170,7 +170,9 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
  * against the hardware operation on the current device: which = 0 FP64 division
  * through a precomputed reciprocal (must equal '/' bit for bit), 1 FP32->FP64
  * widening on the integer pipe (must equal the conversion), 2 FP64->FP32
- * narrowing on the integer pipe (within 1 ulp). *mismatches receives the count. */
+ * narrowing on the integer pipe (within 1 ulp), 3 FP64 minmod with its
+ * integer-pipe sign test (must equal a*b > 0 ? (|a| < |b| ? a : b) : 0 bit for
+ * bit). *mismatches receives the count. */
 int cfd2d_selftest(int which, long long n, unsigned long long seed, long long* mismatches);
 
 /* Select the CUDA device that cfd2d_create* places new solvers on (default: the

@@ -208,8 +208,10 @@ def test_full_size_four_quadrant_step_vs_oracle(capi, oracle, tmp_path):
     assert l1_rel(Ub[0], U[0]) <= MIXED_TOL and l1_rel(Ub[3], U[3]) <= MIXED_TOL
 
 
-@pytest.mark.parametrize("which,name", [(0, "division by reciprocal"), (1, "widening"), (2, "narrowing")])
+@pytest.mark.parametrize("which,name", [(0, "division by reciprocal"), (1, "widening"), (2, "narrowing"),
+                                        (3, "minmod sign test")])
 def test_device_arithmetic_helpers(capi, which, name):
     """The FP64 division through a precomputed reciprocal must equal '/' bit for
-    bit on the device; the integer-pipe conversions must match the hardware's."""
+    bit on the device; the integer-pipe conversions must match the hardware's;
+    the integer-pipe minmod must equal the reference's expression bit for bit."""
     assert capi.selftest(which, 200_000_000 if which == 0 else 50_000_000, seed=12345) == 0, name
