@@ -1,25 +1,71 @@
-// Reverse-mode (vector-Jacobian) pieces of the FP64 step, written by hand: for
-// each forward function f(x) below, vjp_f accumulates x_bar += (df/dx)^T y_bar.
-// Each follows the forward expression in kernels.cuh line by line, so the
-// adjoint is the exact derivative of the discrete scheme the solver runs
-// (branches of min/max, minmod and the HLLC wave pattern are taken as the
-// forward pass took them).
+// Reverse-mode (vector-Jacobian) pieces of the step, written by hand: for each
+// forward function f(x) below, vjp_f accumulates x_bar += (df/dx)^T y_bar. T is
+// the face precision, as in the forward kernels (double: the FP64 drop-in;
+// float: the mixed form's FP32 faces). Each follows the forward expression in
+// kernels.cuh line by line and recomputes the forward values with the forward's
+// own expressions, so the adjoint is the exact derivative of the discrete scheme
+// the solver runs (branches of min/max, minmod and the HLLC wave pattern are
+// taken as the forward pass took them). The reverse arithmetic itself needs no
+// bit parity.
 #pragma once
 #include "kernels.cuh"
 
 namespace cfd2d {
 
-// convertConsToPar: (rho, rho u, rho v, rho E) -> (r, u, v, p)
-__device__ __forceinline__ void vjp_cons2prim(const double* U, double gm1, const Prim<double>& pb, double* Ub) {
-    const double ro = U[0], iro = 1.0 / ro;  // the reverse sweep needs no bit parity: one reciprocal
-    const double u = U[1] * iro, v = U[2] * iro, E = U[3] * iro;
-    const double e = E - 0.5 * (u * u + v * v);
+// Accumulators start at -0: x + (-0) == x for every x, so the first addition folds away.
+template <typename T> __device__ __forceinline__ T acc0() { return T(-0.0); }
+template <typename T> __device__ __forceinline__ Prim<T> zero_prim() {
+    Prim<T> z;
+    z.r = acc0<T>(); z.u = acc0<T>(); z.v = acc0<T>(); z.p = acc0<T>();
+    return z;
+}
+
+// Conversions between the FP64 per-cell quantities and the face precision
+// (integer-pipe narrowing / widening for FP32, identity for FP64).
+template <typename T> __device__ __forceinline__ T to_face(double x);
+template <> __device__ __forceinline__ double to_face<double>(double x) { return x; }
+template <> __device__ __forceinline__ float to_face<float>(double x) { return narrow(x); }
+__device__ __forceinline__ double to_wide(double x) { return x; }
+__device__ __forceinline__ double to_wide(float x) { return widen(x); }
+
+// A running sum in the face precision kept exact for FP32 (Knuth's TwoSum into a
+// value and an error term, so cancelling face contributions lose nothing to the
+// summation) and plain for FP64; value() rounds it once into FP64.
+template <typename T> struct SumAcc;
+template <> struct SumAcc<double> {
+    double s = -0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ double face() const { return s; }
+};
+template <> struct SumAcc<float> {
+    float hi = -0.0f, lo = -0.0f;
+    __device__ __forceinline__ void add(float x) {
+        float t, e;
+        two_sum(hi, x, t, e);
+        hi = t;
+        lo += e;
+    }
+    __device__ __forceinline__ double value() const { return widen(hi) + widen(lo); }
+    __device__ __forceinline__ float face() const { return hi + lo; }
+};
+
+template <typename T> __device__ __forceinline__ const T* invS_of(const DevCase& c);
+template <> __device__ __forceinline__ const double* invS_of<double>(const DevCase& c) { return c.invS; }
+template <> __device__ __forceinline__ const float* invS_of<float>(const DevCase& c) { return c.invS32; }
+
+// convertConsToPar: (rho, rho u, rho v, rho E) -> (r, u, v, p), U in the face precision
+template <typename T>
+__device__ __forceinline__ void vjp_cons2prim(const T* U, T gm1, const Prim<T>& pb, T* Ub) {
+    const T ro = U[0], iro = T(1.0) / ro;
+    const T u = U[1] * iro, v = U[2] * iro, E = U[3] * iro;
+    const T e = E - T(0.5) * (u * u + v * v);
     // p = r e gm1
-    double rb = pb.r + pb.p * e * gm1;
-    const double eb = pb.p * ro * gm1;
+    T rb = pb.r + pb.p * e * gm1;
+    const T eb = pb.p * ro * gm1;
     // e = E - (u^2 + v^2)/2
-    const double Eb = eb;
-    const double ub = pb.u - eb * u, vb = pb.v - eb * v;
+    const T Eb = eb;
+    const T ub = pb.u - eb * u, vb = pb.v - eb * v;
     Ub[1] += ub * iro;
     Ub[2] += vb * iro;
     Ub[3] += Eb * iro;
@@ -28,45 +74,46 @@ __device__ __forceinline__ void vjp_cons2prim(const double* U, double gm1, const
 }
 
 // Tc = (p / (r gm1)) / Cv
-__device__ __forceinline__ void vjp_temperature(const Prim<double>& q, double gm1, double Cv, double Tb,
-                                                Prim<double>& qb) {
-    const double k = 1.0 / (q.r * gm1 * Cv);
+template <typename T>
+__device__ __forceinline__ void vjp_temperature(const Prim<T>& q, T gm1, T Cv, T Tb, Prim<T>& qb) {
+    const T k = T(1.0) / (q.r * gm1 * Cv);
     qb.p += Tb * k;
     qb.r -= Tb * (q.p * k) / q.r;
 }
 
 // ghost_state(b, q, Tc, n, M): the reference's CFDBnd*::run + URS(2) for the density.
 // bp_bar receives d/d(Vx, Vy, T, P) of an inlet's parameters.
-__device__ __forceinline__ void vjp_ghost(const DevBnd& b, const Prim<double>& q, double Tc, double nx, double ny,
-                                          double M, const Prim<double>& gb, Prim<double>& qb, double& Tcb,
-                                          double* bp_bar) {
+template <typename T>
+__device__ __forceinline__ void vjp_ghost(const DevBnd& b, const Prim<T>& q, T Tc, T nx, T ny, T M,
+                                          const Prim<T>& gb, Prim<T>& qb, T& Tcb, T* bp_bar) {
     if (b.kind == BND_INLET) {
-        const double k = M / (b.T * GAS_R);
+        const T bT = T(b.T), bP = T(b.p);
+        const T k = M / (bT * T(GAS_R));
         bp_bar[0] += gb.u;
         bp_bar[1] += gb.v;
         bp_bar[3] += gb.p + gb.r * k;
-        bp_bar[2] -= gb.r * (b.p * k) / b.T;
+        bp_bar[2] -= gb.r * (bP * k) / bT;
         return;
     }
-    const double k = M / (Tc * GAS_R);
+    const T k = M / (Tc * T(GAS_R));
     qb.p += gb.p + gb.r * k;
     Tcb -= gb.r * (q.p * k) / Tc;
     if (b.kind == BND_OUTLET) {
         qb.u += gb.u;
         qb.v += gb.v;
     } else {  // wall: u_g = u - 2 nx Un, v_g = v - 2 ny Un, Un = u nx + v ny
-        const double Unb = -2.0 * (nx * gb.u + ny * gb.v);
+        const T Unb = T(-2.0) * (nx * gb.u + ny * gb.v);
         qb.u += gb.u + Unb * nx;
         qb.v += gb.v + Unb * ny;
     }
 }
 
 // phys_flux(f, r, u, v, p, E, un, n)
-__device__ __forceinline__ void vjp_phys(double r, double u, double v, double p, double E, double un, double nx,
-                                         double ny, const double* fb, double& rb, double& ub, double& vb, double& pb,
-                                         double& Eb, double& unb) {
-    const double m = r * un;
-    const double mb = fb[0] + fb[1] * u + fb[2] * v;
+template <typename T>
+__device__ __forceinline__ void vjp_phys(T r, T u, T v, T p, T E, T un, T nx, T ny, const T* fb, T& rb, T& ub,
+                                         T& vb, T& pb, T& Eb, T& unb) {
+    const T m = r * un;
+    const T mb = fb[0] + fb[1] * u + fb[2] * v;
     ub += fb[1] * m;
     vb += fb[2] * m;
     pb += fb[1] * nx + fb[2] * ny + fb[3] * un;
@@ -76,92 +123,116 @@ __device__ __forceinline__ void vjp_phys(double r, double u, double v, double p,
 }
 
 // Lax-Friedrichs (flux_lax in kernels.cuh)
-__device__ __forceinline__ void vjp_lax(const Prim<double>& L, const Prim<double>& R, double nx, double ny,
-                                        double GAM, const double* fb, Prim<double>& Lb, Prim<double>& Rb) {
-    const double unl = L.u * nx + L.v * ny, unr = R.u * nx + R.v * ny;
-    const double aL = GAM * L.p / L.r, aR = GAM * R.p / R.r;
-    const double cL = sqrt(aL), cR = sqrt(aR);
-    const double s1 = fabs(unl) + cL, s2 = fabs(unr) + cR;
+template <typename T>
+__device__ __forceinline__ void vjp_lax(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
+                                        Prim<T>& Lb, Prim<T>& Rb) {
+    const T unl = L.u * nx + L.v * ny, unr = R.u * nx + R.v * ny;
+    const T aL = GAM * L.p / L.r, aR = GAM * R.p / R.r;
+    const T cL = t_sqrt(aL), cR = t_sqrt(aR);
+    const T s1 = t_abs(unl) + cL, s2 = t_abs(unr) + cR;
     const bool first = s1 > s2;  // t_max(a, b) = a > b ? a : b
-    const double alpha = first ? s1 : s2;
-    const double rol = L.r, rul = L.r * L.u, rvl = L.r * L.v;
-    const double G1 = GAM - 1.0;
-    const double rel = L.p / G1 + 0.5 * L.r * (L.u * L.u + L.v * L.v);
-    const double ror = R.r, rur = R.r * R.u, rvr = R.r * R.v;
-    const double rer = R.p / G1 + 0.5 * R.r * (R.u * R.u + R.v * R.v);
-    const double frl = rol * unl, frr = ror * unr;
-    const double h0 = 0.5 * fb[0], h1 = 0.5 * fb[1], h2 = 0.5 * fb[2], h3 = 0.5 * fb[3];
+    const T alpha = first ? s1 : s2;
+    const T rol = L.r, rul = L.r * L.u, rvl = L.r * L.v;
+    const T rel = div_by(L.p, GAM - T(1.0), IG1) + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
+    const T ror = R.r, rur = R.r * R.u, rvr = R.r * R.v;
+    const T rer = div_by(R.p, GAM - T(1.0), IG1) + T(0.5) * R.r * (R.u * R.u + R.v * R.v);
+    const T frl = rol * unl, frr = ror * unr;
+    const T h0 = T(0.5) * fb[0], h1 = T(0.5) * fb[1], h2 = T(0.5) * fb[2], h3 = T(0.5) * fb[3];
     // f0 = .5(frr + frl - alpha (ror - rol)), f1 = .5(frr uR + frl uL + (pR + pL) nx - alpha (rur - rul))
     // f2 = .5(frr vR + frl vL + (pR + pL) ny - alpha (rvr - rvl)), f3 = .5((rer + pR) unr + (rel + pL) unl - alpha (rer - rel))
-    double frrb = h0 + h1 * R.u + h2 * R.v, frlb = h0 + h1 * L.u + h2 * L.v;
-    double alphab = -(h0 * (ror - rol) + h1 * (rur - rul) + h2 * (rvr - rvl) + h3 * (rer - rel));
-    double rorb = -h0 * alpha, rolb = h0 * alpha, rurb = -h1 * alpha, rulb = h1 * alpha;
-    double rvrb = -h2 * alpha, rvlb = h2 * alpha, rerb = h3 * unr - h3 * alpha, relb = h3 * unl + h3 * alpha;
+    const T frrb = h0 + h1 * R.u + h2 * R.v, frlb = h0 + h1 * L.u + h2 * L.v;
+    const T alphab = -(h0 * (ror - rol) + h1 * (rur - rul) + h2 * (rvr - rvl) + h3 * (rer - rel));
+    T rorb = -h0 * alpha, rolb = h0 * alpha, rurb = -h1 * alpha, rulb = h1 * alpha;
+    T rvrb = -h2 * alpha, rvlb = h2 * alpha, rerb = h3 * unr - h3 * alpha, relb = h3 * unl + h3 * alpha;
     Rb.u += h1 * frr; Lb.u += h1 * frl; Rb.v += h2 * frr; Lb.v += h2 * frl;
     Rb.p += h1 * nx + h2 * ny + h3 * unr; Lb.p += h1 * nx + h2 * ny + h3 * unl;
-    double unrb = h3 * (rer + R.p), unlb = h3 * (rel + L.p);
+    T unrb = h3 * (rer + R.p), unlb = h3 * (rel + L.p);
     // fr = ro un
     rorb += frrb * unr; unrb += frrb * ror; rolb += frlb * unl; unlb += frlb * rol;
     // re = p/G1 + .5 r (u^2 + v^2)
-    Rb.p += rerb / G1; rorb += rerb * 0.5 * (R.u * R.u + R.v * R.v);
+    Rb.p += rerb * IG1; rorb += rerb * T(0.5) * (R.u * R.u + R.v * R.v);
     Rb.u += rerb * R.r * R.u; Rb.v += rerb * R.r * R.v;
-    Lb.p += relb / G1; rolb += relb * 0.5 * (L.u * L.u + L.v * L.v);
+    Lb.p += relb * IG1; rolb += relb * T(0.5) * (L.u * L.u + L.v * L.v);
     Lb.u += relb * L.r * L.u; Lb.v += relb * L.r * L.v;
     // ru, rv
     rorb += rurb * R.u + rvrb * R.v; Rb.u += rurb * R.r; Rb.v += rvrb * R.r;
     rolb += rulb * L.u + rvlb * L.v; Lb.u += rulb * L.r; Lb.v += rvlb * L.r;
     Rb.r += rorb; Lb.r += rolb;
     // alpha = max(|unl| + cL, |unr| + cR)
-    if (first) { unlb += alphab * (unl >= 0 ? 1.0 : -1.0); const double ab = 0.5 * alphab / (cL * L.r); Lb.p += ab * GAM; Lb.r -= ab * aL; }
-    else { unrb += alphab * (unr >= 0 ? 1.0 : -1.0); const double ab = 0.5 * alphab / (cR * R.r); Rb.p += ab * GAM; Rb.r -= ab * aR; }
+    if (first) {
+        unlb += alphab * (unl >= T(0) ? T(1.0) : T(-1.0));
+        const T ab = T(0.5) * alphab / (cL * L.r);
+        Lb.p += ab * GAM; Lb.r -= ab * aL;
+    } else {
+        unrb += alphab * (unr >= T(0) ? T(1.0) : T(-1.0));
+        const T ab = T(0.5) * alphab / (cR * R.r);
+        Rb.p += ab * GAM; Rb.r -= ab * aR;
+    }
     Lb.u += unlb * nx; Lb.v += unlb * ny; Rb.u += unrb * nx; Rb.v += unrb * ny;
 }
 
+// Ss = num / den with the reciprocal iden = 1/den also returned: FP64 through the
+// correctly rounded reciprocal form (the forward's quotient bit for bit), FP32 as
+// the forward divides.
+__device__ __forceinline__ double star_speed(double num, double den, double& iden) {
+    iden = 1.0 / den;
+    return div_rn(num, den, iden);
+}
+__device__ __forceinline__ float star_speed(float num, float den, float& iden) {
+    iden = 1.0f / den;
+    return num / den;
+}
+
 // HLLC in the single-division star-flux form (flux_hllc in kernels.cuh)
-__device__ __forceinline__ void vjp_hllc(const Prim<double>& L, const Prim<double>& R, double nx, double ny,
-                                         double GAM, const double* fb, Prim<double>& Lb, Prim<double>& Rb) {
-    const double IG1 = 1.0 / (GAM - 1.0);
-    const double aL = GAM * L.p / L.r, aR = GAM * R.p / R.r;
-    const double cL = sqrt(aL), cR = sqrt(aR);
-    const double unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
-    const double EL = energy(L.r, L.u, L.v, L.p, IG1);
-    const double ER = energy(R.r, R.u, R.v, R.p, IG1);
-    const double sl1 = unL - cL, sl2 = unR - cR, sr1 = unL + cL, sr2 = unR + cR;
+template <typename T>
+__device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
+                                         Prim<T>& Lb, Prim<T>& Rb) {
+    const T aL = GAM * L.p / L.r, aR = GAM * R.p / R.r;
+    const T cL = t_sqrt(aL), cR = t_sqrt(aR);
+    const T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
+    const T EL = energy(L.r, L.u, L.v, L.p, IG1);
+    const T ER = energy(R.r, R.u, R.v, R.p, IG1);
+    const T sl1 = unL - cL, sl2 = unR - cR, sr1 = unL + cL, sr2 = unR + cR;
     const bool l1 = sl1 < sl2, r1 = sr1 > sr2;
-    const double SL = l1 ? sl1 : sl2, SR = r1 ? sr1 : sr2;
-    double unLb = 0, unRb = 0, ELb = 0, ERb = 0, SLb = 0, SRb = 0, cLb = 0, cRb = 0;
-    if (SL >= 0.0 || SR <= 0.0) {  // supersonic: the upwind side's physical flux
-        if (SL >= 0.0) vjp_phys(L.r, L.u, L.v, L.p, EL, unL, nx, ny, fb, Lb.r, Lb.u, Lb.v, Lb.p, ELb, unLb);
+    const T SL = l1 ? sl1 : sl2, SR = r1 ? sr1 : sr2;
+    T unLb = acc0<T>(), unRb = acc0<T>(), ELb = acc0<T>(), ERb = acc0<T>();
+    T SLb = acc0<T>(), SRb = acc0<T>(), cLb = acc0<T>(), cRb = acc0<T>();
+    if (SL >= T(0.0) || SR <= T(0.0)) {  // supersonic: the upwind side's physical flux
+        if (SL >= T(0.0)) vjp_phys(L.r, L.u, L.v, L.p, EL, unL, nx, ny, fb, Lb.r, Lb.u, Lb.v, Lb.p, ELb, unLb);
         else vjp_phys(R.r, R.u, R.v, R.p, ER, unR, nx, ny, fb, Rb.r, Rb.u, Rb.v, Rb.p, ERb, unRb);
     } else {
-        const double mL = L.r * (SL - unL), mR = R.r * (SR - unR);
-        const double num = fma(-mR, unR, fma(mL, unL, R.p - L.p)), den = mL - mR;
-        const double Ss = num / den;
-        const bool left = Ss >= 0.0;
-        const Prim<double>& K = left ? L : R;
-        const double SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
-        const double m = K.r * unK;
-        const double FK0 = m, FK1 = m * K.u + K.p * nx, FK2 = m * K.v + K.p * ny, FK3 = (EK + K.p) * unK;
-        const double ps = fma(mK, Ss - unK, K.p);
-        const double inv = 1.0 / (SK - Ss);
-        const double sp = SK * ps;
-        const double A0 = SK * K.r - FK0, A1 = SK * (K.r * K.u) - FK1, A2 = SK * (K.r * K.v) - FK2,
-                     A3 = SK * EK - FK3;
-        const double h0 = Ss * A0, h1 = Ss * A1 + sp * nx, h2 = Ss * A2 + sp * ny, h3 = Ss * A3 + sp * Ss;
+        const T mL = L.r * (SL - unL), mR = R.r * (SR - unR);
+        const T num = t_fma(-mR, unR, t_fma(mL, unL, R.p - L.p)), den = mL - mR;
+        T iden;
+        const T Ss = star_speed(num, den, iden);
+        const bool left = Ss >= T(0.0);
+        const Prim<T>& K = left ? L : R;
+        const T SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
+        T FK[4];
+        phys_flux(FK, K.r, K.u, K.v, K.p, EK, unK, nx, ny);
+        const T ps = t_fma(mK, Ss - unK, K.p);
+        const T inv = T(1.0) / (SK - Ss);
+        const T sp = SK * ps;
+        const T A0 = SK * K.r - FK[0], A1 = SK * (K.r * K.u) - FK[1], A2 = SK * (K.r * K.v) - FK[2],
+                A3 = SK * EK - FK[3];
+        const T h0 = Ss * A0, h1 = Ss * A1 + sp * nx, h2 = Ss * A2 + sp * ny, h3 = Ss * A3 + sp * Ss;
         // f_k = h_k inv
-        const double hb0 = fb[0] * inv, hb1 = fb[1] * inv, hb2 = fb[2] * inv, hb3 = fb[3] * inv;
-        const double invb = fb[0] * h0 + fb[1] * h1 + fb[2] * h2 + fb[3] * h3;
-        double Ssb = hb0 * A0 + hb1 * A1 + hb2 * A2 + hb3 * (A3 + sp);
-        const double A0b = hb0 * Ss, A1b = hb1 * Ss, A2b = hb2 * Ss, A3b = hb3 * Ss;
-        const double spb = hb1 * nx + hb2 * ny + hb3 * Ss;
+        const T hb0 = fb[0] * inv, hb1 = fb[1] * inv, hb2 = fb[2] * inv, hb3 = fb[3] * inv;
+        const T invb = fb[0] * h0 + fb[1] * h1 + fb[2] * h2 + fb[3] * h3;
+        T Ssb = hb0 * A0 + hb1 * A1 + hb2 * A2 + hb3 * (A3 + sp);
+        const T A0b = hb0 * Ss, A1b = hb1 * Ss, A2b = hb2 * Ss, A3b = hb3 * Ss;
+        const T spb = hb1 * nx + hb2 * ny + hb3 * Ss;
         // inv = 1/(SK - Ss)
-        double SKb = -invb * inv * inv;
-        Ssb += invb * inv * inv;
+        const T ii = invb * inv * inv;
+        T SKb = -ii;
+        Ssb += ii;
         // sp = SK ps
         SKb += spb * ps;
-        const double psb = spb * SK;
+        const T psb = spb * SK;
         // ps = pK + mK (Ss - unK)
-        double Krb = 0, Kub = 0, Kvb = 0, Kpb = psb, EKb = 0, unKb = -psb * mK, mKb = psb * (Ss - unK);
+        T Krb = acc0<T>(), Kub = acc0<T>(), Kvb = acc0<T>(), Kpb = psb, EKb = acc0<T>();
+        T unKb = -psb * mK;
+        const T mKb = psb * (Ss - unK);
         Ssb += psb * mK;
         // A_k
         SKb += A0b * K.r + A1b * (K.r * K.u) + A2b * (K.r * K.v) + A3b * EK;
@@ -169,18 +240,17 @@ __device__ __forceinline__ void vjp_hllc(const Prim<double>& L, const Prim<doubl
         Kub += A1b * SK * K.r;
         Kvb += A2b * SK * K.r;
         EKb += A3b * SK;
-        const double FKb[4] = {-A0b, -A1b, -A2b, -A3b};
+        const T FKb[4] = {-A0b, -A1b, -A2b, -A3b};
         vjp_phys(K.r, K.u, K.v, K.p, EK, unK, nx, ny, FKb, Krb, Kub, Kvb, Kpb, EKb, unKb);
         // route the K-side adjoints
-        double mLb = 0, mRb = 0;
+        T mLb = acc0<T>(), mRb = acc0<T>();
         if (left) {
             Lb.r += Krb; Lb.u += Kub; Lb.v += Kvb; Lb.p += Kpb; ELb += EKb; unLb += unKb; SLb += SKb; mLb += mKb;
         } else {
             Rb.r += Krb; Rb.u += Kub; Rb.v += Kvb; Rb.p += Kpb; ERb += EKb; unRb += unKb; SRb += SKb; mRb += mKb;
         }
         // Ss = num / den
-        const double iden = 1.0 / den;
-        const double numb = Ssb * iden, denb = -Ssb * Ss * iden;
+        const T numb = Ssb * iden, denb = -Ssb * Ss * iden;
         Rb.p += numb; Lb.p -= numb;
         mLb += numb * unL + denb; unLb += numb * mL;
         mRb += -numb * unR - denb; unRb -= numb * mR;
@@ -192,37 +262,46 @@ __device__ __forceinline__ void vjp_hllc(const Prim<double>& L, const Prim<doubl
         if (r1) { unLb += SRb; cLb += SRb; } else { unRb += SRb; cRb += SRb; }
     }
     // E = p IG1 + .5 r (u^2 + v^2)
-    Lb.p += ELb * IG1; Lb.r += ELb * 0.5 * (L.u * L.u + L.v * L.v); Lb.u += ELb * L.r * L.u; Lb.v += ELb * L.r * L.v;
-    Rb.p += ERb * IG1; Rb.r += ERb * 0.5 * (R.u * R.u + R.v * R.v); Rb.u += ERb * R.r * R.u; Rb.v += ERb * R.r * R.v;
+    Lb.p += ELb * IG1; Lb.r += ELb * T(0.5) * (L.u * L.u + L.v * L.v);
+    Lb.u += ELb * L.r * L.u; Lb.v += ELb * L.r * L.v;
+    Rb.p += ERb * IG1; Rb.r += ERb * T(0.5) * (R.u * R.u + R.v * R.v);
+    Rb.u += ERb * R.r * R.u; Rb.v += ERb * R.r * R.v;
     // un = u nx + v ny
     Lb.u += unLb * nx; Lb.v += unLb * ny; Rb.u += unRb * nx; Rb.v += unRb * ny;
     // c = sqrt(GAM p / r): dc = (GAM dp - a dr) / (2 c r)
-    if (cLb != 0.0) { const double ab = 0.5 * cLb / (cL * L.r); Lb.p += ab * GAM; Lb.r -= ab * aL; }
-    if (cRb != 0.0) { const double ab = 0.5 * cRb / (cR * R.r); Rb.p += ab * GAM; Rb.r -= ab * aR; }
+    if (cLb != T(0.0)) { const T ab = T(0.5) * cLb / (cL * L.r); Lb.p += ab * GAM; Lb.r -= ab * aL; }
+    if (cRb != T(0.0)) { const T ab = T(0.5) * cRb / (cR * R.r); Rb.p += ab * GAM; Rb.r -= ab * aR; }
+}
+
+template <int FLUX, typename T>
+__device__ __forceinline__ void vjp_flux(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
+                                         Prim<T>& Lb, Prim<T>& Rb) {
+    if (FLUX == FLUX_HLLC) vjp_hllc(L, R, nx, ny, GAM, IG1, fb, Lb, Rb);
+    else vjp_lax(L, R, nx, ny, GAM, IG1, fb, Lb, Rb);
 }
 
 // One side's reconstruction p = q + delta(a, nb - q) with the projections
 // a = g . dl already formed (in the forward's operation order): pb -> qb, gb
 // (8: r, p, u, v gradients, through a) and nbb (the minmod neighbour values).
-template <int RECON>
-__device__ __forceinline__ void vjp_reconstruct_a(const Prim<double>& q, const double* a, double dx, double dy,
-                                                  const Prim<double>& nb, const Prim<double>& pb, Prim<double>& qb,
-                                                  double* gb, Prim<double>& nbb) {
-    const double qv[4] = {q.r, q.p, q.u, q.v}, nv[4] = {nb.r, nb.p, nb.u, nb.v};
-    const double pv[4] = {pb.r, pb.p, pb.u, pb.v};
-    double qbv[4] = {0, 0, 0, 0}, nbv[4] = {0, 0, 0, 0};
+// The minmod branch is the forward's own decision (mm_pos, mm_first).
+template <int RECON, typename T>
+__device__ __forceinline__ void vjp_reconstruct_a(const Prim<T>& q, const T* a, T dx, T dy, const Prim<T>& nb,
+                                                  const Prim<T>& pb, Prim<T>& qb, T* gb, Prim<T>& nbb) {
+    const T qv[4] = {q.r, q.p, q.u, q.v}, nv[4] = {nb.r, nb.p, nb.u, nb.v};
+    const T pv[4] = {pb.r, pb.p, pb.u, pb.v};
+    T qbv[4] = {acc0<T>(), acc0<T>(), acc0<T>(), acc0<T>()}, nbv[4] = {acc0<T>(), acc0<T>(), acc0<T>(), acc0<T>()};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const double db = pv[k];
+        const T db = pv[k];
         qbv[k] += db;
         if (RECON == RECON_LINEAR) {
             gb[2 * k] += db * dx;
             gb[2 * k + 1] += db * dy;
             continue;
         }
-        const double b = nv[k] - qv[k];  // minmod(a, b): a*b > 0 ? (|a| < |b| ? a : b) : 0
-        if (a[k] * b > 0.0) {
-            if (fabs(a[k]) < fabs(b)) { gb[2 * k] += db * dx; gb[2 * k + 1] += db * dy; }
+        const T b = nv[k] - qv[k];
+        if (mm_pos(a[k], b)) {
+            if (mm_first(a[k], b)) { gb[2 * k] += db * dx; gb[2 * k + 1] += db * dy; }
             else { nbv[k] += db; qbv[k] -= db; }
         }
     }
@@ -231,19 +310,19 @@ __device__ __forceinline__ void vjp_reconstruct_a(const Prim<double>& q, const d
 }
 
 // Projections a = g . dl of one side's four gradients, as reconstruct() forms them.
-template <int RECON>
-__device__ __forceinline__ void project(const double* g, double dx, double dy, double* a) {
-    a[0] = proj<double, RECON>(g[0], g[1], dx, dy);
-    a[1] = proj<double, RECON>(g[2], g[3], dx, dy);
-    a[2] = proj<double, RECON>(g[4], g[5], dx, dy);
-    a[3] = proj<double, RECON>(g[6], g[7], dx, dy);
+template <int RECON, typename T>
+__device__ __forceinline__ void project(const T* g, T dx, T dy, T* a) {
+    a[0] = proj<T, RECON>(g[0], g[1], dx, dy);
+    a[1] = proj<T, RECON>(g[2], g[3], dx, dy);
+    a[2] = proj<T, RECON>(g[4], g[5], dx, dy);
+    a[3] = proj<T, RECON>(g[6], g[7], dx, dy);
 }
 
 // The forward reconstruction from the projections (kernels.cuh reconstruct).
-template <int RECON>
-__device__ __forceinline__ Prim<double> recon_a(const Prim<double>& q, const double* a, const Prim<double>& nb) {
-    Prim<double> p = q;
-    double d0 = a[0], d1 = a[1], d2 = a[2], d3 = a[3];
+template <int RECON, typename T>
+__device__ __forceinline__ Prim<T> recon_a(const Prim<T>& q, const T* a, const Prim<T>& nb) {
+    Prim<T> p = q;
+    T d0 = a[0], d1 = a[1], d2 = a[2], d3 = a[3];
     if (RECON == RECON_MINMOD) {
         d0 = minmod(d0, nb.r - q.r);
         d1 = minmod(d1, nb.p - q.p);
@@ -252,34 +331,6 @@ __device__ __forceinline__ Prim<double> recon_a(const Prim<double>& q, const dou
     }
     p.r += d0; p.p += d1; p.u += d2; p.v += d3;
     return p;
-}
-
-// One side's reconstruction p = q + delta(g . dl, nb - q) (kernels.cuh reconstruct):
-// pb -> qb, gb (8: r, p, u, v gradients) and nbb (the minmod neighbour values).
-template <int RECON>
-__device__ __forceinline__ void vjp_reconstruct(const Prim<double>& q, const double* g, double dx, double dy,
-                                                const Prim<double>& nb, const Prim<double>& pb, Prim<double>& qb,
-                                                double* gb, Prim<double>& nbb) {
-    const double qv[4] = {q.r, q.p, q.u, q.v}, nv[4] = {nb.r, nb.p, nb.u, nb.v};
-    const double pv[4] = {pb.r, pb.p, pb.u, pb.v};
-    double qbv[4] = {0, 0, 0, 0}, nbv[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const double db = pv[k];
-        qbv[k] += db;
-        if (RECON == RECON_LINEAR) {
-            gb[2 * k] += db * dx;
-            gb[2 * k + 1] += db * dy;
-        } else {
-            const double a = g[2 * k] * dx + g[2 * k + 1] * dy, b = nv[k] - qv[k];
-            if (a * b > 0.0) {
-                if (fabs(a) < fabs(b)) { gb[2 * k] += db * dx; gb[2 * k + 1] += db * dy; }
-                else { nbv[k] += db; qbv[k] -= db; }
-            }
-        }
-    }
-    qb.r += qbv[0]; qb.p += qbv[1]; qb.u += qbv[2]; qb.v += qbv[3];
-    nbb.r += nbv[0]; nbb.p += nbv[1]; nbb.u += nbv[2]; nbb.v += nbv[3];
 }
 
 }  // namespace cfd2d

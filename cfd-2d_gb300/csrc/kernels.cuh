@@ -208,33 +208,39 @@ __device__ __forceinline__ Prim<T> ghost_state(const DevBnd& b, const Prim<T>& q
     return g;
 }
 
-// MINMOD, src/methods/LimiterDGCockburn.cpp:110-123: a*b > 0 ? (|a| < |b| ? a : b) : 0.
-// |a| < |b| compares magnitude bits, which orders non-NaN values like fabs does.
-// The sign test runs on the integer pipe: a zero operand gives a product of +-0
-// or NaN (0 * inf), never > 0; for normal or infinite operands of one sign whose
+// MINMOD, src/methods/LimiterDGCockburn.cpp:110-123: a*b > 0 ? (|a| < |b| ? a : b) : 0,
+// split into its two decisions so that the adjoint takes exactly the forward's branch.
+// mm_pos is the test a*b > 0. On the integer pipe: a zero operand gives a product of
+// +-0 or NaN (0 * inf), never > 0; for normal or infinite operands of one sign whose
 // exponent fields sum to at least 972, |a b| >= 2^(ea+eb-2046) >= 2^-1074, so the
-// rounded product is > 0 (or +inf); NaN or opposite signs fail the test.
-// Subnormal operands and products near the underflow threshold take the FP64
-// multiply and read the sign of its bits (positive, non-NaN doubles are exactly
-// the patterns in (0, 0x7ff0...0]). Bit for bit the reference's result.
-__device__ __forceinline__ double minmod(double a, double b) {
+// rounded product is > 0 (or +inf); NaN or opposite signs fail the test. Subnormal
+// operands and products near the underflow threshold take the FP64 multiply and read
+// the sign of its bits (positive, non-NaN doubles are exactly the patterns in
+// (0, 0x7ff0...0]). mm_first is |a| < |b| on magnitude bits, which orders non-NaN
+// values like fabs does. Bit for bit the reference's result.
+__device__ __forceinline__ bool mm_pos(double a, double b) {
     const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
     const long long ma = ia & 0x7fffffffffffffffll, mb = ib & 0x7fffffffffffffffll;
-    if (ma == 0 || mb == 0) return 0.0;
+    if (ma == 0 || mb == 0) return false;
     const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
-    if (ea >= 1 && eb >= 1 && ea + eb >= 972) {
-        if ((ia ^ ib) < 0 || ma > 0x7ff0000000000000ll || mb > 0x7ff0000000000000ll) return 0.0;
-        return ma < mb ? a : b;
-    }
+    if (ea >= 1 && eb >= 1 && ea + eb >= 972)
+        return (ia ^ ib) >= 0 && ma <= 0x7ff0000000000000ll && mb <= 0x7ff0000000000000ll;
     const long long pb = __double_as_longlong(a * b);
-    if (pb <= 0 || pb > 0x7ff0000000000000ll) return 0.0;
-    return ma < mb ? a : b;
+    return pb > 0 && pb <= 0x7ff0000000000000ll;
 }
-__device__ __forceinline__ float minmod(float a, float b) {
+__device__ __forceinline__ bool mm_first(double a, double b) {
+    return (__double_as_longlong(a) & 0x7fffffffffffffffll) < (__double_as_longlong(b) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ bool mm_pos(float a, float b) {
     const int pb = __float_as_int(a * b);
-    if (pb <= 0 || pb > 0x7f800000) return 0.0f;
-    const int ma = __float_as_int(a) & 0x7fffffff, mb = __float_as_int(b) & 0x7fffffff;
-    return ma < mb ? a : b;
+    return pb > 0 && pb <= 0x7f800000;
+}
+__device__ __forceinline__ bool mm_first(float a, float b) {
+    return (__float_as_int(a) & 0x7fffffff) < (__float_as_int(b) & 0x7fffffff);
+}
+template <typename T>
+__device__ __forceinline__ T minmod(T a, T b) {
+    return mm_pos(a, b) ? (mm_first(a, b) ? a : b) : T(0.0);
 }
 
 // ------------------------------------------------------------------ fluxes

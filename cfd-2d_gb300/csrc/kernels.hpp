@@ -123,11 +123,11 @@ void launch_residual(const DevCase& c, int precision, double* R, cudaStream_t s)
 struct AdjCase {
     const double* X;   // 4*nc stage input state (SoA)
     const double* mu;  // nc x 4 (AoS) cfl * t_bar
-    double* eq;        // ne x 24: q1_bar(4) g1_bar(8) q2_bar(4) g2_bar(8)
+    void* eq;          // ne x 24 in the face precision: q1_bar(4) g1_bar(8) q2_bar(4) g2_bar(8)
     double* eb;        // (ne - n_int) x 4 boundary-parameter adjoints, flux path
     double* eb2;       // (ne - n_int) x 4 boundary-parameter adjoints, gradient path
-    double* qbar;      // nc x 4
-    double* gbar;      // nc x 8
+    double* qbar;      // nc x 4: r, u, v, p
+    void* gbar;        // nc x 8 in the face precision
     double* tb;        // 4*nc (SoA) t_bar of the current stage
     double* acc;       // 4*nc adjoint accumulated for the step's input U^n
     double* lam;       // 4*nc adjoint of the step's output / input
@@ -136,9 +136,11 @@ struct AdjCase {
     int n_bnd;
 };
 
-void launch_adj_flux(const DevCase& c, const AdjCase& a, int flux, int recon, cudaStream_t s);
-void launch_adj_gather(const DevCase& c, const AdjCase& a, cudaStream_t s);
-void launch_adj_cell(const DevCase& c, const AdjCase& a, double coef_t, double coef_acc, int first, cudaStream_t s);
+// precision: PREC_FP64 (FP64 faces) or PREC_MIXED (FP32 faces, FP64 per-cell sums)
+void launch_adj_flux(const DevCase& c, const AdjCase& a, int flux, int recon, int precision, cudaStream_t s);
+void launch_adj_gather(const DevCase& c, const AdjCase& a, int precision, cudaStream_t s);
+void launch_adj_cell(const DevCase& c, const AdjCase& a, double coef_t, double coef_acc, int first, int precision,
+                     cudaStream_t s);
 void launch_adj_step_start(const DevCase& c, const AdjCase& a, double coef_t, double coef_acc, cudaStream_t s);
 void launch_adj_bnd_reduce(const DevCase& c, const AdjCase& a, cudaStream_t s);
 void launch_objective(const DevCase& c, const double* w, int kind, double p_ref, double* partial, int nblocks,

@@ -96,7 +96,7 @@ public:
 private:
     template <typename T> T* dalloc(size_t n);
     void adjoint_setup();
-    void record_step(double* store, double* wg);
+    void record_step(double* store, void* wg);
     DevCase adj_dc_{};
     bool adj_ready_ = false;
     int obj_kind_ = -1;
@@ -116,8 +116,8 @@ private:
     double* adj_final_ = nullptr;
     double* ckpt_ = nullptr;
     double* segstore_ = nullptr;
-    double* wgstore_ = nullptr;   // per recorded stage: W (4 nc) then G (8 nc), FP64 form only
-    size_t wg_slots_ = 0;
+    double* wgstore_ = nullptr;   // per recorded stage: W (4 nc) then G (8 nc), in the face precision
+    size_t wg_slots_ = 0;         // doubles allocated in wgstore_
     bool store_wg_ = false;
     size_t ckpt_slots_ = 0, seg_slots_ = 0;
     int fw_steps_ = 0, fw_k_ = 0;

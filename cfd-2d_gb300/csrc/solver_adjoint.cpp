@@ -37,19 +37,8 @@ void Solver::adjoint_setup() {
     if (task_.flux != FLUX_HLLC && task_.flux != FLUX_LAX)
         throw Error(CFD2D_ERR_INVALID_ARG, "the adjoint differentiates the HLLC and LAX fluxes");
     if (gauss_points_ == 0) throw Error(CFD2D_ERR_INVALID_ARG, "the adjoint needs two-point edges");
-    adj_dc_ = dc_;
-    if (task_.precision == PREC_MIXED) {  // the FP64 adjoint of the mixed forward needs FP64 geometry
-        std::vector<double> is(nc);
-        for (int i = 0; i < nc; i++) is[i] = 1.0 / lay_.S[i];
-        adj_dc_.invS = upload(is);
-        adj_dc_.nx = upload(lay_.nx);
-        adj_dc_.ny = upload(lay_.ny);
-        adj_dc_.l = upload(lay_.l);
-        adj_dc_.dl = upload(lay_.dl);
-        adj_dc_.W64 = dalloc<double>(4 * (size_t)nc);
-        adj_dc_.G64 = dalloc<double>(8 * (size_t)nc);
-    }
-    adj_eq_ = dalloc<double>(24 * (size_t)ne);
+    adj_dc_ = dc_;  // the adjoint runs in the forward's face precision on the forward's geometry
+    adj_eq_ = dalloc<double>(24 * (size_t)ne);  // sized for FP64 faces; FP32 faces use half
     adj_eb_ = dalloc<double>(4 * (size_t)std::max(nb, 1));
     adj_eb2_ = dalloc<double>(4 * (size_t)std::max(nb, 1));
     adj_qbar_ = dalloc<double>(4 * (size_t)nc);
@@ -107,11 +96,13 @@ double Solver::forward(int nsteps, int k, int* status) {
         segstore_ = dalloc<double>((size_t)k * nst * 4 * nc);
         seg_slots_ = (size_t)k * nst;
     }
-    // keep each recorded stage's primitives and gradients when the segment's worth fits in a
-    // quarter of the free device memory (FP64 form; the mixed form's are FP32 and get re-derived)
+    // keep each recorded stage's primitives and gradients (face precision) when the
+    // segment's worth fits in a quarter of the free device memory; otherwise the
+    // backward sweep re-derives them from the recorded stage states
     store_wg_ = false;
-    if (task_.precision == PREC_FP64) {
-        const size_t need = (size_t)k * nst * 12 * nc;
+    {
+        const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
+        const size_t need = ((size_t)k * nst * 12 * nc * fsize + sizeof(double) - 1) / sizeof(double);
         if (need <= wg_slots_) {
             store_wg_ = true;
         } else {
@@ -148,20 +139,24 @@ double Solver::forward(int nsteps, int k, int* status) {
 }
 
 // One forward step that keeps every stage's input state in store[stage] and,
-// when wg is given, the stage's primitives and gradients in wg[stage].
-void Solver::record_step(double* store, double* wg) {
+// when wg is given, the stage's primitives and gradients (face precision) in
+// wg[stage] (12 nc values per stage).
+void Solver::record_step(double* store, void* wg) {
     const size_t nc = dc_.nc;
     const int nst = n_stages(task_.scheme);
     const int p = task_.precision;
+    const size_t fsize = p == PREC_MIXED ? sizeof(float) : sizeof(double);
+    const void* W = p == PREC_MIXED ? (const void*)dc_.W32 : (const void*)dc_.W64;
+    const void* G = p == PREC_MIXED ? (const void*)dc_.G32 : (const void*)dc_.G64;
     for (int st = 0; st < nst; st++) {
         CUDA_CHECK(cudaMemcpyAsync(store + st * 4 * nc, st == 0 ? dc_.A : dc_.B, sizeof(double) * 4 * nc,
                                    cudaMemcpyDeviceToDevice, stream_));
         if (task_.recon != RECON_NONE) launch_grad(dc_, p, stream_);
         if (wg) {
-            double* w = wg + (size_t)st * 12 * nc;
-            CUDA_CHECK(cudaMemcpyAsync(w, dc_.W64, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice, stream_));
+            char* w = static_cast<char*>(wg) + (size_t)st * 12 * nc * fsize;
+            CUDA_CHECK(cudaMemcpyAsync(w, W, fsize * 4 * nc, cudaMemcpyDeviceToDevice, stream_));
             if (task_.recon != RECON_NONE)
-                CUDA_CHECK(cudaMemcpyAsync(w + 4 * nc, dc_.G64, sizeof(double) * 8 * nc, cudaMemcpyDeviceToDevice,
+                CUDA_CHECK(cudaMemcpyAsync(w + 4 * nc * fsize, G, fsize * 8 * nc, cudaMemcpyDeviceToDevice,
                                            stream_));
         }
         launch_flux(dc_, p, task_.flux, task_.recon, stream_);
@@ -184,6 +179,9 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
                                                    "does not differentiate remediation");
     }
     const int nst = n_stages(task_.scheme);
+    const int p = task_.precision;
+    const size_t fsize = p == PREC_MIXED ? sizeof(float) : sizeof(double);
+    auto wg_at = [&](int slot) -> void* { return reinterpret_cast<char*>(wgstore_) + (size_t)slot * 12 * nc * fsize; };
     AdjCase a{};
     a.eq = adj_eq_; a.eb = adj_eb_; a.eb2 = adj_eb2_; a.qbar = adj_qbar_; a.gbar = adj_gbar_;
     a.tb = adj_tb_; a.acc = adj_acc_; a.lam = adj_lam_; a.mu = adj_mu_; a.mu_out = adj_mu_;
@@ -206,7 +204,7 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
                                    cudaMemcpyDeviceToDevice, stream_));
         launch_prims(dc_, task_.precision, stream_);
         for (int j = 0; j < n; j++)
-            record_step(segstore_ + (size_t)j * nst * 4 * nc, store_wg_ ? wgstore_ + (size_t)j * nst * 12 * nc : nullptr);
+            record_step(segstore_ + (size_t)j * nst * 4 * nc, store_wg_ ? wg_at(j * nst) : nullptr);
         for (int j = n - 1; j >= 0; j--) {
             launch_adj_step_start(adj_dc_, a, ct_f, ca_f, stream_);
             for (int st = nst - 1; st >= 0; st--) {
@@ -214,17 +212,23 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
                 cx.A = segstore_ + ((size_t)j * nst + st) * 4 * nc;
                 a.X = cx.A;
                 if (store_wg_) {  // the recorded stage's own W and G
-                    cx.W64 = wgstore_ + ((size_t)j * nst + st) * 12 * nc;
-                    cx.G64 = cx.W64 + 4 * nc;
-                } else {
-                    launch_prims(cx, PREC_FP64, stream_);
-                    if (task_.recon != RECON_NONE) launch_grad(cx, PREC_FP64, stream_);
+                    char* w = static_cast<char*>(wg_at(j * nst + st));
+                    if (p == PREC_MIXED) {
+                        cx.W32 = reinterpret_cast<float*>(w);
+                        cx.G32 = cx.W32 + 4 * nc;
+                    } else {
+                        cx.W64 = reinterpret_cast<double*>(w);
+                        cx.G64 = cx.W64 + 4 * nc;
+                    }
+                } else {  // re-derived by the forward's own kernels from the recorded stage state
+                    launch_prims(cx, p, stream_);
+                    if (task_.recon != RECON_NONE) launch_grad(cx, p, stream_);
                 }
-                launch_adj_flux(cx, a, task_.flux, task_.recon, stream_);
-                launch_adj_gather(cx, a, stream_);
+                launch_adj_flux(cx, a, task_.flux, task_.recon, p, stream_);
+                launch_adj_gather(cx, a, p, stream_);
                 double ct = 1.0, ca = 0.0;
                 if (st > 0) stage_coefs(task_.scheme, st, ct, ca);
-                launch_adj_cell(cx, a, ct, ca, st == 0 ? 1 : 0, stream_);
+                launch_adj_cell(cx, a, ct, ca, st == 0 ? 1 : 0, p, stream_);
             }
         }
     }
