@@ -53,6 +53,14 @@ template <> __device__ __forceinline__ const float* NY_of<float>(const DevCase& 
 template <typename T> __device__ __forceinline__ const T* L_of(const DevCase& c);
 template <> __device__ __forceinline__ const double* L_of<double>(const DevCase& c) { return c.l; }
 template <> __device__ __forceinline__ const float* L_of<float>(const DevCase& c) { return c.l32; }
+template <typename T> struct CellFaces { const T *nx, *ny, *l; };
+template <typename T> __device__ __forceinline__ CellFaces<T> cf_of(const DevCase& c);
+template <> __device__ __forceinline__ CellFaces<double> cf_of<double>(const DevCase& c) {
+    return CellFaces<double>{c.cf_nx, c.cf_ny, c.cf_l};
+}
+template <> __device__ __forceinline__ CellFaces<float> cf_of<float>(const DevCase& c) {
+    return CellFaces<float>{c.cf_nx32, c.cf_ny32, c.cf_l32};
+}
 template <typename T> __device__ __forceinline__ const T* DL_of(const DevCase& c);
 template <> __device__ __forceinline__ const double* DL_of<double>(const DevCase& c) { return c.dl; }
 template <> __device__ __forceinline__ const float* DL_of<float>(const DevCase& c) { return c.dl32; }
@@ -510,20 +518,19 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
     const T* __restrict__ W = W_of<T>(c);
     const Prim<T> q = load_prim(W, i);
     T g[8] = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
+    const CellFaces<T> cf = cf_of<T>(c);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const int f = c.face[k * nc + i];
-        const int e = f >> 1;
-        const bool side2 = f & 1;
-        const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
+        const int nb = c.cf_nb[k * nc + i];
+        const T nx = cf.nx[k * nc + i], ny = cf.ny[k * nc + i], l = cf.l[k * nc + i];
         Prim<T> o;
-        const int j = side2 ? c.ec1[e] : c.ec2[e];
-        if (j >= 0) {
-            o = load_prim(W, j);
-        } else {
+        const bool side2 = nb >= 0 && (nb & 1);
+        if (nb >= 0) {
+            o = load_prim(W, nb >> 1);
+        } else {  // boundary edge -(nb + 1); the cell is its c1
             const MatT<T> mt = matT_of<T>(c, i);
             const T Tc = temperature(q, mt.gm1, mt.Cv);
-            o = ghost_state(c.bnds[c.ebnd[e]], q, Tc, nx, ny, mt.M);
+            o = ghost_state(c.bnds[c.ebnd[-(nb + 1)]], q, Tc, nx, ny, mt.M);
         }
         // x * 0.5 is the correctly rounded x / 2 (exact halving), without a division
         const T hr = (q.r + o.r) * T(0.5), hp = (q.p + o.p) * T(0.5);
@@ -563,17 +570,19 @@ __device__ __forceinline__ T proj(T gx, T gy, T dx, T dy) {
     return gx * dx + gy * dy;
 }
 
+// dq = neighbour value minus own centre value per variable (minmod only; formed
+// once per edge: the two sides' differences are exact negatives of each other).
 template <typename T, int RECON>
-__device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, const Prim<T>& nb) {
+__device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, const Prim<T>& dq) {
     T dr = proj<T, RECON>(g[0], g[1], dx, dy);
     T dp = proj<T, RECON>(g[2], g[3], dx, dy);
     T du = proj<T, RECON>(g[4], g[5], dx, dy);
     T dv = proj<T, RECON>(g[6], g[7], dx, dy);
     if (RECON == RECON_MINMOD) {
-        dr = minmod(dr, nb.r - q.r);
-        dp = minmod(dp, nb.p - q.p);
-        du = minmod(du, nb.u - q.u);
-        dv = minmod(dv, nb.v - q.v);
+        dr = minmod(dr, dq.r);
+        dp = minmod(dp, dq.p);
+        du = minmod(du, dq.u);
+        dv = minmod(dv, dq.v);
     }
     q.r += dr; q.p += dp; q.u += du; q.v += dv;
 }
@@ -606,17 +615,30 @@ __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
         M = mt.M;
         if (RECON == RECON_MINMOD) gc = ghost_state(b, qL, Tc, nx, ny, M);
     }
+    // minmod's neighbour-minus-centre differences of both sides: formed once per edge in
+    // FP64 (the FP64 pipe is the bound there); per Gauss point in FP32 (fewer live registers)
+    Prim<T> dL = qL, dR = qL;
+    if (RECON == RECON_MINMOD && sizeof(T) == 8) {
+        const Prim<T>& nb = inner ? qR : gc;
+        dL.r = nb.r - qL.r; dL.u = nb.u - qL.u; dL.v = nb.v - qL.v; dL.p = nb.p - qL.p;
+        dR.r = neg_if(dL.r, true); dR.u = neg_if(dL.u, true); dR.v = neg_if(dL.v, true); dR.p = neg_if(dL.p, true);
+    }
     T fs[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
     bool hit = false;
 #pragma unroll
     for (int gp = 0; gp < 2; gp++) {
         Prim<T> pL = qL, pR;
+        if (RECON == RECON_MINMOD && sizeof(T) == 4) {
+            const Prim<T>& nb = inner ? qR : gc;
+            dL.r = nb.r - qL.r; dL.u = nb.u - qL.u; dL.v = nb.v - qL.v; dL.p = nb.p - qL.p;
+            dR.r = qL.r - qR.r; dR.u = qL.u - qR.u; dR.v = qL.v - qR.v; dR.p = qL.p - qR.p;
+        }
         if (RECON != RECON_NONE)
-            reconstruct<T, RECON>(pL, gL, DL[(4 * gp) * ne + e], DL[(4 * gp + 1) * ne + e], inner ? qR : gc);
+            reconstruct<T, RECON>(pL, gL, DL[(4 * gp) * ne + e], DL[(4 * gp + 1) * ne + e], dL);
         if (inner) {
             pR = qR;
             if (RECON != RECON_NONE)
-                reconstruct<T, RECON>(pR, gR, DL[(4 * gp + 2) * ne + e], DL[(4 * gp + 3) * ne + e], qL);
+                reconstruct<T, RECON>(pR, gR, DL[(4 * gp + 2) * ne + e], DL[(4 * gp + 3) * ne + e], dR);
         } else {
             pR = ghost_state(b, pL, Tc, nx, ny, M);
         }

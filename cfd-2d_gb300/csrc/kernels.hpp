@@ -51,6 +51,16 @@ struct DevCase {
     LaunchShape shape[N_TUNED_KINDS];
     // geometry
     const int* face;       // 3*nc
+    // the same faces seen from the cell, for the gradient gather (one level of
+    // indirection instead of three): cf_nb = (neighbour << 1) | side, or -(edge + 1)
+    // on the boundary; the edge's normal (outward from c1) and length per face
+    const int* cf_nb;      // 3*nc
+    const double* cf_nx;   // 3*nc (FP64 form)
+    const double* cf_ny;
+    const double* cf_l;
+    const float* cf_nx32;  // 3*nc (mixed form)
+    const float* cf_ny32;
+    const float* cf_l32;
     const int* ec1;        // ne
     const int* ec2;        // ne
     const int* ebnd;       // ne (boundary index, -1 inside)

@@ -81,6 +81,22 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
         c.rem_nb = upload(lay_.rem_nb);
         c.iperm = upload(lay_.iperm);
         const bool mixed = task_.precision == PREC_MIXED;
+        {
+            std::vector<int> nb(3 * (size_t)nc);
+            std::vector<double> fx(3 * (size_t)nc), fy(3 * (size_t)nc), fl(3 * (size_t)nc);
+            for (size_t q = 0; q < 3 * (size_t)nc; q++) {
+                const int f = lay_.face[q], e = f >> 1, side = f & 1;
+                const int j = side ? lay_.ec1[e] : lay_.ec2[e];
+                nb[q] = j >= 0 ? ((j << 1) | side) : -(e + 1);
+                fx[q] = lay_.nx[e]; fy[q] = lay_.ny[e]; fl[q] = lay_.l[e];
+            }
+            c.cf_nb = upload(nb);
+            if (mixed) {
+                c.cf_nx32 = upload(to_f32(fx)); c.cf_ny32 = upload(to_f32(fy)); c.cf_l32 = upload(to_f32(fl));
+            } else {
+                c.cf_nx = upload(fx); c.cf_ny = upload(fy); c.cf_l = upload(fl);
+            }
+        }
         if (mixed) {
             c.nx32 = upload(to_f32(lay_.nx));
             c.ny32 = upload(to_f32(lay_.ny));
