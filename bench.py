@@ -69,6 +69,13 @@ def measured_peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
+def measured_sm_max():
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["sm_max_mhz"])
+    except Exception:
+        return 2070.0
+
+
 def ncu_traffic():
     """Per-launch DRAM bytes of each kernel kind from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "ncu_dram_traffic.txt")
@@ -79,6 +86,31 @@ def ncu_traffic():
                 _, key, val = line.split()[:3]
                 out[key] = float(val)
     return out
+
+
+def ncu_instr():
+    """FP64 / FP32 thread instructions per cell-update of each form, from the committed
+    ncu instruction-count summary (one SSP-RK3 step of the 2,097,152-triangle workload)."""
+    p = os.path.join(ROOT, "profiles", "ncu_instruction_counts_four_quadrant_2M.md")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("instr_per_cell_update"):
+                _, form, kind, val = line.split()[:4]
+                out[(form, kind)] = float(val)
+    return out
+
+
+def cpu_model():
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in r.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 class ClockSampler:
@@ -246,7 +278,7 @@ def cpu_baseline_single(seconds: float = 12.0):
         if time.perf_counter() - a >= seconds or k >= 10:
             break
     dt = time.perf_counter() - a
-    return {"value": m.n_cells * k / dt, "unit": UNIT, "cores": 1, "kind": "port",
+    return {"value": m.n_cells * k / dt, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_model(),
             "sample": f"{k} SSP-RK3 step(s) of the full 2,097,152-triangle workload on one core"}
 
 
@@ -540,6 +572,20 @@ def main():
     mx_bytes = kernel_bytes(mx_dom, nc, ne, 4)
     mx_ach = mx_bytes / (prof["mixed"][mx_dom]["ms_per_launch"] * 1e-3) / 1e9
 
+    # the FP64 ALU ceiling: ncu-counted FP64 thread instructions per cell-update against
+    # GB300's FP64 issue rate (2 per clock and SM) at the clock sampled during the timed runs
+    instr = ncu_instr()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clocks.get("sm_mhz") or measured_sm_max()
+    fp64_peak = 2.0 * sms * mhz * 1e6
+    fp64_ceiling = {"peak_instr_per_s": fp64_peak, "sms": sms, "sm_mhz": mhz,
+                    "source": "profiles/ncu_instruction_counts_four_quadrant_2M.md"}
+    for form, rate in (("fp64", value / world), ("mixed", value_mx / world)):
+        n64 = instr.get((form, "fp64"))
+        if n64:
+            fp64_ceiling[form] = {"fp64_instr_per_cell_update": n64, "fp32_instr_per_cell_update":
+                                  instr.get((form, "fp32")), "achieved_instr_per_s": n64 * rate,
+                                  "frac": n64 * rate / fp64_peak}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms64 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -558,6 +604,7 @@ def main():
                                     "dominant_frac": mx_ach / hbm,
                                     "dominant_traffic": traffic.get(f"{mx_dom}_mixed")},
                           "peak": hbm, "unit": "GB/s", "peak_kind": peak_kind},
+        "fp64_alu_ceiling": fp64_ceiling,
         "mixed": {"value": value_mx, "unit": UNIT, "ms_per_step": msmx / K, "speedup_vs_fp64": ms64 / msmx,
                   "dtype": "f32 faces / f64 accumulate", "error_vs_fp64": err},
         "adjoint_forward_ratio": adj["ratio_backward_over_forward"],
