@@ -9,6 +9,7 @@
 #include <map>
 #include <numeric>
 #include <sstream>
+#include <thread>
 
 #include "cfd2d.h"
 
@@ -19,34 +20,155 @@ namespace {
 std::string slurp(const std::string& path) {
     std::ifstream f(path, std::ios::binary);
     if (!f) throw Error(CFD2D_ERR_FILE_OPENING, "File '" + path + "' opening error.");
-    std::stringstream ss;
-    ss << f.rdbuf();
-    return ss.str();
+    f.seekg(0, std::ios::end);
+    const std::streamoff n = f.tellg();
+    f.seekg(0, std::ios::beg);
+    std::string s(n > 0 ? (size_t)n : 0, '\0');
+    if (n > 0) f.read(&s[0], n);
+    return s;
 }
 
-// Up to n integers from the start of a line (sscanf("%d %d ...") semantics).
-int scan_ints(const char* s, int* out, int n) {
+// f(begin, end) over [0, n) split into contiguous ranges, one per host thread (up to 16);
+// the first exception (in range order) is rethrown after all threads joined.
+template <typename F>
+void parallel_ranges(size_t n, size_t min_per_thread, F&& f) {
+    unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    nt = (unsigned)std::max<size_t>(1, std::min<size_t>(nt, n / std::max<size_t>(1, min_per_thread)));
+    if (nt <= 1) { f(size_t(0), n); return; }
+    std::vector<std::thread> th;
+    std::vector<std::exception_ptr> err(nt);
+    const size_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 0; t < nt; t++) {
+        const size_t a = std::min(n, t * chunk), b = std::min(n, a + chunk);
+        th.emplace_back([&, t, a, b] {
+            try { f(a, b); } catch (...) { err[t] = std::current_exception(); }
+        });
+    }
+    for (auto& x : th) x.join();
+    for (auto& e : err)
+        if (e) std::rethrow_exception(e);
+}
+
+inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f' || c == '\n'; }
+
+// Up to n integers from the start of the line [s, e) (sscanf("%d %d ...") / strtol
+// semantics: optional sign, decimal digits, stop at the first non-number).
+int scan_ints(const char* s, const char* e, int* out, int n) {
     int k = 0;
-    char* end;
     while (k < n) {
-        long v = std::strtol(s, &end, 10);
-        if (end == s) break;
-        out[k++] = (int)v;
-        s = end;
+        while (s < e && is_space(*s)) s++;
+        const char* p = s;
+        bool neg = false;
+        if (p < e && (*p == '+' || *p == '-')) { neg = *p == '-'; p++; }
+        if (p >= e || *p < '0' || *p > '9') break;
+        long v = 0;
+        while (p < e && *p >= '0' && *p <= '9') { v = v * 10 + (*p - '0'); p++; }
+        out[k++] = (int)(neg ? -v : v);
+        s = p;
     }
     return k;
 }
 
-int scan_doubles(const char* s, double* out, int n) {
+// Up to n doubles from the line [s, e), each read by strtod.
+int scan_doubles(const char* s, const char* e, double* out, int n) {
     int k = 0;
-    char* end;
     while (k < n) {
-        double v = std::strtod(s, &end);
+        while (s < e && is_space(*s)) s++;
+        if (s >= e) break;
+        char* end;
+        const double v = std::strtod(s, &end);
         if (end == s) break;
         out[k++] = v;
         s = end;
     }
     return k;
+}
+
+// The first whitespace-delimited token of [s, e), at most 255 characters (sscanf "%255s").
+std::string first_token(const char* s, const char* e) {
+    while (s < e && is_space(*s)) s++;
+    const char* p = s;
+    while (p < e && !is_space(*p) && p - s < 255) p++;
+    return std::string(s, p);
+}
+
+// The UNV text cut into lines with the block delimiters removed: content line k is
+// [text + start[k], text + start[k] + len[k]) (a trailing '\r' dropped), and block
+// b is content lines [block[b], block[b + 1]).
+struct UnvLines {
+    const char* text = nullptr;
+    std::vector<uint64_t> start;
+    std::vector<uint32_t> len;
+    std::vector<size_t> block;
+    const char* s(size_t k) const { return text + start[k]; }
+    const char* e(size_t k) const { return text + start[k] + len[k]; }
+};
+
+// A line whose first "-1" ends it is a block delimiter; every second one closes a
+// block (read_block, src/mesh/MeshReaderSalomeUnv.cpp:267-286). The text is split into
+// chunks at line starts, scanned in parallel and stitched in order.
+UnvLines split_unv(const std::string& text) {
+    UnvLines L;
+    L.text = text.data();
+    const char* T = text.data();
+    const size_t N = text.size();
+    unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (N < (1u << 20)) nt = 1;
+    std::vector<size_t> cut(nt + 1, N);
+    cut[0] = 0;
+    for (unsigned t = 1; t < nt; t++) {
+        size_t p = std::max(cut[t - 1], t * (N / nt));
+        const void* q = p < N ? std::memchr(T + p, '\n', N - p) : nullptr;
+        cut[t] = q ? (size_t)((const char*)q - T) + 1 : N;
+    }
+    cut[nt] = N + 1;  // the (possibly empty) line after the last newline belongs to the last chunk
+    struct Part { std::vector<uint64_t> start; std::vector<uint32_t> len; std::vector<size_t> delim; };
+    std::vector<Part> parts(nt);
+    auto scan = [&](unsigned t) {
+        Part& P = parts[t];
+        size_t p = cut[t];
+        const size_t stop = cut[t + 1];
+        while (p < stop && p <= N) {
+            const void* q = p < N ? std::memchr(T + p, '\n', N - p) : nullptr;
+            const size_t nl = q ? (size_t)((const char*)q - T) : N;
+            size_t e = nl;
+            if (e > p && T[e - 1] == '\r') e--;
+            size_t m = e;  // first "-1"
+            for (size_t i = p; i + 1 < e; i++)
+                if (T[i] == '-' && T[i + 1] == '1') { m = i; break; }
+            if (m != e && m + 2 == e) {
+                P.delim.push_back(P.start.size());
+            } else {
+                P.start.push_back(p);
+                P.len.push_back((uint32_t)(e - p));
+            }
+            if (nl >= N) break;
+            p = nl + 1;
+        }
+    };
+    if (nt == 1) scan(0);
+    else {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; t++) th.emplace_back(scan, t);
+        for (auto& x : th) x.join();
+    }
+    size_t total = 0;
+    for (auto& P : parts) total += P.start.size();
+    L.start.reserve(total);
+    L.len.reserve(total);
+    std::vector<size_t> delim;
+    for (auto& P : parts) {
+        const size_t base = L.start.size();
+        for (size_t d : P.delim) delim.push_back(base + d);
+        L.start.insert(L.start.end(), P.start.begin(), P.start.end());
+        L.len.insert(L.len.end(), P.len.begin(), P.len.end());
+        std::vector<uint64_t>().swap(P.start);
+        std::vector<uint32_t>().swap(P.len);
+    }
+    L.block.push_back(0);
+    for (size_t d = 1; d < delim.size(); d += 2) L.block.push_back(delim[d]);
+    if (L.block.back() < L.start.size()) L.block.push_back(L.start.size());
+    return L;
 }
 
 }  // namespace
@@ -55,104 +177,123 @@ int scan_doubles(const char* s, double* out, int n) {
 
 RawMesh read_unv(const std::string& path) {
     const std::string text = slurp(path);
-    // Lines; a line whose first "-1" ends it is a block delimiter, two of them
-    // close a block (read_block, src/mesh/MeshReaderSalomeUnv.cpp:267-286).
-    std::vector<std::vector<std::string>> blocks;
-    std::vector<std::string> cur;
-    int minus = 0;
-    size_t p = 0;
-    while (p <= text.size()) {
-        size_t q = text.find('\n', p);
-        if (q == std::string::npos) q = text.size();
-        std::string line = text.substr(p, q - p);
-        if (!line.empty() && line.back() == '\r') line.pop_back();
-        p = q + 1;
-        size_t pos = line.find("-1");
-        if (pos != std::string::npos && pos + 2 == line.size()) {
-            if (++minus == 2) {
-                blocks.push_back(std::move(cur));
-                cur.clear();
-                minus = 0;
-            }
-            continue;
-        }
-        cur.push_back(line);
-        if (q == text.size()) break;
-    }
-    if (!cur.empty()) blocks.push_back(std::move(cur));
+    const UnvLines L = split_unv(text);
 
     RawMesh m;
+    m.names.push_back(std::string());
     struct Elem { int kind = 0; int index = -1; };   // 41 cell, 11 edge element
     std::vector<Elem> elements;
     std::vector<int> edge_label;                    // per UNV edge element: label-1
     std::map<std::string, std::vector<int>> groups; // name -> element labels-1 (sorted by name, like std::map)
-    for (auto& b : blocks) {
-        if (b.empty()) continue;
-        int id = std::atoi(b[0].c_str());
+    for (size_t bi = 0; bi + 1 < L.block.size(); bi++) {
+        const size_t b0 = L.block[bi], b1 = L.block[bi + 1], size = b1 - b0;
+        if (size == 0) continue;
+        int id = 0;
+        scan_ints(L.s(b0), L.e(b0), &id, 1);
         if (id == 2411) {
-            for (size_t k = 1; k + 1 < b.size() + 1 && k < b.size(); k += 2) {
-                double c[3] = {0, 0, 0};
-                if (k + 1 >= b.size()) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2411: truncated node record");
-                scan_doubles(b[k + 1].c_str(), c, 3);
-                m.xy.push_back(c[0]);
-                m.xy.push_back(c[1]);
-            }
+            if ((size - 1) % 2 != 0) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2411: truncated node record");
+            const size_t nrec = (size - 1) / 2, base = m.xy.size();
+            m.xy.resize(base + 2 * nrec);
+            parallel_ranges(nrec, 1 << 16, [&](size_t a, size_t b) {
+                for (size_t r = a; r < b; r++) {
+                    double c[3] = {0, 0, 0};
+                    const size_t k = b0 + 2 + 2 * r;
+                    scan_doubles(L.s(k), L.e(k), c, 3);
+                    m.xy[base + 2 * r] = c[0];
+                    m.xy[base + 2 * r + 1] = c[1];
+                }
+            });
         } else if (id == 2412) {
-            size_t k = 1;
-            while (k < b.size()) {
-                int h[6] = {0, 0, 0, 0, 0, 0};
-                scan_ints(b[k].c_str(), h, 6);
-                int label = h[0] - 1, type = h[1];
+            // record starts and kinds in order (header line: label, type, ...), then the
+            // records parsed in parallel into their places
+            std::vector<size_t> rec;
+            std::vector<char> is_tri;
+            size_t k = b0 + 1;
+            while (k < b1) {
+                int h[2] = {0, 0};
+                scan_ints(L.s(k), L.e(k), h, 2);
+                const int type = h[1];
+                rec.push_back(k);
                 k++;
                 if (type == 11) {
-                    if (k + 1 >= b.size()) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2412: truncated edge record");
-                    int nd[2] = {0, 0};
-                    scan_ints(b[k + 1].c_str(), nd, 2);
+                    if (k + 1 >= b1) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2412: truncated edge record");
+                    is_tri.push_back(0);
                     k += 2;
-                    m.bseg.push_back(nd[0] - 1);
-                    m.bseg.push_back(nd[1] - 1);
-                    edge_label.push_back(label);
                 } else if (type == 41) {
-                    if (k >= b.size()) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2412: truncated triangle record");
-                    int nd[3] = {0, 0, 0};
-                    scan_ints(b[k].c_str(), nd, 3);
+                    if (k >= b1) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2412: truncated triangle record");
+                    is_tri.push_back(1);
                     k += 1;
-                    if (label < 0) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2412: bad element label");
-                    if ((int)elements.size() <= label) elements.resize(label + 1);
-                    elements[label].kind = 41;
-                    elements[label].index = m.nc();
-                    for (int j = 0; j < 3; j++) m.tri.push_back(nd[j] - 1);
                 } else {
                     throw Error(CFD2D_ERR_MESH_UNV_UNKNOWN_ELEMENT, "Unknown element type '" + std::to_string(type) + "'.");
                 }
             }
-        } else if (id == 2467) {
-            size_t k = 1;
-            while (k < b.size()) {
-                int h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                scan_ints(b[k].c_str(), h, 8);
-                int n = h[7];
-                k++;
-                if (k >= b.size()) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2467: truncated group");
-                char name[256] = {0};
-                std::sscanf(b[k].c_str(), "%255s", name);
-                k++;
-                std::vector<int> ids;
-                for (int j = 0; j < n / 2; j++, k++) {
-                    if (k >= b.size()) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2467: truncated group entities");
-                    int e[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-                    scan_ints(b[k].c_str(), e, 8);
-                    ids.push_back(e[1] - 1);
-                    ids.push_back(e[5] - 1);
+            const size_t nrec = rec.size();
+            std::vector<int> slot(nrec);  // index among the block's triangles / edge elements
+            size_t ntri = 0, nedge = 0;
+            for (size_t r = 0; r < nrec; r++) slot[r] = is_tri[r] ? (int)ntri++ : (int)nedge++;
+            const size_t tri0 = m.tri.size() / 3, seg0 = m.bseg.size() / 2, lab0 = edge_label.size();
+            m.tri.resize(3 * (tri0 + ntri));
+            m.bseg.resize(2 * (seg0 + nedge));
+            edge_label.resize(lab0 + nedge);
+            std::vector<int> tri_label(ntri);
+            parallel_ranges(nrec, 1 << 15, [&](size_t a, size_t b) {
+                for (size_t r = a; r < b; r++) {
+                    int h[6] = {0, 0, 0, 0, 0, 0};
+                    const size_t q = rec[r];
+                    scan_ints(L.s(q), L.e(q), h, 6);
+                    const int label = h[0] - 1;
+                    if (is_tri[r]) {
+                        int nd[3] = {0, 0, 0};
+                        scan_ints(L.s(q + 1), L.e(q + 1), nd, 3);
+                        const size_t t = tri0 + slot[r];
+                        for (int j = 0; j < 3; j++) m.tri[3 * t + j] = nd[j] - 1;
+                        tri_label[slot[r]] = label;
+                    } else {
+                        int nd[2] = {0, 0};
+                        scan_ints(L.s(q + 2), L.e(q + 2), nd, 2);
+                        const size_t s2 = seg0 + slot[r];
+                        m.bseg[2 * s2] = nd[0] - 1;
+                        m.bseg[2 * s2 + 1] = nd[1] - 1;
+                        edge_label[lab0 + slot[r]] = label;
+                    }
                 }
-                if (n % 2 == 1) {
-                    if (k >= b.size()) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2467: truncated group entities");
+            });
+            for (size_t t = 0; t < ntri; t++) {
+                const int label = tri_label[t];
+                if (label < 0) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2412: bad element label");
+                if ((int)elements.size() <= label) elements.resize(label + 1);
+                elements[label].kind = 41;
+                elements[label].index = (int)(tri0 + t);
+            }
+        } else if (id == 2467) {
+            size_t k = b0 + 1;
+            while (k < b1) {
+                int h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                scan_ints(L.s(k), L.e(k), h, 8);
+                const int n = h[7];
+                k++;
+                if (k >= b1) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2467: truncated group");
+                const std::string name = first_token(L.s(k), L.e(k));
+                k++;
+                const size_t pairs = n > 0 ? (size_t)(n / 2) : 0, odd = n > 0 ? (size_t)(n % 2) : 0;
+                if (k + pairs + odd > b1) throw Error(CFD2D_ERR_MESH_FORMAT, "UNV block 2467: truncated group entities");
+                std::vector<int> ids(2 * pairs + odd);
+                parallel_ranges(pairs, 1 << 15, [&](size_t a, size_t b) {
+                    for (size_t j = a; j < b; j++) {
+                        int e[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                        scan_ints(L.s(k + j), L.e(k + j), e, 8);
+                        ids[2 * j] = e[1] - 1;
+                        ids[2 * j + 1] = e[5] - 1;
+                    }
+                });
+                k += pairs;
+                if (odd) {
                     int e[4] = {0, 0, 0, 0};
-                    scan_ints(b[k].c_str(), e, 4);
-                    ids.push_back(e[1] - 1);
+                    scan_ints(L.s(k), L.e(k), e, 4);
+                    ids[2 * pairs] = e[1] - 1;
                     k++;
                 }
-                groups[std::string(name)] = ids;
+                groups[name] = std::move(ids);
             }
         }
         // blocks 164, 2420 and any other block are skipped
@@ -166,7 +307,6 @@ RawMesh read_unv(const std::string& path) {
     // (find_edge, src/mesh/MeshReaderSalomeUnv.cpp:14-22, 204-210).
     std::map<long long, int> first;
     const int nb = (int)edge_label.size();
-    std::vector<int> edge_elem_of_label;
     for (int s = 0; s < nb; s++) {
         long long a = m.bseg[2 * s], c = m.bseg[2 * s + 1];
         long long key = std::min(a, c) * (1ll << 32) + std::max(a, c);
@@ -180,15 +320,18 @@ RawMesh read_unv(const std::string& path) {
         }
     }
     // Group names, groups visited in name order so the last one wins (:219-248).
-    m.cell_name.assign(nc, std::string());
-    m.bseg_name.assign(nb, std::string());
-    for (auto& g : groups)
+    m.cell_name.assign(nc, 0);
+    m.bseg_name.assign(nb, 0);
+    for (auto& g : groups) {
+        const int gi = (int)m.names.size();
+        m.names.push_back(g.first);
         for (int id : g.second) {
             if (id < 0 || id >= (int)elements.size()) continue;
             const Elem& el = elements[id];
-            if (el.kind == 41) m.cell_name[el.index] = g.first;
-            else if (el.kind == 11) m.bseg_name[el.index] = g.first;
+            if (el.kind == 41) m.cell_name[el.index] = gi;
+            else if (el.kind == 11) m.bseg_name[el.index] = gi;
         }
+    }
     return m;
 }
 
@@ -218,9 +361,17 @@ RawMesh read_triangle(const std::string& base) {
         m.xy.push_back(std::strtod(at(node, 4 + 4 * i + 2).c_str(), nullptr));
     }
     int nc = std::atoi(at(ele, 0).c_str());
+    m.names.push_back(std::string());
+    std::map<std::string, int> name_id;
     for (int i = 0; i < nc; i++) {  // "%d %d %d %d %d": index, nodes, attribute
         for (int j = 0; j < 3; j++) m.tri.push_back(std::atoi(at(ele, 3 + 5 * i + 1 + j).c_str()) - 1);
-        m.cell_name.push_back(std::to_string(std::atoi(at(ele, 3 + 5 * i + 4).c_str())));
+        const std::string nm = std::to_string(std::atoi(at(ele, 3 + 5 * i + 4).c_str()));
+        auto it = name_id.find(nm);
+        if (it == name_id.end()) {
+            it = name_id.emplace(nm, (int)m.names.size()).first;
+            m.names.push_back(nm);
+        }
+        m.cell_name.push_back(it->second);
     }
     for (int i = 0; i < nc; i++)
         for (int j = 0; j < 3; j++) m.neigh.push_back(std::atoi(at(nei, 2 + 4 * i + 1 + j).c_str()) - 1);
@@ -422,58 +573,76 @@ Layout make_layout(const Topo& t, const std::vector<int>& cell_mat, const std::v
     L.iperm.resize(nc);
     for (int i = 0; i < nc; i++) L.iperm[L.perm[i]] = i;
     // edges: interior ones by (lower, upper) storage cell, then boundary ones by cell
-    std::vector<std::pair<long long, int>> key(ne);
+    // (ties between a cell's boundary edges by edge number): a counting sort by the
+    // lower / boundary cell, each cell's few interior edges then ordered by the upper one
+    std::vector<int> cnt(nc + 1, 0), bcnt(nc + 1, 0);
     int n_int = 0;
     for (int e = 0; e < ne; e++) {
-        long long a = L.iperm[t.c1[e]];
-        if (t.c2[e] >= 0) {
-            long long b = L.iperm[t.c2[e]];
-            key[e] = {std::min(a, b) * (1ll << 32) + std::max(a, b), e};
-            n_int++;
-        } else {
-            key[e] = {(1ll << 62) + a * 4, e};
-        }
+        const int a = L.iperm[t.c1[e]];
+        if (t.c2[e] >= 0) { cnt[std::min(a, L.iperm[t.c2[e]]) + 1]++; n_int++; }
+        else bcnt[a + 1]++;
     }
-    std::sort(key.begin(), key.end());
+    for (int i = 0; i < nc; i++) { cnt[i + 1] += cnt[i]; bcnt[i + 1] += bcnt[i]; }
     L.n_int = n_int;
     L.eorig.resize(ne);
+    {
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1), bfill(bcnt.begin(), bcnt.end() - 1);
+        for (int e = 0; e < ne; e++) {  // ascending e: stable within a bucket
+            const int a = L.iperm[t.c1[e]];
+            if (t.c2[e] >= 0) L.eorig[fill[std::min(a, L.iperm[t.c2[e]])]++] = e;
+            else L.eorig[n_int + bfill[a]++] = e;
+        }
+        parallel_ranges((size_t)nc, 1 << 16, [&](size_t i0, size_t i1) {
+            for (size_t i = i0; i < i1; i++) {  // order a bucket's interior edges by the upper cell
+                int* b = L.eorig.data() + cnt[i];
+                const int m = cnt[i + 1] - cnt[i];
+                auto hi = [&](int e) { return std::max(L.iperm[t.c1[e]], L.iperm[t.c2[e]]); };
+                for (int x = 1; x < m; x++)
+                    for (int y = x; y > 0 && hi(b[y - 1]) > hi(b[y]); y--) std::swap(b[y - 1], b[y]);
+            }
+        });
+    }
     std::vector<int> enew(ne);
-    for (int k = 0; k < ne; k++) { L.eorig[k] = key[k].second; enew[key[k].second] = k; }
+    for (int k = 0; k < ne; k++) enew[L.eorig[k]] = k;
     L.ec1.resize(ne); L.ec2.resize(ne); L.ebnd.resize(ne);
     L.nx.resize(ne); L.ny.resize(ne); L.l.resize(ne); L.dl.assign(8 * (size_t)ne, 0.0);
-    for (int k = 0; k < ne; k++) {
-        int e = L.eorig[k];
-        int a = t.c1[e], b = t.c2[e];
-        L.ec1[k] = L.iperm[a];
-        L.ec2[k] = b >= 0 ? L.iperm[b] : -1;
-        L.ebnd[k] = b >= 0 ? -1 : edge_bnd[e];
-        L.nx[k] = t.nx[e]; L.ny[k] = t.ny[e]; L.l[k] = t.l[e];
-        for (int gp = 0; gp < 2; gp++) {  // the reference's points c[1], c[2] minus each centroid
-            double px = t.pts[6 * (size_t)e + 2 + 2 * gp], py = t.pts[6 * (size_t)e + 3 + 2 * gp];
-            L.dl[(size_t)(4 * gp) * ne + k] = px - t.cx[a];
-            L.dl[(size_t)(4 * gp + 1) * ne + k] = py - t.cy[a];
-            if (b >= 0) {
-                L.dl[(size_t)(4 * gp + 2) * ne + k] = px - t.cx[b];
-                L.dl[(size_t)(4 * gp + 3) * ne + k] = py - t.cy[b];
+    parallel_ranges((size_t)ne, 1 << 16, [&](size_t k0, size_t k1) {
+        for (size_t k = k0; k < k1; k++) {
+            int e = L.eorig[k];
+            int a = t.c1[e], b = t.c2[e];
+            L.ec1[k] = L.iperm[a];
+            L.ec2[k] = b >= 0 ? L.iperm[b] : -1;
+            L.ebnd[k] = b >= 0 ? -1 : edge_bnd[e];
+            L.nx[k] = t.nx[e]; L.ny[k] = t.ny[e]; L.l[k] = t.l[e];
+            for (int gp = 0; gp < 2; gp++) {  // the reference's points c[1], c[2] minus each centroid
+                double px = t.pts[6 * (size_t)e + 2 + 2 * gp], py = t.pts[6 * (size_t)e + 3 + 2 * gp];
+                L.dl[(size_t)(4 * gp) * ne + k] = px - t.cx[a];
+                L.dl[(size_t)(4 * gp + 1) * ne + k] = py - t.cy[a];
+                if (b >= 0) {
+                    L.dl[(size_t)(4 * gp + 2) * ne + k] = px - t.cx[b];
+                    L.dl[(size_t)(4 * gp + 3) * ne + k] = py - t.cy[b];
+                }
             }
         }
-    }
+    });
     L.face.resize(3 * (size_t)nc);
     L.rem_nb.resize(3 * (size_t)nc);
     L.S.resize(nc);
     L.cmat.resize(nc);
-    for (int i = 0; i < nc; i++) {
-        int o = L.perm[i];
-        L.S[i] = t.S[o];
-        L.cmat[i] = (uint8_t)cell_mat[o];
-        for (int k = 0; k < 3; k++) {
-            int e = t.cedges[3 * o + k];
-            int side = t.c1[e] == o ? 0 : 1;
-            L.face[(size_t)k * nc + i] = (enew[e] << 1) | side;
-            int j = t.c2[e];
-            L.rem_nb[(size_t)k * nc + i] = j >= 0 ? L.iperm[j] : -1;
+    parallel_ranges((size_t)nc, 1 << 16, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; i++) {
+            int o = L.perm[i];
+            L.S[i] = t.S[o];
+            L.cmat[i] = (uint8_t)cell_mat[o];
+            for (int k = 0; k < 3; k++) {
+                int e = t.cedges[3 * o + k];
+                int side = t.c1[e] == o ? 0 : 1;
+                L.face[(size_t)k * nc + i] = (enew[e] << 1) | side;
+                int j = t.c2[e];
+                L.rem_nb[(size_t)k * nc + i] = j >= 0 ? L.iperm[j] : -1;
+            }
         }
-    }
+    });
     return L;
 }
 

@@ -18,11 +18,12 @@ struct Error : std::runtime_error {
 struct RawMesh {
     std::vector<double> xy;               // 2*nn
     std::vector<int> tri;                 // 3*nc, 0-based node numbers
-    std::vector<std::string> cell_name;   // region name per cell ("" when the cell is in no group)
+    std::vector<std::string> names;       // distinct group / region names; names[0] == ""
+    std::vector<int> cell_name;           // region name of each cell, an index into names (0: in no group)
     bool berkeley = false;
     std::vector<int> neigh;               // Berkeley-Triangle .neigh, 0-based, -2 = none
     std::vector<int> bseg;                // 2*nb boundary segments (UNV edge elements / .poly segments)
-    std::vector<std::string> bseg_name;   // UNV: group name of the segment ("" = none)
+    std::vector<int> bseg_name;           // UNV: group name of the segment, an index into names (0: none)
     std::vector<int> bseg_marker;         // Berkeley: .poly boundary marker
     int nn() const { return (int)xy.size() / 2; }
     int nc() const { return (int)tri.size() / 3; }

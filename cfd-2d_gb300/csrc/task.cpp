@@ -177,12 +177,15 @@ void bind_mesh(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::v
                std::vector<int>& edge_bnd) {
     const int nc = topo.nc, ne = topo.ne;
     cell_region.assign(nc, -1);
-    for (int i = 0; i < nc; i++) {  // getRegion(typeName), src/methods/fvm_tvd.cpp:773-786
-        const std::string& nm = raw.cell_name[i];
+    std::vector<int> region_of_name(raw.names.size(), -1);  // getRegion(typeName), src/methods/fvm_tvd.cpp:773-786
+    for (size_t n = 0; n < raw.names.size(); n++)
         for (size_t r = 0; r < t.regions.size(); r++)
-            if (t.regions[r].name == nm) { cell_region[i] = (int)r; break; }
+            if (t.regions[r].name == raw.names[n]) { region_of_name[n] = (int)r; break; }
+    for (int i = 0; i < nc; i++) {
+        cell_region[i] = region_of_name[raw.cell_name[i]];
         if (cell_region[i] < 0)
-            throw Error(CFD2D_ERR_REGION_UNKNOWN, "ERROR: unknown cell name '" + nm + "' of cell " + std::to_string(i));
+            throw Error(CFD2D_ERR_REGION_UNKNOWN,
+                        "ERROR: unknown cell name '" + raw.names[raw.cell_name[i]] + "' of cell " + std::to_string(i));
     }
     edge_bnd.assign(ne, -1);
     std::map<long long, int> marker;  // Triangle: a later .poly line for the same edge wins (findEdge, src/mesh/grid.cpp:38-48)
@@ -196,7 +199,7 @@ void bind_mesh(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::v
         int s = topo.bseg_of_edge[e];
         int b = -1;
         if (!raw.berkeley) {
-            const std::string nm = s >= 0 ? raw.bseg_name[s] : std::string();
+            const std::string nm = s >= 0 ? raw.names[raw.bseg_name[s]] : std::string();
             for (size_t k = 0; k < t.bnds.size(); k++)
                 if (!nm.empty() && t.bnds[k].name == nm) { b = (int)k; break; }
         } else {

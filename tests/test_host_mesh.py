@@ -24,6 +24,26 @@ def test_unv_reader_matches_reference_grid(capi, tmp_path, name):
         assert bits_equal(m[k], g["grid_" + k]), k
 
 
+@pytest.mark.parametrize("variant", ["crlf", "no_final_newline", "split_across_threads"])
+def test_unv_reader_line_handling(capi, tmp_path, variant):
+    """The reader cuts the file into lines in parallel chunks: CRLF line ends, a last
+    line without a newline and a file large enough to be split across threads (the
+    same records repeated in a block the reader skips) all give the reference's Grid."""
+    g = load_golden("vortex_limits")
+    text = str(g["mesh_unv"])
+    if variant == "crlf":
+        text = text.replace("\n", "\r\n")
+    elif variant == "no_final_newline":
+        text = text.rstrip("\n")
+    else:  # a block id no reader handles, ~4 MB, ahead of the mesh
+        text = "    -1\n  9999\n" + ("  1.0 -1.5 2.0\n" * 250000) + "    -1\n" + text
+    path = write_case(tmp_path, g)
+    (tmp_path / "mesh.unv").write_bytes(text.encode())
+    m = capi.Mesh(task_xml=path).export()
+    for k in KEYS:
+        assert bits_equal(m[k], g["grid_" + k]), k
+
+
 def test_triangle_reader_matches_reference_grid(capi, tmp_path):
     g = load_golden("berkeley_triangle")
     m = capi.Mesh(task_xml=write_case(tmp_path, g)).export()
