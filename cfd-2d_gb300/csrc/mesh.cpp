@@ -1,6 +1,7 @@
 #include "mesh.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -417,17 +418,19 @@ Topo build_topology(int nn, const double* xy, int nc, const int* tri, const int*
         std::vector<int> fill(off.begin(), off.end() - 1), lst(3 * (size_t)nc);
         for (int i = 0; i < nc; i++)
             for (int k = 0; k < 3; k++) lst[fill[tri[3 * i + k]]++] = i;
-        for (int i = 0; i < nc; i++)
-            for (int k = 0; k < 3; k++) {
-                int a = tri[3 * i + k], b = tri[3 * i + (k + 1) % 3];
-                int ia = off[a], ib = off[b], nbh = -2;
-                while (ia < off[a + 1] && ib < off[b + 1]) {
-                    if (lst[ia] < lst[ib]) ia++;
-                    else if (lst[ia] > lst[ib]) ib++;
-                    else { if (lst[ia] != i) nbh = lst[ia]; ia++; ib++; }
+        parallel_ranges((size_t)nc, 1 << 15, [&](size_t i0, size_t i1) {
+            for (int i = (int)i0; i < (int)i1; i++)
+                for (int k = 0; k < 3; k++) {
+                    int a = tri[3 * i + k], b = tri[3 * i + (k + 1) % 3];
+                    int ia = off[a], ib = off[b], nbh = -2;
+                    while (ia < off[a + 1] && ib < off[b + 1]) {
+                        if (lst[ia] < lst[ib]) ia++;
+                        else if (lst[ia] > lst[ib]) ib++;
+                        else { if (lst[ia] != i) nbh = lst[ia]; ia++; ib++; }
+                    }
+                    neigh[3 * i + k] = nbh;
                 }
-                neigh[3 * i + k] = nbh;
-            }
+        });
     }
     int ne = 0;  // count, clearing each neighbour's back reference (:118-135)
     for (int i = 0; i < nc; i++)
@@ -456,6 +459,7 @@ Topo build_topology(int nn, const double* xy, int nc, const int* tri, const int*
     std::sort(keys.begin(), keys.end());
     const double sq3 = 1.0 / std::sqrt(3.0);
     const int npts = berk ? (gauss_points == 2 ? 3 : 1) : 3;
+    // edge numbers, cells and nodes in the reference's order (sequential) ...
     int e = 0;
     for (int i = 0; i < nc; i++)
         for (int j = 0; j < 3; j++) {
@@ -463,11 +467,28 @@ Topo build_topology(int nn, const double* xy, int nc, const int* tri, const int*
             if (p == -1) continue;
             if (p < -2 || p >= nc) throw Error(CFD2D_ERR_MESH_FORMAT, "mesh: bad neighbour index");
             const int* v = tri + 3 * i;
-            int a = berk ? v[(j + 1) % 3] : v[j];
-            int b = berk ? v[(j + 2) % 3] : v[(j + 1) % 3];
-            t.n1[e] = a; t.n2[e] = b;
+            t.n1[e] = berk ? v[(j + 1) % 3] : v[j];
+            t.n2[e] = berk ? v[(j + 2) % 3] : v[(j + 1) % 3];
+            t.c1[e] = i;
+            t.cedges[3 * i + cfi[i]++] = e;
+            if (p > -1) {
+                t.c2[e] = p;
+                if (cfi[p] >= 3) throw Error(CFD2D_ERR_MESH_FORMAT, "mesh: a cell has more than three edges");
+                t.cedges[3 * p + cfi[p]++] = e;
+            } else {
+                t.c2[e] = -1;
+            }
+            e++;
+        }
+    // ... then each edge's points, normal, length and boundary segment (independent, threaded)
+    std::vector<int> missing(std::max(1u, std::min(16u, std::thread::hardware_concurrency())) + 1, ne);
+    std::atomic<int> slot{0};
+    parallel_ranges((size_t)ne, 1 << 15, [&](size_t e0, size_t e1) {
+        int first_missing = ne;
+        for (int q = (int)e0; q < (int)e1; q++) {
+            const int a = t.n1[q], b = t.n2[q], i = t.c1[q];
             double x1 = xy[2 * a], y1 = xy[2 * a + 1], x2 = xy[2 * b], y2 = xy[2 * b + 1];
-            double* P = &t.pts[6 * (size_t)e];
+            double* P = &t.pts[6 * (size_t)q];
             P[0] = (x1 + x2) / 2.0;  // midpoint, then Gauss points at -+1/sqrt(3) of the half length
             P[1] = (y1 + y2) / 2.0;
             if (npts == 3) {
@@ -476,33 +497,29 @@ Topo build_topology(int nn, const double* xy, int nc, const int* tri, const int*
                 P[4] = (x1 + x2) / 2.0 + sq3 * (x2 - x1) / 2.0;
                 P[5] = (y1 + y2) / 2.0 + sq3 * (y2 - y1) / 2.0;
             }
-            t.npts[e] = npts;
+            t.npts[q] = npts;
             double nx = y2 - y1, ny = x1 - x2;
             double l = std::sqrt(nx * nx + ny * ny);
             nx /= l; ny /= l;
-            t.l[e] = l;
-            t.c1[e] = i;
-            t.cedges[3 * i + cfi[i]++] = e;
+            t.l[q] = l;
             if (!berk) {  // turn the normal outward from c1 (:181-187)
                 double vx = t.cx[i] - P[0], vy = t.cy[i] - P[1];
                 if (vx * nx + vy * ny > 0) { nx *= -1; ny *= -1; }
             }
-            t.nx[e] = nx; t.ny[e] = ny;
-            if (p > -1) {
-                t.c2[e] = p;
-                if (cfi[p] >= 3) throw Error(CFD2D_ERR_MESH_FORMAT, "mesh: a cell has more than three edges");
-                t.cedges[3 * p + cfi[p]++] = e;
-            } else {
-                t.c2[e] = -1;
+            t.nx[q] = nx; t.ny[q] = ny;
+            if (t.c2[q] < 0) {
                 long long key = std::min<long long>(a, b) * (1ll << 32) + std::max<long long>(a, b);
                 auto it = std::lower_bound(keys.begin(), keys.end(), std::make_pair(key, -1));
-                if (it != keys.end() && it->first == key) t.bseg_of_edge[e] = it->second;
-                else if (require_segment)
-                    throw Error(CFD2D_ERR_MESH_UNV_NOT_DEFINED_BND_EDGE,
-                                "Boundary edge #" + std::to_string(e) + " not defined in UNV file.");
+                if (it != keys.end() && it->first == key) t.bseg_of_edge[q] = it->second;
+                else if (first_missing == ne) first_missing = q;
             }
-            e++;
         }
+        missing[slot++ % missing.size()] = first_missing;  // one slot per thread
+    });
+    const int first_missing = *std::min_element(missing.begin(), missing.end());
+    if (require_segment && first_missing < ne)
+        throw Error(CFD2D_ERR_MESH_UNV_NOT_DEFINED_BND_EDGE,
+                    "Boundary edge #" + std::to_string(first_missing) + " not defined in UNV file.");
     for (int i = 0; i < nc; i++) {  // Heron, :250-255
         if (cfi[i] != 3) throw Error(CFD2D_ERR_MESH_FORMAT, "mesh: cell " + std::to_string(i) + " is not a closed triangle");
         double a = t.l[t.cedges[3 * i]], b = t.l[t.cedges[3 * i + 1]], c = t.l[t.cedges[3 * i + 2]];
