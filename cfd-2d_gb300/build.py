@@ -37,7 +37,7 @@ def cuda_home() -> str:
     raise RuntimeError("nvcc not found")
 
 
-HOST_SOURCES = ["xml.cpp", "mesh.cpp", "task.cpp", "solver.cpp", "solver_adjoint.cpp", "solver_batch.cpp", "capi.cpp"]
+HOST_SOURCES = ["xml.cpp", "mesh.cpp", "task.cpp", "solver.cpp", "solver_adjoint.cpp", "solver_batch.cpp", "solver_tiles.cpp", "capi.cpp"]
 DEVICE_SOURCES = {"kern_fp64.cu": "false", "kern_common.cu": "false", "kern_mixed.cu": "true",
                   "noalloc.cu": "false", "adjoint.cu": "false", "adjoint_mixed.cu": "true"}
 HEADERS = ["xml.hpp", "mesh.hpp", "task.hpp", "solver.hpp", "kernels.hpp", "kernels.cuh", "kern_inst.cuh",

@@ -259,6 +259,8 @@ class Task:
     reconstruction: str | None = None
     time_scheme: str | None = None
     precision: str | None = None
+    reorder: str | None = None        # NONE / RCM / HILBERT
+    fused_stage: str | None = None    # "0" keeps the mixed form on its per-kernel path
     method: str = "FVM_TVD"
 
 
@@ -275,7 +277,8 @@ def write_task_xml(t: Task) -> str:
          f'    <FILE_OUTPUT_STEP value="{int(t.file_output_step)}" />',
          f'    <LOG_OUTPUT_STEP value="{int(t.log_output_step)}" />']
     for tag, val in (("FLUX", t.flux), ("RECONSTRUCTION", t.reconstruction),
-                     ("TIME_SCHEME", t.time_scheme), ("PRECISION", t.precision)):
+                     ("TIME_SCHEME", t.time_scheme), ("PRECISION", t.precision), ("REORDER", t.reorder),
+                     ("FUSED_STAGE", t.fused_stage)):
         if val is not None:
             L.append(f'    <{tag} value="{val}" />')
     L += ["  </control>", "  <limits>", f'    <ro min="{_v(rmin)}" max="{_v(rmax)}" />',

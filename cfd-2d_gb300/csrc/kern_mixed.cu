@@ -3,3 +3,43 @@
 #define KT float
 #define KFN(name) launch_##name##_mixed
 #include "kern_inst.cuh"
+
+namespace cfd2d {
+namespace {
+template <int FLUX, int RECON, int SCHEME>
+void fused_by_stage(const DevCase& c, const DevTiles& t, int stage, const float* wi, float* wo, cudaStream_t s) {
+    const size_t smem = 16 * ((size_t)t.max_cells + 2 * (size_t)t.max_grad + (size_t)t.max_edges);
+    auto go = [&](auto kern) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<t.n_tiles, 256, smem, s>>>(c, t, wi, wo);
+    };
+    if (stage == 0) go(k_stage_fused<FLUX, RECON, SCHEME, 0>);
+    else if (stage == 1) go(k_stage_fused<FLUX, RECON, SCHEME, 1>);
+    else if (SCHEME == TIME_SSPRK3) go(k_stage_fused<FLUX, RECON, TIME_SSPRK3, 2>);
+}
+template <int FLUX, int RECON>
+void fused_by_scheme(const DevCase& c, const DevTiles& t, int scheme, int stage, const float* wi, float* wo,
+                     cudaStream_t s) {
+    if (scheme == TIME_SSPRK3) fused_by_stage<FLUX, RECON, TIME_SSPRK3>(c, t, stage, wi, wo, s);
+    else fused_by_stage<FLUX, RECON, TIME_HEUN>(c, t, stage, wi, wo, s);
+}
+template <int FLUX>
+void fused_by_recon(const DevCase& c, const DevTiles& t, int recon, int scheme, int stage, const float* wi,
+                    float* wo, cudaStream_t s) {
+    if (recon == RECON_NONE) fused_by_scheme<FLUX, RECON_NONE>(c, t, scheme, stage, wi, wo, s);
+    else if (recon == RECON_LINEAR) fused_by_scheme<FLUX, RECON_LINEAR>(c, t, scheme, stage, wi, wo, s);
+    else fused_by_scheme<FLUX, RECON_MINMOD>(c, t, scheme, stage, wi, wo, s);
+}
+}  // namespace
+
+// One fused stage of the mixed form (SSP-RK3 or Heun): gradients, fluxes and update per tile.
+void launch_stage_fused_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,
+                              const float* w_in, float* w_out, cudaStream_t s) {
+    switch (flux) {
+    case FLUX_LAX: fused_by_recon<FLUX_LAX>(c, t, recon, scheme, stage, w_in, w_out, s); break;
+    case FLUX_ROE: fused_by_recon<FLUX_ROE>(c, t, recon, scheme, stage, w_in, w_out, s); break;
+    case FLUX_HLLC: fused_by_recon<FLUX_HLLC>(c, t, recon, scheme, stage, w_in, w_out, s); break;
+    default: fused_by_recon<FLUX_GODUNOV>(c, t, recon, scheme, stage, w_in, w_out, s); break;
+    }
+}
+}  // namespace cfd2d

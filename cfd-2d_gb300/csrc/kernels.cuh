@@ -512,6 +512,39 @@ __device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& 
 // Green-Gauss gradients of r, p, u, v (calcGrad, src/methods/fvm_tvd.cpp:242-301),
 // gathered per cell over its faces in ascending original edge order. FP64 divides
 // by S like the reference; the mixed form multiplies by 1/S in FP32.
+// One face of the Green-Gauss sum: g +-= (q + o)/2 n l (c2 subtracts, c1 adds).
+template <typename T>
+__device__ __forceinline__ void grad_face(T* g, const Prim<T>& q, const Prim<T>& o, T nx, T ny, T l, bool side2) {
+    // x * 0.5 is the correctly rounded x / 2 (exact halving), without a division
+    const T hr = (q.r + o.r) * T(0.5), hp = (q.p + o.p) * T(0.5);
+    const T hu = (q.u + o.u) * T(0.5), hv = (q.v + o.v) * T(0.5);
+    const T v[8] = {hr * nx * l, hr * ny * l, hp * nx * l, hp * ny * l,
+                    hu * nx * l, hu * ny * l, hv * nx * l, hv * ny * l};
+#pragma unroll
+    for (int m = 0; m < 8; m++) g[m] = g[m] + neg_if(v[m], side2);
+}
+// The ghost of the unreconstructed centre state across boundary edge e (the cell is its c1).
+template <typename T>
+__device__ __forceinline__ Prim<T> grad_ghost(const DevCase& c, int i, int e, const Prim<T>& q, T nx, T ny) {
+    const MatT<T> mt = matT_of<T>(c, i);
+    const T Tc = temperature(q, mt.gm1, mt.Cv);
+    return ghost_state(c.bnds[c.ebnd[e]], q, Tc, nx, ny, mt.M);
+}
+// The sum divided by the area: FP64 through the host-rounded reciprocal (correctly
+// rounded), FP32 as a product with 1/S.
+template <typename T>
+__device__ __forceinline__ void grad_finish(const DevCase& c, int i, T* g) {
+    if constexpr (sizeof(T) == 8) {
+        const double s = c.S[i], y = c.invS[i];  // y = RN(1/S), computed on the host
+#pragma unroll
+        for (int m = 0; m < 8; m++) g[m] = div_rn(g[m], s, y);
+    } else {
+        const float is = c.invS32[i];
+#pragma unroll
+        for (int m = 0; m < 8; m++) g[m] = g[m] * is;
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
     const int nc = c.nc;
@@ -523,32 +556,11 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
     for (int k = 0; k < 3; k++) {
         const int nb = c.cf_nb[k * nc + i];
         const T nx = cf.nx[k * nc + i], ny = cf.ny[k * nc + i], l = cf.l[k * nc + i];
-        Prim<T> o;
         const bool side2 = nb >= 0 && (nb & 1);
-        if (nb >= 0) {
-            o = load_prim(W, nb >> 1);
-        } else {  // boundary edge -(nb + 1); the cell is its c1
-            const MatT<T> mt = matT_of<T>(c, i);
-            const T Tc = temperature(q, mt.gm1, mt.Cv);
-            o = ghost_state(c.bnds[c.ebnd[-(nb + 1)]], q, Tc, nx, ny, mt.M);
-        }
-        // x * 0.5 is the correctly rounded x / 2 (exact halving), without a division
-        const T hr = (q.r + o.r) * T(0.5), hp = (q.p + o.p) * T(0.5);
-        const T hu = (q.u + o.u) * T(0.5), hv = (q.v + o.v) * T(0.5);
-        const T v[8] = {hr * nx * l, hr * ny * l, hp * nx * l, hp * ny * l,
-                        hu * nx * l, hu * ny * l, hv * nx * l, hv * ny * l};
-#pragma unroll
-        for (int m = 0; m < 8; m++) g[m] = g[m] + neg_if(v[m], side2);  // c2 subtracts, c1 adds
+        const Prim<T> o = nb >= 0 ? load_prim(W, nb >> 1) : grad_ghost(c, i, -(nb + 1), q, nx, ny);
+        grad_face(g, q, o, nx, ny, l, side2);
     }
-    if constexpr (sizeof(T) == 8) {
-        const double s = c.S[i], y = c.invS[i];  // y = RN(1/S), computed on the host
-#pragma unroll
-        for (int m = 0; m < 8; m++) g[m] = div_rn(g[m], s, y);
-    } else {
-        const float is = c.invS32[i];
-#pragma unroll
-        for (int m = 0; m < 8; m++) g[m] = g[m] * is;
-    }
+    grad_finish(c, i, g);
     st8(G_of<T>(c), i, g);
 }
 
@@ -588,27 +600,21 @@ __device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, 
 }
 
 // Edge flux over the edge's two Gauss points, times l/2 (src/methods/fvm_tvd.cpp:329-352).
+// The edge flux from the two cells' primitives and gradients, both Gauss points,
+// times l/2 (src/methods/fvm_tvd.cpp:329-352): out[4] is what F holds for edge e.
 template <typename T, int FLUX, int RECON>
-__device__ __forceinline__ void flux_one(const DevCase& c, int e) {
+__device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const Prim<T>& qL, const T* gL,
+                                          const Prim<T>& qR, const T* gR, T* out) {
+    // qR: the second cell's primitives on interior edges (e < n_int), qL on boundary edges
     const int ne = c.ne;
-    const T* __restrict__ W = W_of<T>(c);
-    const T* __restrict__ G = G_of<T>(c);
     const T* __restrict__ DL = DL_of<T>(c);
     const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
     const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
-    const int c1 = c.ec1[e];
     const bool inner = e < c.n_int;
-    const Prim<T> qL = load_prim(W, c1);
-    T gL[8], gR[8];
-    if (RECON != RECON_NONE) ld8(G, c1, gL);
-    Prim<T> qR = qL, gc = qL;
+    Prim<T> gc = qL;
     DevBnd b{};
     T Tc = T(0), M = T(0);
-    if (inner) {
-        const int c2 = c.ec2[e];
-        qR = load_prim(W, c2);
-        if (RECON != RECON_NONE) ld8(G, c2, gR);
-    } else {
+    if (!inner) {
         b = c.bnds[c.ebnd[e]];
         const MatT<T> mt = matT_of<T>(c, c1);
         Tc = temperature(qL, mt.gm1, mt.Cv);
@@ -652,7 +658,27 @@ __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
     }
     if (hit) atomicOr(c.err, ERRBIT_NEWTON_CAP);
     const T lh = l * T(0.5);
-    st4(F_of<T>(c), e, fs[0] * lh, fs[1] * lh, fs[2] * lh, fs[3] * lh);
+    out[0] = fs[0] * lh; out[1] = fs[1] * lh; out[2] = fs[2] * lh; out[3] = fs[3] * lh;
+}
+
+template <typename T, int FLUX, int RECON>
+__device__ __forceinline__ void flux_one(const DevCase& c, int e) {
+    const T* __restrict__ W = W_of<T>(c);
+    const T* __restrict__ G = G_of<T>(c);
+    const int c1 = c.ec1[e];
+    const bool inner = e < c.n_int;
+    const Prim<T> qL = load_prim(W, c1);
+    T gL[8], gR[8];
+    if (RECON != RECON_NONE) ld8(G, c1, gL);
+    Prim<T> qR = qL;
+    if (inner) {
+        const int c2 = c.ec2[e];
+        qR = load_prim(W, c2);
+        if (RECON != RECON_NONE) ld8(G, c2, gR);
+    }
+    T out[4];
+    flux_core<T, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out);
+    st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
 }
 
 template <typename T, int FLUX, int RECON, bool STRIDE>
@@ -700,6 +726,17 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// The three signed FP32 face fluxes summed exactly as an FP32 pair, rounded once into FP64.
+__device__ __forceinline__ void residual_pair_sum(const float t[3][4], double* R) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float s1, e1, s2, e2;
+        two_sum(t[0][q], t[1][q], s1, e1);
+        two_sum(s1, t[2][q], s2, e2);
+        R[q] = widen(s2) + widen(e1 + e2);
+    }
+}
+
 // Residual of cell i: the reference's ro_int..re_int (src/methods/fvm_tvd.cpp:353-363).
 // FP64 faces: 0 -/+ F in ascending original edge order, the reference's own sums.
 // FP32 faces: the three signed fluxes summed exactly as an FP32 pair, then rounded
@@ -728,13 +765,7 @@ __device__ __forceinline__ void gather_residual(const DevCase& c, int i, double*
 #pragma unroll
             for (int q = 0; q < 4; q++) t[k][q] = neg_if(v[q], !(f & 1));
         }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            float s1, e1, s2, e2;
-            two_sum(t[0][q], t[1][q], s1, e1);
-            two_sum(s1, t[2][q], s2, e2);
-            R[q] = widen(s2) + widen(e1 + e2);
-        }
+        residual_pair_sum(t, R);
     }
 }
 
@@ -773,21 +804,37 @@ __device__ __forceinline__ bool outside_limits(const DevCase& c, const Prim<T>& 
 // SCHEME/STAGE: Euler (0), Heun (0,1; src/methods/fvm_tvd.cpp:366-447), SSP-RK3 Shu-Osher (0,1,2).
 // The last stage checks the limits (in the face precision) and, for a local time
 // step, computes the next step's cTau in FP64.
-template <typename T, int SCHEME, int STAGE>
-__device__ __forceinline__ void update_one(const DevCase& c, int i) {
-    constexpr bool FINAL = (SCHEME == TIME_EULER && STAGE == 0) || (SCHEME == TIME_HEUN && STAGE == 1) ||
-                           (SCHEME == TIME_SSPRK3 && STAGE == 2);
+template <int SCHEME, int STAGE>
+struct StageKind {
+    static constexpr bool FINAL = (SCHEME == TIME_EULER && STAGE == 0) || (SCHEME == TIME_HEUN && STAGE == 1) ||
+                                  (SCHEME == TIME_SSPRK3 && STAGE == 2);
+};
+
+// Start of a cell's stage update: the step's cTau, and the frozen (LIM-flagged)
+// cells, which are not updated (later stages read B). Returns false for those.
+template <int SCHEME, int STAGE>
+__device__ __forceinline__ bool update_begin(const DevCase& c, int i) {
+    constexpr bool FINAL = StageKind<SCHEME, STAGE>::FINAL;
     const int nc = c.nc;
     if (STAGE == 0 && c.steady) c.ctau[i] = c.ctau_next[i];  // the step now running uses ctau_next
-    if (c.flags[i] & 0x2u) {  // cellIsLim: no update; later stages read B
+    if (c.flags[i] & 0x2u) {  // cellIsLim
         if (STAGE == 0 && !FINAL)
 #pragma unroll
             for (int k = 0; k < 4; k++) c.B[k * nc + i] = c.A[k * nc + i];
         if (FINAL) atomicAdd(c.n_lim, 1);
-        return;
+        return false;
     }
-    double R[4];
-    gather_residual<T>(c, i, R);
+    return true;
+}
+
+// The stage update of cell i from its residual R: U += cTau/S R, the scheme's
+// combination, the next primitives into Wout; the last stage checks the limits
+// (in the face precision) and, for a local time step, computes the next step's
+// cTau in FP64.
+template <typename T, int SCHEME, int STAGE>
+__device__ __forceinline__ void update_finish(const DevCase& c, int i, const double* R, T* __restrict__ Wout) {
+    constexpr bool FINAL = StageKind<SCHEME, STAGE>::FINAL;
+    const int nc = c.nc;
     const double cf = c.cfl[i];
     const double* __restrict__ src = STAGE == 0 ? c.A : c.B;
     double u0 = src[i] + cf * R[0], u1 = src[nc + i] + cf * R[1], u2 = src[2 * nc + i] + cf * R[2],
@@ -806,7 +853,7 @@ __device__ __forceinline__ void update_one(const DevCase& c, int i) {
     }
     dst[i] = u0; dst[nc + i] = u1; dst[2 * nc + i] = u2; dst[3 * nc + i] = u3;
     const Prim<T> w = prim_face_of<T>(u0, u1, u2, u3, c, i);
-    store_prim(Wm_of<T>(c), i, w);
+    store_prim(Wout, i, w);
     if (FINAL) {
         if (outside_limits(c, w)) {
             c.flags[i] |= 0x2u;
@@ -817,6 +864,110 @@ __device__ __forceinline__ void update_one(const DevCase& c, int i) {
             const DevMat mt = mat_of(c, i);
             local_dt(c, i, cons2prim<double>(u0, u1, u2, u3, mt.gm1), mt);
         }
+    }
+}
+
+// One Runge-Kutta stage update with the residual gathered from the edge fluxes.
+// SCHEME/STAGE: Euler (0), Heun (0,1; src/methods/fvm_tvd.cpp:366-447), SSP-RK3 Shu-Osher (0,1,2).
+template <typename T, int SCHEME, int STAGE>
+__device__ __forceinline__ void update_one(const DevCase& c, int i) {
+    if (!update_begin<SCHEME, STAGE>(c, i)) return;
+    double R[4];
+    gather_residual<T>(c, i, R);
+    update_finish<T, SCHEME, STAGE>(c, i, R, Wm_of<T>(c));
+}
+
+// The mixed form's whole Runge-Kutta stage for one tile of cells (one CTA per tile,
+// 256 threads): the tile's and its two-ring halo's primitives are staged in shared
+// memory, then gradients of the own and first-ring cells, the fluxes of the own
+// cells' edges and the own cells' updates run from shared memory. Edges on the tile
+// border are evaluated by both tiles, each time with the same inputs and the same
+// code as k_grad / k_flux / k_update, so the results are those kernels' bit for
+// bit. Primitives are read from w_in and written to w_out (another buffer: the
+// neighbouring tiles still read the old values as their halo).
+template <int FLUX, int RECON, int SCHEME, int STAGE>
+__global__ void __launch_bounds__(256, 6) k_stage_fused(const DevCase c, const DevTiles tl,
+                                                     const float* __restrict__ w_in, float* __restrict__ w_out) {
+    extern __shared__ float4 smem[];
+    const int t = blockIdx.x;
+    const int own0 = t * tl.tile, n_own = min(tl.tile, c.nc - own0);
+    const int h0 = tl.halo_off[t], nh = tl.halo_off[t + 1] - h0, nh1 = tl.n_h1[t];
+    const int nL = n_own + nh, nG = n_own + nh1;
+    const int e0 = tl.edge_off[t], nE = tl.edge_off[t + 1] - e0;
+    const int2* __restrict__ gf = tl.gface + 3 * (size_t)tl.gface_off[t];
+    float4* Ws = smem;                     // nL primitives (r, u, v, p)
+    float4* Gs = Ws + tl.max_cells;        // 2 per gradient cell
+    float4* Fs = Gs + 2 * tl.max_grad;     // one flux record per edge
+    const float4* W4 = reinterpret_cast<const float4*>(w_in);
+    for (int k = threadIdx.x; k < nL; k += blockDim.x) {
+        const int g = k < n_own ? own0 + k : tl.halo[h0 + k - n_own];
+        Ws[k] = __ldg(W4 + g);
+    }
+    __syncthreads();
+    auto prim = [&](int k) {
+        const float4 a = Ws[k];
+        Prim<float> q;
+        q.r = a.x; q.u = a.y; q.v = a.z; q.p = a.w;
+        return q;
+    };
+    if (RECON != RECON_NONE) {
+        for (int k = threadIdx.x; k < nG; k += blockDim.x) {
+            const int i = k < n_own ? own0 + k : tl.halo[h0 + k - n_own];
+            const Prim<float> q = prim(k);
+            float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                const int2 fr = gf[3 * k + f];
+                const int e = fr.x >> 1, nb = fr.y & 0xffff;
+                const float nx = c.nx32[e], ny = c.ny32[e], l = c.l32[e];
+                const Prim<float> o = nb != 0xffff ? prim(nb) : grad_ghost(c, i, e, q, nx, ny);
+                grad_face(g, q, o, nx, ny, l, (fr.x & 1) != 0);
+            }
+            grad_finish(c, i, g);
+            Gs[2 * k] = make_float4(g[0], g[1], g[2], g[3]);
+            Gs[2 * k + 1] = make_float4(g[4], g[5], g[6], g[7]);
+        }
+        __syncthreads();
+    }
+    for (int k = threadIdx.x; k < nE; k += blockDim.x) {
+        const int2 te = tl.tedge[e0 + k];
+        const int e = te.x, l1 = te.y & 0xffff, l2 = (int)((unsigned)te.y >> 16);
+        const Prim<float> qL = prim(l1);
+        const Prim<float> qR = l2 != 0xffff ? prim(l2) : qL;
+        float gL[8], gR[8];
+        if (RECON != RECON_NONE) {
+            const float4 a = Gs[2 * l1], b = Gs[2 * l1 + 1];
+            gL[0] = a.x; gL[1] = a.y; gL[2] = a.z; gL[3] = a.w; gL[4] = b.x; gL[5] = b.y; gL[6] = b.z; gL[7] = b.w;
+            if (l2 != 0xffff) {
+                const float4 x = Gs[2 * l2], y = Gs[2 * l2 + 1];
+                gR[0] = x.x; gR[1] = x.y; gR[2] = x.z; gR[3] = x.w; gR[4] = y.x; gR[5] = y.y; gR[6] = y.z; gR[7] = y.w;
+            }
+        }
+        float out[4];
+        const int c1 = l1 < n_own ? own0 + l1 : tl.halo[h0 + l1 - n_own];
+        flux_core<float, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out);
+        Fs[k] = make_float4(out[0], out[1], out[2], out[3]);
+    }
+    __syncthreads();
+    float4* Wo = reinterpret_cast<float4*>(w_out);
+    for (int k = threadIdx.x; k < n_own; k += blockDim.x) {
+        const int i = own0 + k;
+        if (!update_begin<SCHEME, STAGE>(c, i)) {
+            Wo[i] = Ws[k];  // frozen cell: its primitives do not change
+            continue;
+        }
+        float tv[3][4];
+#pragma unroll
+        for (int f = 0; f < 3; f++) {
+            const int2 fr = gf[3 * k + f];
+            const float4 v = Fs[(unsigned)fr.y >> 16];
+            const bool add = (fr.x & 1) != 0;  // c2 adds the edge flux, c1 subtracts it
+            tv[f][0] = neg_if(v.x, !add); tv[f][1] = neg_if(v.y, !add);
+            tv[f][2] = neg_if(v.z, !add); tv[f][3] = neg_if(v.w, !add);
+        }
+        double R[4];
+        residual_pair_sum(tv, R);
+        update_finish<float, SCHEME, STAGE>(c, i, R, w_out);
     }
 }
 

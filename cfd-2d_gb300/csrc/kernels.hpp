@@ -130,6 +130,25 @@ void launch_permute_flags(const DevCase& c, const unsigned* src_store, unsigned*
 void launch_residual(const DevCase& c, int precision, double* R, cudaStream_t s);
 // ---- discrete adjoint (adjoint.cu)
 // Adjoint work arrays of one backward stage.
+// Tiles of the mixed form's fused stage kernel (one CTA per tile): tile t owns the
+// storage cells [t*tile, (t+1)*tile) and reads a halo of two cell rings around them.
+// Local cell numbers: own cells first, then the first ring (H1), then the second
+// (H2). Gradients are formed for own + H1 cells, fluxes for the edges of own cells.
+struct DevTiles {
+    int n_tiles = 0, tile = 0;
+    int max_cells = 0, max_grad = 0, max_edges = 0;  // shared-memory capacities (max over tiles)
+    const int* halo_off = nullptr;   // n_tiles + 1, into halo
+    const int* halo = nullptr;       // H1 then H2 storage cells of each tile
+    const int* n_h1 = nullptr;       // n_tiles
+    const int* edge_off = nullptr;   // n_tiles + 1, into tedge
+    const int2* tedge = nullptr;     // flux edges: x = storage edge, y = local c1 | local c2 << 16 (0xffff: boundary)
+    const int* gface_off = nullptr;  // n_tiles + 1, into gface (in cells; 3 entries per cell)
+    const int2* gface = nullptr;     // per gradient cell and face: x = (edge << 1) | side,
+                                     // y = local neighbour (0xffff: boundary) | local flux edge << 16 (own cells)
+};
+void launch_stage_fused_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,
+                              const float* w_in, float* w_out, cudaStream_t s);
+
 struct AdjCase {
     const double* X;   // 4*nc stage input state (SoA)
     const double* mu;  // nc x 4 (AoS) cfl * t_bar

@@ -581,11 +581,50 @@ std::vector<int> rcm_order(const Topo& t) {
     return order;
 }
 
-Layout make_layout(const Topo& t, const std::vector<int>& cell_mat, const std::vector<int>& edge_bnd, bool rcm) {
+// Cells along a Hilbert curve through their centroids (quantised to a 2^16 x 2^16
+// grid over the bounding box; ties by cell number): consecutive cells form compact
+// patches, which the tiled kernels need. The curve index follows the standard
+// quadrant-rotation construction (Hilbert 1891; e.g. Butz 1971).
+std::vector<int> hilbert_order(const Topo& t) {
+    const int nc = t.nc;
+    double x0 = 0, x1 = 0, y0 = 0, y1 = 0;
+    for (int i = 0; i < nc; i++) {
+        if (i == 0 || t.cx[i] < x0) x0 = t.cx[i];
+        if (i == 0 || t.cx[i] > x1) x1 = t.cx[i];
+        if (i == 0 || t.cy[i] < y0) y0 = t.cy[i];
+        if (i == 0 || t.cy[i] > y1) y1 = t.cy[i];
+    }
+    const double span = std::max(std::max(x1 - x0, y1 - y0), 1e-300);
+    const uint32_t n = 1u << 16;
+    std::vector<std::pair<uint64_t, int>> key(nc);
+    parallel_ranges((size_t)nc, 1 << 16, [&](size_t i0, size_t i1) {
+        for (size_t i = i0; i < i1; i++) {
+            uint32_t x = (uint32_t)std::min<double>(n - 1, std::floor((t.cx[i] - x0) / span * n));
+            uint32_t y = (uint32_t)std::min<double>(n - 1, std::floor((t.cy[i] - y0) / span * n));
+            uint64_t d = 0;
+            for (uint32_t q = n / 2; q > 0; q /= 2) {
+                const uint32_t rx = (x & q) ? 1u : 0u, ry = (y & q) ? 1u : 0u;
+                d += (uint64_t)q * q * ((3u * rx) ^ ry);
+                if (ry == 0) {  // rotate the quadrant so the sub-curve joins its neighbours
+                    if (rx == 1) { x = n - 1 - x; y = n - 1 - y; }
+                    std::swap(x, y);
+                }
+            }
+            key[i] = {d, (int)i};
+        }
+    });
+    std::sort(key.begin(), key.end());
+    std::vector<int> order(nc);
+    for (int i = 0; i < nc; i++) order[i] = key[i].second;
+    return order;
+}
+
+Layout make_layout(const Topo& t, const std::vector<int>& cell_mat, const std::vector<int>& edge_bnd, int order) {
     Layout L;
     const int nc = t.nc, ne = t.ne;
     L.nc = nc; L.ne = ne;
-    if (rcm) L.perm = rcm_order(t);
+    if (order == ORDER_RCM) L.perm = rcm_order(t);
+    else if (order == ORDER_HILBERT) L.perm = hilbert_order(t);
     else { L.perm.resize(nc); std::iota(L.perm.begin(), L.perm.end(), 0); }
     L.iperm.resize(nc);
     for (int i = 0; i < nc; i++) L.iperm[L.perm[i]] = i;

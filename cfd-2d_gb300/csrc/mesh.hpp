@@ -70,6 +70,9 @@ struct Layout {
 
 // Reverse Cuthill-McKee order of the cell graph (storage -> original).
 std::vector<int> rcm_order(const Topo& t);
-Layout make_layout(const Topo& t, const std::vector<int>& cell_mat, const std::vector<int>& edge_bnd, bool rcm);
+// Hilbert-curve order of the cell centroids (storage -> original).
+std::vector<int> hilbert_order(const Topo& t);
+enum CellOrder { ORDER_NONE = 0, ORDER_RCM = 1, ORDER_HILBERT = 2 };
+Layout make_layout(const Topo& t, const std::vector<int>& cell_mat, const std::vector<int>& edge_bnd, int order);
 
 }  // namespace cfd2d

@@ -67,7 +67,8 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
     const int nc = topo_.nc;
     cell_mat_.resize(nc);
     for (int i = 0; i < nc; i++) cell_mat_[i] = task_.regions[cell_region[i]].matId;
-    lay_ = make_layout(topo_, cell_mat_, edge_bnd, task_.reorder != 0);
+    const int order = task_.reorder >= 0 ? task_.reorder : (task_.fused == 1 ? ORDER_HILBERT : ORDER_RCM);
+    lay_ = make_layout(topo_, cell_mat_, edge_bnd, order);
     const int ne = lay_.ne;
     CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     try {
@@ -185,6 +186,7 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
         compute_tau();
         CUDA_CHECK(cudaStreamSynchronize(stream_));
         if (!task_.steady && inst_.empty()) log_line("time step: %25.16E\n", tau_);  // calcTimeStep, :238
+        build_tiles();
         build_graph();
     } catch (...) {
         for (void* p : allocs_) cudaFree(p);
@@ -238,6 +240,18 @@ void Solver::enqueue_step(cudaEvent_t* ev, int* kinds, int* nev) {
         if (begin) kinds[*nev / 2] = kind;
         CUDA_CHECK(cudaEventRecord(ev[(*nev)++], stream_));
     };
+    if (fused_ && gauss_points_ != 0) {  // one tiled kernel per stage, primitives rotated through wrot_
+        for (int st = 0; st < nst; st++) {
+            mark(1, true);
+            launch_stage_fused_mixed(dc_, tiles_, task_.flux, task_.recon, task_.scheme, st, wrot_[st],
+                                     wrot_[(st + 1) % nst], stream_);
+            mark(1, false);
+        }
+        mark(3, true);
+        launch_remediate(dc_, p, stream_);
+        mark(3, false);
+        return;
+    }
     for (int st = 0; st < nst; st++) {
         if (gauss_points_ == 0) {  // 1-point edges: the Gauss-point loop is empty, no flux
             size_t b = 4 * (size_t)dc_.ne * (p == PREC_MIXED ? sizeof(float) : sizeof(double));

@@ -122,6 +122,11 @@ private:
     size_t ckpt_slots_ = 0, seg_slots_ = 0;
     int fw_steps_ = 0, fw_k_ = 0;
     template <typename T> T* upload(const std::vector<T>& v);
+    // mixed form, SSP-RK3 / Heun: tiles for the fused stage kernel (solver_tiles.cpp)
+    void build_tiles();
+    DevTiles tiles_{};
+    bool fused_ = false;
+    float* wrot_[3] = {nullptr, nullptr, nullptr};  // primitives rotated through the stages; wrot_[0] == dc_.W32
     void compute_tau();
     void enqueue_step(cudaEvent_t* ev = nullptr, int* kinds = nullptr, int* nev = nullptr);
     void build_graph();

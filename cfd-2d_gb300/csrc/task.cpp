@@ -74,7 +74,8 @@ TaskConfig parse_task(const std::string& path) {
                    RECON_LINEAR);
     t.scheme = pick(ctl, "TIME_SCHEME", {{"EULER", TIME_EULER}, {"HEUN", TIME_HEUN}, {"SSPRK3", TIME_SSPRK3}}, TIME_HEUN);
     t.precision = pick(ctl, "PRECISION", {{"FP64", PREC_FP64}, {"MIXED", PREC_MIXED}}, PREC_FP64);
-    t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}}, 1);
+    t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}, {"HILBERT", 2}}, -1);
+    t.fused = pick(ctl, "FUSED_STAGE", {{"0", 0}, {"1", 1}, {"OFF", 0}, {"ON", 1}}, -1);
     if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = attr_i(n, "value");
     if (t.newton_cap < 1) t.newton_cap = 1;
 

@@ -25,7 +25,8 @@ struct TaskConfig {
     int gauss_points = -1;    // <mesh><gaussPoints>: Triangle meshes get 1 point (no flux) unless 2
     // method selections; absent elements give the reference's method
     int flux = FLUX_GODUNOV, recon = RECON_LINEAR, scheme = TIME_HEUN, precision = PREC_FP64;
-    int reorder = 1;          // RCM cell order
+    int reorder = -1;         // cell order: 0 file order, 1 RCM, 2 Hilbert; -1: RCM (Hilbert with the fused stage)
+    int fused = -1;           // mixed form, SSP-RK3 / Heun: 1 runs one tiled kernel per stage (opt-in)
     int newton_cap = 100;     // iteration cap of the exact Riemann solver
 };
 

@@ -1,0 +1,86 @@
+"""The mixed form's opt-in fused stage kernel (gradients, fluxes and update of a
+tile of cells in one launch, from shared memory) against the same form on its
+per-kernel path: identical inputs and identical arithmetic, so identical bits."""
+import numpy as np
+import pytest
+
+from cfd2d import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(capi, tmp_path, t, m, U0=None, **kw):
+    out = []
+    kw.setdefault("reorder", "HILBERT")
+    for fused in ("0", "1"):
+        t.precision = "MIXED"
+        t.fused_stage = fused
+        for k, v in kw.items():
+            setattr(t, k, v)
+        d = tmp_path / ("a" if fused == "0" else "b")
+        d.mkdir(exist_ok=True)
+        s = capi.Solver(cases.write_task(t, m, str(d)), mesh=m)
+        if U0 is not None:
+            s.set_state(U0, reset_time_step=True)
+        out.append(s)
+    return out
+
+
+def _is_fused(s):
+    """Profile one step (it is taken): the fused path launches no separate gradient or update kernels."""
+    ms, cnt = s.profile_steps(1)
+    return cnt[0] == 0 and cnt[2] == 0 and cnt[1] > 0
+
+
+@pytest.mark.parametrize("flux,recon,scheme", [("HLLC", "MINMOD", "SSPRK3"), ("ROE", "MINMOD", "HEUN"),
+                                               ("LAX", "LINEAR", "SSPRK3"), ("HLLC", "NONE", "HEUN"),
+                                               ("GODUNOV", "LINEAR", "SSPRK3")])
+def test_fused_equals_per_kernel_vortex(capi, tmp_path, flux, recon, scheme):
+    kinds = ("BOUND_INLET", "BOUND_OUTLET", "BOUND_WALL_SLIP", "BOUND_WALL_NO_SLIP")
+    t, m, U0 = cases.vortex(96, flux=flux, recon=recon, scheme=scheme, steps=12, bnd_kinds=kinds)
+    a, b = _pair(capi, tmp_path, t, m, U0)
+    assert not _is_fused(a) and _is_fused(b)
+    a.step(12)
+    b.step(12)
+    assert np.array_equal(a.state(), b.state())
+    assert np.array_equal(a.time_step(), b.time_step())
+
+
+def test_fused_equals_per_kernel_local_time_step(capi, tmp_path):
+    t, m, U0 = cases.vortex(80, flux="HLLC", recon="MINMOD", scheme="SSPRK3", steps=10, steady=1)
+    a, b = _pair(capi, tmp_path, t, m, U0)
+    a.step(10)
+    b.step(10)
+    assert np.array_equal(a.state(), b.state())
+    assert np.array_equal(a.time_step(), b.time_step())
+
+
+def test_fused_equals_per_kernel_limits_and_remediation(capi, tmp_path):
+    """A |u| limit below the vortex peak flags cells (frozen, then remediated)."""
+    t, m, U0 = cases.vortex(64, flux="HLLC", recon="MINMOD", scheme="SSPRK3", steps=30)
+    t.limits = (1e-8, 1e8, 1e-8, 1e8, 1.55)
+    a, b = _pair(capi, tmp_path, t, m, U0)
+    a.step(30)
+    b.step(30)
+    assert np.array_equal(a.flags(), b.flags())
+    assert (a.flags() & 2).any() or (a.flags() > 0).any()
+    assert np.array_equal(a.state(), b.state())
+
+
+def test_fused_four_quadrant_full_size(capi, tmp_path):
+    """2,097,152 triangles, HLLC + minmod + SSP-RK3, 5 steps: the bench workload."""
+    t, m, _ = cases.four_quadrant(1024, steps=5)
+    a, b = _pair(capi, tmp_path, t, m)
+    a.step(5)
+    b.step(5)
+    assert np.array_equal(a.state(), b.state())
+
+
+def test_fused_with_rcm_order(capi, tmp_path):
+    """Long thin tiles (RCM order) still fit and still give the per-kernel bits."""
+    t, m, U0 = cases.vortex(64, flux="HLLC", recon="MINMOD", scheme="SSPRK3", steps=8)
+    a, b = _pair(capi, tmp_path, t, m, U0, reorder="RCM")
+    assert not _is_fused(a) and _is_fused(b)
+    a.step(8)
+    b.step(8)
+    assert np.array_equal(a.state(), b.state())
