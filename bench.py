@@ -477,11 +477,23 @@ def main():
         s = capi.Solver(cases.write_task(t, m, tempfile.mkdtemp()), mesh=m)
         s.set_objective(0, w, 1.0)
         s.set_state(U0)
-        J = s.forward(K, max(1, K // 2))
+        s.step(W)
+        s.set_state(U0)
+        a = time.perf_counter()
+        s.step(K)
+        fw = time.perf_counter() - a
+        s.set_state(U0)
+        every = max(1, K // 10)
+        a = time.perf_counter()
+        J = s.forward(K, every)
+        b = time.perf_counter()
         g, _ = s.backward()
+        c = time.perf_counter()
         if rank == 0:
-            print(json.dumps({"profiling_run": True, "workload": "adjoint", "steps": K, "J": J,
-                              "grad_norm": float(np.linalg.norm(g))}), flush=True)
+            print(json.dumps({"profiling_run": True, "workload": "adjoint", "steps": K, "checkpoint_every": every,
+                              "J": J, "grad_norm": float(np.linalg.norm(g)), "forward_ms": fw * 1e3,
+                              "backward_ms": (c - b) * 1e3, "ratio_backward_over_forward": (c - b) / fw}),
+                  flush=True)
         return
 
     d = tempfile.mkdtemp(prefix="cfd2d_bench_")

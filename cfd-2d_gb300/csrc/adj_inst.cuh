@@ -26,7 +26,9 @@ namespace {
 inline int adj_nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 template <typename T, int FLUX, int RECON>
-__global__ void __launch_bounds__(256) k_adj_flux(const DevCase c, const AdjCase a) {
+// FP32 faces: at most 128 registers (two 256-thread blocks' worth per SM), measured
+// faster than the compiler's unconstrained choice; FP64 faces: unconstrained.
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 0) k_adj_flux(const DevCase c, const AdjCase a) {
     const int ne = c.ne;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= ne) return;

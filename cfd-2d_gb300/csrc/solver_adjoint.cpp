@@ -198,10 +198,10 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
     double ct_f, ca_f;
     final_coefs(task_.scheme, ct_f, ca_f);
     const int nseg = (fw_steps_ + fw_k_ - 1) / fw_k_;
-    for (int seg = nseg - 1; seg >= 0; seg--) {
-        const int n = std::min(fw_k_, fw_steps_ - seg * fw_k_);
-        CUDA_CHECK(cudaMemcpyAsync(dc_.A, ckpt_ + (size_t)seg * 4 * nc, sizeof(double) * 4 * nc,
-                                   cudaMemcpyDeviceToDevice, stream_));
+    // One segment after its checkpoint is restored: recompute its n steps, recording the
+    // stages, then walk them backwards. Captured once per segment length into a CUDA
+    // graph and replayed, so the host issues one launch per segment.
+    auto segment = [&](int n) {
         launch_prims(dc_, task_.precision, stream_);
         for (int j = 0; j < n; j++)
             record_step(segstore_ + (size_t)j * nst * 4 * nc, store_wg_ ? wg_at(j * nst) : nullptr);
@@ -231,6 +231,42 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
                 launch_adj_cell(cx, a, ct, ca, st == 0 ? 1 : 0, p, stream_);
             }
         }
+    };
+    std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+    auto release = [&]() {
+        for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+        graphs.clear();
+    };
+    try {
+        for (int seg = nseg - 1; seg >= 0; seg--) {
+            const int n = std::min(fw_k_, fw_steps_ - seg * fw_k_);
+            CUDA_CHECK(cudaMemcpyAsync(dc_.A, ckpt_ + (size_t)seg * 4 * nc, sizeof(double) * 4 * nc,
+                                       cudaMemcpyDeviceToDevice, stream_));
+            cudaGraphExec_t exec = nullptr;
+            for (auto& g : graphs)
+                if (g.first == n) exec = g.second;
+            if (!exec) {
+                cudaGraph_t graph = nullptr;
+                CUDA_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+                try {
+                    segment(n);
+                } catch (...) {
+                    cudaStreamEndCapture(stream_, &graph);
+                    if (graph) cudaGraphDestroy(graph);
+                    throw;
+                }
+                CUDA_CHECK(cudaStreamEndCapture(stream_, &graph));
+                const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                CUDA_CHECK(e);
+                graphs.emplace_back(n, exec);
+            }
+            CUDA_CHECK(cudaGraphLaunch(exec, stream_));
+        }
+    } catch (...) {
+        cudaStreamSynchronize(stream_);
+        release();
+        throw;
     }
     launch_adj_bnd_reduce(adj_dc_, a, stream_);
     // the solver's state is the forward's final state again
@@ -246,6 +282,7 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
         CUDA_CHECK(cudaMemcpyAsync(dJdbnd, adj_dbnd_, sizeof(double) * 4 * task_.bnds.size(), cudaMemcpyDeviceToHost,
                                    stream_));
     CUDA_CHECK(cudaStreamSynchronize(stream_));
+    release();
 }
 
 }  // namespace cfd2d
