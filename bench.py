@@ -451,6 +451,7 @@ def main():
     ap.add_argument("--workload", default="four_quadrant", choices=["four_quadrant", "batched", "combined", "adjoint"],
                     help="four_quadrant: the headline 2.1M-triangle line; batched: 256 uneven vortex instances")
     ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--adj-n", type=int, default=256, help="squares per side of the adjoint-only run's vortex")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -471,7 +472,7 @@ def main():
         combined_workload(args, capi, cases, world, rank, dist, W, K)
         return
     if args.workload == "adjoint":  # one checkpointed forward + backward of K steps (profiling runs)
-        t, m, U0, w, _ = cases.vortex_adjoint(256, steps=K)
+        t, m, U0, w, _ = cases.vortex_adjoint(args.adj_n, steps=K)
         if args.forms.strip() == "mixed":
             t.precision = "MIXED"
         s = capi.Solver(cases.write_task(t, m, tempfile.mkdtemp()), mesh=m)
