@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
 
 #include "cfd2d.h"
 
@@ -199,6 +200,18 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
 
 Solver::~Solver() {
     use_device();
+    if (vtk_thread_.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(vtk_mu_);
+            vtk_stop_ = true;
+        }
+        vtk_cv_.notify_all();
+        vtk_thread_.join();
+    }
+    for (int k = 0; k < 2; k++) {
+        if (snap_host_[k]) cudaFreeHost(snap_host_[k]);
+        if (snap_ev_[k]) cudaEventDestroy(snap_ev_[k]);
+    }
     if (gexec_) cudaGraphExecDestroy(gexec_);
     if (graph_) cudaGraphDestroy(graph_);
     if (stream_) cudaStreamSynchronize(stream_);
@@ -356,7 +369,7 @@ int Solver::step(int n) {
 
 int Solver::run() {  // FVM_TVD::run, src/methods/fvm_tvd.cpp:303-462
     use_device();
-    if (steps_ == 0) save_vtk(0);
+    if (steps_ == 0) save_vtk_async(0);
     int status = CFD2D_OK;
     const unsigned smax = (unsigned)task_.step_max;
     while (t_ < task_.tmax && (unsigned)steps_ < smax) {
@@ -368,11 +381,12 @@ int Solver::run() {  // FVM_TVD::run, src/methods/fvm_tvd.cpp:303-462
         if (save || print) {
             int s = read_status();
             if (s != CFD2D_OK) status = s;
-            if (save) save_vtk(steps_);
+            if (save) save_vtk_async(steps_);
             if (print) log_line("step: %d\t\ttime step: %.16f\n", steps_, t_);
         }
     }
     int s = read_status();
+    vtk_flush();
     return s != CFD2D_OK ? s : status;
 }
 
@@ -451,18 +465,21 @@ void Solver::conservation(double sums[4]) {
 }
 
 // FVM_TVD::save, src/methods/fvm_tvd.cpp:501-600 (same fields, formats and quirks).
-void Solver::save_vtk(int step) {
-    const int nc = topo_.nc, nn = topo_.nn;
-    std::vector<double> U(4 * (size_t)nc), ct(nc);
-    get_state(U.data(), U.data() + nc, U.data() + 2 * (size_t)nc, U.data() + 3 * (size_t)nc);
-    get_ctau(ct.data());
-    char name[64];
-    std::snprintf(name, sizeof name, "res_%010d.vtk", step);
+namespace {
+
+// The VTK file of one state, exactly as FVM_TVD::save writes it (file name, fields,
+// number formats, the single newline at the end of each field, the 8-per-line
+// total pressure, the "Velosity" spelling; src/methods/fvm_tvd.cpp:501-600). The
+// numbers are formatted on host threads, a block of items per thread, and written
+// in order, so the bytes are those of a sequential fprintf loop.
+void write_vtk_file(const char* name, const Topo& topo, const std::vector<TaskMaterial>& mats,
+                    const std::vector<int>& cell_mat, const double* U, const double* ct) {
+    const int nc = topo.nc, nn = topo.nn;
     FILE* fp = std::fopen(name, "w");
     if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + name + "' opening error.");
     struct P { double r, u, v, p, cz, T, gam; };
     auto par = [&](int i) {
-        const TaskMaterial& m = task_.mats[cell_mat_[i]];
+        const TaskMaterial& m = mats[cell_mat[i]];
         double Cv = m.Cp - GAS_R / m.M, gam = m.Cp / Cv;
         P q;
         q.r = U[i];
@@ -477,24 +494,49 @@ void Solver::save_vtk(int step) {
         q.gam = gam;
         return q;
     };
+    const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    constexpr int kBlock = 1 << 15;
+    // items [0, n): item(i, out) appends item i's text; blocks formatted in parallel, written in order
+    auto section = [&](int n, auto item) {
+        std::vector<std::string> buf(nth);
+        for (int base = 0; base < n; base += (int)nth * kBlock) {
+            auto work = [&](unsigned t) {
+                std::string& o = buf[t];
+                o.clear();
+                const int a = base + (int)t * kBlock, b = std::min(n, a + kBlock);
+                for (int i = a; i < b; i++) item(i, o);
+            };
+            std::vector<std::thread> th;
+            for (unsigned t = 1; t < nth; t++) th.emplace_back(work, t);
+            work(0);
+            for (auto& x : th) x.join();
+            for (auto& o : buf) std::fwrite(o.data(), 1, o.size(), fp);
+        }
+    };
+    auto app = [](std::string& o, const char* fmt, auto... v) {
+        char tmp[128];
+        const int k = std::snprintf(tmp, sizeof tmp, fmt, v...);
+        o.append(tmp, (size_t)std::max(0, std::min(k, (int)sizeof tmp - 1)));
+    };
     std::fprintf(fp, "# vtk DataFile Version 2.0\nGASDIN data file\nASCII\nDATASET UNSTRUCTURED_GRID\n");
     std::fprintf(fp, "POINTS %d float\n", nn);
-    for (int i = 0; i < nn; i++) std::fprintf(fp, "%f %f %f  ", topo_.xy[2 * i], topo_.xy[2 * i + 1], 0.0);
+    section(nn, [&](int i, std::string& o) { app(o, "%f %f %f  ", topo.xy[2 * i], topo.xy[2 * i + 1], 0.0); });
     std::fprintf(fp, "\n");
     std::fprintf(fp, "CELLS %d %d\n", nc, 4 * nc);
-    for (int i = 0; i < nc; i++)
-        std::fprintf(fp, "3 %d %d %d\n", topo_.tri[3 * i], topo_.tri[3 * i + 1], topo_.tri[3 * i + 2]);
+    section(nc, [&](int i, std::string& o) {
+        app(o, "3 %d %d %d\n", topo.tri[3 * i], topo.tri[3 * i + 1], topo.tri[3 * i + 2]);
+    });
     std::fprintf(fp, "\n");
     std::fprintf(fp, "CELL_TYPES %d\n", nc);
-    for (int i = 0; i < nc; i++) std::fprintf(fp, "5\n");
+    section(nc, [&](int, std::string& o) { o.append("5\n"); });
     std::fprintf(fp, "\n");
     // the reference's "i+1 % 8 == 0" is i+1 == 0: one newline at the end of each field
     auto field = [&](const char* head, auto val) {
         std::fputs(head, fp);
-        for (int i = 0; i < nc; i++) {
-            std::fprintf(fp, "%25.16f ", val(i));
-            if (i + 1 == nc) std::fprintf(fp, "\n");
-        }
+        section(nc, [&](int i, std::string& o) {
+            app(o, "%25.16f ", val(i));
+            if (i + 1 == nc) o.append("\n");
+        });
     };
     std::fprintf(fp, "CELL_DATA %d\n", nc);
     field("SCALARS Density float 1\nLOOKUP_TABLE default\n", [&](int i) { return par(i).r; });
@@ -505,24 +547,125 @@ void Solver::save_vtk(int step) {
         return (q.u * q.u + q.v * q.v) / q.cz;
     });
     std::fprintf(fp, "VECTORS Velosity float\n");
-    for (int i = 0; i < nc; i++) {
+    section(nc, [&](int i, std::string& o) {
         P q = par(i);
-        std::fprintf(fp, "%25.16f %25.16f %25.16f ", q.u, q.v, 0.0);
-        if (i + 1 == nc) std::fprintf(fp, "\n");
-    }
+        app(o, "%25.16f %25.16f %25.16f ", q.u, q.v, 0.0);
+        if (i + 1 == nc) o.append("\n");
+    });
     std::fprintf(fp, "SCALARS Total_pressure float 1\nLOOKUP_TABLE default\n");
-    for (int i = 0; i < nc; i++) {
+    section(nc, [&](int i, std::string& o) {
         P q = par(i);
         double agam = q.gam - 1.0;
         double M2 = (q.u * q.u + q.v * q.v) / (q.gam * q.p / q.r);
-        std::fprintf(fp, "%f ", q.p * std::pow(1.0 + 0.5 * M2 * agam, q.gam / (q.gam - 1.0)));
-        if ((i + 1) % 8 == 0 || i + 1 == nc) std::fprintf(fp, "\n");
-    }
+        app(o, "%f ", q.p * std::pow(1.0 + 0.5 * M2 * agam, q.gam / (q.gam - 1.0)));
+        if ((i + 1) % 8 == 0 || i + 1 == nc) o.append("\n");
+    });
     field("SCALARS TAU float 1\nLOOKUP_TABLE default\n", [&](int i) { return ct[i]; });
+    const bool bad = std::ferror(fp) != 0;
     std::fclose(fp);
+    if (bad) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + name + "' write error.");
+}
+
+void announce_vtk(const char* name) {
     if (g_verbosity > 0) {
         std::printf("File '%s' saved...\n", name);
         std::fflush(stdout);
+    }
+}
+
+}  // namespace
+
+void Solver::save_vtk(int step) {
+    const int nc = topo_.nc;
+    std::vector<double> U(4 * (size_t)nc), ct(nc);
+    get_state(U.data(), U.data() + nc, U.data() + 2 * (size_t)nc, U.data() + 3 * (size_t)nc);
+    get_ctau(ct.data());
+    char name[64];
+    std::snprintf(name, sizeof name, "res_%010d.vtk", step);
+    write_vtk_file(name, topo_, task_.mats, cell_mat_, U.data(), ct.data());
+    announce_vtk(name);
+}
+
+// run()'s output: the state (and cTau) are copied on the solver's stream into one of
+// two pinned host buffers, and a writer thread formats and writes the file while the
+// GPU keeps stepping; a buffer is reused once its file is written.
+void Solver::save_vtk_async(int step) {
+    const int nc = topo_.nc;
+    if (!snap_host_[0]) {
+        for (int k = 0; k < 2; k++) {
+            CUDA_CHECK(cudaMallocHost(&snap_host_[k], sizeof(double) * 5 * (size_t)nc));
+            CUDA_CHECK(cudaEventCreateWithFlags(&snap_ev_[k], cudaEventDisableTiming));
+        }
+        vtk_stop_ = false;
+        vtk_thread_ = std::thread([this] { vtk_writer(); });
+    }
+    int k = -1;
+    {
+        std::unique_lock<std::mutex> lk(vtk_mu_);
+        vtk_cv_.wait(lk, [&] { return !snap_busy_[0] || !snap_busy_[1] || vtk_err_; });
+        if (vtk_err_) {
+            auto e = vtk_err_;
+            vtk_err_ = nullptr;
+            std::rethrow_exception(e);
+        }
+        k = snap_busy_[0] ? 1 : 0;
+        snap_busy_[k] = true;
+    }
+    double* h = snap_host_[k];
+    launch_scatter_state(dc_, dc_.A, stage_, stream_);
+    CUDA_CHECK(cudaMemcpyAsync(h, stage_, sizeof(double) * 4 * nc, cudaMemcpyDeviceToHost, stream_));
+    launch_permute_scalar(dc_, dc_.ctau, stage_, stream_);
+    CUDA_CHECK(cudaMemcpyAsync(h + 4 * (size_t)nc, stage_, sizeof(double) * nc, cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaEventRecord(snap_ev_[k], stream_));
+    char name[64];
+    std::snprintf(name, sizeof name, "res_%010d.vtk", step);
+    {
+        std::lock_guard<std::mutex> lk(vtk_mu_);
+        vtk_jobs_.push_back({step, k});
+    }
+    vtk_cv_.notify_all();
+    announce_vtk(name);  // in run()'s order of log lines
+}
+
+void Solver::vtk_writer() {
+    cudaSetDevice(dev_);
+    for (;;) {
+        VtkJob job;
+        {
+            std::unique_lock<std::mutex> lk(vtk_mu_);
+            vtk_cv_.wait(lk, [&] { return vtk_stop_ || !vtk_jobs_.empty(); });
+            if (vtk_jobs_.empty()) return;
+            job = vtk_jobs_.front();
+            vtk_jobs_.pop_front();
+        }
+        try {
+            const cudaError_t e = cudaEventSynchronize(snap_ev_[job.buf]);
+            if (e != cudaSuccess) throw Error(CFD2D_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+            char name[64];
+            std::snprintf(name, sizeof name, "res_%010d.vtk", job.step);
+            const double* h = snap_host_[job.buf];
+            write_vtk_file(name, topo_, task_.mats, cell_mat_, h, h + 4 * (size_t)topo_.nc);
+        } catch (...) {
+            std::lock_guard<std::mutex> lk(vtk_mu_);
+            if (!vtk_err_) vtk_err_ = std::current_exception();
+        }
+        {
+            std::lock_guard<std::mutex> lk(vtk_mu_);
+            snap_busy_[job.buf] = false;
+        }
+        vtk_cv_.notify_all();
+    }
+}
+
+// Wait for every file run() has issued; rethrow the first write error.
+void Solver::vtk_flush() {
+    if (!vtk_thread_.joinable()) return;
+    std::unique_lock<std::mutex> lk(vtk_mu_);
+    vtk_cv_.wait(lk, [&] { return vtk_jobs_.empty() && !snap_busy_[0] && !snap_busy_[1]; });
+    if (vtk_err_) {
+        auto e = vtk_err_;
+        vtk_err_ = nullptr;
+        std::rethrow_exception(e);
     }
 }
 

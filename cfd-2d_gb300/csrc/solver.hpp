@@ -3,7 +3,12 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <condition_variable>
+#include <deque>
+#include <exception>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cfd2d.h"
@@ -58,6 +63,9 @@ public:
     void residual(double* R);
     void conservation(double sums[4]);
     void save_vtk(int step);
+    // run()'s output: snapshot on the stream, file written by a host thread
+    void save_vtk_async(int step);
+    void vtk_flush();
     // device time of n steps (CUDA events around the graph launches on the solver's stream)
     double timed_steps(int n);
     // n steps launched one kernel at a time with events around each launch;
@@ -122,6 +130,17 @@ private:
     size_t ckpt_slots_ = 0, seg_slots_ = 0;
     int fw_steps_ = 0, fw_k_ = 0;
     template <typename T> T* upload(const std::vector<T>& v);
+    struct VtkJob { int step = 0, buf = 0; };
+    void vtk_writer();
+    std::thread vtk_thread_;
+    std::mutex vtk_mu_;
+    std::condition_variable vtk_cv_;
+    std::deque<VtkJob> vtk_jobs_;
+    bool vtk_stop_ = false;
+    bool snap_busy_[2] = {false, false};
+    double* snap_host_[2] = {nullptr, nullptr};
+    cudaEvent_t snap_ev_[2] = {nullptr, nullptr};
+    std::exception_ptr vtk_err_;
     // mixed form, SSP-RK3 / Heun: tiles for the fused stage kernel (solver_tiles.cpp)
     void build_tiles();
     DevTiles tiles_{};
