@@ -260,7 +260,8 @@ class Task:
     time_scheme: str | None = None
     precision: str | None = None
     reorder: str | None = None        # NONE / RCM / HILBERT
-    fused_stage: str | None = None    # "0" keeps the mixed form on its per-kernel path
+    fused_stage: str | None = None    # "1" runs the mixed form's stages as one tiled kernel
+    adjoint_store: str | None = None  # NONE / PRIMITIVES / ALL: what the adjoint keeps per recorded stage
     method: str = "FVM_TVD"
 
 
@@ -278,7 +279,7 @@ def write_task_xml(t: Task) -> str:
          f'    <LOG_OUTPUT_STEP value="{int(t.log_output_step)}" />']
     for tag, val in (("FLUX", t.flux), ("RECONSTRUCTION", t.reconstruction),
                      ("TIME_SCHEME", t.time_scheme), ("PRECISION", t.precision), ("REORDER", t.reorder),
-                     ("FUSED_STAGE", t.fused_stage)):
+                     ("FUSED_STAGE", t.fused_stage), ("ADJOINT_STORE", t.adjoint_store)):
         if val is not None:
             L.append(f'    <{tag} value="{val}" />')
     L += ["  </control>", "  <limits>", f'    <ro min="{_v(rmin)}" max="{_v(rmax)}" />',

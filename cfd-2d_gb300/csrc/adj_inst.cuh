@@ -146,7 +146,9 @@ __global__ void __launch_bounds__(256) k_adj_gather(const DevCase c, const AdjCa
 }
 
 // coef_t / coef_acc: the scheme's stage algebra (the previous stage's t_bar and
-// the step input's share); first: this is stage 0, write the step's lambda.
+// the step input's share); first: this is stage 0, write the step's lambda and,
+// with (coef_t, coef_acc) the last stage's coefficients, start the step before it
+// (t_bar, acc and mu from lambda: what k_adj_step_start does for the first step).
 template <typename T>
 __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase a, double coef_t, double coef_acc,
                                                   int first) {
@@ -154,8 +156,6 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nc) return;
     const MatT<T> mt = matT_of<T>(c, i);
-    const T U[4] = {to_face<T>(a.X[i]), to_face<T>(a.X[nc + i]), to_face<T>(a.X[2 * nc + i]),
-                    to_face<T>(a.X[3 * nc + i])};
     const Prim<T> q = load_prim(W_of<T>(c), i);
     const T* iS = invS_of<T>(c);
     const T* gbar = static_cast<const T*>(a.gbar);
@@ -209,11 +209,20 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
         qb.p = to_face<T>(q0[3] + qs[3].value());
     }
     T V[4] = {acc0<T>(), acc0<T>(), acc0<T>(), acc0<T>()};
-    vjp_cons2prim(U, mt.gm1, qb, V);
+    vjp_cons2prim_q(q, mt.gm1, qb, V);
     double ux[4];
     for (int k = 0; k < 4; k++) ux[k] = a.tb[k * nc + i] + to_wide(V[k]);
-    if (first) {
-        for (int k = 0; k < 4; k++) a.lam[k * nc + i] = a.acc[k * nc + i] + ux[k];
+    if (first) {  // lambda of the step input, and (coef_t, coef_acc = the last stage's) the next step's start
+        const double cf = c.cfl[i];
+        double t[4];
+        for (int k = 0; k < 4; k++) {
+            const double l = a.acc[k * nc + i] + ux[k];
+            a.lam[k * nc + i] = l;
+            t[k] = coef_t * l;
+            a.tb[k * nc + i] = t[k];
+            a.acc[k * nc + i] = coef_acc * l;
+        }
+        st4(a.mu_out, i, cf * t[0], cf * t[1], cf * t[2], cf * t[3]);
     } else {
         const double cf = c.cfl[i];
         double t[4];

@@ -73,6 +73,24 @@ __device__ __forceinline__ void vjp_cons2prim(const T* U, T gm1, const Prim<T>& 
     Ub[0] += rb;
 }
 
+// The same VJP with the conserved state expressed through the stage's primitives
+// (E = p/(r gm1) + (u^2 + v^2)/2): no read of the FP64 state.
+template <typename T>
+__device__ __forceinline__ void vjp_cons2prim_q(const Prim<T>& q, T gm1, const Prim<T>& pb, T* Ub) {
+    const T ro = q.r, iro = T(1.0) / ro, u = q.u, v = q.v;
+    const T e = q.p / (ro * gm1);
+    const T E = e + T(0.5) * (u * u + v * v);
+    T rb = pb.r + pb.p * e * gm1;
+    const T eb = pb.p * ro * gm1;
+    const T Eb = eb;
+    const T ub = pb.u - eb * u, vb = pb.v - eb * v;
+    Ub[1] += ub * iro;
+    Ub[2] += vb * iro;
+    Ub[3] += Eb * iro;
+    rb -= (ub * u + vb * v + Eb * E) * iro;
+    Ub[0] += rb;
+}
+
 // Tc = (p / (r gm1)) / Cv
 template <typename T>
 __device__ __forceinline__ void vjp_temperature(const Prim<T>& q, T gm1, T Cv, T Tb, Prim<T>& qb) {

@@ -126,7 +126,8 @@ private:
     double* segstore_ = nullptr;
     double* wgstore_ = nullptr;   // per recorded stage: W (4 nc) then G (8 nc), in the face precision
     size_t wg_slots_ = 0;         // doubles allocated in wgstore_
-    bool store_wg_ = false;
+    bool store_wg_ = false;       // the recorded stages' W are kept
+    bool store_g_ = false;        // ... and their G
     size_t ckpt_slots_ = 0, seg_slots_ = 0;
     int fw_steps_ = 0, fw_k_ = 0;
     template <typename T> T* upload(const std::vector<T>& v);

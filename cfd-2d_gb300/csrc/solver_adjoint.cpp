@@ -99,20 +99,26 @@ double Solver::forward(int nsteps, int k, int* status) {
     // keep each recorded stage's primitives and gradients (face precision) when the
     // segment's worth fits in a quarter of the free device memory; otherwise the
     // backward sweep re-derives them from the recorded stage states
+    // (or, when only they fit in half of it, the primitives alone: the gradients are then
+    // re-derived per stage, the primitives' conversion is saved)
     store_wg_ = false;
+    store_g_ = false;
     {
         const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
         const size_t need = ((size_t)k * nst * 12 * nc * fsize + sizeof(double) - 1) / sizeof(double);
-        if (need <= wg_slots_) {
+        const size_t need_w = ((size_t)k * nst * 4 * nc * fsize + sizeof(double) - 1) / sizeof(double);
+        size_t free_b = 0, total_b = 0;
+        if (need > wg_slots_) CUDA_CHECK(cudaMemGetInfo(&free_b, &total_b));
+        const int mode = task_.adj_store;
+        if (mode == 2 || (mode < 0 && (need <= wg_slots_ || need * sizeof(double) <= free_b / 4))) {
+            store_wg_ = store_g_ = true;
+        } else if (mode == 1 || (mode < 0 && (need_w <= wg_slots_ || need_w * sizeof(double) <= free_b / 2))) {
             store_wg_ = true;
-        } else {
-            size_t free_b = 0, total_b = 0;
-            CUDA_CHECK(cudaMemGetInfo(&free_b, &total_b));
-            if (need * sizeof(double) <= free_b / 4) {
-                wgstore_ = dalloc<double>(need);
-                wg_slots_ = need;
-                store_wg_ = true;
-            }
+        }
+        const size_t want = store_g_ ? need : (store_wg_ ? need_w : 0);
+        if (want > wg_slots_) {
+            wgstore_ = dalloc<double>(want);
+            wg_slots_ = want;
         }
     }
     CUDA_CHECK(cudaMemsetAsync(dc_.flags, 0, sizeof(unsigned) * nc, stream_));
@@ -139,8 +145,8 @@ double Solver::forward(int nsteps, int k, int* status) {
 }
 
 // One forward step that keeps every stage's input state in store[stage] and,
-// when wg is given, the stage's primitives and gradients (face precision) in
-// wg[stage] (12 nc values per stage).
+// when wg is given, the stage's primitives (and, with store_g_, gradients) in the
+// face precision in wg[stage] (12 or 4 nc values per stage).
 void Solver::record_step(double* store, void* wg) {
     const size_t nc = dc_.nc;
     const int nst = n_stages(task_.scheme);
@@ -153,9 +159,9 @@ void Solver::record_step(double* store, void* wg) {
                                    cudaMemcpyDeviceToDevice, stream_));
         if (task_.recon != RECON_NONE) launch_grad(dc_, p, stream_);
         if (wg) {
-            char* w = static_cast<char*>(wg) + (size_t)st * 12 * nc * fsize;
+            char* w = static_cast<char*>(wg) + (size_t)st * (store_g_ ? 12 : 4) * nc * fsize;
             CUDA_CHECK(cudaMemcpyAsync(w, W, fsize * 4 * nc, cudaMemcpyDeviceToDevice, stream_));
-            if (task_.recon != RECON_NONE)
+            if (task_.recon != RECON_NONE && store_g_)
                 CUDA_CHECK(cudaMemcpyAsync(w + 4 * nc * fsize, G, fsize * 8 * nc, cudaMemcpyDeviceToDevice,
                                            stream_));
         }
@@ -181,7 +187,8 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
     const int nst = n_stages(task_.scheme);
     const int p = task_.precision;
     const size_t fsize = p == PREC_MIXED ? sizeof(float) : sizeof(double);
-    auto wg_at = [&](int slot) -> void* { return reinterpret_cast<char*>(wgstore_) + (size_t)slot * 12 * nc * fsize; };
+    const size_t per_stage = (store_g_ ? 12 : 4) * nc * fsize;
+    auto wg_at = [&](int slot) -> void* { return reinterpret_cast<char*>(wgstore_) + (size_t)slot * per_stage; };
     AdjCase a{};
     a.eq = adj_eq_; a.eb = adj_eb_; a.eb2 = adj_eb2_; a.qbar = adj_qbar_; a.gbar = adj_gbar_;
     a.tb = adj_tb_; a.acc = adj_acc_; a.lam = adj_lam_; a.mu = adj_mu_; a.mu_out = adj_mu_;
@@ -201,38 +208,40 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
     // One segment after its checkpoint is restored: recompute its n steps, recording the
     // stages, then walk them backwards. Captured once per segment length into a CUDA
     // graph and replayed, so the host issues one launch per segment.
-    auto segment = [&](int n) {
+    auto segment = [&](int n, bool first_step) {  // first_step: the forward's last step, started from dJ/dU
         launch_prims(dc_, task_.precision, stream_);
         for (int j = 0; j < n; j++)
             record_step(segstore_ + (size_t)j * nst * 4 * nc, store_wg_ ? wg_at(j * nst) : nullptr);
         for (int j = n - 1; j >= 0; j--) {
-            launch_adj_step_start(adj_dc_, a, ct_f, ca_f, stream_);
+            // every later step is started by the stage-0 kernel of the step after it
+            if (first_step && j == n - 1) launch_adj_step_start(adj_dc_, a, ct_f, ca_f, stream_);
             for (int st = nst - 1; st >= 0; st--) {
                 DevCase cx = adj_dc_;
                 cx.A = segstore_ + ((size_t)j * nst + st) * 4 * nc;
                 a.X = cx.A;
-                if (store_wg_) {  // the recorded stage's own W and G
+                if (store_wg_) {  // the recorded stage's own W (and G)
                     char* w = static_cast<char*>(wg_at(j * nst + st));
                     if (p == PREC_MIXED) {
                         cx.W32 = reinterpret_cast<float*>(w);
-                        cx.G32 = cx.W32 + 4 * nc;
+                        if (store_g_) cx.G32 = cx.W32 + 4 * nc;
                     } else {
                         cx.W64 = reinterpret_cast<double*>(w);
-                        cx.G64 = cx.W64 + 4 * nc;
+                        if (store_g_) cx.G64 = cx.W64 + 4 * nc;
                     }
+                    if (!store_g_ && task_.recon != RECON_NONE) launch_grad(cx, p, stream_);
                 } else {  // re-derived by the forward's own kernels from the recorded stage state
                     launch_prims(cx, p, stream_);
                     if (task_.recon != RECON_NONE) launch_grad(cx, p, stream_);
                 }
                 launch_adj_flux(cx, a, task_.flux, task_.recon, p, stream_);
                 launch_adj_gather(cx, a, p, stream_);
-                double ct = 1.0, ca = 0.0;
+                double ct = ct_f, ca = ca_f;
                 if (st > 0) stage_coefs(task_.scheme, st, ct, ca);
                 launch_adj_cell(cx, a, ct, ca, st == 0 ? 1 : 0, p, stream_);
             }
         }
     };
-    std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+    std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // key: 2 n + (first step)
     auto release = [&]() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         graphs.clear();
@@ -242,14 +251,16 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
             const int n = std::min(fw_k_, fw_steps_ - seg * fw_k_);
             CUDA_CHECK(cudaMemcpyAsync(dc_.A, ckpt_ + (size_t)seg * 4 * nc, sizeof(double) * 4 * nc,
                                        cudaMemcpyDeviceToDevice, stream_));
+            const bool first = seg == nseg - 1;
+            const int key = 2 * n + (first ? 1 : 0);
             cudaGraphExec_t exec = nullptr;
             for (auto& g : graphs)
-                if (g.first == n) exec = g.second;
+                if (g.first == key) exec = g.second;
             if (!exec) {
                 cudaGraph_t graph = nullptr;
                 CUDA_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
                 try {
-                    segment(n);
+                    segment(n, first);
                 } catch (...) {
                     cudaStreamEndCapture(stream_, &graph);
                     if (graph) cudaGraphDestroy(graph);
@@ -259,7 +270,7 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
                 const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
                 cudaGraphDestroy(graph);
                 CUDA_CHECK(e);
-                graphs.emplace_back(n, exec);
+                graphs.emplace_back(key, exec);
             }
             CUDA_CHECK(cudaGraphLaunch(exec, stream_));
         }

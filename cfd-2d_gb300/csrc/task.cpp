@@ -76,6 +76,7 @@ TaskConfig parse_task(const std::string& path) {
     t.precision = pick(ctl, "PRECISION", {{"FP64", PREC_FP64}, {"MIXED", PREC_MIXED}}, PREC_FP64);
     t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}, {"HILBERT", 2}}, -1);
     t.fused = pick(ctl, "FUSED_STAGE", {{"0", 0}, {"1", 1}, {"OFF", 0}, {"ON", 1}}, -1);
+    t.adj_store = pick(ctl, "ADJOINT_STORE", {{"AUTO", -1}, {"NONE", 0}, {"PRIMITIVES", 1}, {"ALL", 2}}, -1);
     if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = attr_i(n, "value");
     if (t.newton_cap < 1) t.newton_cap = 1;
 

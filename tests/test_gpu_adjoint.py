@@ -141,3 +141,25 @@ def test_full_size_adjoint_64_directions(capi, tmp_path):
     errs = np.array(errs)
     # a direction may straddle a minmod or wave-pattern switch; none may exceed 10x the bar
     assert np.median(errs) <= TOL and errs.max() <= 10 * TOL, errs
+
+
+@pytest.mark.parametrize("precision", [None, "MIXED"])
+def test_adjoint_store_modes_give_the_same_gradient(capi, tmp_path, precision):
+    """Recorded stages keep their states only, their primitives too, or primitives and
+    gradients: whatever is not kept is re-derived by the forward's own kernels, so the
+    gradient is the same bit for bit."""
+    t, m, U0, w, _ = cases.vortex_adjoint(32, steps=9)
+    t.precision = precision
+    grads = []
+    for mode in ("NONE", "PRIMITIVES", "ALL"):
+        t.adjoint_store = mode
+        d = tmp_path / mode
+        d.mkdir()
+        s = capi.Solver(cases.write_task(t, m, str(d)), mesh=m)
+        s.set_objective(0, w, 1.0)
+        s.set_state(U0)
+        s.forward(9, 4)
+        g, gb = s.backward()
+        grads.append((g, gb))
+    for g, gb in grads[1:]:
+        assert np.array_equal(g, grads[0][0]) and np.array_equal(gb, grads[0][1])
