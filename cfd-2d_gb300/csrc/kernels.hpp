@@ -150,7 +150,6 @@ void launch_stage_fused_mixed(const DevCase& c, const DevTiles& t, int flux, int
                               const float* w_in, float* w_out, cudaStream_t s);
 
 struct AdjCase {
-    const double* X;   // 4*nc stage input state (SoA)
     const double* mu;  // nc x 4 (AoS) cfl * t_bar
     void* eq;          // ne x 24 in the face precision: q1_bar(4) g1_bar(8) q2_bar(4) g2_bar(8)
     double* eb;        // (ne - n_int) x 4 boundary-parameter adjoints, flux path

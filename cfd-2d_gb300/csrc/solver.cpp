@@ -198,6 +198,15 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
     }
 }
 
+void Solver::release(void* p, size_t bytes) {
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+    auto it = std::find(allocs_.begin(), allocs_.end(), p);
+    if (it == allocs_.end()) return;
+    allocs_.erase(it);
+    cudaFree(p);
+    bytes_ -= std::min(bytes_, bytes);
+}
+
 Solver::~Solver() {
     use_device();
     if (vtk_thread_.joinable()) {

@@ -103,6 +103,8 @@ public:
 
 private:
     template <typename T> T* dalloc(size_t n);
+    // free one dalloc'd buffer (after the stream is idle) and forget it
+    void release(void* p, size_t bytes);
     void adjoint_setup();
     void record_step(double* store, void* wg);
     DevCase adj_dc_{};

@@ -92,33 +92,44 @@ double Solver::forward(int nsteps, int k, int* status) {
         ckpt_slots_ = nseg;
     }
     const int nst = n_stages(task_.scheme);
-    if ((size_t)k * nst > seg_slots_) {
-        segstore_ = dalloc<double>((size_t)k * nst * 4 * nc);
-        seg_slots_ = (size_t)k * nst;
-    }
-    // keep each recorded stage's primitives and gradients (face precision) when the
-    // segment's worth fits in a quarter of the free device memory; otherwise the
-    // backward sweep re-derives them from the recorded stage states
-    // (or, when only they fit in half of it, the primitives alone: the gradients are then
-    // re-derived per stage, the primitives' conversion is saved)
+    // What the backward sweep keeps of each recorded stage. The reverse kernels read
+    // only the stage's primitives W and gradients G (face precision), so the first
+    // choice is W and G, then W alone (G re-derived per stage); the FP64 stage states
+    // (from which both are re-derived) only when W does not fit either. "Fits": within
+    // 80% of the free device memory beyond what is allocated already.
     store_wg_ = false;
     store_g_ = false;
     {
         const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
-        const size_t need = ((size_t)k * nst * 12 * nc * fsize + sizeof(double) - 1) / sizeof(double);
-        const size_t need_w = ((size_t)k * nst * 4 * nc * fsize + sizeof(double) - 1) / sizeof(double);
+        const size_t dbl = sizeof(double);
+        const size_t need = ((size_t)k * nst * 12 * nc * fsize + dbl - 1) / dbl;   // W and G, in doubles
+        const size_t need_w = ((size_t)k * nst * 4 * nc * fsize + dbl - 1) / dbl;  // W
+        const size_t need_x = (size_t)k * nst * 4 * nc;                            // FP64 states
         size_t free_b = 0, total_b = 0;
-        if (need > wg_slots_) CUDA_CHECK(cudaMemGetInfo(&free_b, &total_b));
+        CUDA_CHECK(cudaMemGetInfo(&free_b, &total_b));
+        const size_t have = wg_slots_ * dbl + seg_slots_ * 4 * nc * dbl;  // reusable if released
+        auto fits = [&](size_t doubles) { return doubles <= wg_slots_ || doubles * dbl <= (free_b + have) / 10 * 8; };
         const int mode = task_.adj_store;
-        if (mode == 2 || (mode < 0 && (need <= wg_slots_ || need * sizeof(double) <= free_b / 4))) {
+        if (mode == 2 || (mode < 0 && fits(need))) {
             store_wg_ = store_g_ = true;
-        } else if (mode == 1 || (mode < 0 && (need_w <= wg_slots_ || need_w * sizeof(double) <= free_b / 2))) {
+        } else if (mode == 1 || (mode < 0 && fits(need_w))) {
             store_wg_ = true;
         }
         const size_t want = store_g_ ? need : (store_wg_ ? need_w : 0);
+        if (store_wg_ && segstore_) {  // the states are not kept: give their memory back first
+            release(segstore_, seg_slots_ * 4 * nc * dbl);
+            segstore_ = nullptr;
+            seg_slots_ = 0;
+        }
         if (want > wg_slots_) {
+            if (wgstore_) release(wgstore_, wg_slots_ * dbl);
             wgstore_ = dalloc<double>(want);
             wg_slots_ = want;
+        }
+        if (!store_wg_ && (size_t)k * nst > seg_slots_) {
+            if (segstore_) release(segstore_, seg_slots_ * 4 * nc * dbl);
+            segstore_ = dalloc<double>(need_x);
+            seg_slots_ = (size_t)k * nst;
         }
     }
     CUDA_CHECK(cudaMemsetAsync(dc_.flags, 0, sizeof(unsigned) * nc, stream_));
@@ -144,8 +155,8 @@ double Solver::forward(int nsteps, int k, int* status) {
     return J;
 }
 
-// One forward step that keeps every stage's input state in store[stage] and,
-// when wg is given, the stage's primitives (and, with store_g_, gradients) in the
+// One forward step that keeps, when given, every stage's input state in
+// store[stage] or the stage's primitives (and, with store_g_, gradients) in the
 // face precision in wg[stage] (12 or 4 nc values per stage).
 void Solver::record_step(double* store, void* wg) {
     const size_t nc = dc_.nc;
@@ -155,8 +166,9 @@ void Solver::record_step(double* store, void* wg) {
     const void* W = p == PREC_MIXED ? (const void*)dc_.W32 : (const void*)dc_.W64;
     const void* G = p == PREC_MIXED ? (const void*)dc_.G32 : (const void*)dc_.G64;
     for (int st = 0; st < nst; st++) {
-        CUDA_CHECK(cudaMemcpyAsync(store + st * 4 * nc, st == 0 ? dc_.A : dc_.B, sizeof(double) * 4 * nc,
-                                   cudaMemcpyDeviceToDevice, stream_));
+        if (store)
+            CUDA_CHECK(cudaMemcpyAsync(store + st * 4 * nc, st == 0 ? dc_.A : dc_.B, sizeof(double) * 4 * nc,
+                                       cudaMemcpyDeviceToDevice, stream_));
         if (task_.recon != RECON_NONE) launch_grad(dc_, p, stream_);
         if (wg) {
             char* w = static_cast<char*>(wg) + (size_t)st * (store_g_ ? 12 : 4) * nc * fsize;
@@ -211,14 +223,14 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
     auto segment = [&](int n, bool first_step) {  // first_step: the forward's last step, started from dJ/dU
         launch_prims(dc_, task_.precision, stream_);
         for (int j = 0; j < n; j++)
-            record_step(segstore_ + (size_t)j * nst * 4 * nc, store_wg_ ? wg_at(j * nst) : nullptr);
+            record_step(store_wg_ ? nullptr : segstore_ + (size_t)j * nst * 4 * nc,
+                        store_wg_ ? wg_at(j * nst) : nullptr);
         for (int j = n - 1; j >= 0; j--) {
             // every later step is started by the stage-0 kernel of the step after it
             if (first_step && j == n - 1) launch_adj_step_start(adj_dc_, a, ct_f, ca_f, stream_);
             for (int st = nst - 1; st >= 0; st--) {
                 DevCase cx = adj_dc_;
-                cx.A = segstore_ + ((size_t)j * nst + st) * 4 * nc;
-                a.X = cx.A;
+                if (!store_wg_) cx.A = segstore_ + ((size_t)j * nst + st) * 4 * nc;
                 if (store_wg_) {  // the recorded stage's own W (and G)
                     char* w = static_cast<char*>(wg_at(j * nst + st));
                     if (p == PREC_MIXED) {
