@@ -65,3 +65,22 @@ def test_run_loop_honours_step_max(capi, tmp_path):
     assert inf.step == int(g["steps"])
     assert abs(inf.time - int(g["steps"]) * float(g["ref_tau"])) <= 1e-15
     assert np.max(np.abs(s.state() - g["ref_U"])) <= 1e-12 * np.max(np.abs(g["ref_U"]))
+
+
+def test_run_reports_a_vtk_write_failure(capi, tmp_path):
+    """run() writes its files from a host thread; a file that cannot be written
+    (here a directory stands where res_0000000020.vtk goes) is run()'s error status,
+    after every other file has been written."""
+    g = load_golden("shock_tube_4bc")
+    s = capi.Solver(write_case(tmp_path, g))
+    (tmp_path / "res_0000000020.vtk").mkdir()
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        with pytest.raises(capi.CfdError) as e:
+            s.run()
+        assert e.value.code == 301
+    finally:
+        os.chdir(cwd)
+    assert (tmp_path / "res_0000000000.vtk").is_file()
+    assert s.get_info().step == int(g["steps"])
