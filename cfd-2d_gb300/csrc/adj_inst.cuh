@@ -175,18 +175,18 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
         const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
         const T wi = (side2 ? T(-0.5) : T(0.5)) * l * iSi;
         // d g_i / d q_i and d g_i / d (neighbour or ghost): the same weight
-        const T s0 = wi * (nx * gi[0] + ny * gi[1]), s1 = wi * (nx * gi[2] + ny * gi[3]);
-        const T s2 = wi * (nx * gi[4] + ny * gi[5]), s3 = wi * (nx * gi[6] + ny * gi[7]);
+        const T s0 = wi * madd(nx * gi[0], ny, gi[1]), s1 = wi * madd(nx * gi[2], ny, gi[3]);
+        const T s2 = wi * madd(nx * gi[4], ny, gi[5]), s3 = wi * madd(nx * gi[6], ny, gi[7]);
         qs[0].add(s0); qs[3].add(s1); qs[1].add(s2); qs[2].add(s3);
         const int j = side2 ? c.ec1[e] : c.ec2[e];
         if (j >= 0) {  // the neighbour's gradient uses this cell's value with the opposite orientation
             T gj[8];
             ld8(gbar, j, gj);
             const T wj = (side2 ? T(0.5) : T(-0.5)) * l * iS[j];
-            qs[0].add(wj * (nx * gj[0] + ny * gj[1]));
-            qs[3].add(wj * (nx * gj[2] + ny * gj[3]));
-            qs[1].add(wj * (nx * gj[4] + ny * gj[5]));
-            qs[2].add(wj * (nx * gj[6] + ny * gj[7]));
+            qs[0].add(wj * madd(nx * gj[0], ny, gj[1]));
+            qs[3].add(wj * madd(nx * gj[2], ny, gj[3]));
+            qs[1].add(wj * madd(nx * gj[4], ny, gj[5]));
+            qs[2].add(wj * madd(nx * gj[6], ny, gj[7]));
         } else {  // boundary face: the ghost of the unreconstructed centre state
             const DevBnd b = c.bnds[c.ebnd[e]];
             const T Tc = temperature(q, mt.gm1, mt.Cv);

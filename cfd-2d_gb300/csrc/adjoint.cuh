@@ -12,6 +12,11 @@
 
 namespace cfd2d {
 
+// x + a b with one rounding. The reverse sweep's sums of products need no bit parity,
+// so they are fused explicitly (the FP64 translation unit is built without automatic
+// contraction, which the recomputed forward values need).
+template <typename T> __device__ __forceinline__ T madd(T x, T a, T b) { return t_fma(a, b, x); }
+
 // Accumulators start at -0: x + (-0) == x for every x, so the first addition folds away.
 template <typename T> __device__ __forceinline__ T acc0() { return T(-0.0); }
 template <typename T> __device__ __forceinline__ Prim<T> zero_prim() {
@@ -79,15 +84,15 @@ template <typename T>
 __device__ __forceinline__ void vjp_cons2prim_q(const Prim<T>& q, T gm1, const Prim<T>& pb, T* Ub) {
     const T ro = q.r, iro = T(1.0) / ro, u = q.u, v = q.v;
     const T e = q.p / (ro * gm1);
-    const T E = e + T(0.5) * (u * u + v * v);
-    T rb = pb.r + pb.p * e * gm1;
+    const T E = madd(e, T(0.5), t_fma(u, u, v * v));
+    T rb = madd(pb.r, pb.p * e, gm1);
     const T eb = pb.p * ro * gm1;
     const T Eb = eb;
-    const T ub = pb.u - eb * u, vb = pb.v - eb * v;
-    Ub[1] += ub * iro;
-    Ub[2] += vb * iro;
-    Ub[3] += Eb * iro;
-    rb -= (ub * u + vb * v + Eb * E) * iro;
+    const T ub = madd(pb.u, -eb, u), vb = madd(pb.v, -eb, v);
+    Ub[1] = madd(Ub[1], ub, iro);
+    Ub[2] = madd(Ub[2], vb, iro);
+    Ub[3] = madd(Ub[3], Eb, iro);
+    rb = madd(rb, -madd(madd(ub * u, vb, v), Eb, E), iro);
     Ub[0] += rb;
 }
 
@@ -131,13 +136,13 @@ template <typename T>
 __device__ __forceinline__ void vjp_phys(T r, T u, T v, T p, T E, T un, T nx, T ny, const T* fb, T& rb, T& ub,
                                          T& vb, T& pb, T& Eb, T& unb) {
     const T m = r * un;
-    const T mb = fb[0] + fb[1] * u + fb[2] * v;
-    ub += fb[1] * m;
-    vb += fb[2] * m;
-    pb += fb[1] * nx + fb[2] * ny + fb[3] * un;
-    Eb += fb[3] * un;
-    unb += fb[3] * (E + p) + mb * r;
-    rb += mb * un;
+    const T mb = madd(madd(fb[0], fb[1], u), fb[2], v);
+    ub = madd(ub, fb[1], m);
+    vb = madd(vb, fb[2], m);
+    pb = madd(madd(madd(pb, fb[1], nx), fb[2], ny), fb[3], un);
+    Eb = madd(Eb, fb[3], un);
+    unb = madd(madd(unb, fb[3], E + p), mb, r);
+    rb = madd(rb, mb, un);
 }
 
 // Lax-Friedrichs (flux_lax in kernels.cuh)
@@ -231,33 +236,35 @@ __device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T n
         const T ps = t_fma(mK, Ss - unK, K.p);
         const T inv = T(1.0) / (SK - Ss);
         const T sp = SK * ps;
-        const T A0 = SK * K.r - FK[0], A1 = SK * (K.r * K.u) - FK[1], A2 = SK * (K.r * K.v) - FK[2],
-                A3 = SK * EK - FK[3];
-        const T h0 = Ss * A0, h1 = Ss * A1 + sp * nx, h2 = Ss * A2 + sp * ny, h3 = Ss * A3 + sp * Ss;
+        // A_k and h_k only feed the derivatives: fused freely
+        const T A0 = madd(-FK[0], SK, K.r), A1 = madd(-FK[1], SK, K.r * K.u), A2 = madd(-FK[2], SK, K.r * K.v),
+                A3 = madd(-FK[3], SK, EK);
+        const T h0 = Ss * A0, h1 = madd(Ss * A1, sp, nx), h2 = madd(Ss * A2, sp, ny), h3 = madd(Ss * A3, sp, Ss);
         // f_k = h_k inv
         const T hb0 = fb[0] * inv, hb1 = fb[1] * inv, hb2 = fb[2] * inv, hb3 = fb[3] * inv;
-        const T invb = fb[0] * h0 + fb[1] * h1 + fb[2] * h2 + fb[3] * h3;
-        T Ssb = hb0 * A0 + hb1 * A1 + hb2 * A2 + hb3 * (A3 + sp);
+        const T invb = madd(madd(madd(fb[0] * h0, fb[1], h1), fb[2], h2), fb[3], h3);
+        T Ssb = madd(madd(madd(hb0 * A0, hb1, A1), hb2, A2), hb3, A3 + sp);
         const T A0b = hb0 * Ss, A1b = hb1 * Ss, A2b = hb2 * Ss, A3b = hb3 * Ss;
-        const T spb = hb1 * nx + hb2 * ny + hb3 * Ss;
+        const T spb = madd(madd(hb1 * nx, hb2, ny), hb3, Ss);
         // inv = 1/(SK - Ss)
         const T ii = invb * inv * inv;
         T SKb = -ii;
         Ssb += ii;
         // sp = SK ps
-        SKb += spb * ps;
+        SKb = madd(SKb, spb, ps);
         const T psb = spb * SK;
         // ps = pK + mK (Ss - unK)
         T Krb = acc0<T>(), Kub = acc0<T>(), Kvb = acc0<T>(), Kpb = psb, EKb = acc0<T>();
         T unKb = -psb * mK;
         const T mKb = psb * (Ss - unK);
-        Ssb += psb * mK;
+        Ssb = madd(Ssb, psb, mK);
         // A_k
-        SKb += A0b * K.r + A1b * (K.r * K.u) + A2b * (K.r * K.v) + A3b * EK;
-        Krb += A0b * SK + A1b * SK * K.u + A2b * SK * K.v;
-        Kub += A1b * SK * K.r;
-        Kvb += A2b * SK * K.r;
-        EKb += A3b * SK;
+        SKb = madd(madd(madd(madd(SKb, A0b, K.r), A1b, K.r * K.u), A2b, K.r * K.v), A3b, EK);
+        const T A1S = A1b * SK, A2S = A2b * SK;
+        Krb = madd(madd(madd(Krb, A0b, SK), A1S, K.u), A2S, K.v);
+        Kub = madd(Kub, A1S, K.r);
+        Kvb = madd(Kvb, A2S, K.r);
+        EKb = madd(EKb, A3b, SK);
         const T FKb[4] = {-A0b, -A1b, -A2b, -A3b};
         vjp_phys(K.r, K.u, K.v, K.p, EK, unK, nx, ny, FKb, Krb, Kub, Kvb, Kpb, EKb, unKb);
         // route the K-side adjoints
@@ -270,25 +277,29 @@ __device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T n
         // Ss = num / den
         const T numb = Ssb * iden, denb = -Ssb * Ss * iden;
         Rb.p += numb; Lb.p -= numb;
-        mLb += numb * unL + denb; unLb += numb * mL;
-        mRb += -numb * unR - denb; unRb -= numb * mR;
+        mLb = madd(mLb + denb, numb, unL); unLb = madd(unLb, numb, mL);
+        mRb = madd(mRb - denb, -numb, unR); unRb = madd(unRb, -numb, mR);
         // mL = rL (SL - unL), mR = rR (SR - unR)
-        Lb.r += mLb * (SL - unL); SLb += mLb * L.r; unLb -= mLb * L.r;
-        Rb.r += mRb * (SR - unR); SRb += mRb * R.r; unRb -= mRb * R.r;
+        Lb.r = madd(Lb.r, mLb, SL - unL); SLb = madd(SLb, mLb, L.r); unLb = madd(unLb, -mLb, L.r);
+        Rb.r = madd(Rb.r, mRb, SR - unR); SRb = madd(SRb, mRb, R.r); unRb = madd(unRb, -mRb, R.r);
         // SL = min(sl1, sl2), SR = max(sr1, sr2)
         if (l1) { unLb += SLb; cLb -= SLb; } else { unRb += SLb; cRb -= SLb; }
         if (r1) { unLb += SRb; cLb += SRb; } else { unRb += SRb; cRb += SRb; }
     }
     // E = p IG1 + .5 r (u^2 + v^2)
-    Lb.p += ELb * IG1; Lb.r += ELb * T(0.5) * (L.u * L.u + L.v * L.v);
-    Lb.u += ELb * L.r * L.u; Lb.v += ELb * L.r * L.v;
-    Rb.p += ERb * IG1; Rb.r += ERb * T(0.5) * (R.u * R.u + R.v * R.v);
-    Rb.u += ERb * R.r * R.u; Rb.v += ERb * R.r * R.v;
+    {
+        const T eL = ELb * L.r, eR = ERb * R.r;
+        Lb.p = madd(Lb.p, ELb, IG1); Lb.r = madd(Lb.r, ELb * T(0.5), t_fma(L.u, L.u, L.v * L.v));
+        Lb.u = madd(Lb.u, eL, L.u); Lb.v = madd(Lb.v, eL, L.v);
+        Rb.p = madd(Rb.p, ERb, IG1); Rb.r = madd(Rb.r, ERb * T(0.5), t_fma(R.u, R.u, R.v * R.v));
+        Rb.u = madd(Rb.u, eR, R.u); Rb.v = madd(Rb.v, eR, R.v);
+    }
     // un = u nx + v ny
-    Lb.u += unLb * nx; Lb.v += unLb * ny; Rb.u += unRb * nx; Rb.v += unRb * ny;
+    Lb.u = madd(Lb.u, unLb, nx); Lb.v = madd(Lb.v, unLb, ny);
+    Rb.u = madd(Rb.u, unRb, nx); Rb.v = madd(Rb.v, unRb, ny);
     // c = sqrt(GAM p / r): dc = (GAM dp - a dr) / (2 c r)
-    if (cLb != T(0.0)) { const T ab = T(0.5) * cLb / (cL * L.r); Lb.p += ab * GAM; Lb.r -= ab * aL; }
-    if (cRb != T(0.0)) { const T ab = T(0.5) * cRb / (cR * R.r); Rb.p += ab * GAM; Rb.r -= ab * aR; }
+    if (cLb != T(0.0)) { const T ab = T(0.5) * cLb / (cL * L.r); Lb.p = madd(Lb.p, ab, GAM); Lb.r = madd(Lb.r, -ab, aL); }
+    if (cRb != T(0.0)) { const T ab = T(0.5) * cRb / (cR * R.r); Rb.p = madd(Rb.p, ab, GAM); Rb.r = madd(Rb.r, -ab, aR); }
 }
 
 template <int FLUX, typename T>
@@ -313,13 +324,13 @@ __device__ __forceinline__ void vjp_reconstruct_a(const Prim<T>& q, const T* a, 
         const T db = pv[k];
         qbv[k] += db;
         if (RECON == RECON_LINEAR) {
-            gb[2 * k] += db * dx;
-            gb[2 * k + 1] += db * dy;
+            gb[2 * k] = madd(gb[2 * k], db, dx);
+            gb[2 * k + 1] = madd(gb[2 * k + 1], db, dy);
             continue;
         }
         const T b = nv[k] - qv[k];
         if (mm_pos(a[k], b)) {
-            if (mm_first(a[k], b)) { gb[2 * k] += db * dx; gb[2 * k + 1] += db * dy; }
+            if (mm_first(a[k], b)) { gb[2 * k] = madd(gb[2 * k], db, dx); gb[2 * k + 1] = madd(gb[2 * k + 1], db, dy); }
             else { nbv[k] += db; qbv[k] -= db; }
         }
     }
