@@ -1,3 +1,4 @@
+#include <algorithm>
 // Mixed form: reconstruction and Riemann fluxes in FP32; residual sums, state
 // update, limits and time steps in FP64 (kernels.cuh, k_update).
 #define KT float
@@ -8,10 +9,15 @@ namespace cfd2d {
 namespace {
 template <int FLUX, int RECON, int SCHEME>
 void fused_by_stage(const DevCase& c, const DevTiles& t, int stage, const float* wi, float* wo, cudaStream_t s) {
-    const size_t smem = 16 * ((size_t)t.max_cells + 2 * (size_t)t.max_grad + (size_t)t.max_edges);
+    const size_t smem = 16 * (2 * (size_t)t.max_cells + 2 * (size_t)t.max_grad + (size_t)t.max_edges);
     auto go = [&](auto kern) {
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kern<<<t.n_tiles, 256, smem, s>>>(c, t, wi, wo);
+        int per_sm = 0, sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem);
+        const int grid = std::max(1, std::min(t.n_tiles, std::max(1, per_sm) * std::max(1, sms)));
+        kern<<<grid, 256, smem, s>>>(c, t, wi, wo);
     };
     if (stage == 0) go(k_stage_fused<FLUX, RECON, SCHEME, 0>);
     else if (stage == 1) go(k_stage_fused<FLUX, RECON, SCHEME, 1>);

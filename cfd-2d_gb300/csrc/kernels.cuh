@@ -877,98 +877,123 @@ __device__ __forceinline__ void update_one(const DevCase& c, int i) {
     update_finish<T, SCHEME, STAGE>(c, i, R, Wm_of<T>(c));
 }
 
-// The mixed form's whole Runge-Kutta stage for one tile of cells (one CTA per tile,
-// 256 threads): the tile's and its two-ring halo's primitives are staged in shared
-// memory, then gradients of the own and first-ring cells, the fluxes of the own
+// 16-byte asynchronous global -> shared copies (cp.async, completion tracked per
+// commit group; the waits are hardware waits, no polling).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// The mixed form's whole Runge-Kutta stage for tiles of cells (persistent CTAs of 256
+// threads, each looping over tiles): a tile's and its two-ring halo's primitives are
+// staged in shared memory (fetched with cp.async while the CTA works on its previous
+// tile), then gradients of the own and first-ring cells, the fluxes of the own
 // cells' edges and the own cells' updates run from shared memory. Edges on the tile
 // border are evaluated by both tiles, each time with the same inputs and the same
 // code as k_grad / k_flux / k_update, so the results are those kernels' bit for
 // bit. Primitives are read from w_in and written to w_out (another buffer: the
 // neighbouring tiles still read the old values as their halo).
 template <int FLUX, int RECON, int SCHEME, int STAGE>
-__global__ void __launch_bounds__(256, 6) k_stage_fused(const DevCase c, const DevTiles tl,
+__global__ void __launch_bounds__(256, 5) k_stage_fused(const DevCase c, const DevTiles tl,
                                                      const float* __restrict__ w_in, float* __restrict__ w_out) {
     extern __shared__ float4 smem[];
-    const int t = blockIdx.x;
-    const int own0 = t * tl.tile, n_own = min(tl.tile, c.nc - own0);
-    const int h0 = tl.halo_off[t], nh = tl.halo_off[t + 1] - h0, nh1 = tl.n_h1[t];
-    const int nL = n_own + nh, nG = n_own + nh1;
-    const int e0 = tl.edge_off[t], nE = tl.edge_off[t + 1] - e0;
-    const int2* __restrict__ gf = tl.gface + 3 * (size_t)tl.gface_off[t];
-    float4* Ws = smem;                     // nL primitives (r, u, v, p)
-    float4* Gs = Ws + tl.max_cells;        // 2 per gradient cell
-    float4* Fs = Gs + 2 * tl.max_grad;     // one flux record per edge
+    float4* Wb[2] = {smem, smem + tl.max_cells};  // primitives of the tile in work / the next tile
+    float4* Gs = smem + 2 * tl.max_cells;          // 2 per gradient cell
+    float4* Fs = Gs + 2 * tl.max_grad;             // one flux record per edge
     const float4* W4 = reinterpret_cast<const float4*>(w_in);
-    for (int k = threadIdx.x; k < nL; k += blockDim.x) {
-        const int g = k < n_own ? own0 + k : tl.halo[h0 + k - n_own];
-        Ws[k] = __ldg(W4 + g);
-    }
-    __syncthreads();
-    auto prim = [&](int k) {
-        const float4 a = Ws[k];
-        Prim<float> q;
-        q.r = a.x; q.u = a.y; q.v = a.z; q.p = a.w;
-        return q;
+    float4* Wo = reinterpret_cast<float4*>(w_out);
+    auto fetch = [&](int t, float4* dst) {
+        const int own0 = t * tl.tile, n_own = min(tl.tile, c.nc - own0);
+        const int h0 = tl.halo_off[t], nL = n_own + tl.halo_off[t + 1] - h0;
+        for (int k = threadIdx.x; k < nL; k += blockDim.x)
+            cp_async16(dst + k, W4 + (k < n_own ? own0 + k : tl.halo[h0 + k - n_own]));
     };
-    if (RECON != RECON_NONE) {
-        for (int k = threadIdx.x; k < nG; k += blockDim.x) {
-            const int i = k < n_own ? own0 + k : tl.halo[h0 + k - n_own];
-            const Prim<float> q = prim(k);
-            float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int b = 0;
+    if ((int)blockIdx.x < tl.n_tiles) fetch(blockIdx.x, Wb[0]);
+    cp_async_commit();
+    for (int t = blockIdx.x; t < tl.n_tiles; t += gridDim.x, b ^= 1) {
+        const int tn = t + gridDim.x;
+        if (tn < tl.n_tiles) fetch(tn, Wb[b ^ 1]);
+        cp_async_commit();
+        cp_async_wait<1>();  // this tile's copies have landed (the next tile's may be in flight)
+        __syncthreads();
+        const float4* Ws = Wb[b];
+        const int own0 = t * tl.tile, n_own = min(tl.tile, c.nc - own0);
+        const int h0 = tl.halo_off[t], nh1 = tl.n_h1[t];
+        const int nG = n_own + nh1;
+        const int e0 = tl.edge_off[t], nE = tl.edge_off[t + 1] - e0;
+        const int2* __restrict__ gf = tl.gface + 3 * (size_t)tl.gface_off[t];
+        auto prim = [&](int k) {
+            const float4 a = Ws[k];
+            Prim<float> q;
+            q.r = a.x; q.u = a.y; q.v = a.z; q.p = a.w;
+            return q;
+        };
+        if (RECON != RECON_NONE) {
+            for (int k = threadIdx.x; k < nG; k += blockDim.x) {
+                const int i = k < n_own ? own0 + k : tl.halo[h0 + k - n_own];
+                const Prim<float> q = prim(k);
+                float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int f = 0; f < 3; f++) {
+                    const int2 fr = gf[3 * k + f];
+                    const int e = fr.x >> 1, nb = fr.y & 0xffff;
+                    const float nx = c.nx32[e], ny = c.ny32[e], l = c.l32[e];
+                    const Prim<float> o = nb != 0xffff ? prim(nb) : grad_ghost(c, i, e, q, nx, ny);
+                    grad_face(g, q, o, nx, ny, l, (fr.x & 1) != 0);
+                }
+                grad_finish(c, i, g);
+                Gs[2 * k] = make_float4(g[0], g[1], g[2], g[3]);
+                Gs[2 * k + 1] = make_float4(g[4], g[5], g[6], g[7]);
+            }
+            __syncthreads();
+        }
+        for (int k = threadIdx.x; k < nE; k += blockDim.x) {
+            const int2 te = tl.tedge[e0 + k];
+            const int e = te.x, l1 = te.y & 0xffff, l2 = (int)((unsigned)te.y >> 16);
+            const Prim<float> qL = prim(l1);
+            const Prim<float> qR = l2 != 0xffff ? prim(l2) : qL;
+            float gL[8], gR[8];
+            if (RECON != RECON_NONE) {
+                const float4 a = Gs[2 * l1], bb = Gs[2 * l1 + 1];
+                gL[0] = a.x; gL[1] = a.y; gL[2] = a.z; gL[3] = a.w; gL[4] = bb.x; gL[5] = bb.y; gL[6] = bb.z; gL[7] = bb.w;
+                if (l2 != 0xffff) {
+                    const float4 x = Gs[2 * l2], y = Gs[2 * l2 + 1];
+                    gR[0] = x.x; gR[1] = x.y; gR[2] = x.z; gR[3] = x.w; gR[4] = y.x; gR[5] = y.y; gR[6] = y.z; gR[7] = y.w;
+                }
+            }
+            float out[4];
+            const int c1 = l1 < n_own ? own0 + l1 : tl.halo[h0 + l1 - n_own];
+            flux_core<float, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out);
+            Fs[k] = make_float4(out[0], out[1], out[2], out[3]);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < n_own; k += blockDim.x) {
+            const int i = own0 + k;
+            if (!update_begin<SCHEME, STAGE>(c, i)) {
+                Wo[i] = Ws[k];  // frozen cell: its primitives do not change
+                continue;
+            }
+            float tv[3][4];
 #pragma unroll
             for (int f = 0; f < 3; f++) {
                 const int2 fr = gf[3 * k + f];
-                const int e = fr.x >> 1, nb = fr.y & 0xffff;
-                const float nx = c.nx32[e], ny = c.ny32[e], l = c.l32[e];
-                const Prim<float> o = nb != 0xffff ? prim(nb) : grad_ghost(c, i, e, q, nx, ny);
-                grad_face(g, q, o, nx, ny, l, (fr.x & 1) != 0);
+                const float4 v = Fs[(unsigned)fr.y >> 16];
+                const bool add = (fr.x & 1) != 0;  // c2 adds the edge flux, c1 subtracts it
+                tv[f][0] = neg_if(v.x, !add); tv[f][1] = neg_if(v.y, !add);
+                tv[f][2] = neg_if(v.z, !add); tv[f][3] = neg_if(v.w, !add);
             }
-            grad_finish(c, i, g);
-            Gs[2 * k] = make_float4(g[0], g[1], g[2], g[3]);
-            Gs[2 * k + 1] = make_float4(g[4], g[5], g[6], g[7]);
+            double R[4];
+            residual_pair_sum(tv, R);
+            update_finish<float, SCHEME, STAGE>(c, i, R, w_out);
         }
-        __syncthreads();
+        __syncthreads();  // shared buffers are free for the next round
     }
-    for (int k = threadIdx.x; k < nE; k += blockDim.x) {
-        const int2 te = tl.tedge[e0 + k];
-        const int e = te.x, l1 = te.y & 0xffff, l2 = (int)((unsigned)te.y >> 16);
-        const Prim<float> qL = prim(l1);
-        const Prim<float> qR = l2 != 0xffff ? prim(l2) : qL;
-        float gL[8], gR[8];
-        if (RECON != RECON_NONE) {
-            const float4 a = Gs[2 * l1], b = Gs[2 * l1 + 1];
-            gL[0] = a.x; gL[1] = a.y; gL[2] = a.z; gL[3] = a.w; gL[4] = b.x; gL[5] = b.y; gL[6] = b.z; gL[7] = b.w;
-            if (l2 != 0xffff) {
-                const float4 x = Gs[2 * l2], y = Gs[2 * l2 + 1];
-                gR[0] = x.x; gR[1] = x.y; gR[2] = x.z; gR[3] = x.w; gR[4] = y.x; gR[5] = y.y; gR[6] = y.z; gR[7] = y.w;
-            }
-        }
-        float out[4];
-        const int c1 = l1 < n_own ? own0 + l1 : tl.halo[h0 + l1 - n_own];
-        flux_core<float, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out);
-        Fs[k] = make_float4(out[0], out[1], out[2], out[3]);
-    }
-    __syncthreads();
-    float4* Wo = reinterpret_cast<float4*>(w_out);
-    for (int k = threadIdx.x; k < n_own; k += blockDim.x) {
-        const int i = own0 + k;
-        if (!update_begin<SCHEME, STAGE>(c, i)) {
-            Wo[i] = Ws[k];  // frozen cell: its primitives do not change
-            continue;
-        }
-        float tv[3][4];
-#pragma unroll
-        for (int f = 0; f < 3; f++) {
-            const int2 fr = gf[3 * k + f];
-            const float4 v = Fs[(unsigned)fr.y >> 16];
-            const bool add = (fr.x & 1) != 0;  // c2 adds the edge flux, c1 subtracts it
-            tv[f][0] = neg_if(v.x, !add); tv[f][1] = neg_if(v.y, !add);
-            tv[f][2] = neg_if(v.z, !add); tv[f][3] = neg_if(v.w, !add);
-        }
-        double R[4];
-        residual_pair_sum(tv, R);
-        update_finish<float, SCHEME, STAGE>(c, i, R, w_out);
-    }
+    cp_async_wait<0>();
 }
 
 template <typename T, int SCHEME, int STAGE, bool STRIDE>

@@ -2,9 +2,10 @@
 // owns a run of storage cells (compact when the cells are in Hilbert order) and lists
 // its two-ring halo, the edges of its own cells and, per gradient cell, its faces in
 // local numbering. Measured on the 2,097,152-triangle four-quadrant case the fused
-// stage runs at 0.65 ms/step against 0.61 ms for the per-kernel path (its load,
-// gradient, flux and update phases serialise on barriers and wait on memory with
-// only a few resident tiles per SM), so it is opt-in.
+// stage runs at 0.645 ms/step against 0.61 ms for the per-kernel path (its gradient,
+// flux and update phases serialise on barriers and wait on geometry and state
+// loads with only a few resident tiles per SM; fetching the next tile's primitives
+// during the current tile did not change that), so it is opt-in.
 #include <algorithm>
 #include <thread>
 #include <vector>
@@ -117,7 +118,7 @@ void Solver::build_tiles() {
         max_grad = std::max(max_grad, n_own + tl[t].nh1);
         max_edges = std::max(max_edges, (int)tl[t].tedge.size());
     }
-    const size_t smem = 16 * ((size_t)max_cells + 2 * (size_t)max_grad + (size_t)max_edges);
+    const size_t smem = 16 * (2 * (size_t)max_cells + 2 * (size_t)max_grad + (size_t)max_edges);
     if (smem > kMaxSmem) return;
     std::vector<int> halo;
     std::vector<int2> tedge, gface;
