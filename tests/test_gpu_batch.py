@@ -62,3 +62,31 @@ def test_autotuned_shapes_keep_results(capi, tmp_path):
     ref, _ = _batch(capi, _sub(tmp_path, "c"), insts)
     ref.step(5)
     assert bits_equal(a.state(), ref.state()) and bits_equal(b.state(), ref.state())
+
+
+@pytest.mark.parametrize("precision", [None, "MIXED"])
+def test_batch_adjoint_equals_single_adjoints(capi, tmp_path, precision):
+    """The discrete adjoint over the union mesh: each instance's slice of dJ/dU0 and
+    of dJ/d(boundary parameters) equals its own single-instance adjoint bit for bit
+    (J of the batch is the sum of the instances' J)."""
+    insts = cases.batched_vortices(3, min_cells=300, max_cells=2500, steps=6, flux="HLLC", precision=precision)
+    b, paths = _batch(capi, tmp_path, insts)
+    rng = np.random.default_rng(11)
+    ws = [rng.uniform(0.0, 1.0, m.n_cells) for _, m, _ in insts]
+    b.set_objective(0, np.concatenate(ws), 1.0)
+    b.set_state(np.concatenate([U0 for _, _, U0 in insts], axis=1), reset_time_step=True)
+    Jb = b.forward(6, 3)
+    g, gb = b.backward()
+    J = 0.0
+    nb = 0
+    for k, (t, m, U0) in enumerate(insts):
+        s = capi.Solver(paths[k], mesh=m)
+        s.set_objective(0, ws[k], 1.0)
+        s.set_state(U0, reset_time_step=True)
+        J += s.forward(6, 3)
+        gk, gbk = s.backward()
+        off, nc, _, _ = b.instance(k)
+        assert bits_equal(g[:, off:off + nc], gk)
+        assert bits_equal(gb[nb:nb + len(gbk)], gbk)
+        nb += len(gbk)
+    assert abs(Jb - J) <= 1e-14 * abs(J)
