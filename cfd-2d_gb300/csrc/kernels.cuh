@@ -567,11 +567,11 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
 template <typename T, bool STRIDE>
 __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!STRIDE) {  // one thread per item
+    if constexpr (!STRIDE) {  // one thread per item
         if (i0 < c.nc) grad_one<T>(c, i0);
-        return;
+    } else {
+        for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) grad_one<T>(c, i);  // persistent grid
     }
-    for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) grad_one<T>(c, i);  // persistent grid
 }
 
 // Projection g . dl of one gradient: the reference's reconstruction (LINEAR)
@@ -684,11 +684,11 @@ __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
 template <typename T, int FLUX, int RECON, bool STRIDE>
 __global__ void __launch_bounds__(256) k_flux(const DevCase c) {
     const int e0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!STRIDE) {  // one thread per item
+    if constexpr (!STRIDE) {  // one thread per item
         if (e0 < c.ne) flux_one<T, FLUX, RECON>(c, e0);
-        return;
+    } else {
+        for (int e = e0; e < c.ne; e += gridDim.x * blockDim.x) flux_one<T, FLUX, RECON>(c, e);  // persistent grid
     }
-    for (int e = e0; e < c.ne; e += gridDim.x * blockDim.x) flux_one<T, FLUX, RECON>(c, e);  // persistent grid
 }
 
 // FP32 <-> FP64 conversions on the integer pipe. GB300's FP64 unit issues ~2
@@ -999,11 +999,11 @@ __global__ void __launch_bounds__(256, 5) k_stage_fused(const DevCase c, const D
 template <typename T, int SCHEME, int STAGE, bool STRIDE>
 __global__ void __launch_bounds__(256) k_update(const DevCase c) {
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!STRIDE) {  // one thread per item
+    if constexpr (!STRIDE) {  // one thread per item
         if (i0 < c.nc) update_one<T, SCHEME, STAGE>(c, i0);
-        return;
+    } else {
+        for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) update_one<T, SCHEME, STAGE>(c, i);  // persistent grid
     }
-    for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) update_one<T, SCHEME, STAGE>(c, i);  // persistent grid
 }
 
 // remediateLimCells, src/methods/fvm_tvd.cpp:464-499: flagged cells, in original

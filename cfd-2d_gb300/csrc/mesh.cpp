@@ -573,7 +573,9 @@ std::vector<int> rcm_order(const Topo& t) {
                 int w = adj[3 * u + k];
                 if (!seen[w]) { seen[w] = 1; nb[m++] = w; }
             }
-            std::sort(nb, nb + m, [&](int x, int y) { return deg[x] != deg[y] ? deg[x] < deg[y] : x < y; });
+            auto before = [&](int x, int y) { return deg[x] != deg[y] ? deg[x] < deg[y] : x < y; };
+            for (int a = 1; a < m; a++)  // at most three: insertion sort
+                for (int b = a; b > 0 && before(nb[b], nb[b - 1]); b--) std::swap(nb[b], nb[b - 1]);
             for (int k = 0; k < m; k++) order.push_back(nb[k]);
         }
     }
