@@ -552,6 +552,17 @@ def main():
         prof[name] = {k: {"ms_per_launch": float(ms[i] / max(cnt[i], 1)), "launches": int(cnt[i]),
                           "share": float(ms[i] / max(ms.sum(), 1e-30))} for i, k in enumerate(KINDS)}
 
+    # the configuration's full length: both forms continued to 1000 steps, then compared
+    full_steps = 1000
+    for sv in (s64, smx):
+        rest = full_steps - sv.get_info().step
+        if rest > 0:
+            sv.step(rest)
+    U64, Umx = s64.state(), smx.state()
+    err_full = {"l1_rho": l1(Umx[0], U64[0]), "l1_rhoE": l1(Umx[3], U64[3]),
+                "linf_rho": linf(Umx[0], U64[0]), "linf_rhoE": linf(Umx[3], U64[3]),
+                "steps": int(s64.get_info().step)}
+
     # end to end through the C ABI: H2D of the step's input state from pinned memory,
     # one step, D2H of the result into pinned memory, every step
     Ke = min(K, 20)
@@ -619,7 +630,8 @@ def main():
                           "peak": hbm, "unit": "GB/s", "peak_kind": peak_kind},
         "fp64_alu_ceiling": fp64_ceiling,
         "mixed": {"value": value_mx, "unit": UNIT, "ms_per_step": msmx / K, "speedup_vs_fp64": ms64 / msmx,
-                  "dtype": "f32 faces / f64 accumulate", "error_vs_fp64": err},
+                  "dtype": "f32 faces / f64 accumulate", "error_vs_fp64": err,
+                  "error_vs_fp64_full_length": err_full},
         "adjoint_forward_ratio": adj["ratio_backward_over_forward"],
         "adjoint": adj,
         "kernels": prof,
