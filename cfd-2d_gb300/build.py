@@ -89,7 +89,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         for out in ex.map(lambda c: _run(c, verbose), jobs):
             logs.append(out)
     if jobs or not os.path.exists(LIB):
-        _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart"], verbose)
+        _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart", "-ldl"], verbose)
     main_src = os.path.join(CSRC, "main.cpp")
     if os.path.exists(main_src) and (force or _stale(EXE, [main_src, LIB])):
         _run(["g++", "-std=c++17", "-O2", "-I", INC, main_src, "-o", EXE, "-L", LIB_DIR, "-lcfd2d_gpu",

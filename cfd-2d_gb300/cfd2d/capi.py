@@ -66,6 +66,8 @@ SIGNATURES = {
     "cfd2d_set_boundary": [_P, _I, _D],
     "cfd2d_timed_steps": [_P, _I, _D],
     "cfd2d_profile_steps": [_P, _I, _D, _IP],
+    "cfd2d_save_state": [_P, C.c_char_p],
+    "cfd2d_load_state": [_P, C.c_char_p],
     "cfd2d_residual_first_order_static": [_I, _I, _P, _P, _P, _P, _P, _I, _IP, _D, C.c_double, C.c_double, _I,
                                           _P, _P, _P],
     "cfd2d_selftest": [_I, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
@@ -208,6 +210,12 @@ class Solver:
         s = np.empty(4)
         check(lib().cfd2d_conservation(self.h, _d(s)))
         return s
+
+    def save_state(self, path: str):
+        check(lib().cfd2d_save_state(self.h, path.encode()))
+
+    def load_state(self, path: str):
+        check(lib().cfd2d_load_state(self.h, path.encode()))
 
     def save_vtk(self, step: int):
         check(lib().cfd2d_save_vtk(self.h, int(step)))

@@ -6,6 +6,8 @@
 #include <memory>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "cfd2d.h"
 #include "mesh.hpp"
 #include "solver.hpp"
@@ -23,6 +25,15 @@ struct cfd2d_mesh {
 namespace {
 
 thread_local std::string g_err;
+
+// An NVTX range around each entry point that does GPU work (visible to Nsight
+// Systems / Compute; without a tool attached NVTX calls are no-ops).
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 
 int fail(int code, const std::string& msg) {
     g_err = msg;
@@ -110,6 +121,7 @@ std::vector<int> edge_bnd_from_desc(const cfd2d_mesh_desc* m, const cfd2d::Topo&
 extern "C" {
 
 int cfd2d_create(const char* task_xml_path, cfd2d_t** out) {
+    Range r("cfd2d_create");
     return guarded([&] {
         if (!task_xml_path || !out) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
         *out = nullptr;
@@ -126,6 +138,7 @@ int cfd2d_create(const char* task_xml_path, cfd2d_t** out) {
 }
 
 int cfd2d_create_with_mesh(const char* task_xml_path, const cfd2d_mesh_desc* mesh, cfd2d_t** out) {
+    Range r("cfd2d_create_with_mesh");
     return guarded([&] {
         if (!task_xml_path || !out) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
         *out = nullptr;
@@ -146,6 +159,7 @@ int cfd2d_create_with_mesh(const char* task_xml_path, const cfd2d_mesh_desc* mes
 }
 
 int cfd2d_batch_create(int n, const char* const* task_xml_paths, const cfd2d_mesh_desc* meshes, cfd2d_t** out) {
+    Range r("cfd2d_batch_create");
     return guarded([&] {
         if (n < 1 || !task_xml_paths || !out) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
         *out = nullptr;
@@ -201,6 +215,7 @@ int cfd2d_batch_instance(const cfd2d_t* h, int k, int* cell_offset, int* n_cells
 }
 
 int cfd2d_autotune(cfd2d_t* h, const char* json_path) {
+    Range r("cfd2d_autotune");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
         h->s->autotune(json_path, 5);
@@ -217,6 +232,7 @@ int cfd2d_load_tuning(cfd2d_t* h, const char* json_path) {
 }
 
 int cfd2d_step(cfd2d_t* h, int nsteps) {
+    Range r("cfd2d_step");
     return guarded([&] {
         if (!h || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
         int s = h->s->step(nsteps);
@@ -227,6 +243,7 @@ int cfd2d_step(cfd2d_t* h, int nsteps) {
 }
 
 int cfd2d_run(cfd2d_t* h) {
+    Range r("cfd2d_run");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
         return h->s->run();
@@ -264,6 +281,7 @@ int cfd2d_get_info(const cfd2d_t* h, cfd2d_info_t* info) {
 }
 
 int cfd2d_get_state(cfd2d_t* h, double* ro, double* ru, double* rv, double* re) {
+    Range r("cfd2d_get_state");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
         h->s->get_state(ro, ru, rv, re);
@@ -273,6 +291,7 @@ int cfd2d_get_state(cfd2d_t* h, double* ro, double* ru, double* rv, double* re) 
 
 int cfd2d_set_state(cfd2d_t* h, const double* ro, const double* ru, const double* rv, const double* re,
                     int reset_time_step) {
+    Range r("cfd2d_set_state");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
         h->s->set_state(ro, ru, rv, re, reset_time_step != 0);
@@ -297,6 +316,7 @@ int cfd2d_get_flags(cfd2d_t* h, unsigned* flags) {
 }
 
 int cfd2d_residual(cfd2d_t* h, double* R) {
+    Range r("cfd2d_residual");
     return guarded([&] {
         if (!h || !R) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
         h->s->residual(R);
@@ -313,9 +333,28 @@ int cfd2d_conservation(cfd2d_t* h, double sums[4]) {
 }
 
 int cfd2d_save_vtk(cfd2d_t* h, int step) {
+    Range r("cfd2d_save_vtk");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
         h->s->save_vtk(step);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_save_state(cfd2d_t* h, const char* path) {
+    Range r("cfd2d_save_state");
+    return guarded([&] {
+        if (!h || !path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->save_state(path);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_load_state(cfd2d_t* h, const char* path) {
+    Range r("cfd2d_load_state");
+    return guarded([&] {
+        if (!h || !path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        h->s->load_state(path);
         return CFD2D_OK;
     });
 }
@@ -329,6 +368,7 @@ int cfd2d_set_objective(cfd2d_t* h, int kind, const double* weights, double p_re
 }
 
 int cfd2d_forward(cfd2d_t* h, int nsteps, int checkpoint_every, double* J) {
+    Range r("cfd2d_forward");
     return guarded([&] {
         if (!h || !J) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
         int st = CFD2D_OK;
@@ -338,6 +378,7 @@ int cfd2d_forward(cfd2d_t* h, int nsteps, int checkpoint_every, double* J) {
 }
 
 int cfd2d_backward(cfd2d_t* h, double* dJdU0, double* dJdbnd) {
+    Range r("cfd2d_backward");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
         h->s->backward(dJdU0, dJdbnd);
@@ -354,6 +395,7 @@ int cfd2d_set_boundary(cfd2d_t* h, int b, const double par[4]) {
 }
 
 int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms) {
+    Range r("cfd2d_timed_steps");
     return guarded([&] {
         if (!h || !device_ms || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
         *device_ms = h->s->timed_steps(nsteps);
@@ -362,6 +404,7 @@ int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms) {
 }
 
 int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_launches[4]) {
+    Range r("cfd2d_profile_steps");
     return guarded([&] {
         if (!h || !kernel_ms || !kernel_launches || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
         h->s->profile_steps(nsteps, kernel_ms, kernel_launches);

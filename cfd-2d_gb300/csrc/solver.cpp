@@ -444,6 +444,70 @@ void Solver::get_flags(unsigned* out) {
     CUDA_CHECK(cudaStreamSynchronize(stream_));
 }
 
+// Binary restart file: "CFD2DST1", cell count, steps, time, global time step, then the
+// conserved state (4 x nc, cell order of the mesh files), cTau (nc) and the flag words
+// (nc), all little-endian as the host writes them.
+namespace {
+constexpr char kStateMagic[8] = {'C', 'F', 'D', '2', 'D', 'S', 'T', '1'};
+}
+
+void Solver::save_state(const char* path) {
+    use_device();
+    const int nc = dc_.nc;
+    std::vector<double> U(4 * (size_t)nc), ct(nc);
+    std::vector<unsigned> fl(nc);
+    get_state(U.data(), U.data() + nc, U.data() + 2 * (size_t)nc, U.data() + 3 * (size_t)nc);
+    get_ctau(ct.data());
+    get_flags(fl.data());
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' opening error.");
+    const int64_t hdr[2] = {nc, steps_};
+    const double hd[2] = {t_, tau_};
+    bool ok = std::fwrite(kStateMagic, 1, 8, fp) == 8 && std::fwrite(hdr, sizeof hdr, 1, fp) == 1 &&
+              std::fwrite(hd, sizeof hd, 1, fp) == 1 &&
+              std::fwrite(U.data(), sizeof(double), U.size(), fp) == U.size() &&
+              std::fwrite(ct.data(), sizeof(double), ct.size(), fp) == ct.size() &&
+              std::fwrite(fl.data(), sizeof(unsigned), fl.size(), fp) == fl.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' write error.");
+}
+
+void Solver::load_state(const char* path) {
+    use_device();
+    const int nc = dc_.nc;
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' opening error.");
+    char magic[8];
+    int64_t hdr[2];
+    double hd[2];
+    std::vector<double> U(4 * (size_t)nc), ct(nc);
+    std::vector<unsigned> fl(nc);
+    bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, kStateMagic, 8) == 0 &&
+              std::fread(hdr, sizeof hdr, 1, fp) == 1 && hdr[0] == nc && std::fread(hd, sizeof hd, 1, fp) == 1 &&
+              std::fread(U.data(), sizeof(double), U.size(), fp) == U.size() &&
+              std::fread(ct.data(), sizeof(double), ct.size(), fp) == ct.size() &&
+              std::fread(fl.data(), sizeof(unsigned), fl.size(), fp) == fl.size();
+    std::fclose(fp);
+    if (!ok) throw Error(CFD2D_ERR_MESH_FORMAT, std::string("File '") + path + "' is not a state of this mesh.");
+    set_state(U.data(), U.data() + nc, U.data() + 2 * (size_t)nc, U.data() + 3 * (size_t)nc, false);
+    steps_ = (int)hdr[1];
+    t_ = hd[0];
+    tau_ = hd[1];
+    // storage order: cell i holds file cell perm[i]
+    std::vector<double> cts(nc);
+    std::vector<unsigned> fls(nc);
+    for (int i = 0; i < nc; i++) {
+        cts[i] = ct[lay_.perm[i]];
+        fls[i] = fl[lay_.perm[i]];
+    }
+    CUDA_CHECK(cudaMemcpyAsync(dc_.flags, fls.data(), sizeof(unsigned) * nc, cudaMemcpyHostToDevice, stream_));
+    // STEADY=0: the saved global step; STEADY=1: the next step runs on ctau_next, which
+    // set_state derived from the state, and cTau reads as saved
+    if (!task_.steady) launch_fill_cfl(dc_, tau_, stream_);
+    CUDA_CHECK(cudaMemcpyAsync(dc_.ctau, cts.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
 void Solver::residual(double* R) {
     use_device();
     const int p = task_.precision;

@@ -63,6 +63,9 @@ public:
     void residual(double* R);
     void conservation(double sums[4]);
     void save_vtk(int step);
+    // restart files: the state, cTau, flags, step count and time
+    void save_state(const char* path);
+    void load_state(const char* path);
     // run()'s output: snapshot on the stream, file written by a host thread
     void save_vtk_async(int step);
     void vtk_flush();

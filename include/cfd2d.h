@@ -118,6 +118,12 @@ int cfd2d_residual(cfd2d_t* h, double* R);
 int cfd2d_conservation(cfd2d_t* h, double sums[4]);
 /* FVM_TVD::save (src/methods/fvm_tvd.cpp:501-600): res_%010d.vtk in the working directory. */
 int cfd2d_save_vtk(cfd2d_t* h, int step);
+/* Restart files (no counterpart in the reference, which cannot restart): the
+ * conserved state, cTau, the cell flags, the step count and the time, in the
+ * mesh files' cell order. cfd2d_load_state into a handle made from the same task
+ * and mesh continues the run exactly as if it had not stopped. */
+int cfd2d_save_state(cfd2d_t* h, const char* path);
+int cfd2d_load_state(cfd2d_t* h, const char* path);
 
 /* ---- batches -------------------------------------------------------------- */
 /* No counterpart in the reference (one FVM_TVD per process there): n
