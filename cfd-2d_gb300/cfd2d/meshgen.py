@@ -307,3 +307,89 @@ def write_task_xml(t: Task) -> str:
     L += ["  </boundaries>", "  <mesh>", f'    <name value="{t.mesh_name}" />',
           f'    <filesType value="{t.mesh_type}" />', "  </mesh>", "</task>", ""]
     return "\n".join(L)
+
+
+# ------------------------------------------------- task.xml of FVM_TVD_IMPLICIT
+
+@dataclass
+class ImplicitRegion:
+    cell_type: int          # the .ele attribute of its cells
+    u: float
+    v: float
+    T: float
+    p: float
+    mat: int = 0
+
+
+@dataclass
+class ImplicitBoundary:
+    edge_type: int          # the .poly marker of its segments
+    kind: str               # BOUND_INLET / BOUND_OUTLET / BOUND_WALL
+    T: float = 1.0
+    p: float = 1.0
+    u: float = 0.0
+    v: float = 0.0
+
+
+@dataclass
+class ImplicitTask:
+    """task.xml of the reference's FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-176):
+    Triangle files read by Grid::initFromFiles, regions bound by cell type, boundaries by
+    edge type; the CFL block is read for steady runs only."""
+    regions: list
+    boundaries: list
+    steady: int = 0
+    tau: float = 1.0e-3
+    tmax: float = 1.0e8
+    step_max: int = 10
+    file_output_step: int = 1000000
+    log_output_step: int = 1000000
+    flux: str = "LAX"                  # GODUNOV / LAX
+    cfl: tuple = (1.0, 1.0, 1.0, 1000000, 1.0e9)  # start, scale, max, step, max_limited_cells
+    smoothing: tuple = (0, 0.0)        # using, coefficient
+    limits: tuple = (1.0e-8, 1.0e8, 1.0e-8, 1.0e8, 1.0e8)
+    materials: list = field(default_factory=lambda: [("gas", 8.314472, 3.5, 0.0, 0.0)])
+    mesh_name: str = "mesh"
+    precision: str | None = None       # GPU option: FP64 (default)
+    reorder: str | None = None
+
+
+def write_implicit_task_xml(t: ImplicitTask) -> str:
+    rmin, rmax, pmin, pmax, umax = t.limits
+    start, scale, cmax, cstep, maxlim = t.cfl
+    L = ['<?xml version="1.0" encoding="UTF-8"?>', '<task method="FVM_TVD_IMPLICIT">', "  <control>",
+         f'    <STEADY value="{int(t.steady)}" />', f'    <TAU value="{_v(t.tau)}" />',
+         f'    <TMAX value="{_v(t.tmax)}" />', f'    <STEP_MAX value="{int(t.step_max)}" />',
+         f'    <FILE_OUTPUT_STEP value="{int(t.file_output_step)}" />',
+         f'    <LOG_OUTPUT_STEP value="{int(t.log_output_step)}" />', f'    <FLUX value="{t.flux}" />',
+         "    <CFL>", f'      <start value="{_v(start)}" />', f'      <scale value="{_v(scale)}" />',
+         f'      <max value="{_v(cmax)}" />', f'      <step value="{int(cstep)}" />',
+         f'      <max_limited_cells value="{_v(maxlim)}" />', "    </CFL>"]
+    for tag, val in (("PRECISION", t.precision), ("REORDER", t.reorder)):
+        if val is not None:
+            L.append(f'    <{tag} value="{val}" />')
+    L += ["  </control>", "  <smoothing>", f'    <using value="{int(t.smoothing[0])}" />',
+          f'    <coefficient value="{_v(t.smoothing[1])}" />', "  </smoothing>",
+          "  <limits>", f'    <ro min="{_v(rmin)}" max="{_v(rmax)}" />',
+          f'    <p min="{_v(pmin)}" max="{_v(pmax)}" />', f'    <u max="{_v(umax)}" />', "  </limits>",
+          f'  <materials count="{len(t.materials)}">']
+    for k, (name, M, Cp, K, ML) in enumerate(t.materials):
+        L += [f'    <material id="{k}">', f"      <name>{name}</name>", "      <parameters>",
+              f'        <M value="{_v(M)}" />', f'        <Cp value="{_v(Cp)}" />',
+              f'        <K value="{_v(K)}" />', f'        <ML value="{_v(ML)}" />',
+              "      </parameters>", "    </material>"]
+    L += ["  </materials>", f'  <regions count="{len(t.regions)}">']
+    for k, r in enumerate(t.regions):
+        L += [f'    <region id="{k}">', f'      <material id="{r.mat}" />', f'      <cell type="{int(r.cell_type)}" />',
+              "      <parameters>", f'        <Vx value="{_v(r.u)}" />', f'        <Vy value="{_v(r.v)}" />',
+              f'        <T value="{_v(r.T)}" />', f'        <P value="{_v(r.p)}" />', "      </parameters>",
+              "    </region>"]
+    L += ["  </regions>", f'  <boundaries count="{len(t.boundaries)}">']
+    for b in t.boundaries:
+        L += [f'    <boundCond edgeType="{int(b.edge_type)}">', f"      <type>{b.kind}</type>"]
+        if b.kind == "BOUND_INLET":
+            L += ["      <parameters>", f'        <T value="{_v(b.T)}" />', f'        <P value="{_v(b.p)}" />',
+                  f'        <Vx value="{_v(b.u)}" />', f'        <Vy value="{_v(b.v)}" />', "      </parameters>"]
+        L.append("    </boundCond>")
+    L += ["  </boundaries>", "  <mesh>", f'    <name value="{t.mesh_name}" />', "  </mesh>", "</task>", ""]
+    return "\n".join(L)

@@ -150,9 +150,9 @@ int orc_mesh_build(int nn, const double* xy, int nc, const int* tri, const int* 
             double* P = m->pts + 6 * (size_t)e;
             P[0] = (x1 + x2) / 2.0;
             P[1] = (y1 + y2) / 2.0;
-            if (berkeley) {
+            if (berkeley == 1) {
                 m->npts[e] = 1; /* src/mesh/MeshReaderBerkleyTriangle.cpp:102-105 */
-            } else {            /* src/mesh/MeshReaderSalomeUnv.cpp:158-169 */
+            } else {            /* src/mesh/MeshReaderSalomeUnv.cpp:158-169, src/mesh/grid.cpp:153-162 */
                 m->npts[e] = 3;
                 P[2] = (x1 + x2) / 2.0 - sq3 * (x2 - x1) / 2.0;
                 P[3] = (y1 + y2) / 2.0 - sq3 * (y2 - y1) / 2.0;
@@ -822,5 +822,581 @@ void orc_solver_free(orc_solver* s) {
     free(s->ro_old); free(s->ru_old); free(s->rv_old); free(s->re_old);
     free(s->ro_int); free(s->ru_int); free(s->rv_int); free(s->re_int);
     free(s->grad); free(s->cTau); free(s->flag);
+    free(s);
+}
+
+/* ================================================================ FVM_TVD_IMPLICIT
+ *
+ * Restatement of the reference's implicit method (src/methods/fvm_tvd_implicit.cpp):
+ * per step a Roe-linearised block system (S/cTau I + sum_faces l A+-) dU = -sum F l,
+ * assembled by the reference's edge loop, solved by restarted GMRES, then the
+ * reference's smoothing, update with limits, remediation and CFL control. The
+ * reference solves with HYPRE's GMRES (src/methods/solvers/SolverHypreGmres.cpp),
+ * which is not part of the reference tree; orc_gmres_block restates the published
+ * GMRES (Saad and Schultz 1986, Givens rotations, modified Gram-Schmidt) with the
+ * reference's parameters and HYPRE's stopping rule |r| <= eps |b|. */
+
+struct orc_imp {
+    const orc_mesh* m;
+    orc_imp_params p;
+    int nm;
+    double *matM, *matCp;
+    int* cell_mat;
+    int nbnd;
+    int* bkind;
+    double* bpar;               /* nbnd x (T, P, Vx, Vy), the order of Boundary::par */
+    double *ro, *ru, *rv, *re;
+    double* grad;               /* nc x 8 */
+    double* cTau;
+    double* tmpArr;
+    int* tmpArrInt;
+    unsigned* flag;
+    double *diag, *off, *rhs;   /* nc x 16, nc x 3 x 16 (faces in Cell::edgesInd order), nc x 4 */
+    int* nbr;                   /* nc x 3: the cell across each face, -1 on the boundary */
+    double* x;                  /* 4 nc, x[4 c + k] like MatrixSolver::x */
+    double t, CFL;
+    int step, solverErr;
+    int last_iters, last_status;
+    double last_rel;
+    int newton_hit;
+};
+
+/* FVM_TVD_IMPLICIT::convertConsToPar, :1053-1063 (URS(0) then URS(1)) */
+static void imp_cons2par(const orc_imp* s, int i, Par* par) {
+    int mt = s->cell_mat[i];
+    par->r = s->ro[i];
+    par->u = s->ru[i] / s->ro[i];
+    par->v = s->rv[i] / s->ro[i];
+    par->E = s->re[i] / s->ro[i];
+    par->e = par->E - 0.5 * (par->u * par->u + par->v * par->v);
+    urs(s->matM[mt], s->matCp[mt], par, 0);
+    urs(s->matM[mt], s->matCp[mt], par, 1);
+}
+
+/* FVM_TVD_IMPLICIT::convertParToCons, :1045-1051 */
+static void imp_par2cons(orc_imp* s, int i, const Par* par) {
+    s->ro[i] = par->r;
+    s->ru[i] = par->r * par->u;
+    s->rv[i] = par->r * par->v;
+    s->re[i] = par->r * (par->e + 0.5 * (par->u * par->u + par->v * par->v));
+}
+
+/* FVM_TVD_IMPLICIT::boundaryCond, :963-1008 */
+static void imp_boundary(const orc_imp* s, int e, const Par* pL, Par* pR) {
+    const orc_mesh* m = s->m;
+    int b = m->bnd[e];
+    const double* bp = s->bpar + 4 * b;
+    int mt = s->cell_mat[m->c1[e]];
+    switch (s->bkind[b]) {
+    case ORC_IBND_INLET:
+        pR->T = bp[0]; pR->p = bp[1]; pR->u = bp[2]; pR->v = bp[3];
+        urs(s->matM[mt], s->matCp[mt], pR, 2);
+        urs(s->matM[mt], s->matCp[mt], pR, 1);
+        break;
+    case ORC_IBND_OUTLET:
+        *pR = *pL;
+        break;
+    default: { /* BOUND_WALL */
+        *pR = *pL;
+        double Un = pL->u * m->nx[e] + pL->v * m->ny[e];
+        double Vx = m->nx[e] * Un * 2.0, Vy = m->ny[e] * Un * 2.0;
+        pR->u = pL->u - Vx;
+        pR->v = pL->v - Vy;
+    }
+    }
+}
+
+/* reconstruct(iFace, pL, pR), :446-457: the cell-centre states */
+static void imp_centre_states(const orc_imp* s, int e, Par* pL, Par* pR) {
+    const orc_mesh* m = s->m;
+    imp_cons2par(s, m->c1[e], pL);
+    if (m->c2[e] > -1) imp_cons2par(s, m->c2[e], pR);
+    else imp_boundary(s, e, pL, pR);
+}
+
+/* reconstruct(iFace, pL, pR, p), :459-494: linear on interior faces, centre + ghost on the boundary */
+static void imp_point_states(const orc_imp* s, int e, int gp, Par* pL, Par* pR) {
+    const orc_mesh* m = s->m;
+    int c1 = m->c1[e], c2 = m->c2[e];
+    double px = m->pts[6 * (size_t)e + 2 * gp], py = m->pts[6 * (size_t)e + 2 * gp + 1];
+    if (c2 > -1) {
+        imp_cons2par(s, c1, pL);
+        imp_cons2par(s, c2, pR);
+        const double* g1 = s->grad + 8 * (size_t)c1;
+        const double* g2 = s->grad + 8 * (size_t)c2;
+        double d1x = px - m->cx[c1], d1y = py - m->cy[c1];
+        double d2x = px - m->cx[c2], d2y = py - m->cy[c2];
+        pL->r += g1[0] * d1x + g1[1] * d1y;
+        pL->p += g1[2] * d1x + g1[3] * d1y;
+        pL->u += g1[4] * d1x + g1[5] * d1y;
+        pL->v += g1[6] * d1x + g1[7] * d1y;
+        pR->r += g2[0] * d2x + g2[1] * d2y;
+        pR->p += g2[2] * d2x + g2[3] * d2y;
+        pR->u += g2[4] * d2x + g2[5] * d2y;
+        pR->v += g2[6] * d2x + g2[7] * d2y;
+    } else {
+        imp_cons2par(s, c1, pL);
+        imp_boundary(s, e, pL, pR);
+    }
+}
+
+/* FVM_TVD_IMPLICIT::calcGrad, :185-250 */
+static void imp_calc_grad(orc_imp* s) {
+    const orc_mesh* m = s->m;
+    double* g = s->grad;
+    memset(g, 0, sizeof(double) * 8 * (size_t)m->nc);
+    for (int e = 0; e < m->ne; e++) {
+        int c1 = m->c1[e], c2 = m->c2[e];
+        Par pL, pR;
+        imp_centre_states(s, e, &pL, &pR);
+        double nx = m->nx[e], ny = m->ny[e], l = m->l[e];
+        double v[8];
+        v[0] = (pL.r + pR.r) / 2 * nx * l; v[1] = (pL.r + pR.r) / 2 * ny * l;
+        v[2] = (pL.p + pR.p) / 2 * nx * l; v[3] = (pL.p + pR.p) / 2 * ny * l;
+        v[4] = (pL.u + pR.u) / 2 * nx * l; v[5] = (pL.u + pR.u) / 2 * ny * l;
+        v[6] = (pL.v + pR.v) / 2 * nx * l; v[7] = (pL.v + pR.v) / 2 * ny * l;
+        for (int k = 0; k < 8; k++) g[8 * (size_t)c1 + k] += v[k];
+        if (c2 > -1) for (int k = 0; k < 8; k++) g[8 * (size_t)c2 + k] -= v[k];
+    }
+    for (int i = 0; i < m->nc; i++) {
+        double si = m->S[i];
+        for (int k = 0; k < 8; k++) g[8 * (size_t)i + k] /= si;
+    }
+}
+
+/* roe_orig, src/global.cpp:407-441 (W components 0) */
+static void roe_average(Par* a, const Par* pL, const Par* pR, double GAM) {
+    double AGAM = (GAM - 1.0);
+    double fG = GAM;
+    double fSB = sqrt(pL->r), fSE = sqrt(pR->r);
+    double fS_ = 1.0 / (fSB + fSE);
+    double RI = fSB * fSE;
+    double UI = (fSB * pL->u + fSE * pR->u) * fS_;
+    double VI = (fSB * pL->v + fSE * pR->v) * fS_;
+    double WI = (fSB * 0.0 + fSE * 0.0) * fS_;
+    double EB = pL->p / (pL->r * AGAM), EE = pR->p / (pR->r * AGAM);
+    double HB = EB + (pL->u * pL->u + pL->v * pL->v + 0.0 * 0.0) * 0.5 + pL->p / pL->r;
+    double HE = EE + (pR->u * pR->u + pR->v * pR->v + 0.0 * 0.0) * 0.5 + pR->p / pR->r;
+    double HI = (fSB * HB + fSE * HE) * fS_;
+    double PI = (HI - (UI * UI + VI * VI + WI * WI) * 0.5) * RI * (fG - 1.0) / fG;
+    double EI = PI / (RI * AGAM);
+    /* calcRoeAverage, :418-444 */
+    a->r = RI; a->e = EI; a->p = PI; a->u = UI; a->v = VI;
+    a->cz = sqrt(GAM * a->p / a->r);
+    a->E = a->e + 0.5 * (a->u * a->u + a->v * a->v);
+}
+
+typedef double M4[4][4];
+
+static void mult4(M4 d, M4 a, M4 b) { /* multMtx4, :262-275 */
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            double sum = 0;
+            for (int k = 0; k < 4; ++k) sum += a[i][k] * b[k][j];
+            d[i][j] = sum;
+        }
+}
+
+/* eigenValues / rightEigenVector / leftEigenVector, :321-356 */
+static void eigen_values(M4 d, double c, double u, double nx, double v, double ny) {
+    for (int i = 0; i < 4; ++i) for (int j = 0; j < 4; ++j) d[i][j] = 0;
+    double qn = u * nx + v * ny;
+    d[0][0] = qn - c; d[1][1] = qn; d[2][2] = qn + c; d[3][3] = qn;
+}
+static void right_eigen(M4 d, double c, double u, double nx, double v, double ny, double H) {
+    double qn = u * nx + v * ny, q2 = u * u + v * v;
+    double lx = -ny, ly = nx;
+    double ql = u * lx + v * ly;
+    d[0][0] = 1.0;         d[0][1] = 1.0;    d[0][2] = 1.0;         d[0][3] = 0.0;
+    d[1][0] = u - c * nx;  d[1][1] = u;      d[1][2] = u + c * nx;  d[1][3] = lx;
+    d[2][0] = v - c * ny;  d[2][1] = v;      d[2][2] = v + c * ny;  d[2][3] = ly;
+    d[3][0] = H - qn * c;  d[3][1] = q2 / 2; d[3][2] = H + qn * c;  d[3][3] = ql;
+}
+static void left_eigen(M4 d, double c, double GAM, double u, double nx, double v, double ny) {
+    double qn = u * nx + v * ny, q2 = u * u + v * v;
+    double lx = -ny, ly = nx;
+    double ql = u * lx + v * ly;
+    double g1 = GAM - 1.0, c2 = c * c;
+    d[0][0] = 0.5 * (0.5 * q2 * g1 / c2 + qn / c); d[0][1] = -0.5 * (g1 * u / c2 + nx / c);
+    d[0][2] = -0.5 * (g1 * v / c2 + ny / c);      d[0][3] = 0.5 * g1 / c2;
+    d[1][0] = 1 - 0.5 * q2 * g1 / c2;             d[1][1] = g1 * u / c2;
+    d[1][2] = g1 * v / c2;                        d[1][3] = -g1 / c2;
+    d[2][0] = 0.5 * (0.5 * q2 * g1 / c2 - qn / c); d[2][1] = -0.5 * (g1 * u / c2 - nx / c);
+    d[2][2] = -0.5 * (g1 * v / c2 - ny / c);      d[2][3] = 0.5 * g1 / c2;
+    d[3][0] = -ql;                                d[3][1] = lx;
+    d[3][2] = ly;                                 d[3][3] = 0;
+}
+/* calcAP / calcAM, :358-392: 0.5 R diag(max(lam,0)) L, 0.5 R diag(min(lam,0)) L */
+static void calc_apm(M4 d, M4 R, M4 E, M4 L, int plus) {
+    M4 t;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            d[i][j] = plus ? (E[i][j] > 0 ? E[i][j] : 0) : (E[i][j] < 0 ? E[i][j] : 0);
+    mult4(t, R, d);
+    mult4(d, t, L);
+    for (int i = 0; i < 4; ++i) for (int j = 0; j < 4; ++j) d[i][j] *= 0.5;
+}
+
+/* A+ and A- of face normal (nx, ny), times l */
+static void jacobians(const Par* a, double GAM, double nx, double ny, double l, M4 AP, M4 AM) {
+    M4 E, R, L;
+    double H = a->E + a->p / a->r;
+    eigen_values(E, a->cz, a->u, nx, a->v, ny);
+    right_eigen(R, a->cz, a->u, nx, a->v, ny, H);
+    left_eigen(L, a->cz, GAM, a->u, nx, a->v, ny);
+    calc_apm(AP, R, E, L, 1);
+    calc_apm(AM, R, E, L, 0);
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) { AM[i][j] *= l; AP[i][j] *= l; }
+}
+
+static void blk_add(double* b, M4 a) { for (int i = 0; i < 4; i++) for (int j = 0; j < 4; j++) b[4 * i + j] += a[i][j]; }
+static int face_slot(const orc_mesh* m, int c, int e) {
+    for (int k = 0; k < 3; k++) if (m->cedges[3 * c + k] == e) return k;
+    return -1;
+}
+
+/* calcFlux, :905-961 */
+static int imp_flux(const orc_imp* s, double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
+    if (s->p.flux == ORC_FLUX_LAX) { flux_lax(f, pL, pR, nx, ny, GAM); return 0; }
+    return flux_godunov(f, pL, pR, nx, ny, GAM, s->p.newton_cap);
+}
+
+/* The edge loop of FVM_TVD_IMPLICIT::run, :529-646, and the diagonal of :655-673. */
+static void imp_assemble(orc_imp* s) {
+    const orc_mesh* m = s->m;
+    int nc = m->nc;
+    const double GAM = 1.4; /* __GAM, :527 */
+    memset(s->diag, 0, sizeof(double) * 16 * (size_t)nc);
+    memset(s->off, 0, sizeof(double) * 48 * (size_t)nc);
+    memset(s->rhs, 0, sizeof(double) * 4 * (size_t)nc);
+    memset(s->tmpArr, 0, sizeof(double) * (size_t)nc);
+    imp_calc_grad(s);
+    for (int e = 0; e < m->ne; e++) {
+        int c1 = m->c1[e], c2 = m->c2[e];
+        double l = m->l[e], nx = m->nx[e], ny = m->ny[e];
+        Par cellL, cellR, avg;
+        imp_centre_states(s, e, &cellL, &cellR);
+        roe_average(&avg, &cellL, &cellR, GAM);
+        if (s->p.steady) {
+            double lambda = sqrt(avg.u * avg.u + avg.v * avg.v) + avg.cz;
+            lambda *= l;
+            s->tmpArr[c1] += lambda;
+            if (c2 >= 0) s->tmpArr[c2] += lambda;
+        }
+        M4 AP, AM;
+        jacobians(&avg, GAM, nx, ny, l, AP, AM);
+        blk_add(s->diag + 16 * (size_t)c1, AP);
+        if (c2 >= 0) {
+            blk_add(s->off + 48 * (size_t)c1 + 16 * face_slot(m, c1, e), AM);
+            jacobians(&avg, GAM, -nx, -ny, l, AP, AM);
+            blk_add(s->diag + 16 * (size_t)c2, AP);
+            blk_add(s->off + 48 * (size_t)c2 + 16 * face_slot(m, c2, e), AM);
+        }
+        /* the flux of the centre states (:600-601) is computed by the reference and unused */
+        double fr = 0.0, fu = 0.0, fv = 0.0, fe = 0.0;
+        for (int gp = 1; gp < m->npts[e]; ++gp) {
+            double f[4];
+            imp_point_states(s, e, gp, &cellL, &cellR);
+            s->newton_hit |= imp_flux(s, f, &cellL, &cellR, nx, ny, GAM);
+            fr += f[0]; fu += f[1]; fv += f[2]; fe += f[3];
+        }
+        double* b1 = s->rhs + 4 * (size_t)c1;
+        b1[0] -= 0.5 * l * fr; b1[1] -= 0.5 * l * fu; b1[2] -= 0.5 * l * fv; b1[3] -= 0.5 * l * fe;
+        if (c2 >= 0) {
+            double* b2 = s->rhs + 4 * (size_t)c2;
+            b2[0] += 0.5 * l * fr; b2[1] += 0.5 * l * fu; b2[2] += 0.5 * l * fv; b2[3] += 0.5 * l * fe;
+        }
+    }
+    if (s->p.steady)
+        for (int i = 0; i < nc; i++) s->cTau[i] = 2.0 * s->CFL * m->S[i] / (s->tmpArr[i] + 1.0e-100);
+    for (int i = 0; i < nc; i++) {
+        M4 d;
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) d[a][b] = a == b ? m->S[i] / s->cTau[i] : 0.0;
+        blk_add(s->diag + 16 * (size_t)i, d);
+    }
+}
+
+/* y = A x of the block system: per cell its diagonal block, then its faces' blocks in order */
+static void block_matvec(int nc, const int* nbr, const double* diag, const double* off, const double* x, double* y) {
+    for (int c = 0; c < nc; c++)
+        for (int i = 0; i < 4; i++) {
+            double sum = 0.0;
+            const double* d = diag + 16 * (size_t)c + 4 * i;
+            for (int j = 0; j < 4; j++) sum += d[j] * x[4 * (size_t)c + j];
+            for (int k = 0; k < 3; k++) {
+                int nb = nbr[3 * (size_t)c + k];
+                if (nb < 0) continue;
+                const double* o = off + 48 * (size_t)c + 16 * k + 4 * i;
+                for (int j = 0; j < 4; j++) sum += o[j] * x[4 * (size_t)nb + j];
+            }
+            y[4 * (size_t)c + i] = sum;
+        }
+}
+
+static double vdot(size_t n, const double* a, const double* b) {
+    double s = 0.0;
+    for (size_t i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
+int orc_gmres_block(int nc, const int* nbr, const double* diag, const double* off, const double* b, double* x,
+                    double eps, int maxit, int kdim, int* iters, double* final_rel) {
+    size_t n = 4 * (size_t)nc;
+    int m = kdim < 1 ? 1 : kdim;
+    double* V = (double*)calloc(n * (size_t)(m + 1), sizeof(double));
+    double* w = (double*)malloc(sizeof(double) * (n ? n : 1));
+    double* H = (double*)calloc((size_t)(m + 1) * m, sizeof(double)); /* H[i*m + j] */
+    double* cs = (double*)calloc((size_t)m, sizeof(double));
+    double* sn = (double*)calloc((size_t)m, sizeof(double));
+    double* g = (double*)calloc((size_t)m + 1, sizeof(double));
+    double* y = (double*)calloc((size_t)m, sizeof(double));
+    memset(x, 0, sizeof(double) * n);
+    double bnorm = sqrt(vdot(n, b, b));
+    double epsilon = eps * bnorm;
+    int it = 0, status = 0;
+    double rnorm = bnorm;
+    memcpy(w, b, sizeof(double) * n); /* r0 = b - A 0 */
+    if (bnorm > 0.0) {
+        for (;;) { /* restart cycles */
+            double beta = sqrt(vdot(n, w, w));
+            rnorm = beta;
+            if (beta <= epsilon || it >= maxit) break;
+            for (size_t q = 0; q < n; q++) V[q] = w[q] / beta;
+            memset(g, 0, sizeof(double) * (size_t)(m + 1));
+            g[0] = beta;
+            int j = 0;
+            for (; j < m && it < maxit; j++) {
+                it++;
+                double* vj1 = V + n * (size_t)(j + 1);
+                block_matvec(nc, nbr, diag, off, V + n * (size_t)j, vj1);
+                for (int i = 0; i <= j; i++) { /* modified Gram-Schmidt */
+                    double h = vdot(n, vj1, V + n * (size_t)i);
+                    H[i * m + j] = h;
+                    for (size_t q = 0; q < n; q++) vj1[q] -= h * V[n * (size_t)i + q];
+                }
+                double hn = sqrt(vdot(n, vj1, vj1));
+                H[(j + 1) * m + j] = hn;
+                if (hn != 0.0) for (size_t q = 0; q < n; q++) vj1[q] /= hn;
+                for (int i = 0; i < j; i++) { /* previous rotations */
+                    double a = H[i * m + j], c = H[(i + 1) * m + j];
+                    H[i * m + j] = cs[i] * a + sn[i] * c;
+                    H[(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+                }
+                double a = H[j * m + j], c = H[(j + 1) * m + j];
+                double r = sqrt(a * a + c * c);
+                if (r == 0.0) { cs[j] = 1.0; sn[j] = 0.0; }
+                else { cs[j] = a / r; sn[j] = c / r; }
+                H[j * m + j] = cs[j] * a + sn[j] * c;
+                H[(j + 1) * m + j] = 0.0;
+                g[j + 1] = -sn[j] * g[j];
+                g[j] = cs[j] * g[j];
+                rnorm = fabs(g[j + 1]);
+                if (rnorm <= epsilon) { j++; break; }
+            }
+            for (int i = j - 1; i >= 0; i--) { /* back substitution */
+                double sum = g[i];
+                for (int k = i + 1; k < j; k++) sum -= H[i * m + k] * y[k];
+                y[i] = sum / H[i * m + i];
+            }
+            for (int i = 0; i < j; i++)
+                for (size_t q = 0; q < n; q++) x[q] += y[i] * V[n * (size_t)i + q];
+            block_matvec(nc, nbr, diag, off, x, w); /* the true residual */
+            for (size_t q = 0; q < n; q++) w[q] = b[q] - w[q];
+            rnorm = sqrt(vdot(n, w, w));
+            if (rnorm <= epsilon || it >= maxit) break;
+        }
+    }
+    double rel = bnorm > 0.0 ? rnorm / bnorm : 0.0;
+    if (it >= maxit) status |= ORC_SOLVE_MAX_ITER;
+    if (rel >= eps || !isfinite(rel)) status |= ORC_SOLVE_CONVERG;
+    if (iters) *iters = it;
+    if (final_rel) *final_rel = rel;
+    free(V); free(w); free(H); free(cs); free(sn); free(g); free(y);
+    return status;
+}
+
+/* smoothingDelta, :818-837 */
+static void imp_smoothing(orc_imp* s, double* p) {
+    const orc_mesh* m = s->m;
+    for (int shift = 0; shift < 4; shift++) {
+        memset(s->tmpArr, 0, sizeof(double) * (size_t)m->nc);
+        memset(s->tmpArrInt, 0, sizeof(int) * (size_t)m->nc);
+        for (int e = 0; e < m->ne; e++) {
+            if (m->c2[e] >= 0) {
+                int c1 = m->c1[e], c2 = m->c2[e];
+                if (!(s->flag[c2] & 0x2u)) { s->tmpArr[c1] += p[c2 * 4 + shift]; s->tmpArrInt[c1]++; }
+                if (!(s->flag[c1] & 0x2u)) { s->tmpArr[c2] += p[c1 * 4 + shift]; s->tmpArrInt[c2]++; }
+            }
+        }
+        for (int i = 0; i < m->nc; i++) {
+            int q = i * 4 + shift;
+            p[q] = (p[q] + s->p.smoothing_par * s->tmpArr[i]) / (1.0 + s->p.smoothing_par * s->tmpArrInt[i]);
+        }
+    }
+}
+
+/* FVM_TVD_IMPLICIT::remediateLimCells, :764-800 */
+static void imp_remediate(orc_imp* s) {
+    const orc_mesh* m = s->m;
+    for (int i = 0; i < m->nc; i++) {
+        if (!(s->flag[i] & 0x2u)) continue;
+        double sRO = 0.0, sRU = 0.0, sRV = 0.0, sRE = 0.0, S = 0.0;
+        for (int k = 0; k < 3; k++) {
+            int e = m->cedges[3 * i + k];
+            int j = m->c2[e];
+            if (j == i) j = m->c1[e];
+            if (j >= 0) {
+                double sj = m->S[j];
+                S += sj;
+                sRO += s->ro[j] * sj; sRU += s->ru[j] * sj; sRV += s->rv[j] * sj; sRE += s->re[j] * sj;
+            }
+        }
+        if (S >= s->p.tau_xml * s->p.tau_xml) {
+            s->ro[i] = sRO / S; s->ru[i] = sRU / S; s->rv[i] = sRV / S; s->re[i] = sRE / S;
+        }
+        s->flag[i] += 0x010000u;
+        if (s->flag[i] & 0x200000u) s->flag[i] &= 0x001110u;
+    }
+}
+
+static void imp_dec_cfl(orc_imp* s) { /* :1065-1072 */
+    if (s->CFL > 0.1) { s->CFL *= 0.75; if (s->CFL < 0.1) s->CFL = 0.1; }
+}
+static void imp_inc_cfl(orc_imp* s) { /* :1074-1081 */
+    if (s->CFL < s->p.cfl_max) { s->CFL *= s->p.cfl_scale; if (s->CFL > s->p.cfl_max) s->CFL = s->p.cfl_max; }
+}
+
+int orc_imp_create(const orc_mesh* m, const orc_imp_params* prm, int nm, const double* mat, const int* cell_mat,
+                   int nbnd, const int* bnd_kind, const double* bnd_par, const double* U0, orc_imp** out) {
+    orc_imp* s = (orc_imp*)calloc(1, sizeof(orc_imp));
+    int nc = m->nc;
+    s->m = m; s->p = *prm; s->nm = nm; s->nbnd = nbnd;
+    s->matM = dalloc(nm); s->matCp = dalloc(nm);
+    for (int k = 0; k < nm; k++) { s->matM[k] = mat[2 * k]; s->matCp[k] = mat[2 * k + 1]; }
+    s->cell_mat = (int*)malloc(sizeof(int) * (size_t)(nc > 0 ? nc : 1));
+    memcpy(s->cell_mat, cell_mat, sizeof(int) * (size_t)nc);
+    s->bkind = (int*)malloc(sizeof(int) * (size_t)(nbnd > 0 ? nbnd : 1));
+    s->bpar = dalloc(4 * nbnd);
+    if (nbnd) { memcpy(s->bkind, bnd_kind, sizeof(int) * nbnd); memcpy(s->bpar, bnd_par, sizeof(double) * 4 * nbnd); }
+    s->ro = dalloc(nc); s->ru = dalloc(nc); s->rv = dalloc(nc); s->re = dalloc(nc);
+    s->grad = dalloc(8 * nc);
+    s->cTau = dalloc(nc);
+    s->tmpArr = dalloc(nc);
+    s->tmpArrInt = (int*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(int));
+    s->flag = (unsigned*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(unsigned));
+    s->diag = dalloc(16 * nc); s->off = dalloc(48 * nc); s->rhs = dalloc(4 * nc); s->x = dalloc(4 * nc);
+    s->nbr = (int*)malloc(sizeof(int) * 3 * (size_t)(nc > 0 ? nc : 1));
+    for (int c = 0; c < nc; c++)
+        for (int k = 0; k < 3; k++) {
+            int e = m->cedges[3 * c + k];
+            int j = m->c1[e] == c ? m->c2[e] : m->c1[e];
+            s->nbr[3 * c + k] = j;
+        }
+    for (int e = 0; e < m->ne; e++)
+        if (m->c2[e] < 0 && (m->bnd[e] < 0 || m->bnd[e] >= nbnd)) { orc_imp_free(s); return -1; }
+    orc_imp_set_state(s, U0);
+    s->CFL = prm->cfl;
+    if (!prm->steady) for (int i = 0; i < nc; i++) s->cTau[i] = prm->tau_xml; /* calcTimeStep, :301-307 */
+    *out = s;
+    return 0;
+}
+
+void orc_imp_set_state(orc_imp* s, const double* U) {
+    int nc = s->m->nc;
+    memcpy(s->ro, U, sizeof(double) * nc);
+    memcpy(s->ru, U + nc, sizeof(double) * nc);
+    memcpy(s->rv, U + 2 * (size_t)nc, sizeof(double) * nc);
+    memcpy(s->re, U + 3 * (size_t)nc, sizeof(double) * nc);
+}
+
+void orc_imp_get_state(const orc_imp* s, double* U, double* ctau, unsigned* flags) {
+    int nc = s->m->nc;
+    if (U) {
+        memcpy(U, s->ro, sizeof(double) * nc);
+        memcpy(U + nc, s->ru, sizeof(double) * nc);
+        memcpy(U + 2 * (size_t)nc, s->rv, sizeof(double) * nc);
+        memcpy(U + 3 * (size_t)nc, s->re, sizeof(double) * nc);
+    }
+    if (ctau) memcpy(ctau, s->cTau, sizeof(double) * nc);
+    if (flags) memcpy(flags, s->flag, sizeof(unsigned) * nc);
+}
+
+void orc_imp_system(orc_imp* s, double* diag, double* off, double* rhs, double* ctau) {
+    int nc = s->m->nc;
+    imp_assemble(s);
+    if (diag) memcpy(diag, s->diag, sizeof(double) * 16 * (size_t)nc);
+    if (off) memcpy(off, s->off, sizeof(double) * 48 * (size_t)nc);
+    if (rhs) memcpy(rhs, s->rhs, sizeof(double) * 4 * (size_t)nc);
+    if (ctau) memcpy(ctau, s->cTau, sizeof(double) * nc);
+}
+
+/* Apply the update of a solved system: :680-708, then remediation and the CFL rules. */
+static void imp_apply(orc_imp* s, const double* dx) {
+    const orc_mesh* m = s->m;
+    const double GAM = 1.4;
+    for (int c = 0, ind = 0; c < m->nc; c++, ind += 4) {
+        if (s->flag[c] & 0x2u) continue;
+        s->ro[c] += dx[ind + 0]; s->ru[c] += dx[ind + 1];
+        s->rv[c] += dx[ind + 2]; s->re[c] += dx[ind + 3];
+        Par par; imp_cons2par(s, c, &par);
+        if (par.r > s->p.lim_rmax) { par.r = s->p.lim_rmax; s->flag[c] |= 0x2u; }
+        if (par.r < s->p.lim_rmin) { par.r = s->p.lim_rmin; s->flag[c] |= 0x2u; }
+        if (fabs(par.u) > s->p.lim_umax) { par.u = s->p.lim_umax * par.u / fabs(par.u); s->flag[c] |= 0x2u; }
+        if (fabs(par.v) > s->p.lim_umax) { par.v = s->p.lim_umax * par.v / fabs(par.v); s->flag[c] |= 0x2u; }
+        if (par.p > s->p.lim_pmax) { par.p = s->p.lim_pmax; s->flag[c] |= 0x2u; }
+        if (par.p < s->p.lim_pmin) { par.p = s->p.lim_pmin; s->flag[c] |= 0x2u; }
+        if (s->flag[c] & 0x2u) { par.e = par.p / ((GAM - 1) * par.r); imp_par2cons(s, c, &par); }
+    }
+    imp_remediate(s);
+}
+
+int orc_imp_lim_count(const orc_imp* s) {
+    int n = 0;
+    for (int i = 0; i < s->m->nc; i++) if (s->flag[i] & 0x2u) n++;
+    return n;
+}
+
+/* nsteps passes of the loop body of FVM_TVD_IMPLICIT::run, :517-733 */
+int orc_imp_step(orc_imp* s, int nsteps) {
+    s->newton_hit = 0;
+    for (int k = 0; k < nsteps; k++) {
+        if (!s->p.steady) s->t += s->p.tau_xml;
+        if (!s->solverErr) s->step++;
+        imp_assemble(s);
+        int iters = 0; double rel = 0.0;
+        s->solverErr = orc_gmres_block(s->m->nc, s->nbr, s->diag, s->off, s->rhs, s->x, s->p.gmres_eps,
+                                       s->p.gmres_maxit, s->p.gmres_kdim, &iters, &rel);
+        s->last_iters = iters; s->last_rel = rel; s->last_status = s->solverErr;
+        if (s->solverErr == 0) {
+            if (s->p.smoothing) imp_smoothing(s, s->x);
+            imp_apply(s, s->x);
+            int lim = orc_imp_lim_count(s);
+            if (s->p.steady && lim >= s->p.max_lim_cells) imp_dec_cfl(s);
+            if (s->p.steady && s->p.cfl_step > 0 && s->step % s->p.cfl_step == 0) imp_inc_cfl(s);
+        } else {
+            if (s->p.steady) imp_dec_cfl(s);
+            else s->solverErr = 0;
+        }
+    }
+    return s->newton_hit;
+}
+
+void orc_imp_info(const orc_imp* s, double* t, double* cfl, int* step, int* iters, double* rel, int* status) {
+    if (t) *t = s->t;
+    if (cfl) *cfl = s->CFL;
+    if (step) *step = s->step;
+    if (iters) *iters = s->last_iters;
+    if (rel) *rel = s->last_rel;
+    if (status) *status = s->last_status;
+}
+
+void orc_imp_free(orc_imp* s) {
+    if (!s) return;
+    free(s->matM); free(s->matCp); free(s->cell_mat); free(s->bkind); free(s->bpar);
+    free(s->ro); free(s->ru); free(s->rv); free(s->re);
+    free(s->grad); free(s->cTau); free(s->tmpArr); free(s->tmpArrInt); free(s->flag);
+    free(s->diag); free(s->off); free(s->rhs); free(s->x); free(s->nbr);
     free(s);
 }

@@ -14,6 +14,13 @@
  * explicit Euler, SSP-RK3) reuse the same structure, conventions and ghost
  * states; their formulas are the published ones named at each function.
  *
+ * The implicit method (orc_imp_*) is pinned the same way against the reference's
+ * FVM_TVD_IMPLICIT compiled from its sources (oracle/ref/ref_implicit.cpp), which
+ * needs a matrix solver in place of HYPRE (absent from the reference tree): both
+ * sides then use orc_gmres_block, and the assembled systems, updates, limits,
+ * remediation and CFL control agree bit for bit. The GMRES itself follows the
+ * published algorithm (parity unpinned against HYPRE's own code).
+ *
  * Arithmetic order follows the reference expression by expression; build with
  * -ffp-contract=off so no multiply-add is fused.
  */
@@ -42,9 +49,11 @@ typedef struct {
 
 /* Edge structure by the Salome-UNV reader's rules (3 points per edge: midpoint +
  * 2 Gauss points; normals flipped outward from c1), or by the Berkeley-Triangle
- * reader's rules when berkeley != 0 (1 point per edge, neighbour j opposite node j
- * taken from neigh[], no flip). bseg: nb node pairs, bseg_bnd: their boundary
- * index. Returns 0 or a negative error. */
+ * reader's rules when berkeley == 1 (1 point per edge, neighbour j opposite node j
+ * taken from neigh[], no flip), or by Grid::initFromFiles (src/mesh/grid.cpp:51-252,
+ * the loader of FVM_TVD_IMPLICIT) when berkeley == 2: the Triangle topology with
+ * the midpoint and 2 Gauss points per edge. bseg: nb node pairs, bseg_bnd: their
+ * boundary index. Returns 0 or a negative error. */
 int orc_mesh_build(int nn, const double* xy, int nc, const int* tri, const int* neigh_berkeley,
                    int nb, const int* bseg, const int* bseg_bnd, int berkeley, orc_mesh** out);
 void orc_mesh_sizes(const orc_mesh* m, int* nc, int* ne);
@@ -71,6 +80,50 @@ void orc_set_state(orc_solver* s, const double* U4);
  * reference's ro_int..re_int after the edge loop), 4 x nc. */
 void orc_residual(orc_solver* s, double* R4);
 void orc_solver_free(orc_solver* s);
+
+/* ---------------------------------------------------------------- FVM_TVD_IMPLICIT
+ * Restatement of src/methods/fvm_tvd_implicit.cpp: Roe-linearised block system per
+ * step, GMRES, smoothing, update with limits, remediation, CFL control. Boundary
+ * kinds are the implicit method's own (Boundary::BOUND_*, par = T, P, Vx, Vy). */
+enum { ORC_IBND_INLET = 1, ORC_IBND_OUTLET = 2, ORC_IBND_WALL = 3 };
+/* MatrixSolver::RESULT_*, src/methods/solvers/MatrixSolver.h:13-16 */
+enum { ORC_SOLVE_MAX_ITER = 0x2, ORC_SOLVE_CONVERG = 0x4 };
+
+typedef struct orc_imp orc_imp;
+typedef struct {
+    int flux;                /* ORC_FLUX_GODUNOV or ORC_FLUX_LAX */
+    int steady;
+    int smoothing;
+    int cfl_step;            /* <CFL><step> */
+    int gmres_maxit, gmres_kdim;
+    int newton_cap;
+    int pad;
+    double tau_xml;
+    double cfl, cfl_scale, cfl_max, max_lim_cells;  /* <CFL> start, scale, max, max_limited_cells */
+    double smoothing_par;
+    double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
+    double gmres_eps;
+} orc_imp_params;
+
+/* The mesh must come from orc_mesh_build(..., berkeley = 2) for the reference's
+ * loader; every boundary edge needs a boundary index < nbnd (else -1). */
+int orc_imp_create(const orc_mesh* m, const orc_imp_params* prm, int nm, const double* mat, const int* cell_mat,
+                   int nbnd, const int* bnd_kind, const double* bnd_par, const double* U0, orc_imp** out);
+/* nsteps passes of run()'s loop body; returns 1 if the Newton cap was hit */
+int orc_imp_step(orc_imp* s, int nsteps);
+void orc_imp_get_state(const orc_imp* s, double* U4, double* ctau, unsigned* flags);
+void orc_imp_set_state(orc_imp* s, const double* U4);
+/* The block system of the current state: per cell its diagonal block (16, row
+ * major), its three faces' off-diagonal blocks in Cell::edgesInd order (48; zero
+ * on boundary faces) and right-hand side (4); cTau as used for the diagonal. */
+void orc_imp_system(orc_imp* s, double* diag, double* off, double* rhs, double* ctau);
+int orc_imp_lim_count(const orc_imp* s);
+void orc_imp_info(const orc_imp* s, double* t, double* cfl, int* step, int* iters, double* rel, int* status);
+void orc_imp_free(orc_imp* s);
+/* GMRES(kdim) on the block system (nbr: nc x 3, -1 on boundary faces), x0 = 0;
+ * returns ORC_SOLVE_* bits like MatrixSolver::solve. */
+int orc_gmres_block(int nc, const int* nbr, const double* diag, const double* off, const double* b, double* x,
+                    double eps, int maxit, int kdim, int* iters, double* final_rel);
 
 #ifdef __cplusplus
 }

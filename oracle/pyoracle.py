@@ -15,11 +15,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "build", "libcfd2d_oracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "ref_fvm_tvd")
+REF_IMP_BIN = os.path.join(HERE, "_ref", "ref_fvm_tvd_implicit")
 
 FLUX = {"GODUNOV": 0, "LAX": 1, "ROE": 2, "HLLC": 3}
 RECON = {"NONE": 0, "LINEAR": 1, "MINMOD": 2}
 TIME = {"EULER": 0, "HEUN": 1, "SSPRK3": 2}
 BND = {"BOUND_INLET": 1, "BOUND_OUTLET": 2, "BOUND_WALL_SLIP": 3, "BOUND_WALL_NO_SLIP": 4}
+IBND = {"BOUND_INLET": 1, "BOUND_OUTLET": 2, "BOUND_WALL": 3}
 
 
 class Params(C.Structure):
@@ -28,6 +30,15 @@ class Params(C.Structure):
                 ("tau_xml", C.c_double), ("cfl", C.c_double),
                 ("lim_rmin", C.c_double), ("lim_rmax", C.c_double), ("lim_pmin", C.c_double),
                 ("lim_pmax", C.c_double), ("lim_umax", C.c_double), ("gam_flux", C.c_double)]
+
+
+class ImpParams(C.Structure):
+    _fields_ = [("flux", C.c_int), ("steady", C.c_int), ("smoothing", C.c_int), ("cfl_step", C.c_int),
+                ("gmres_maxit", C.c_int), ("gmres_kdim", C.c_int), ("newton_cap", C.c_int), ("pad", C.c_int),
+                ("tau_xml", C.c_double), ("cfl", C.c_double), ("cfl_scale", C.c_double), ("cfl_max", C.c_double),
+                ("max_lim_cells", C.c_double), ("smoothing_par", C.c_double),
+                ("lim_rmin", C.c_double), ("lim_rmax", C.c_double), ("lim_pmin", C.c_double),
+                ("lim_pmax", C.c_double), ("lim_umax", C.c_double), ("gmres_eps", C.c_double)]
 
 
 def build(quiet: bool = True) -> str:
@@ -61,6 +72,15 @@ def lib():
         L.orc_set_state.argtypes = [P, D]
         L.orc_residual.argtypes = [P, D]
         L.orc_solver_free.argtypes = [P]
+        L.orc_imp_create.argtypes = [P, C.POINTER(ImpParams), I, D, IP, I, IP, D, D, C.POINTER(P)]
+        L.orc_imp_step.argtypes = [P, I]
+        L.orc_imp_get_state.argtypes = [P, D, D, U]
+        L.orc_imp_set_state.argtypes = [P, D]
+        L.orc_imp_system.argtypes = [P, D, D, D, D]
+        L.orc_imp_lim_count.argtypes = [P]
+        L.orc_imp_info.argtypes = [P, D, D, IP, IP, D, IP]
+        L.orc_imp_free.argtypes = [P]
+        L.orc_gmres_block.argtypes = [I, IP, D, D, D, D, C.c_double, I, I, IP, D]
         _lib = L
     return _lib
 
@@ -76,7 +96,7 @@ def _i(a):
 class OracleMesh:
     """Edge structure built by the reference's reader rules (see cfd2d_oracle.h)."""
 
-    def __init__(self, nodes, tris, bsegs, bseg_bnd, berkeley_neigh=None):
+    def __init__(self, nodes, tris, bsegs, bseg_bnd, berkeley_neigh=None, legacy=False):
         L = lib()
         self.nodes = np.ascontiguousarray(nodes, np.float64)
         self.tris = np.ascontiguousarray(tris, np.int32)
@@ -86,7 +106,7 @@ class OracleMesh:
         h = C.c_void_p()
         rc = L.orc_mesh_build(len(self.nodes), _d(self.nodes), len(self.tris), _i(self.tris),
                               _i(nb) if nb is not None else None, len(bs), _i(bs), _i(bb),
-                              1 if nb is not None else 0, C.byref(h))
+                              (2 if legacy else 1) if nb is not None else 0, C.byref(h))
         if rc != 0:
             raise RuntimeError(f"oracle mesh build failed ({rc})")
         self.h = h
@@ -167,6 +187,113 @@ class OracleSolver:
         if getattr(self, "h", None) and _lib is not None:
             _lib.orc_solver_free(self.h)
             self.h = None
+
+
+class OracleImplicit:
+    """The oracle's FVM_TVD_IMPLICIT (orc_imp_* in cfd2d_oracle.c)."""
+
+    def __init__(self, mesh: OracleMesh, *, flux="LAX", steady=0, tau=1e-3, cfl=(1.0, 1.0, 1.0, 1000000, 1e9),
+                 smoothing=(0, 0.0), limits=(1e-8, 1e8, 1e-8, 1e8, 1e8), gmres=(1e-7, 20, 30), newton_cap=1000,
+                 materials=((8.314472, 3.5),), cell_mat=None, bnd_kind=(), bnd_par=None, U0=None):
+        L = lib()
+        self.mesh = mesh
+        start, scale, cmax, cstep, maxlim = cfl
+        p = ImpParams(FLUX[flux], int(steady), int(smoothing[0]), int(cstep), int(gmres[1]), int(gmres[2]),
+                      int(newton_cap), 0, float(tau), float(start), float(scale), float(cmax), float(maxlim),
+                      float(smoothing[1]), *[float(x) for x in limits], float(gmres[0]))
+        mat = np.ascontiguousarray(np.asarray(materials, np.float64).reshape(-1, 2))
+        cm = np.ascontiguousarray(np.zeros(mesh.nc, np.int32) if cell_mat is None else cell_mat, np.int32)
+        bk = np.ascontiguousarray([IBND[k] if isinstance(k, str) else int(k) for k in bnd_kind], np.int32)
+        bp = np.ascontiguousarray(np.zeros((len(bk), 4)) if bnd_par is None else bnd_par, np.float64)
+        U = np.ascontiguousarray(U0, np.float64).reshape(4, mesh.nc)
+        h = C.c_void_p()
+        rc = L.orc_imp_create(mesh.h, C.byref(p), len(mat), _d(mat), _i(cm), len(bk),
+                              _i(bk) if len(bk) else None, _d(bp), _d(U), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"oracle implicit create failed ({rc})")
+        self.h = h
+
+    def step(self, n: int) -> int:
+        return lib().orc_imp_step(self.h, int(n))
+
+    def state(self):
+        nc = self.mesh.nc
+        U = np.zeros((4, nc)); ct = np.zeros(nc); fl = np.zeros(nc, np.uint32)
+        lib().orc_imp_get_state(self.h, _d(U), _d(ct), fl.ctypes.data_as(C.POINTER(C.c_uint)))
+        return U, ct, fl
+
+    def set_state(self, U):
+        lib().orc_imp_set_state(self.h, _d(np.ascontiguousarray(U, np.float64)))
+
+    def system(self):
+        nc = self.mesh.nc
+        diag = np.zeros((nc, 4, 4)); off = np.zeros((nc, 3, 4, 4)); rhs = np.zeros((nc, 4)); ct = np.zeros(nc)
+        lib().orc_imp_system(self.h, _d(diag), _d(off), _d(rhs), _d(ct))
+        return diag, off, rhs, ct
+
+    def info(self) -> dict:
+        t, cfl, rel = C.c_double(), C.c_double(), C.c_double()
+        step, it, st = C.c_int(), C.c_int(), C.c_int()
+        lib().orc_imp_info(self.h, C.byref(t), C.byref(cfl), C.byref(step), C.byref(it), C.byref(rel), C.byref(st))
+        return dict(t=t.value, cfl=cfl.value, step=step.value, iters=it.value, rel=rel.value, status=st.value,
+                    n_lim=lib().orc_imp_lim_count(self.h))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_imp_free(self.h)
+            self.h = None
+
+
+def implicit_from_task(task, mesh, omesh: OracleMesh | None = None, U0=None, **over) -> OracleImplicit:
+    """Oracle implicit solver configured like FVM_TVD_IMPLICIT::init from ``task`` (an ImplicitTask);
+    ``mesh.cell_region`` indexes task.regions, ``mesh.bseg_bnd`` task.boundaries."""
+    from cfd2d import meshgen
+    if omesh is None:  # .neigh as the loader holds it: 0-based, -2 for none
+        nb = meshgen.triangle_neighbours(mesh.tris)
+        omesh = OracleMesh(mesh.nodes, mesh.tris, mesh.bsegs, mesh.bseg_bnd,
+                           berkeley_neigh=np.where(nb >= 0, nb, -2), legacy=True)
+    mats = [(m[1], m[2]) for m in task.materials]
+    cell_mat = np.asarray([r.mat for r in task.regions], np.int32)[mesh.cell_region]
+    if U0 is None:
+        reg_U = np.stack([region_state(*mats[r.mat], r.u, r.v, r.T, r.p) for r in task.regions])
+        U0 = reg_U[mesh.cell_region].T.copy()
+    bk = [b.kind for b in task.boundaries]
+    bp = np.asarray([[b.T, b.p, b.u, b.v] for b in task.boundaries], np.float64).reshape(-1, 4)
+    kw = dict(flux=task.flux, steady=task.steady, tau=task.tau, cfl=task.cfl, smoothing=task.smoothing,
+              limits=task.limits, materials=mats, cell_mat=cell_mat, bnd_kind=bk, bnd_par=bp, U0=U0)
+    kw.update(over)
+    return OracleImplicit(omesh, **kw)
+
+
+def run_reference_implicit(task_xml: str, tri_files: dict, U0=None, timeout=300, workdir=None) -> dict:
+    """Run the reference's own FVM_TVD_IMPLICIT (oracle/_ref/ref_fvm_tvd_implicit) on one case;
+    tri_files: extension -> text of mesh.node/.ele/.neigh/.poly."""
+    if not os.path.exists(REF_IMP_BIN):
+        raise FileNotFoundError(REF_IMP_BIN + " (build with: make -C oracle reference)")
+    with tempfile.TemporaryDirectory(dir=workdir) as d:
+        open(os.path.join(d, "task.xml"), "w").write(task_xml)
+        for ext, text in tri_files.items():
+            open(os.path.join(d, "mesh" + ext), "w").write(text)
+        args = [REF_IMP_BIN, "task.xml", "out"]
+        if U0 is not None:
+            np.ascontiguousarray(U0, np.float64).tofile(os.path.join(d, "init.bin"))
+            args.append("init.bin")
+        r = subprocess.run(args, cwd=d, capture_output=True, text=True, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError("reference run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+        out = {}
+        for tag in ("init", "state"):
+            raw = open(os.path.join(d, f"out.{tag}.bin"), "rb").read()
+            nc, iters = (int(x) for x in np.frombuffer(raw[:8], np.int32))
+            tau, secs, cfl, rel = np.frombuffer(raw, np.float64, 4, 16)
+            off = 48
+            U = np.frombuffer(raw, np.float64, 4 * nc, off).reshape(4, nc).copy(); off += 32 * nc
+            ct = np.frombuffer(raw, np.float64, nc, off).copy(); off += 8 * nc
+            fl = np.frombuffer(raw, np.uint32, nc, off).copy()
+            out[tag] = dict(U=U, cTau=ct, flags=fl, tau=float(tau), seconds=float(secs), cfl=float(cfl),
+                            iters=iters, rel=float(rel))
+        out["stdout"] = r.stdout
+        return out
 
 
 # ------------------------------------------------------------- task helpers
