@@ -37,11 +37,15 @@ def cuda_home() -> str:
     raise RuntimeError("nvcc not found")
 
 
-HOST_SOURCES = ["xml.cpp", "mesh.cpp", "task.cpp", "solver.cpp", "solver_adjoint.cpp", "solver_batch.cpp", "solver_tiles.cpp", "capi.cpp"]
+HOST_SOURCES = ["xml.cpp", "mesh.cpp", "task.cpp", "solver.cpp", "solver_adjoint.cpp", "solver_batch.cpp",
+                "solver_tiles.cpp", "implicit.cpp", "capi.cpp"]
+# -fmad per translation unit: "false" for the bit-exact FP64 path, "true" for the mixed form
+# (with fast math), "fma" for FMA contraction with IEEE division and square root
 DEVICE_SOURCES = {"kern_fp64.cu": "false", "kern_common.cu": "false", "kern_mixed.cu": "true",
-                  "noalloc.cu": "false", "adjoint.cu": "false", "adjoint_mixed.cu": "true"}
+                  "noalloc.cu": "false", "adjoint.cu": "false", "adjoint_mixed.cu": "true",
+                  "implicit.cu": "false", "gmres.cu": "fma"}
 HEADERS = ["xml.hpp", "mesh.hpp", "task.hpp", "solver.hpp", "kernels.hpp", "kernels.cuh", "kern_inst.cuh",
-           "adjoint.cuh", "adj_inst.cuh"]
+           "adjoint.cuh", "adj_inst.cuh", "implicit.hpp"]
 
 
 def _stale(out: str, deps) -> bool:
@@ -81,7 +85,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(out)
         if force or _stale(out, [src] + hdrs):
             extra = ["-use_fast_math"] if fmad == "true" else []
-            jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", f"-fmad={fmad}", *extra, "-Xptxas", "-v",
+            fm = "true" if fmad == "fma" else fmad
+            jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", f"-fmad={fm}", *extra, "-Xptxas", "-v",
                          "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INC, "-I", CSRC,
                          "-c", src, "-o", out])
     logs = []

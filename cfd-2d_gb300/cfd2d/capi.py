@@ -39,6 +39,11 @@ class Info(C.Structure):
                 ("device_bytes", C.c_size_t), ("n_instances", C.c_int)]
 
 
+class ImplicitStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("n_limited", C.c_int), ("pad", C.c_int),
+                ("rel_residual", C.c_double), ("cfl", C.c_double)]
+
+
 # every symbol include/cfd2d.h declares, with its ctypes signature
 _P, _I, _D = C.c_void_p, C.c_int, C.POINTER(C.c_double)
 _IP, _UP = C.POINTER(C.c_int), C.POINTER(C.c_uint)
@@ -70,6 +75,8 @@ SIGNATURES = {
     "cfd2d_load_state": [_P, C.c_char_p],
     "cfd2d_residual_first_order_static": [_I, _I, _P, _P, _P, _P, _P, _I, _IP, _D, C.c_double, C.c_double, _I,
                                           _P, _P, _P],
+    "cfd2d_implicit_system": [_P, _D, _D, _D, _D],
+    "cfd2d_implicit_stats": [_P, C.POINTER(ImplicitStats)],
     "cfd2d_selftest": [_I, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
     "cfd2d_set_device": [_I],
     "cfd2d_last_error": [C.c_char_p, C.c_size_t],
@@ -259,6 +266,18 @@ class Solver:
         ms = np.zeros(4); cnt = np.zeros(4, np.int32)
         check(lib().cfd2d_profile_steps(self.h, int(n), _d(ms), _i(cnt)))
         return ms, cnt
+
+    def implicit_system(self):
+        """FVM_TVD_IMPLICIT: (diag (nc,4,4), off (nc,3,4,4), rhs (nc,4), cTau (nc)) of the current state."""
+        nc = self.get_info().n_cells
+        diag = np.zeros((nc, 4, 4)); off = np.zeros((nc, 3, 4, 4)); rhs = np.zeros((nc, 4)); ct = np.zeros(nc)
+        check(lib().cfd2d_implicit_system(self.h, _d(diag), _d(off), _d(rhs), _d(ct)))
+        return diag, off, rhs, ct
+
+    def implicit_stats(self) -> dict:
+        st = ImplicitStats()
+        check(lib().cfd2d_implicit_stats(self.h, C.byref(st)))
+        return dict(iters=st.iterations, status=st.status, n_lim=st.n_limited, rel=st.rel_residual, cfl=st.cfl)
 
     def state_into(self, ptrs):
         """get_state into four raw host pointers (e.g. pinned buffers)."""

@@ -197,15 +197,17 @@ def triangle_neighbours(tris: np.ndarray) -> np.ndarray:
     return nb.astype(np.int32)
 
 
-def write_triangle(mesh: Mesh, bnd_markers) -> dict:
+def write_triangle(mesh: Mesh, bnd_markers, region_attr=None) -> dict:
     """Berkeley-Triangle files (.node .ele .neigh .poly), 1-based, as the reference reads them
-    (src/mesh/MeshReaderBerkleyTriangle.cpp:3-170). The .ele attribute is the region index,
-    which becomes the cell's region name ("0", "1", ...); the .poly marker of a boundary
-    segment is ``bnd_markers[bseg_bnd]`` and binds to a boundCond by its edgeType."""
+    (src/mesh/MeshReaderBerkleyTriangle.cpp:3-170). The .ele attribute is the region index
+    (or ``region_attr[cell_region]``, e.g. the implicit method's cell types), which becomes the
+    cell's region name ("0", "1", ...); the .poly marker of a boundary segment is
+    ``bnd_markers[bseg_bnd]`` and binds to a boundCond by its edgeType."""
     nn, nc = len(mesh.nodes), len(mesh.tris)
+    attr = mesh.cell_region if region_attr is None else np.asarray(region_attr)[mesh.cell_region]
     node = [f"{nn} 2 0 1"] + [f"{i + 1} {repr(float(x))} {repr(float(y))} 0" for i, (x, y) in enumerate(mesh.nodes)]
     ele = [f"{nc} 3 1"] + [f"{i + 1} {a + 1} {b + 1} {c + 1} {int(r)}"
-                           for i, ((a, b, c), r) in enumerate(zip(mesh.tris, mesh.cell_region))]
+                           for i, ((a, b, c), r) in enumerate(zip(mesh.tris, attr))]
     nb = triangle_neighbours(mesh.tris)
     neigh = [f"{nc} 3"] + [f"{i + 1} {x + 1 if x >= 0 else -1} {y + 1 if y >= 0 else -1} {z + 1 if z >= 0 else -1}"
                            for i, (x, y, z) in enumerate(nb)]

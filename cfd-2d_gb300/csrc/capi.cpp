@@ -2,6 +2,7 @@
 // returns a status code; the message of the last failure is kept per thread.
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -9,12 +10,15 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include "cfd2d.h"
+#include "implicit.hpp"
 #include "mesh.hpp"
 #include "solver.hpp"
 #include "task.hpp"
 
+// One handle: the explicit solver (s) or the implicit one (imp).
 struct cfd2d_solver {
     std::unique_ptr<cfd2d::Solver> s;
+    std::unique_ptr<cfd2d::ImplicitSolver> imp;
 };
 
 struct cfd2d_mesh {
@@ -73,6 +77,14 @@ std::string resolve(const cfd2d::TaskConfig& t, const std::string& name, const c
 void load_task_mesh(const cfd2d::TaskConfig& t, cfd2d::Topo& topo, std::vector<int>& cell_region,
                     std::vector<int>& edge_bnd, int& gauss_points) {
     cfd2d::RawMesh raw;
+    if (t.method == cfd2d::METHOD_FVM_TVD_IMPLICIT) {  // Grid::initFromFiles, src/mesh/grid.cpp:51-252
+        raw = cfd2d::read_triangle(resolve(t, t.mesh_name, ".node"));
+        gauss_points = 2;
+        topo = cfd2d::build_topology(raw.nn(), raw.xy.data(), raw.nc(), raw.tri.data(), raw.neigh.data(),
+                                     (int)raw.bseg.size() / 2, raw.bseg.data(), false, 2);
+        cfd2d::bind_mesh_implicit(t, raw, topo, cell_region, edge_bnd);
+        return;
+    }
     if (t.mesh_type == "salome_unv") {
         raw = cfd2d::read_unv(resolve(t, t.mesh_name, ""));
         gauss_points = 2;
@@ -89,6 +101,25 @@ void load_task_mesh(const cfd2d::TaskConfig& t, cfd2d::Topo& topo, std::vector<i
                                  raw.berkeley ? raw.neigh.data() : nullptr, (int)raw.bseg.size() / 2,
                                  raw.bseg.data(), !raw.berkeley, gauss_points);
     cfd2d::bind_mesh(t, raw, topo, cell_region, edge_bnd);
+}
+
+// Neighbours as the Triangle generator's .neigh lists them (neighbour j across the
+// edge opposite node j, -2 for none after the loader's decrement), from the triangles.
+std::vector<int> triangle_neigh(int nc, const int* tri) {
+    std::vector<std::pair<long long, int>> keys(3 * (size_t)nc);
+    for (int i = 0; i < nc; i++)
+        for (int j = 0; j < 3; j++) {
+            long long a = tri[3 * i + (j + 1) % 3], b = tri[3 * i + (j + 2) % 3];
+            keys[3 * (size_t)i + j] = {std::min(a, b) * (1ll << 32) + std::max(a, b), 3 * i + j};
+        }
+    std::sort(keys.begin(), keys.end());
+    std::vector<int> nb(3 * (size_t)nc, -2);
+    for (size_t q = 0; q + 1 < keys.size(); q++)
+        if (keys[q].first == keys[q + 1].first) {
+            nb[keys[q].second] = keys[q + 1].second / 3;
+            nb[keys[q + 1].second] = keys[q].second / 3;
+        }
+    return nb;
 }
 
 void check_desc(const cfd2d_mesh_desc* m) {
@@ -116,6 +147,13 @@ std::vector<int> edge_bnd_from_desc(const cfd2d_mesh_desc* m, const cfd2d::Topo&
     return eb;
 }
 
+// The explicit solver of a handle; entry points of the explicit method only fail on
+// an implicit handle.
+cfd2d::Solver& ex(const cfd2d_t* h) {
+    if (!h->s) throw cfd2d::Error(CFD2D_ERR_INVALID_ARG, "not available for the FVM_TVD_IMPLICIT method");
+    return *h->s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -131,7 +169,10 @@ int cfd2d_create(const char* task_xml_path, cfd2d_t** out) {
         int gp = 2;
         load_task_mesh(t, topo, cr, eb, gp);
         auto h = std::make_unique<cfd2d_solver>();
-        h->s = std::make_unique<cfd2d::Solver>(t, std::move(topo), cr, eb, gp);
+        if (t.method == cfd2d::METHOD_FVM_TVD_IMPLICIT)
+            h->imp = std::make_unique<cfd2d::ImplicitSolver>(t, std::move(topo), cr, eb);
+        else
+            h->s = std::make_unique<cfd2d::Solver>(t, std::move(topo), cr, eb, gp);
         *out = h.release();
         return CFD2D_OK;
     });
@@ -145,13 +186,21 @@ int cfd2d_create_with_mesh(const char* task_xml_path, const cfd2d_mesh_desc* mes
         check_desc(mesh);
         if (!mesh->cell_region) return fail(CFD2D_ERR_INVALID_ARG, "cell_region is required");
         cfd2d::TaskConfig t = cfd2d::parse_task(task_xml_path);
-        cfd2d::Topo topo = topo_from_desc(mesh, nullptr, 2);
+        const bool imp = t.method == cfd2d::METHOD_FVM_TVD_IMPLICIT;
+        std::vector<int> tn;
+        if (imp) tn = triangle_neigh(mesh->n_cells, mesh->tri);
+        cfd2d::Topo topo = topo_from_desc(mesh, imp ? tn.data() : nullptr, 2);
         std::vector<int> cr(mesh->cell_region, mesh->cell_region + mesh->n_cells);
         for (int r : cr)
             if (r < 0 || r >= (int)t.regions.size())
                 return fail(CFD2D_ERR_REGION_UNKNOWN, "cell_region refers to a missing region");
         std::vector<int> eb = edge_bnd_from_desc(mesh, topo, (int)t.bnds.size());
         auto h = std::make_unique<cfd2d_solver>();
+        if (imp) {
+            h->imp = std::make_unique<cfd2d::ImplicitSolver>(t, std::move(topo), cr, eb);
+            *out = h.release();
+            return CFD2D_OK;
+        }
         h->s = std::make_unique<cfd2d::Solver>(t, std::move(topo), cr, eb, 2);
         *out = h.release();
         return CFD2D_OK;
@@ -196,6 +245,14 @@ int cfd2d_batch_create(int n, const char* const* task_xml_paths, const cfd2d_mes
 int cfd2d_batch_instance(const cfd2d_t* h, int k, int* cell_offset, int* n_cells, double* tau, double* time) {
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        if (h->imp) {
+            if (k != 0) return fail(CFD2D_ERR_INVALID_ARG, "instance out of range");
+            if (cell_offset) *cell_offset = 0;
+            if (n_cells) *n_cells = h->imp->topo().nc;
+            if (tau) *tau = h->imp->task().tau;
+            if (time) *time = h->imp->time();
+            return CFD2D_OK;
+        }
         const cfd2d::Solver& s = *h->s;
         if (k < 0 || k >= s.n_instances()) return fail(CFD2D_ERR_INVALID_ARG, "instance out of range");
         if (!s.is_batch()) {
@@ -218,7 +275,7 @@ int cfd2d_autotune(cfd2d_t* h, const char* json_path) {
     Range r("cfd2d_autotune");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        h->s->autotune(json_path, 5);
+        ex(h).autotune(json_path, 5);
         return CFD2D_OK;
     });
 }
@@ -226,7 +283,7 @@ int cfd2d_autotune(cfd2d_t* h, const char* json_path) {
 int cfd2d_load_tuning(cfd2d_t* h, const char* json_path) {
     return guarded([&] {
         if (!h || !json_path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->load_tuning(json_path);
+        ex(h).load_tuning(json_path);
         return CFD2D_OK;
     });
 }
@@ -235,7 +292,7 @@ int cfd2d_step(cfd2d_t* h, int nsteps) {
     Range r("cfd2d_step");
     return guarded([&] {
         if (!h || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
-        int s = h->s->step(nsteps);
+        int s = h->imp ? h->imp->step(nsteps) : ex(h).step(nsteps);
         if (s != CFD2D_OK) g_err = s == CFD2D_ERR_NEWTON_CAP ? "exact Riemann solver hit its iteration cap"
                                                             : "non-positive or NaN density/pressure";
         return s;
@@ -246,7 +303,7 @@ int cfd2d_run(cfd2d_t* h) {
     Range r("cfd2d_run");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        return h->s->run();
+        return h->imp ? h->imp->run() : ex(h).run();
     });
 }
 
@@ -260,8 +317,26 @@ int cfd2d_destroy(cfd2d_t* h) {
 int cfd2d_get_info(const cfd2d_t* h, cfd2d_info_t* info) {
     return guarded([&] {
         if (!h || !info) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        const cfd2d::Solver& s = *h->s;
         std::memset(info, 0, sizeof *info);
+        if (h->imp) {
+            const cfd2d::ImplicitSolver& m = *h->imp;
+            info->n_cells = m.topo().nc;
+            info->n_edges = m.topo().ne;
+            info->n_boundary_edges = m.layout().ne - m.layout().n_int;
+            info->n_nodes = m.topo().nn;
+            info->step = m.n_steps();
+            info->flux = m.task().flux;
+            info->recon = m.task().recon;
+            info->scheme = m.task().scheme;
+            info->precision = m.task().precision;
+            info->steady = m.task().steady;
+            info->time = m.time();
+            info->tau = m.task().tau;
+            info->device_bytes = m.device_bytes();
+            info->n_instances = 1;
+            return CFD2D_OK;
+        }
+        const cfd2d::Solver& s = *h->s;
         info->n_cells = s.topo().nc;
         info->n_edges = s.topo().ne;
         info->n_boundary_edges = s.layout().ne - s.layout().n_int;
@@ -284,7 +359,8 @@ int cfd2d_get_state(cfd2d_t* h, double* ro, double* ru, double* rv, double* re) 
     Range r("cfd2d_get_state");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        h->s->get_state(ro, ru, rv, re);
+        if (h->imp) h->imp->get_state(ro, ru, rv, re);
+        else ex(h).get_state(ro, ru, rv, re);
         return CFD2D_OK;
     });
 }
@@ -294,7 +370,8 @@ int cfd2d_set_state(cfd2d_t* h, const double* ro, const double* ru, const double
     Range r("cfd2d_set_state");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        h->s->set_state(ro, ru, rv, re, reset_time_step != 0);
+        if (h->imp) h->imp->set_state(ro, ru, rv, re);
+        else ex(h).set_state(ro, ru, rv, re, reset_time_step != 0);
         return CFD2D_OK;
     });
 }
@@ -302,7 +379,8 @@ int cfd2d_set_state(cfd2d_t* h, const double* ro, const double* ru, const double
 int cfd2d_get_time_step(cfd2d_t* h, double* ctau) {
     return guarded([&] {
         if (!h || !ctau) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->get_ctau(ctau);
+        if (h->imp) h->imp->get_ctau(ctau);
+        else ex(h).get_ctau(ctau);
         return CFD2D_OK;
     });
 }
@@ -310,7 +388,8 @@ int cfd2d_get_time_step(cfd2d_t* h, double* ctau) {
 int cfd2d_get_flags(cfd2d_t* h, unsigned* flags) {
     return guarded([&] {
         if (!h || !flags) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->get_flags(flags);
+        if (h->imp) h->imp->get_flags(flags);
+        else ex(h).get_flags(flags);
         return CFD2D_OK;
     });
 }
@@ -319,7 +398,7 @@ int cfd2d_residual(cfd2d_t* h, double* R) {
     Range r("cfd2d_residual");
     return guarded([&] {
         if (!h || !R) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->residual(R);
+        ex(h).residual(R);
         return CFD2D_OK;
     });
 }
@@ -327,7 +406,7 @@ int cfd2d_residual(cfd2d_t* h, double* R) {
 int cfd2d_conservation(cfd2d_t* h, double sums[4]) {
     return guarded([&] {
         if (!h || !sums) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->conservation(sums);
+        ex(h).conservation(sums);
         return CFD2D_OK;
     });
 }
@@ -336,7 +415,8 @@ int cfd2d_save_vtk(cfd2d_t* h, int step) {
     Range r("cfd2d_save_vtk");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        h->s->save_vtk(step);
+        if (h->imp) h->imp->save_vtk(step);
+        else ex(h).save_vtk(step);
         return CFD2D_OK;
     });
 }
@@ -345,7 +425,7 @@ int cfd2d_save_state(cfd2d_t* h, const char* path) {
     Range r("cfd2d_save_state");
     return guarded([&] {
         if (!h || !path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->save_state(path);
+        ex(h).save_state(path);
         return CFD2D_OK;
     });
 }
@@ -354,7 +434,7 @@ int cfd2d_load_state(cfd2d_t* h, const char* path) {
     Range r("cfd2d_load_state");
     return guarded([&] {
         if (!h || !path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->load_state(path);
+        ex(h).load_state(path);
         return CFD2D_OK;
     });
 }
@@ -362,7 +442,7 @@ int cfd2d_load_state(cfd2d_t* h, const char* path) {
 int cfd2d_set_objective(cfd2d_t* h, int kind, const double* weights, double p_ref) {
     return guarded([&] {
         if (!h || !weights) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->set_objective(kind, weights, p_ref);
+        ex(h).set_objective(kind, weights, p_ref);
         return CFD2D_OK;
     });
 }
@@ -372,7 +452,7 @@ int cfd2d_forward(cfd2d_t* h, int nsteps, int checkpoint_every, double* J) {
     return guarded([&] {
         if (!h || !J) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
         int st = CFD2D_OK;
-        *J = h->s->forward(nsteps, checkpoint_every, &st);
+        *J = ex(h).forward(nsteps, checkpoint_every, &st);
         return st;
     });
 }
@@ -381,7 +461,7 @@ int cfd2d_backward(cfd2d_t* h, double* dJdU0, double* dJdbnd) {
     Range r("cfd2d_backward");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        h->s->backward(dJdU0, dJdbnd);
+        ex(h).backward(dJdU0, dJdbnd);
         return CFD2D_OK;
     });
 }
@@ -389,7 +469,7 @@ int cfd2d_backward(cfd2d_t* h, double* dJdU0, double* dJdbnd) {
 int cfd2d_set_boundary(cfd2d_t* h, int b, const double par[4]) {
     return guarded([&] {
         if (!h || !par) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        h->s->set_boundary_params(b, par);
+        ex(h).set_boundary_params(b, par);
         return CFD2D_OK;
     });
 }
@@ -398,7 +478,7 @@ int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms) {
     Range r("cfd2d_timed_steps");
     return guarded([&] {
         if (!h || !device_ms || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
-        *device_ms = h->s->timed_steps(nsteps);
+        *device_ms = h->imp ? h->imp->timed_steps(nsteps) : ex(h).timed_steps(nsteps);
         return CFD2D_OK;
     });
 }
@@ -407,7 +487,31 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
     Range r("cfd2d_profile_steps");
     return guarded([&] {
         if (!h || !kernel_ms || !kernel_launches || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
-        h->s->profile_steps(nsteps, kernel_ms, kernel_launches);
+        ex(h).profile_steps(nsteps, kernel_ms, kernel_launches);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_implicit_system(cfd2d_t* h, double* diag, double* off, double* rhs, double* ctau) {
+    Range r("cfd2d_implicit_system");
+    return guarded([&] {
+        if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
+        if (!h->imp) return fail(CFD2D_ERR_INVALID_ARG, "not an FVM_TVD_IMPLICIT handle");
+        h->imp->system(diag, off, rhs, ctau);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_implicit_stats(const cfd2d_t* h, cfd2d_implicit_stats_t* st) {
+    return guarded([&] {
+        if (!h || !st) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        if (!h->imp) return fail(CFD2D_ERR_INVALID_ARG, "not an FVM_TVD_IMPLICIT handle");
+        std::memset(st, 0, sizeof *st);
+        st->iterations = h->imp->last_iters();
+        st->status = h->imp->last_status();
+        st->n_limited = h->imp->last_n_lim();
+        st->rel_residual = h->imp->last_rel();
+        st->cfl = h->imp->cfl();
         return CFD2D_OK;
     });
 }

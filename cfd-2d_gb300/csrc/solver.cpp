@@ -538,19 +538,20 @@ void Solver::conservation(double sums[4]) {
 }
 
 // FVM_TVD::save, src/methods/fvm_tvd.cpp:501-600 (same fields, formats and quirks).
-namespace {
 
 // The VTK file of one state, exactly as FVM_TVD::save writes it (file name, fields,
 // number formats, the single newline at the end of each field, the 8-per-line
 // total pressure, the "Velosity" spelling; src/methods/fvm_tvd.cpp:501-600). The
 // numbers are formatted on host threads, a block of items per thread, and written
 // in order, so the bytes are those of a sequential fprintf loop.
+// With implicit_format, FVM_TVD_IMPLICIT::save's variant (src/methods/fvm_tvd_implicit.cpp:
+// 840-903): Mach number |u|/c, a Total_energy field, total pressure in %25.16e.
 void write_vtk_file(const char* name, const Topo& topo, const std::vector<TaskMaterial>& mats,
-                    const std::vector<int>& cell_mat, const double* U, const double* ct) {
+                    const std::vector<int>& cell_mat, const double* U, const double* ct, bool implicit_format) {
     const int nc = topo.nc, nn = topo.nn;
     FILE* fp = std::fopen(name, "w");
     if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + name + "' opening error.");
-    struct P { double r, u, v, p, cz, T, gam; };
+    struct P { double r, u, v, p, cz, T, gam, E; };
     auto par = [&](int i) {
         const TaskMaterial& m = mats[cell_mat[i]];
         double Cv = m.Cp - GAS_R / m.M, gam = m.Cp / Cv;
@@ -559,6 +560,7 @@ void write_vtk_file(const char* name, const Topo& topo, const std::vector<TaskMa
         q.u = U[nc + i] / U[i];
         q.v = U[2 * (size_t)nc + i] / U[i];
         double E = U[3 * (size_t)nc + i] / U[i];
+        q.E = E;
         double e = E - 0.5 * (q.u * q.u + q.v * q.v);
         q.p = q.r * e * (gam - 1);
         q.cz = std::sqrt(gam * q.p / q.r);
@@ -617,7 +619,7 @@ void write_vtk_file(const char* name, const Topo& topo, const std::vector<TaskMa
     field("SCALARS Temperature float 1\nLOOKUP_TABLE default\n", [&](int i) { return par(i).T; });
     field("SCALARS MachNumber float 1\nLOOKUP_TABLE default\n", [&](int i) {
         P q = par(i);
-        return (q.u * q.u + q.v * q.v) / q.cz;
+        return implicit_format ? std::sqrt(q.u * q.u + q.v * q.v) / q.cz : (q.u * q.u + q.v * q.v) / q.cz;
     });
     std::fprintf(fp, "VECTORS Velosity float\n");
     section(nc, [&](int i, std::string& o) {
@@ -625,12 +627,18 @@ void write_vtk_file(const char* name, const Topo& topo, const std::vector<TaskMa
         app(o, "%25.16f %25.16f %25.16f ", q.u, q.v, 0.0);
         if (i + 1 == nc) o.append("\n");
     });
+    if (implicit_format) field("SCALARS Total_energy float 1\nLOOKUP_TABLE default\n", [&](int i) { return par(i).E; });
     std::fprintf(fp, "SCALARS Total_pressure float 1\nLOOKUP_TABLE default\n");
     section(nc, [&](int i, std::string& o) {
         P q = par(i);
         double agam = q.gam - 1.0;
-        double M2 = (q.u * q.u + q.v * q.v) / (q.gam * q.p / q.r);
-        app(o, "%f ", q.p * std::pow(1.0 + 0.5 * M2 * agam, q.gam / (q.gam - 1.0)));
+        if (implicit_format) {
+            double M2 = (q.u * q.u + q.v * q.v) / (q.cz * q.cz);
+            app(o, "%25.16e ", q.p * std::pow(1.0 + 0.5 * M2 * agam, q.gam / agam));
+        } else {
+            double M2 = (q.u * q.u + q.v * q.v) / (q.gam * q.p / q.r);
+            app(o, "%f ", q.p * std::pow(1.0 + 0.5 * M2 * agam, q.gam / (q.gam - 1.0)));
+        }
         if ((i + 1) % 8 == 0 || i + 1 == nc) o.append("\n");
     });
     field("SCALARS TAU float 1\nLOOKUP_TABLE default\n", [&](int i) { return ct[i]; });
@@ -645,8 +653,6 @@ void announce_vtk(const char* name) {
         std::fflush(stdout);
     }
 }
-
-}  // namespace
 
 void Solver::save_vtk(int step) {
     const int nc = topo_.nc;

@@ -19,6 +19,11 @@
 namespace cfd2d {
 
 void log_line(const char* fmt, ...);
+// The VTK file of one state (U: 4 x nc conserved, ct: cTau; reference cell order) as
+// FVM_TVD::save writes it, or as FVM_TVD_IMPLICIT::save does with implicit_format.
+void write_vtk_file(const char* name, const Topo& topo, const std::vector<TaskMaterial>& mats,
+                    const std::vector<int>& cell_mat, const double* U, const double* ct, bool implicit_format = false);
+void announce_vtk(const char* name);
 void set_verbosity(int v);
 void set_log_file(const char* path);
 

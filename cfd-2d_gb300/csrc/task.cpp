@@ -1,5 +1,6 @@
 #include "task.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -40,6 +41,114 @@ int pick(const XmlNode* ctl, const char* tag, std::initializer_list<std::pair<co
     throw Error(CFD2D_ERR_TASK, std::string("task.xml: unknown ") + tag + " '" + v + "'");
 }
 
+void parse_limits(TaskConfig& t, const XmlNode* task) {
+    const XmlNode* lim = need(task, "limits", "task");
+    t.lim_rmin = attr_d(need(lim, "ro", "limits"), "min");
+    t.lim_rmax = attr_d(need(lim, "ro", "limits"), "max");
+    t.lim_pmin = attr_d(need(lim, "p", "limits"), "min");
+    t.lim_pmax = attr_d(need(lim, "p", "limits"), "max");
+    t.lim_umax = attr_d(need(lim, "u", "limits"), "max");
+}
+
+int parse_materials(TaskConfig& t, const XmlNode* task) {
+    const XmlNode* mats = need(task, "materials", "task");
+    int nm = attr_i(mats, "count");
+    auto mlist = mats->children_named("material");
+    if (nm < 1 || nm > (int)mlist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <materials count> does not match");
+    if (nm > 255) throw Error(CFD2D_ERR_TASK, "task.xml: more than 255 materials");
+    for (int i = 0; i < nm; i++) {
+        TaskMaterial m;
+        m.id = attr_i(mlist[i], "id");
+        m.name = need(mlist[i], "name", "material")->text;
+        const XmlNode* p = need(mlist[i], "parameters", "material");
+        m.M = attr_d(need(p, "M", "parameters"), "value");
+        m.Cp = attr_d(need(p, "Cp", "parameters"), "value");
+        m.K = attr_d(need(p, "K", "parameters"), "value");
+        m.ML = attr_d(need(p, "ML", "parameters"), "value");
+        t.mats.push_back(m);
+    }
+    return nm;
+}
+
+// FVM_TVD_IMPLICIT::init, src/methods/fvm_tvd_implicit.cpp:13-176
+void parse_implicit(TaskConfig& t, const XmlNode* task) {
+    t.method = METHOD_FVM_TVD_IMPLICIT;
+    const XmlNode* ctl = need(task, "control", "task");
+    t.steady = attr_i(need(ctl, "STEADY", "control"), "value") == 0 ? 0 : 1;
+    t.tau = attr_d(need(ctl, "TAU", "control"), "value");
+    t.tmax = attr_d(need(ctl, "TMAX", "control"), "value");
+    t.step_max = attr_i(need(ctl, "STEP_MAX", "control"), "value");
+    t.file_step = attr_i(need(ctl, "FILE_OUTPUT_STEP", "control"), "value");
+    t.print_step = attr_i(need(ctl, "LOG_OUTPUT_STEP", "control"), "value");
+    const char* flx = need(ctl, "FLUX", "control")->attr("value");
+    t.flux = flx && std::strcmp(flx, "LAX") == 0 ? FLUX_LAX : FLUX_GODUNOV;  // anything else: GODUNOV
+    t.recon = RECON_LINEAR;
+    t.scheme = TIME_EULER;
+    t.precision = pick(ctl, "PRECISION", {{"FP64", PREC_FP64}}, PREC_FP64);
+    t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}, {"HILBERT", 2}}, -1);
+    if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = std::max(1, attr_i(n, "value"));
+    if (t.steady) {
+        const XmlNode* c = need(ctl, "CFL", "control");
+        t.cfl = attr_d(need(c, "start", "CFL"), "value");
+        t.cfl_scale = attr_d(need(c, "scale", "CFL"), "value");
+        t.cfl_max = attr_d(need(c, "max", "CFL"), "value");
+        t.cfl_step = attr_i(need(c, "step", "CFL"), "value");
+        t.max_lim_cells = attr_d(need(c, "max_limited_cells", "CFL"), "value");
+    }
+    const XmlNode* sm = need(task, "smoothing", "task");
+    t.smoothing = attr_i(need(sm, "using", "smoothing"), "value") == 1 ? 1 : 0;
+    t.smoothing_par = attr_d(need(sm, "coefficient", "smoothing"), "value");
+    parse_limits(t, task);
+    const int nm = parse_materials(t, task);
+    const XmlNode* regs = need(task, "regions", "task");
+    int nr = attr_i(regs, "count");
+    auto rlist = regs->children_named("region");
+    if (nr < 1 || nr > (int)rlist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <regions count> does not match");
+    for (int i = 0; i < nr; i++) {
+        TaskRegion r;
+        r.id = attr_i(rlist[i], "id");
+        r.matId = attr_i(need(rlist[i], "material", "region"), "id");
+        r.cellType = attr_i(need(rlist[i], "cell", "region"), "type");
+        const XmlNode* p = need(rlist[i], "parameters", "region");
+        r.u = attr_d(need(p, "Vx", "parameters"), "value");
+        r.v = attr_d(need(p, "Vy", "parameters"), "value");
+        r.T = attr_d(need(p, "T", "parameters"), "value");
+        r.p = attr_d(need(p, "P", "parameters"), "value");
+        if (r.matId < 0 || r.matId >= nm) throw Error(CFD2D_ERR_TASK, "task.xml: region refers to a missing material");
+        t.regions.push_back(r);
+    }
+    const XmlNode* bnds = need(task, "boundaries", "task");
+    int nb = attr_i(bnds, "count");
+    auto blist = bnds->children_named("boundCond");
+    if (nb < 0 || nb > (int)blist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <boundaries count> does not match");
+    for (int i = 0; i < nb; i++) {
+        TaskBound tb;
+        tb.edgeType = attr_i(blist[i], "edgeType");
+        const char* type = need(blist[i], "type", "boundCond")->text.c_str();
+        if (std::strcmp(type, "BOUND_WALL") == 0) {
+            tb.kind = 3;
+        } else if (std::strcmp(type, "BOUND_OUTLET") == 0) {
+            tb.kind = 2;
+        } else if (std::strcmp(type, "BOUND_INLET") == 0) {
+            tb.kind = 1;
+            const XmlNode* p = need(blist[i], "parameters", "boundCond");
+            tb.par[2] = attr_d(need(p, "T", "parameters"), "value");  // par = (Vx, Vy, T, P)
+            tb.par[3] = attr_d(need(p, "P", "parameters"), "value");
+            tb.par[0] = attr_d(need(p, "Vx", "parameters"), "value");
+            tb.par[1] = attr_d(need(p, "Vy", "parameters"), "value");
+        } else {
+            throw Error(CFD2D_ERR_BOUND_UNKNOWN, std::string("ERROR: unsupported boundary condition type '") + type + "'");
+        }
+        t.bnds.push_back(tb);
+    }
+    const XmlNode* mesh = need(task, "mesh", "task");
+    const char* mn = need(mesh, "name", "mesh")->attr("value");
+    if (!mn) throw Error(CFD2D_ERR_TASK, "task.xml: <mesh> needs a name value");
+    t.mesh_name = mn;
+    t.mesh_type = "berkeley_triangle";  // Grid::initFromFiles, src/mesh/grid.cpp:51-252
+    t.gauss_points = 2;                 // with the midpoint and two Gauss points per edge
+}
+
 }  // namespace
 
 TaskConfig parse_task(const std::string& path) {
@@ -56,6 +165,10 @@ TaskConfig parse_task(const std::string& path) {
     const XmlNode* task = doc->child("task");
     if (!task) throw Error(CFD2D_ERR_TASK, "task.xml: no <task> element");
     const char* method = task->attr("method");
+    if (method && std::strcmp(method, "FVM_TVD_IMPLICIT") == 0) {
+        parse_implicit(t, task);
+        return t;
+    }
     if (method && std::strcmp(method, "FVM_TVD") != 0 && std::strcmp(method, "FVM_TVD_GPU") != 0)
         throw Error(CFD2D_ERR_TASK, std::string("ERROR: method '") + method + "' is not served by this library.");
 
@@ -80,29 +193,8 @@ TaskConfig parse_task(const std::string& path) {
     if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = attr_i(n, "value");
     if (t.newton_cap < 1) t.newton_cap = 1;
 
-    const XmlNode* lim = need(task, "limits", "task");
-    t.lim_rmin = attr_d(need(lim, "ro", "limits"), "min");
-    t.lim_rmax = attr_d(need(lim, "ro", "limits"), "max");
-    t.lim_pmin = attr_d(need(lim, "p", "limits"), "min");
-    t.lim_pmax = attr_d(need(lim, "p", "limits"), "max");
-    t.lim_umax = attr_d(need(lim, "u", "limits"), "max");
-
-    const XmlNode* mats = need(task, "materials", "task");
-    int nm = attr_i(mats, "count");
-    auto mlist = mats->children_named("material");
-    if (nm < 1 || nm > (int)mlist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <materials count> does not match");
-    if (nm > 255) throw Error(CFD2D_ERR_TASK, "task.xml: more than 255 materials");
-    for (int i = 0; i < nm; i++) {
-        TaskMaterial m;
-        m.id = attr_i(mlist[i], "id");
-        m.name = need(mlist[i], "name", "material")->text;
-        const XmlNode* p = need(mlist[i], "parameters", "material");
-        m.M = attr_d(need(p, "M", "parameters"), "value");
-        m.Cp = attr_d(need(p, "Cp", "parameters"), "value");
-        m.K = attr_d(need(p, "K", "parameters"), "value");
-        m.ML = attr_d(need(p, "ML", "parameters"), "value");
-        t.mats.push_back(m);
-    }
+    parse_limits(t, task);
+    const int nm = parse_materials(t, task);
 
     const XmlNode* regs = need(task, "regions", "task");
     int nr = attr_i(regs, "count");
@@ -211,6 +303,42 @@ void bind_mesh(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::v
             for (size_t k = 0; k < t.bnds.size(); k++)
                 if (type != 0 && t.bnds[k].edgeType == type) { b = (int)k; break; }
         }
+        if (b < 0)
+            throw Error(CFD2D_ERR_EDGE_UNKNOWN,
+                        "ERROR (boundary condition): unknown edge type of edge " + std::to_string(e) + "...");
+        edge_bnd[e] = b;
+    }
+}
+
+void bind_mesh_implicit(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::vector<int>& cell_region,
+                        std::vector<int>& edge_bnd) {
+    const int nc = topo.nc, ne = topo.ne;
+    cell_region.assign(nc, -1);
+    std::vector<int> region_of_name(raw.names.size(), -1);
+    for (size_t n = 0; n < raw.names.size(); n++) {
+        const int type = std::atoi(raw.names[n].c_str());  // the .ele attribute
+        for (size_t r = 0; r < t.regions.size(); r++)
+            if (t.regions[r].cellType == type) { region_of_name[n] = (int)r; break; }
+    }
+    for (int i = 0; i < nc; i++) {
+        cell_region[i] = region_of_name[raw.cell_name[i]];
+        if (cell_region[i] < 0)
+            throw Error(CFD2D_ERR_REGION_UNKNOWN, "ERROR: unknown cell type " + raw.names[raw.cell_name[i]] + "...");
+    }
+    edge_bnd.assign(ne, -1);
+    std::map<long long, int> marker;  // a later .poly line for the same edge wins (src/mesh/grid.cpp:214-221)
+    for (size_t s = 0; s < raw.bseg_marker.size(); s++) {
+        long long a = raw.bseg[2 * s], b = raw.bseg[2 * s + 1];
+        marker[std::min(a, b) * (1ll << 32) + std::max(a, b)] = raw.bseg_marker[s];
+    }
+    for (int e = 0; e < ne; e++) {
+        if (topo.c2[e] >= 0) continue;
+        long long a = topo.n1[e], c = topo.n2[e];
+        auto it = marker.find(std::min(a, c) * (1ll << 32) + std::max(a, c));
+        const int type = it != marker.end() ? it->second : -1;
+        int b = -1;
+        for (size_t k = 0; k < t.bnds.size(); k++)
+            if (t.bnds[k].edgeType == type) { b = (int)k; break; }
         if (b < 0)
             throw Error(CFD2D_ERR_EDGE_UNKNOWN,
                         "ERROR (boundary condition): unknown edge type of edge " + std::to_string(e) + "...");

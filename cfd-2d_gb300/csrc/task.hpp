@@ -12,8 +12,11 @@ struct TaskMaterial { std::string name; int id = 0; double M = 0, Cp = 0, K = 0,
 struct TaskRegion { int id = 0, matId = 0, cellType = 0; std::string name; double u = 0, v = 0, T = 0, p = 0; };
 struct TaskBound { int edgeType = 0; int kind = 0; std::string name; double par[4] = {0, 0, 0, 0}; };
 
+enum MethodKind { METHOD_FVM_TVD = 0, METHOD_FVM_TVD_IMPLICIT = 1 };
+
 struct TaskConfig {
     std::string path, dir;
+    int method = METHOD_FVM_TVD;
     int steady = 1;
     double tau = 0, tmax = 0, cfl = 0;
     int step_max = 0, file_step = 1, print_step = 1;
@@ -29,6 +32,15 @@ struct TaskConfig {
     int fused = -1;           // mixed form, SSP-RK3 / Heun: 1 runs one tiled kernel per stage (opt-in)
     int adj_store = -1;       // adjoint segment store: 0 states only, 1 + primitives, 2 + gradients, -1 by memory
     int newton_cap = 100;     // iteration cap of the exact Riemann solver
+    // FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-176): <CFL> start (in cfl),
+    // scale, max, step, max_limited_cells; <smoothing>; the matrix solver's parameters
+    // (run() hard-codes 20 iterations and 1e-7, SolverHypreGmres.h the Krylov dimension 30)
+    double cfl_scale = 1.0, cfl_max = 1.0, max_lim_cells = 0.0;
+    int cfl_step = 1;
+    int smoothing = 0;
+    double smoothing_par = 0.0;
+    double gmres_eps = 1.0e-7;
+    int gmres_maxit = 20, gmres_kdim = 30;
 };
 
 TaskConfig parse_task(const std::string& path);
@@ -40,5 +52,10 @@ void region_state(const TaskMaterial& m, const TaskRegion& r, double U[4]);
 // boundary edge (by name for UNV groups, by edgeType for Triangle markers).
 void bind_mesh(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::vector<int>& cell_region,
                std::vector<int>& edge_bnd);
+// FVM_TVD_IMPLICIT's binding: region by the cell's integer type (the .ele attribute,
+// getRegionByCellType, :1024-1032), boundary by the edge's type (the .poly marker, -1
+// for a boundary edge the .poly does not list; boundaryCond, :963-975).
+void bind_mesh_implicit(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::vector<int>& cell_region,
+                        std::vector<int>& edge_bnd);
 
 }  // namespace cfd2d

@@ -181,6 +181,34 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
  * bit). *mismatches receives the count. */
 int cfd2d_selftest(int which, long long n, unsigned long long seed, long long* mismatches);
 
+/* ---- FVM_TVD_IMPLICIT ---------------------------------------------------- */
+/* A task.xml with <task method="FVM_TVD_IMPLICIT"> (src/methods/fvm_tvd_implicit.cpp,
+ * selected by name in Solver::initMethod, src/methods/solver.cpp:42-45) creates an
+ * implicit handle through cfd2d_create / cfd2d_create_with_mesh: the mesh is read as
+ * Grid::initFromFiles does (Triangle files <name>.node/.ele/.neigh/.poly, midpoint and
+ * two Gauss points per edge), regions bind by cell type and boundaries by edge type.
+ * cfd2d_step / run / get_info / get_state / set_state / get_time_step / get_flags /
+ * save_vtk / timed_steps / destroy serve it (one step = one pass of
+ * FVM_TVD_IMPLICIT::run's loop: assembly, GMRES, smoothing, update, remediation, CFL
+ * rules); the explicit-only entry points return CFD2D_ERR_INVALID_ARG on it. */
+typedef struct {
+    int iterations;       /* GMRES iterations of the last solve */
+    int status;           /* MatrixSolver result bits (src/methods/solvers/MatrixSolver.h:13-16):
+                             0 solved, 2 iteration limit reached, 4 not converged */
+    int n_limited;        /* cells flagged CELL_FLAG_LIM after the last update (getLimitedCellsCount) */
+    int pad;
+    double rel_residual;  /* |b - A x| / |b| of the last solve */
+    double cfl;           /* the CFL number of the steady rules (incCFL / decCFL) */
+} cfd2d_implicit_stats_t;
+/* The block system of the current state as the next step assembles it (the state is
+ * not advanced): per cell, in the reference's cell order, the diagonal 4x4 block
+ * (16, row major; S/cTau I + sum of l A+), the three faces' 4x4 blocks (48; l A- of
+ * the face, in Cell::edgesInd order, zero on boundary faces) and the right-hand side
+ * (4; -sum F l/2), and cTau. Unknowns are x[4 c + k] as in MatrixSolver. Any pointer
+ * may be NULL. */
+int cfd2d_implicit_system(cfd2d_t* h, double* diag, double* off, double* rhs, double* ctau);
+int cfd2d_implicit_stats(const cfd2d_t* h, cfd2d_implicit_stats_t* stats);
+
 /* Select the CUDA device that cfd2d_create* places new solvers on (default: the
  * calling thread's current device). A solver keeps its device for life. */
 int cfd2d_set_device(int device);

@@ -293,6 +293,7 @@ def run_reference_implicit(task_xml: str, tri_files: dict, U0=None, timeout=300,
             out[tag] = dict(U=U, cTau=ct, flags=fl, tau=float(tau), seconds=float(secs), cfl=float(cfl),
                             iters=iters, rel=float(rel))
         out["stdout"] = r.stdout
+        out["vtk"] = {f: open(os.path.join(d, f)).read() for f in sorted(os.listdir(d)) if f.endswith(".vtk")}
         return out
 
 

@@ -20,8 +20,14 @@ def pytest_configure(config):
 
 
 def golden_names():
+    """Fixtures of the explicit method (reference FVM_TVD runs on UNV meshes)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not p.endswith("berkeley_triangle.npz"))
+                  if not p.endswith("berkeley_triangle.npz") and not os.path.basename(p).startswith("implicit_"))
+
+
+def implicit_golden_names():
+    """Fixtures of the implicit method (reference FVM_TVD_IMPLICIT runs, make_golden_implicit.py)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "implicit_*.npz")))
 
 
 def load_golden(name):
