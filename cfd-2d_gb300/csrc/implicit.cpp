@@ -83,6 +83,15 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
         for (int i = 0; i < nc; i++) is[i] = 1.0 / lay_.S[i];
         c.invS = upload(is);
         c.rem_nb = upload(lay_.rem_nb);
+        {  // the matrix-vector product's neighbours; a boundary face's block is zero, so it reads the cell itself
+            std::vector<int> nb(3 * (size_t)nc);
+            for (int k = 0; k < 3; k++)
+                for (int i = 0; i < nc; i++) {
+                    const int f = lay_.face[(size_t)k * nc + i], e = f >> 1;
+                    nb[(size_t)k * nc + i] = e < lay_.n_int ? ((f & 1) ? lay_.ec1[e] : lay_.ec2[e]) : i;
+                }
+            c.nbr = upload(nb);
+        }
         c.iperm = upload(lay_.iperm);
         std::vector<DevMat> mats;
         for (auto& m : task_.mats) {
@@ -110,6 +119,7 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
         c.W = dalloc<double>(n4);
         c.G = dalloc<double>(8 * (size_t)nc);
         c.F = dalloc<double>(4 * (size_t)ne);
+        c.R = dalloc<double>(4 * (size_t)ne);
         c.ctau = dalloc<double>(nc);
         c.cfl = dalloc<double>(1);
         c.flags = dalloc<unsigned>(nc);
@@ -121,7 +131,7 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
         c.x2 = task_.smoothing ? dalloc<double>(n4) : c.x;
         c.V = dalloc<double>((size_t)(c.kdim + 1) * n4);
         c.r = dalloc<double>(n4);
-        c.part = dalloc<double>(2 * (size_t)kRedBlocks);
+        c.part = dalloc<double>((size_t)(kGmresMaxKdim + 1) * kRedBlocks);
         c.ctl = dalloc<GmresCtl>(1);
         c.n_lim = dalloc<int>(1);
         stage_ = dalloc<double>(48 * (size_t)nc);

@@ -61,6 +61,28 @@ __global__ void __launch_bounds__(256) k_imp_grad(const ImpCase c) {
     st8(c.G, i, g);
 }
 
+// calcRoeAverage (:418-444) over roe_orig (src/global.cpp:407-441) with W = 0:
+// the W terms add +0 to sums of squares and change no bit, so they are left out.
+struct Roe { double r, u, v, p, E, cz; };
+__device__ __forceinline__ Roe roe_average(const Prim<double>& L, const Prim<double>& R, double GAM) {
+    const double AGAM = (GAM - 1.0);
+    const double fSB = sqrt(L.r), fSE = sqrt(R.r);
+    const double fS_ = 1.0 / (fSB + fSE);
+    Roe a;
+    a.r = fSB * fSE;
+    a.u = (fSB * L.u + fSE * R.u) * fS_;
+    a.v = (fSB * L.v + fSE * R.v) * fS_;
+    const double EB = L.p / (L.r * AGAM), EE = R.p / (R.r * AGAM);
+    const double HB = EB + (L.u * L.u + L.v * L.v) * 0.5 + L.p / L.r;
+    const double HE = EE + (R.u * R.u + R.v * R.v) * 0.5 + R.p / R.r;
+    const double HI = (fSB * HB + fSE * HE) * fS_;
+    a.p = (HI - (a.u * a.u + a.v * a.v) * 0.5) * a.r * (GAM - 1.0) / GAM;
+    const double e = a.p / (a.r * AGAM);
+    a.cz = sqrt(GAM * a.p / a.r);
+    a.E = e + 0.5 * (a.u * a.u + a.v * a.v);
+    return a;
+}
+
 // The two Gauss-point fluxes of an edge times l/2 (run's loop, :602-628): interior
 // faces reconstruct linearly from both centres (reconstruct(iFace, pL, pR, p),
 // :459-494), boundary faces take the centre state and its ghost.
@@ -101,40 +123,24 @@ __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
     if (hit) atomicOr(c.err, ERRBIT_NEWTON_CAP);
     const double lh = 0.5 * l;  // right4 -= 0.5*l*fr, :630-641
     st4(c.F, e, fs[0] * lh, fs[1] * lh, fs[2] * lh, fs[3] * lh);
-}
-
-// calcRoeAverage (:418-444) over roe_orig (src/global.cpp:407-441) with W = 0:
-// the W terms add +0 to sums of squares and change no bit, so they are left out.
-struct Roe { double r, u, v, p, E, cz; };
-__device__ __forceinline__ Roe roe_average(const Prim<double>& L, const Prim<double>& R, double GAM) {
-    const double AGAM = (GAM - 1.0);
-    const double fSB = sqrt(L.r), fSE = sqrt(R.r);
-    const double fS_ = 1.0 / (fSB + fSE);
-    Roe a;
-    a.r = fSB * fSE;
-    a.u = (fSB * L.u + fSE * R.u) * fS_;
-    a.v = (fSB * L.v + fSE * R.v) * fS_;
-    const double EB = L.p / (L.r * AGAM), EE = R.p / (R.r * AGAM);
-    const double HB = EB + (L.u * L.u + L.v * L.v) * 0.5 + L.p / L.r;
-    const double HE = EE + (R.u * R.u + R.v * R.v) * 0.5 + R.p / R.r;
-    const double HI = (fSB * HB + fSE * HE) * fS_;
-    a.p = (HI - (a.u * a.u + a.v * a.v) * 0.5) * a.r * (GAM - 1.0) / GAM;
-    const double e = a.p / (a.r * AGAM);
-    a.cz = sqrt(GAM * a.p / a.r);
-    a.E = e + 0.5 * (a.u * a.u + a.v * a.v);
-    return a;
+    // calcRoeAverage of the edge's centre states (cellL = c1, cellR = c2 or the ghost,
+    // :531-534), for both cells' block rows
+    const Prim<double> cR = e < c.n_int ? load_prim(c.W, c.ec2[e]) : imp_ghost(c.bnds[c.ebnd[e]], qL, nx, ny, imat(c, c1).M);
+    const Roe a = roe_average(qL, cR, GAM);
+    st4(c.R, e, a.u, a.v, a.cz, a.E + a.p / a.r);  // H of eigenValues' callers, :547
 }
 
 // One face's 0.5 l R diag(lam+-) L (eigenValues / rightEigenVector / leftEigenVector /
-// calcAP / calcAM, :321-392, scaled by l in run, :558-565), with the normal (nx, ny)
-// of the side being assembled. R diag(lam) has one product per entry (the other three
-// products of the reference's 4x4 multiply are zeros, which change no sum), the
-// product with L keeps the reference's order of four products summed from 0.
+// calcAP / calcAM, :321-392, scaled by l in run, :558-565) from the Roe state (u, v, c,
+// H), with the normal (nx, ny) of the side being assembled. The reference forms
+// R diag(lam+) and R diag(lam-) as full 4x4 products and multiplies each by L, summing
+// four products from 0 per entry. An entry of R diag(lam+) is R[i][k] lam+_k or zero, and
+// a zero term never changes such a sum (started from +0 it cannot become -0), so column k
+// contributes to A+ only where lam_k > 0 and to A- only where lam_k < 0, in the
+// reference's order of k: the same bits with half the products.
 // Adds A+ into dg (the cell's diagonal block); returns A- in am.
-__device__ __forceinline__ void face_jacobians(const Roe& a, double GAM, double nx, double ny, double l,
-                                               double* dg, double* am) {
-    const double c = a.cz, u = a.u, v = a.v;
-    const double H = a.E + a.p / a.r;
+__device__ __forceinline__ void face_jacobians(double u, double v, double c, double H, double GAM, double nx,
+                                               double ny, double l, double* dg, double* am) {
     const double qn = u * nx + v * ny;
     const double q2 = u * u + v * v;
     const double lx = -ny, ly = nx;
@@ -155,12 +161,6 @@ __device__ __forceinline__ void face_jacobians(const Roe& a, double GAM, double 
                           0.5 * (A0 - B0), -0.5 * (Cu - Dn), -0.5 * (Ev - Fn), G0,
                           neg_if(ql, true), lx,              ly,               0.0};
     const double lam[4] = {qn - c, qn, qn + c, qn};
-    double lp[4], lm[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        lp[k] = lam[k] > 0 ? lam[k] : 0;
-        lm[k] = lam[k] < 0 ? lam[k] : 0;
-    }
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         double Rr[4];
@@ -168,19 +168,22 @@ __device__ __forceinline__ void face_jacobians(const Roe& a, double GAM, double 
         if (i == 1) { Rr[0] = u - c * nx; Rr[1] = u; Rr[2] = u + c * nx; Rr[3] = lx; }
         if (i == 2) { Rr[0] = v - c * ny; Rr[1] = v; Rr[2] = v + c * ny; Rr[3] = ly; }
         if (i == 3) { Rr[0] = H - qn * c; Rr[1] = q2 / 2; Rr[2] = H + qn * c; Rr[3] = ql; }
-        double tp[4], tm[4];
+        double sp[4] = {0.0, 0.0, 0.0, 0.0}, sm[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-        for (int k = 0; k < 4; k++) { tp[k] = Rr[k] * lp[k]; tm[k] = Rr[k] * lm[k]; }
+        for (int k = 0; k < 4; k++) {
+            const double t = Rr[k] * lam[k];
+            if (lam[k] > 0) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) sp[j] = sp[j] + t * L[4 * k + j];
+            } else if (lam[k] < 0) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) sm[j] = sm[j] + t * L[4 * k + j];
+            }
+        }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            double sp = 0.0, sm = 0.0;
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                sp = sp + tp[k] * L[4 * k + j];
-                sm = sm + tm[k] * L[4 * k + j];
-            }
-            dg[4 * i + j] = dg[4 * i + j] + sp * 0.5 * l;
-            am[4 * i + j] = 0.0 + sm * 0.5 * l;
+            dg[4 * i + j] = dg[4 * i + j] + sp[j] * 0.5 * l;
+            am[4 * i + j] = 0.0 + sm[j] * 0.5 * l;
         }
     }
 }
@@ -194,7 +197,6 @@ __global__ void __launch_bounds__(128) k_imp_assemble(const ImpCase c) {
     if (i >= c.nc) return;
     const int nc = c.nc;
     const double GAM = c.gam_flux;
-    const Prim<double> q = load_prim(c.W, i);
     double dg[16];
 #pragma unroll
     for (int m = 0; m < 16; m++) dg[m] = 0.0;
@@ -209,21 +211,18 @@ __global__ void __launch_bounds__(128) k_imp_assemble(const ImpCase c) {
 #pragma unroll
         for (int m = 0; m < 4; m++) rhs[m] = rhs[m] + neg_if(fe[m], !side2);
         const double nx = c.nx[e], ny = c.ny[e], l = c.l[e];
-        Prim<double> cL, cR;  // reconstruct(iFace, cellL, cellR): c1's state, c2's or the ghost
-        if (!side2) {
-            cL = q;
-            cR = e < c.n_int ? load_prim(c.W, c.ec2[e]) : imp_ghost(c.bnds[c.ebnd[e]], q, nx, ny, imat(c, i).M);
-        } else {
-            cL = load_prim(c.W, c.ec1[e]);
-            cR = q;
-        }
-        const Roe a = roe_average(cL, cR, GAM);
-        if (c.steady) lam = lam + (sqrt(a.u * a.u + a.v * a.v) + a.cz) * l;
+        double a[4];  // the edge's Roe state (u, v, c, H), formed once by k_imp_flux
+        ld4(c.R, e, a);
+        if (c.steady) lam = lam + (sqrt(a[0] * a[0] + a[1] * a[1]) + a[2]) * l;
         double am[16];
-        face_jacobians(a, GAM, neg_if(nx, side2), neg_if(ny, side2), l, dg, am);
-        double* O = c.O + (size_t)(16 * k) * nc + i;
+        face_jacobians(a[0], a[1], a[2], a[3], GAM, neg_if(nx, side2), neg_if(ny, side2), l, dg, am);
+        const bool inner = e < c.n_int;
 #pragma unroll
-        for (int m = 0; m < 16; m++) O[(size_t)m * nc] = e < c.n_int ? am[m] : 0.0;
+        for (int q = 0; q < 4; q++) {
+            double2* o = reinterpret_cast<double2*>(c.O + oblk(nc, i, k, 0, q));
+            o[0] = inner ? make_double2(am[q], am[4 + q]) : make_double2(0.0, 0.0);
+            o[1] = inner ? make_double2(am[8 + q], am[12 + q]) : make_double2(0.0, 0.0);
+        }
     }
     const double S = c.S[i];
     double tau;
@@ -235,7 +234,13 @@ __global__ void __launch_bounds__(128) k_imp_assemble(const ImpCase c) {
     }
     const double sd = S / tau;
 #pragma unroll
-    for (int m = 0; m < 16; m++) c.D[(size_t)m * nc + i] = dg[m] + ((m % 5) == 0 ? sd : 0.0);
+    for (int m = 0; m < 16; m++) dg[m] = dg[m] + ((m % 5) == 0 ? sd : 0.0);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        double2* d = reinterpret_cast<double2*>(c.D + dblk(nc, i, 0, q));
+        d[0] = make_double2(dg[q], dg[4 + q]);
+        d[1] = make_double2(dg[8 + q], dg[12 + q]);
+    }
     st4(c.b, i, rhs[0], rhs[1], rhs[2], rhs[3]);
 }
 
@@ -373,9 +378,9 @@ __global__ void __launch_bounds__(256) k_imp_permute(const ImpCase c, double* __
     if (o >= c.nc) return;
     const int i = c.iperm[o], nc = c.nc;
     if (which == 0)
-        for (int m = 0; m < 16; m++) dst[16 * (size_t)o + m] = c.D[(size_t)m * nc + i];
+        for (int m = 0; m < 16; m++) dst[16 * (size_t)o + m] = c.D[dblk(nc, i, m >> 2, m & 3)];
     else if (which == 1)
-        for (int m = 0; m < 48; m++) dst[48 * (size_t)o + m] = c.O[(size_t)m * nc + i];
+        for (int m = 0; m < 48; m++) dst[48 * (size_t)o + m] = c.O[oblk(nc, i, m >> 4, (m >> 2) & 3, m & 3)];
     else
         for (int m = 0; m < 4; m++) dst[4 * (size_t)o + m] = c.b[4 * (size_t)i + m];
 }

@@ -8,9 +8,10 @@
 // limited-cell count; the host applies the CFL rules. One CUDA graph per step.
 //
 // Layout in HBM (storage = RCM cell order, faces of a cell in ascending original edge
-// order as Cell::edgesInd lists them): diagonal blocks D[16][nc] and face blocks
-// O[3][16][nc] (entry-major, so that one thread per cell row reads and writes them
-// coalesced), right-hand side and every Krylov vector as [nc][4] (x[4c + k], the
+// order as Cell::edgesInd lists them): diagonal blocks D[column][nc][row] and face
+// blocks O[face][column][nc][row] (the matrix-vector product runs four threads per
+// cell, one per row, and every load of a block column is one contiguous run across a
+// warp), right-hand side and every Krylov vector as [nc][4] (x[4c + k], the
 // reference's numbering of unknowns).
 #pragma once
 #include <cuda_runtime.h>
@@ -23,6 +24,12 @@
 #include "task.hpp"
 
 namespace cfd2d {
+
+// entry (row r, column q) of cell i's diagonal block and of its face k's block
+__host__ __device__ inline size_t dblk(int nc, int i, int r, int q) { return ((size_t)q * nc + i) * 4 + r; }
+__host__ __device__ inline size_t oblk(int nc, int i, int k, int r, int q) {
+    return ((size_t)(4 * k + q) * nc + i) * 4 + r;
+}
 
 // Boundary kinds of the implicit method (Boundary::BOUND_*, src/global.h:233-235).
 enum ImpBndKind { IBND_INLET = 1, IBND_OUTLET = 2, IBND_WALL = 3 };
@@ -37,6 +44,8 @@ struct GmresCtl {
     double bnorm, eps_abs, rnorm, rel;
     double H[(kGmresMaxKdim + 1) * kGmresMaxKdim];  // H[i * kdim + j]
     double cs[kGmresMaxKdim], sn[kGmresMaxKdim], g[kGmresMaxKdim + 1], y[kGmresMaxKdim];
+    double s[kGmresMaxKdim + 1];     // Krylov vector k is s[k] V_k (V_k stored unscaled)
+    double coef[kGmresMaxKdim];      // h_ij s_i of the column being orthogonalised
     int it;        // iterations over all cycles
     int cols;      // columns of the current cycle
     int done;      // the cycle's Arnoldi loop has ended
@@ -70,6 +79,7 @@ struct ImpCase {
     const double* S;          // nc
     const double* invS;       // nc, RN(1/S)
     const int* rem_nb;        // 3*nc remediation neighbours
+    const int* nbr;           // 3*nc the cell across each face (storage), or the cell itself on the boundary
     const int* iperm;         // original -> storage
     const uint8_t* cmat;      // nc or nullptr
     const DevMat* mats;
@@ -80,6 +90,7 @@ struct ImpCase {
     double* W;                // nc x 4 primitives r, u, v, p
     double* G;                // nc x 8 gradients
     double* F;                // ne x 4 edge fluxes times l/2
+    double* R;                // ne x 4 Roe state of the edge's centre states: u, v, c, H
     double* ctau;             // nc
     double* cfl;              // 1: the CFL number of the steady rules
     unsigned* flags;          // nc
@@ -92,7 +103,7 @@ struct ImpCase {
     double* x2;               // 4*nc (smoothing output)
     double* V;                // (kdim + 1) * 4*nc Krylov basis
     double* r;                // 4*nc residual of a restart
-    double* part;             // 2 x kRedBlocks partial sums (double-buffered)
+    double* part;             // (kGmresMaxKdim + 1) x kRedBlocks partial sums of the reductions
     GmresCtl* ctl;
     int* n_lim;               // 1
 };
