@@ -437,6 +437,99 @@ def batched_workload(args, capi, cases, world, rank, dist, W, K):
             "gpu_launches": K * (3 * 3 + 1)}), flush=True)
 
 
+IMP_N = 1024
+IMP_TAU = 0.002
+
+
+def implicit_cpu_baseline(n=IMP_N, steps=1):
+    """The oracle's FVM_TVD_IMPLICIT on one host core: a bounded sample of the same workload
+    (one step of the full mesh, ~10-20 s of CPU work)."""
+    from cfd2d import cases
+    from oracle import pyoracle
+    pyoracle.build()
+    t, m, U0 = cases.vortex_implicit(n, tau=IMP_TAU)
+    o = pyoracle.implicit_from_task(t, m, U0=U0)
+    a = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - a
+    return {"value": m.n_cells * steps / dt, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_model(),
+            "sample": f"{steps} implicit step(s) of the same vortex at {n}x{n}x2 = {m.n_cells} triangles on one core "
+                      f"(GMRES iterations {o.info()['iters']})"}
+
+
+def implicit_workload(args, capi, cases, world, rank, dist, W, K):
+    """FVM_TVD_IMPLICIT, the reference's implicit method: isentropic vortex on [0,10]^2,
+    1024x1024x2 = 2,097,152 jittered triangles (seed 4), free-stream inlets, unsteady
+    TAU 0.002 (CFL ~0.45), per step the Roe-linearised block system assembled from the
+    centre states and the Gauss-point fluxes (LAX; GODUNOV reported beside it), solved
+    by GMRES (Krylov dimension 30, 20 iterations, 1e-7, the reference's parameters),
+    then the update with limits. Device time from CUDA events over the step graphs."""
+    n = args.imp_n
+    d = tempfile.mkdtemp(prefix="cfd2d_imp_")
+    out = {}
+    fluxes = ("LAX", "GODUNOV") if args.imp_flux == "both" else (args.imp_flux,)
+    for flux in fluxes:
+        t, m, U0 = cases.vortex_implicit(n, flux=flux, tau=IMP_TAU)
+        dk = os.path.join(d, flux)
+        os.makedirs(dk, exist_ok=True)
+        s = capi.Solver(cases.write_implicit_task(t, m, dk), mesh=m)
+        s.set_state(U0)
+        s.step(W)
+        barrier(dist)
+        ms = reduce_max(dist, s.timed_steps(K))
+        st = s.implicit_stats()
+        out[flux] = {"ms_per_step": ms / K, "value": world * m.n_cells * K / (ms * 1e-3),
+                     "gmres_iterations": st["iters"], "gmres_rel_residual": st["rel"], "status": st["status"]}
+        if not args.no_profile:
+            prof_ms, prof_n = s.profile_steps(2)
+            phases = ["gradients", "fluxes_roe", "assembly", "gmres_update"]
+            tot = max(float(prof_ms.sum()), 1e-30)
+            out[flux]["phases"] = {k: {"ms_per_step": float(prof_ms[i] / 2), "share": float(prof_ms[i] / tot),
+                                       "launches_per_step": int(prof_n[i] // 2)} for i, k in enumerate(phases)}
+        cells, bytes_dev = m.n_cells, s.get_info().device_bytes
+        if flux == fluxes[0] and not args.no_e2e:
+            # end to end through the C ABI with pinned host buffers
+            import torch
+            nc = m.n_cells
+            pin_in = torch.empty((4, nc), dtype=torch.float64).pin_memory()
+            pin_out = torch.empty((4, nc), dtype=torch.float64).pin_memory()
+            pin_in.copy_(torch.from_numpy(s.state()))
+            pi = [pin_in[k].data_ptr() for k in range(4)]
+            po = [pin_out[k].data_ptr() for k in range(4)]
+            Ke = min(K, 10)
+            barrier(dist)
+            a = time.perf_counter()
+            for _ in range(Ke):
+                s.set_state_from(pi)
+                s.step(1)
+                s.state_into(po)
+            e2e_s = reduce_max(dist, (time.perf_counter() - a) / Ke)
+            out["e2e"] = {"value": world * nc / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 32 * nc,
+                          "d2h_bytes_per_step": 32 * nc, "steps": Ke,
+                          "path": "cfd2d_set_state + cfd2d_step(1) + cfd2d_get_state, pinned host buffers"}
+        s.close()
+    lax = out[fluxes[0]]
+    # FP64 operations of the matrix-vector product (64 multiply-adds per cell), the GMRES
+    # kernel the step spends most in: achieved rate against GB300's FP64 issue rate
+    if rank == 0:
+        line = {
+            "metric": "implicit-method cell-updates/s at 2.1M triangles (FVM_TVD_IMPLICIT, GMRES per step)",
+            "value": lax["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": lax["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"isentropic vortex on [0,10]^2, {n}x{n}x2 = {cells} jittered triangles (seed 4), "
+                                   f"free-stream inlets, {fluxes[0]} flux, unsteady TAU {IMP_TAU}, GMRES (30, 20 iterations, "
+                                   "1e-7)", "cells": cells, "device_bytes": bytes_dev,
+                       "l2": "no flush: a step streams ~10 GB (Krylov basis 1.4 GB, block matrix 1.1 GB)"},
+            "lax": out.get("LAX"), "godunov": out.get("GODUNOV"), "e2e": out.get("e2e"),
+        }
+        if "phases" in lax:
+            line["gpu_launches"] = K * sum(v["launches_per_step"] for v in lax["phases"].values())
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = implicit_cpu_baseline()
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -448,10 +541,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--n", type=int, default=N_SIDE, help="squares per side (profiling runs only)")
-    ap.add_argument("--workload", default="four_quadrant", choices=["four_quadrant", "batched", "combined", "adjoint"],
+    ap.add_argument("--workload", default="four_quadrant",
+                    choices=["four_quadrant", "batched", "combined", "adjoint", "implicit"],
                     help="four_quadrant: the headline 2.1M-triangle line; batched: 256 uneven vortex instances")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--adj-n", type=int, default=256, help="squares per side of the adjoint-only run's vortex")
+    ap.add_argument("--imp-n", type=int, default=IMP_N, help="squares per side of the implicit workload's vortex")
+    ap.add_argument("--imp-flux", default="both", choices=["both", "LAX", "GODUNOV"])
     args = ap.parse_args()
     world, rank, local, dist = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -470,6 +566,9 @@ def main():
         return
     if args.workload == "combined":
         combined_workload(args, capi, cases, world, rank, dist, W, K)
+        return
+    if args.workload == "implicit":
+        implicit_workload(args, capi, cases, world, rank, dist, W, K)
         return
     if args.workload == "adjoint":  # one checkpointed forward + backward of K steps (profiling runs)
         t, m, U0, w, _ = cases.vortex_adjoint(args.adj_n, steps=K)

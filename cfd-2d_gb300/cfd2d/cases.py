@@ -120,3 +120,31 @@ def batched_vortices(count: int = 256, *, seed=3, min_cells=10_000, max_cells=40
                           scheme=scheme, cfl=cfl, steps=steps, precision=precision)
         out.append((t, m, U0))
     return out
+
+
+def vortex_implicit(n: int, *, flux="LAX", tau=0.002, steps=100, beta=5.0, seed=4, jitter=0.1, steady=0,
+                    cfl=(1.0, 1.0, 1.0, 1000000, 1.0e9)):
+    """The isentropic vortex (strength beta at (5, 5), free stream rho=u=p=1) on [0,10]^2 for the
+    implicit method FVM_TVD_IMPLICIT: n x n x 2 triangles, all boundaries BOUND_INLET with the
+    free stream, time step tau (unsteady) or the CFL rules (steady)."""
+    m = mg.jittered_square(n, 0.0, 10.0, 0.0, 10.0, jitter, seed)
+    m.bseg_bnd = np.zeros(len(m.bsegs), np.int32)
+    bnds = [mg.ImplicitBoundary(edge_type=1, kind="BOUND_INLET", T=1.0, p=1.0, u=1.0, v=0.0)]
+    t = mg.ImplicitTask(regions=[mg.ImplicitRegion(cell_type=0, u=1.0, v=0.0, T=1.0, p=1.0)], boundaries=bnds,
+                        steady=steady, tau=tau, step_max=steps, flux=flux, cfl=cfl)
+    U0 = mg.isentropic_vortex(m.centroids(), beta, 5.0, 5.0)
+    return t, m, U0
+
+
+def write_implicit_task(task, mesh, directory=None, with_mesh_files=False) -> str:
+    """task.xml of an implicit task (and optionally its Triangle mesh files); returns the task path."""
+    d = directory or tempfile.mkdtemp(prefix="cfd2d_imp_")
+    path = os.path.join(d, "task.xml")
+    with open(path, "w") as f:
+        f.write(mg.write_implicit_task_xml(task))
+    if with_mesh_files:
+        files = mg.write_triangle(mesh, [b.edge_type for b in task.boundaries], [r.cell_type for r in task.regions])
+        for ext, txt in files.items():
+            with open(os.path.join(d, task.mesh_name + ext), "w") as f:
+                f.write(txt)
+    return path

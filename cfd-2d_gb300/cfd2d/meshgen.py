@@ -335,7 +335,7 @@ class ImplicitBoundary:
 
 @dataclass
 class ImplicitTask:
-    """task.xml of the reference's FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-176):
+    """task.xml of the reference's FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-184):
     Triangle files read by Grid::initFromFiles, regions bound by cell type, boundaries by
     edge type; the CFL block is read for steady runs only."""
     regions: list

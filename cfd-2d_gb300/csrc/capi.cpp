@@ -487,7 +487,8 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
     Range r("cfd2d_profile_steps");
     return guarded([&] {
         if (!h || !kernel_ms || !kernel_launches || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
-        ex(h).profile_steps(nsteps, kernel_ms, kernel_launches);
+        if (h->imp) h->imp->profile_steps(nsteps, kernel_ms, kernel_launches);
+        else ex(h).profile_steps(nsteps, kernel_ms, kernel_launches);
         return CFD2D_OK;
     });
 }

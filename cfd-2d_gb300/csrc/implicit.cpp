@@ -66,7 +66,7 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
         c.eps = task_.gmres_eps;
         c.smoothing_par = task_.smoothing_par;
         c.tau_xml = task_.tau;
-        c.gam_flux = 1.4;  // __GAM, src/methods/fvm_tvd_implicit.cpp:527
+        c.gam_flux = 1.4;  // __GAM, src/methods/fvm_tvd_implicit.cpp:536
         c.ig1_flux = 1.0 / (c.gam_flux - 1.0);
         c.lim_rmin = task_.lim_rmin; c.lim_rmax = task_.lim_rmax;
         c.lim_pmin = task_.lim_pmin; c.lim_pmax = task_.lim_pmax; c.lim_umax = task_.lim_umax;
@@ -140,7 +140,7 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
         CUDA_CHECK(cudaMemsetAsync(c.flags, 0, sizeof(unsigned) * nc, stream_));
         CUDA_CHECK(cudaMemsetAsync(c.err, 0, sizeof(unsigned), stream_));
         CUDA_CHECK(cudaMemsetAsync(c.ctl, 0, sizeof(GmresCtl), stream_));
-        // initial state from the regions (:166-170), storage order
+        // initial state from the regions (:176-180), storage order
         std::vector<double> U(n4);
         std::vector<std::array<double, 4>> reg(task_.regions.size());
         for (size_t r = 0; r < reg.size(); r++)
@@ -150,7 +150,7 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
             for (int k = 0; k < 4; k++) U[(size_t)k * nc + i] = u[k];
         }
         CUDA_CHECK(cudaMemcpyAsync(c.A, U.data(), U.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
-        // calcTimeStep, :277-308: STEADY=0 gives every cell TAU; STEADY=1 forms cTau in each
+        // calcTimeStep, :296-333: STEADY=0 gives every cell TAU; STEADY=1 forms cTau in each
         // step's assembly and leaves the array unset before the first (new double[], read by
         // save(0)): zero here, which is what a fresh allocation reads as
         std::vector<double> ct(nc, task_.steady ? 0.0 : task_.tau);
@@ -206,7 +206,7 @@ void ImplicitSolver::build_graphs() {
     g_restart_ = capture(false);
 }
 
-// One pass of run()'s loop body, :517-733. The host keeps t, the step counter and the
+// One pass of run()'s loop body, :527-735. The host keeps t, the step counter and the
 // CFL rules; the solve status, iteration count and limited-cell count come back in
 // the control block.
 void ImplicitSolver::one_step() {
@@ -222,7 +222,7 @@ void ImplicitSolver::one_step() {
     solver_err_ = last_.status;
     const double cfl0 = cfl_;
     if (solver_err_ == SOLVE_OK) {
-        if (task_.steady && last_.n_lim >= task_.max_lim_cells) {  // decCFL, :1065-1072
+        if (task_.steady && last_.n_lim >= task_.max_lim_cells) {  // decCFL, :1070-1077
             if (cfl_ > 0.1) {
                 cfl_ *= 0.75;
                 if (cfl_ < 0.1) cfl_ = 0.1;
@@ -243,7 +243,7 @@ void ImplicitSolver::one_step() {
     if (cfl_ != cfl0) CUDA_CHECK(cudaMemcpyAsync(ic_.cfl, &cfl_, sizeof(double), cudaMemcpyHostToDevice, stream_));
 }
 
-// incCFL, :1074-1081, at the end of a successful step
+// incCFL, :1079-1086, at the end of a successful step
 static bool inc_cfl(double& cfl, const TaskConfig& t) {
     if (cfl < t.cfl_max) {
         cfl *= t.cfl_scale;
@@ -269,9 +269,9 @@ int ImplicitSolver::step(int n) {
     return CFD2D_OK;
 }
 
-int ImplicitSolver::run() {  // FVM_TVD_IMPLICIT::run, :478-746
+int ImplicitSolver::run() {  // FVM_TVD_IMPLICIT::run, :478-738
     use_device();
-    if (steps_ == 0) save_vtk(0);  // init's save(0), :175
+    if (steps_ == 0) save_vtk(0);  // init's save(0), :183
     const int nc = topo_.nc, ne = topo_.ne;
     (void)nc;
     log_line(task_.steady ? "Steady-State Flow\n" : "Unsteady-State Flow\n");
@@ -382,6 +382,50 @@ void ImplicitSolver::save_vtk(int step) {
     std::snprintf(name, sizeof name, "res_%010d.vtk", step);
     write_vtk_file(name, topo_, task_.mats, cell_mat, U.data(), ct.data(), true);
     announce_vtk(name);
+}
+
+void ImplicitSolver::profile_steps(int n, double ms[4], int launches[4]) {
+    use_device();
+    for (int k = 0; k < 4; k++) { ms[k] = 0.0; launches[k] = 0; }
+    cudaEvent_t ev[5];
+    for (auto& e : ev) CUDA_CHECK(cudaEventCreate(&e));
+    // kernels of one GMRES cycle and the update: reset, |src|, v0; per column spmv, the
+    // inner-product passes (12 vectors each), hcol, orth, givens; solve, x, residual,
+    // finish; post_begin, [smoothing], update, remediation, count
+    const int jmax = std::min(ic_.kdim, ic_.maxit);
+    int gm_launches = 3 + 4 + 4 + (task_.smoothing ? 1 : 0);
+    for (int j = 0; j < jmax; j++) gm_launches += 4 + (j + 12) / 12;
+    for (int s = 0; s < n; s++) {
+        if (!task_.steady) t_ += task_.tau;
+        if (!solver_err_) steps_++;
+        CUDA_CHECK(cudaEventRecord(ev[0], stream_));
+        imp_launch_prims(ic_, stream_);
+        imp_launch_grad(ic_, stream_);
+        CUDA_CHECK(cudaEventRecord(ev[1], stream_));
+        imp_launch_flux(ic_, stream_);
+        CUDA_CHECK(cudaEventRecord(ev[2], stream_));
+        imp_launch_assemble(ic_, stream_);
+        CUDA_CHECK(cudaEventRecord(ev[3], stream_));
+        imp_launch_gmres_cycle(ic_, true, stream_);
+        imp_launch_post(ic_, stream_);
+        CUDA_CHECK(cudaEventRecord(ev[4], stream_));
+        CUDA_CHECK(cudaMemcpyAsync(ctl_host_, ic_.ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, stream_));
+        CUDA_CHECK(cudaStreamSynchronize(stream_));
+        for (int k = 0; k < 4; k++) {
+            float t = 0;
+            CUDA_CHECK(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+            ms[k] += t;
+        }
+        launches[0] += 2; launches[1] += 1; launches[2] += 1; launches[3] += gm_launches;
+        for (int guard = 0; ctl_host_->restart && guard <= task_.gmres_maxit; guard++) {
+            CUDA_CHECK(cudaGraphLaunch(g_restart_, stream_));
+            CUDA_CHECK(cudaStreamSynchronize(stream_));
+        }
+        last_ = *ctl_host_;
+        solver_err_ = last_.status;
+        if (solver_err_ != SOLVE_OK && !task_.steady) solver_err_ = 0;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
 }
 
 double ImplicitSolver::timed_steps(int n) {

@@ -33,11 +33,11 @@ __global__ void __launch_bounds__(256) k_imp_prims(const ImpCase c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.nc) return;
     const int nc = c.nc;
-    // convertConsToPar, :1053-1063 (URS(0): p = r e (gam - 1))
+    // convertConsToPar, :1058-1068 (URS(0): p = r e (gam - 1))
     store_prim(c.W, i, cons2prim<double>(c.A[i], c.A[nc + i], c.A[2 * nc + i], c.A[3 * nc + i], imat(c, i).gm1));
 }
 
-// calcGrad, :185-250: per cell over its faces in ascending edge order, the
+// calcGrad, :186-252: per cell over its faces in ascending edge order, the
 // unreconstructed centre states and the implicit method's ghosts.
 __global__ void __launch_bounds__(256) k_imp_grad(const ImpCase c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256) k_imp_grad(const ImpCase c) {
     st8(c.G, i, g);
 }
 
-// calcRoeAverage (:418-444) over roe_orig (src/global.cpp:407-441) with W = 0:
+// calcRoeAverage (:408-429) over roe_orig (src/global.cpp:407-441) with W = 0:
 // the W terms add +0 to sums of squares and change no bit, so they are left out.
 struct Roe { double r, u, v, p, E, cz; };
 __device__ __forceinline__ Roe roe_average(const Prim<double>& L, const Prim<double>& R, double GAM) {
@@ -83,9 +83,9 @@ __device__ __forceinline__ Roe roe_average(const Prim<double>& L, const Prim<dou
     return a;
 }
 
-// The two Gauss-point fluxes of an edge times l/2 (run's loop, :602-628): interior
+// The two Gauss-point fluxes of an edge times l/2 (run's loop, :612-633): interior
 // faces reconstruct linearly from both centres (reconstruct(iFace, pL, pR, p),
-// :459-494), boundary faces take the centre state and its ghost.
+// :444-476), boundary faces take the centre state and its ghost.
 __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
@@ -121,17 +121,17 @@ __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
     }
     if (hit) atomicOr(c.err, ERRBIT_NEWTON_CAP);
-    const double lh = 0.5 * l;  // right4 -= 0.5*l*fr, :630-641
+    const double lh = 0.5 * l;  // right4 -= 0.5*l*fr, :623-633
     st4(c.F, e, fs[0] * lh, fs[1] * lh, fs[2] * lh, fs[3] * lh);
     // calcRoeAverage of the edge's centre states (cellL = c1, cellR = c2 or the ghost,
-    // :531-534), for both cells' block rows
+    // :553-554), for both cells' block rows
     const Prim<double> cR = e < c.n_int ? load_prim(c.W, c.ec2[e]) : imp_ghost(c.bnds[c.ebnd[e]], qL, nx, ny, imat(c, c1).M);
     const Roe a = roe_average(qL, cR, GAM);
-    st4(c.R, e, a.u, a.v, a.cz, a.E + a.p / a.r);  // H of eigenValues' callers, :547
+    st4(c.R, e, a.u, a.v, a.cz, a.E + a.p / a.r);  // H of eigenValues' callers, :565
 }
 
 // One face's 0.5 l R diag(lam+-) L (eigenValues / rightEigenVector / leftEigenVector /
-// calcAP / calcAM, :321-392, scaled by l in run, :558-565) from the Roe state (u, v, c,
+// calcAP / calcAM, :335-406, scaled by l in run, :572-600) from the Roe state (u, v, c,
 // H), with the normal (nx, ny) of the side being assembled. The reference forms
 // R diag(lam+) and R diag(lam-) as full 4x4 products and multiplies each by L, summing
 // four products from 0 per entry. An entry of R diag(lam+) is R[i][k] lam+_k or zero, and
@@ -188,8 +188,8 @@ __device__ __forceinline__ void face_jacobians(double u, double v, double c, dou
     }
 }
 
-// One block row of the system per cell (run's edge loop, :529-646, gathered per
-// cell in ascending edge order, and the diagonal S/cTau of :655-673): the Roe
+// One block row of the system per cell (run's edge loop, :541-634, gathered per
+// cell in ascending edge order, and the diagonal S/cTau of :640-664): the Roe
 // average of the face's two centre states, the spectral radius (steady), A+ into
 // the diagonal block, A- as the face's block, and the right-hand side -sum F l/2.
 __global__ void __launch_bounds__(128) k_imp_assemble(const ImpCase c) {
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(128) k_imp_assemble(const ImpCase c) {
 
 __device__ __forceinline__ bool solve_ok(const GmresCtl* g) { return g->final_ && !g->restart && g->status == 0; }
 
-// smoothingDelta, :818-837, for the four components at once (each pass reads and
+// smoothingDelta, :790-808, for the four components at once (each pass reads and
 // writes one component only): x2 = (x + a sum_nb x_nb) / (1 + a n_nb) over the
 // unlimited neighbours in ascending edge order. (The reference indexes its
 // neighbour sums with 4 i + shift instead of i, past their end; the sums of cell i
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(256) k_imp_smooth(const ImpCase c) {
         (xi[3] + a * s[3]) / den);
 }
 
-// The update of a solved system with the limits, :680-708.
+// The update of a solved system with the limits, :675-692.
 __global__ void __launch_bounds__(256) k_imp_update(const ImpCase c, const double* __restrict__ dx) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool ok = solve_ok(c.ctl);
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(256) k_imp_update(const ImpCase c, const doubl
     if (__syncthreads_or(lim) && threadIdx.x == 0) atomicAdd(c.n_lim, 1);
 }
 
-// FVM_TVD_IMPLICIT::remediateLimCells, :764-800: flagged cells in original order,
+// FVM_TVD_IMPLICIT::remediateLimCells, :740-780: flagged cells in original order,
 // one after another; the area-weighted mean of the cells across their faces, taken
 // when those areas sum to at least TAU^2; flag aging.
 __global__ void __launch_bounds__(1024) k_imp_remediate(const ImpCase c) {
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(1024) k_imp_remediate(const ImpCase c) {
     }
 }
 
-// getLimitedCellsCount, :802-808
+// getLimitedCellsCount, :782-788
 __global__ void __launch_bounds__(256) k_imp_count(const ImpCase c) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool lim = i < c.nc && (c.flags[i] & 0x2u);

@@ -135,6 +135,10 @@ public:
     void system(double* diag, double* off, double* rhs, double* ctau);
     void save_vtk(int step);
     double timed_steps(int n);
+    // n steps launched phase by phase with CUDA events around each phase: ms and launch
+    // counts of 0 primitives + gradients, 1 Gauss-point fluxes + Roe states, 2 block-row
+    // assembly, 3 GMRES + update (the steps are taken)
+    void profile_steps(int n, double ms[4], int launches[4]);
 
     const TaskConfig& task() const { return task_; }
     const Topo& topo() const { return topo_; }

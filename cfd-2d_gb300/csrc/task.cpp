@@ -70,7 +70,7 @@ int parse_materials(TaskConfig& t, const XmlNode* task) {
     return nm;
 }
 
-// FVM_TVD_IMPLICIT::init, src/methods/fvm_tvd_implicit.cpp:13-176
+// FVM_TVD_IMPLICIT::init, src/methods/fvm_tvd_implicit.cpp:13-184
 void parse_implicit(TaskConfig& t, const XmlNode* task) {
     t.method = METHOD_FVM_TVD_IMPLICIT;
     const XmlNode* ctl = need(task, "control", "task");

@@ -32,7 +32,7 @@ struct TaskConfig {
     int fused = -1;           // mixed form, SSP-RK3 / Heun: 1 runs one tiled kernel per stage (opt-in)
     int adj_store = -1;       // adjoint segment store: 0 states only, 1 + primitives, 2 + gradients, -1 by memory
     int newton_cap = 100;     // iteration cap of the exact Riemann solver
-    // FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-176): <CFL> start (in cfl),
+    // FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-184): <CFL> start (in cfl),
     // scale, max, step, max_limited_cells; <smoothing>; the matrix solver's parameters
     // (run() hard-codes 20 iterations and 1e-7, SolverHypreGmres.h the Krylov dimension 30)
     double cfl_scale = 1.0, cfl_max = 1.0, max_lim_cells = 0.0;
@@ -53,7 +53,7 @@ void region_state(const TaskMaterial& m, const TaskRegion& r, double U[4]);
 void bind_mesh(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::vector<int>& cell_region,
                std::vector<int>& edge_bnd);
 // FVM_TVD_IMPLICIT's binding: region by the cell's integer type (the .ele attribute,
-// getRegionByCellType, :1024-1032), boundary by the edge's type (the .poly marker, -1
+// getRegionByCellType, :1027-1036), boundary by the edge's type (the .poly marker, -1
 // for a boundary edge the .poly does not list; boundaryCond, :963-975).
 void bind_mesh_implicit(const TaskConfig& t, const RawMesh& raw, const Topo& topo, std::vector<int>& cell_region,
                         std::vector<int>& edge_bnd);

@@ -169,7 +169,10 @@ int cfd2d_set_boundary(cfd2d_t* h, int b, const double par[4]);
 int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms);
 /* nsteps steps launched kernel by kernel with CUDA events around each launch:
  * per kernel kind (0 gradients, 1 edge fluxes, 2 stage updates, 3 remediation)
- * the total device ms and the number of launches (the steps are taken). */
+ * the total device ms and the number of launches (the steps are taken). On an
+ * FVM_TVD_IMPLICIT handle the kinds are phases of the step: 0 primitives and
+ * gradients, 1 Gauss-point fluxes and Roe states, 2 block-row assembly, 3 GMRES and
+ * the update. */
 int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_launches[4]);
 
 /* Built-in check of the device arithmetic helpers on n seeded random operands,
@@ -183,7 +186,7 @@ int cfd2d_selftest(int which, long long n, unsigned long long seed, long long* m
 
 /* ---- FVM_TVD_IMPLICIT ---------------------------------------------------- */
 /* A task.xml with <task method="FVM_TVD_IMPLICIT"> (src/methods/fvm_tvd_implicit.cpp,
- * selected by name in Solver::initMethod, src/methods/solver.cpp:42-45) creates an
+ * selected by name in Solver::initMethod, src/methods/solver.cpp:41-44) creates an
  * implicit handle through cfd2d_create / cfd2d_create_with_mesh: the mesh is read as
  * Grid::initFromFiles does (Triangle files <name>.node/.ele/.neigh/.poly, midpoint and
  * two Gauss points per edge), regions bind by cell type and boundaries by edge type.

@@ -861,7 +861,7 @@ struct orc_imp {
     int newton_hit;
 };
 
-/* FVM_TVD_IMPLICIT::convertConsToPar, :1053-1063 (URS(0) then URS(1)) */
+/* FVM_TVD_IMPLICIT::convertConsToPar, :1058-1068 (URS(0) then URS(1)) */
 static void imp_cons2par(const orc_imp* s, int i, Par* par) {
     int mt = s->cell_mat[i];
     par->r = s->ro[i];
@@ -873,7 +873,7 @@ static void imp_cons2par(const orc_imp* s, int i, Par* par) {
     urs(s->matM[mt], s->matCp[mt], par, 1);
 }
 
-/* FVM_TVD_IMPLICIT::convertParToCons, :1045-1051 */
+/* FVM_TVD_IMPLICIT::convertParToCons, :1050-1056 */
 static void imp_par2cons(orc_imp* s, int i, const Par* par) {
     s->ro[i] = par->r;
     s->ru[i] = par->r * par->u;
@@ -906,7 +906,7 @@ static void imp_boundary(const orc_imp* s, int e, const Par* pL, Par* pR) {
     }
 }
 
-/* reconstruct(iFace, pL, pR), :446-457: the cell-centre states */
+/* reconstruct(iFace, pL, pR), :431-442: the cell-centre states */
 static void imp_centre_states(const orc_imp* s, int e, Par* pL, Par* pR) {
     const orc_mesh* m = s->m;
     imp_cons2par(s, m->c1[e], pL);
@@ -914,7 +914,7 @@ static void imp_centre_states(const orc_imp* s, int e, Par* pL, Par* pR) {
     else imp_boundary(s, e, pL, pR);
 }
 
-/* reconstruct(iFace, pL, pR, p), :459-494: linear on interior faces, centre + ghost on the boundary */
+/* reconstruct(iFace, pL, pR, p), :444-476: linear on interior faces, centre + ghost on the boundary */
 static void imp_point_states(const orc_imp* s, int e, int gp, Par* pL, Par* pR) {
     const orc_mesh* m = s->m;
     int c1 = m->c1[e], c2 = m->c2[e];
@@ -940,7 +940,7 @@ static void imp_point_states(const orc_imp* s, int e, int gp, Par* pL, Par* pR) 
     }
 }
 
-/* FVM_TVD_IMPLICIT::calcGrad, :185-250 */
+/* FVM_TVD_IMPLICIT::calcGrad, :186-252 */
 static void imp_calc_grad(orc_imp* s) {
     const orc_mesh* m = s->m;
     double* g = s->grad;
@@ -980,7 +980,7 @@ static void roe_average(Par* a, const Par* pL, const Par* pR, double GAM) {
     double HI = (fSB * HB + fSE * HE) * fS_;
     double PI = (HI - (UI * UI + VI * VI + WI * WI) * 0.5) * RI * (fG - 1.0) / fG;
     double EI = PI / (RI * AGAM);
-    /* calcRoeAverage, :418-444 */
+    /* calcRoeAverage, :408-429 */
     a->r = RI; a->e = EI; a->p = PI; a->u = UI; a->v = VI;
     a->cz = sqrt(GAM * a->p / a->r);
     a->E = a->e + 0.5 * (a->u * a->u + a->v * a->v);
@@ -988,7 +988,7 @@ static void roe_average(Par* a, const Par* pL, const Par* pR, double GAM) {
 
 typedef double M4[4][4];
 
-static void mult4(M4 d, M4 a, M4 b) { /* multMtx4, :262-275 */
+static void mult4(M4 d, M4 a, M4 b) { /* multMtx4, :264-277 */
     for (int i = 0; i < 4; ++i)
         for (int j = 0; j < 4; ++j) {
             double sum = 0;
@@ -997,7 +997,7 @@ static void mult4(M4 d, M4 a, M4 b) { /* multMtx4, :262-275 */
         }
 }
 
-/* eigenValues / rightEigenVector / leftEigenVector, :321-356 */
+/* eigenValues / rightEigenVector / leftEigenVector, :335-370 */
 static void eigen_values(M4 d, double c, double u, double nx, double v, double ny) {
     for (int i = 0; i < 4; ++i) for (int j = 0; j < 4; ++j) d[i][j] = 0;
     double qn = u * nx + v * ny;
@@ -1026,7 +1026,7 @@ static void left_eigen(M4 d, double c, double GAM, double u, double nx, double v
     d[3][0] = -ql;                                d[3][1] = lx;
     d[3][2] = ly;                                 d[3][3] = 0;
 }
-/* calcAP / calcAM, :358-392: 0.5 R diag(max(lam,0)) L, 0.5 R diag(min(lam,0)) L */
+/* calcAP / calcAM, :371-406: 0.5 R diag(max(lam,0)) L, 0.5 R diag(min(lam,0)) L */
 static void calc_apm(M4 d, M4 R, M4 E, M4 L, int plus) {
     M4 t;
     for (int i = 0; i < 4; ++i)
@@ -1056,17 +1056,17 @@ static int face_slot(const orc_mesh* m, int c, int e) {
     return -1;
 }
 
-/* calcFlux, :905-961 */
+/* calcFlux, :917-961 */
 static int imp_flux(const orc_imp* s, double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
     if (s->p.flux == ORC_FLUX_LAX) { flux_lax(f, pL, pR, nx, ny, GAM); return 0; }
     return flux_godunov(f, pL, pR, nx, ny, GAM, s->p.newton_cap);
 }
 
-/* The edge loop of FVM_TVD_IMPLICIT::run, :529-646, and the diagonal of :655-673. */
+/* The edge loop of FVM_TVD_IMPLICIT::run, :541-634, and the diagonal of :640-664. */
 static void imp_assemble(orc_imp* s) {
     const orc_mesh* m = s->m;
     int nc = m->nc;
-    const double GAM = 1.4; /* __GAM, :527 */
+    const double GAM = 1.4; /* __GAM, :536 */
     memset(s->diag, 0, sizeof(double) * 16 * (size_t)nc);
     memset(s->off, 0, sizeof(double) * 48 * (size_t)nc);
     memset(s->rhs, 0, sizeof(double) * 4 * (size_t)nc);
@@ -1093,7 +1093,7 @@ static void imp_assemble(orc_imp* s) {
             blk_add(s->diag + 16 * (size_t)c2, AP);
             blk_add(s->off + 48 * (size_t)c2 + 16 * face_slot(m, c2, e), AM);
         }
-        /* the flux of the centre states (:600-601) is computed by the reference and unused */
+        /* the flux of the centre states (:608) is computed by the reference and unused */
         double fr = 0.0, fu = 0.0, fv = 0.0, fe = 0.0;
         for (int gp = 1; gp < m->npts[e]; ++gp) {
             double f[4];
@@ -1217,7 +1217,7 @@ int orc_gmres_block(int nc, const int* nbr, const double* diag, const double* of
     return status;
 }
 
-/* smoothingDelta, :818-837 */
+/* smoothingDelta, :790-808 */
 static void imp_smoothing(orc_imp* s, double* p) {
     const orc_mesh* m = s->m;
     for (int shift = 0; shift < 4; shift++) {
@@ -1237,7 +1237,7 @@ static void imp_smoothing(orc_imp* s, double* p) {
     }
 }
 
-/* FVM_TVD_IMPLICIT::remediateLimCells, :764-800 */
+/* FVM_TVD_IMPLICIT::remediateLimCells, :740-780 */
 static void imp_remediate(orc_imp* s) {
     const orc_mesh* m = s->m;
     for (int i = 0; i < m->nc; i++) {
@@ -1261,10 +1261,10 @@ static void imp_remediate(orc_imp* s) {
     }
 }
 
-static void imp_dec_cfl(orc_imp* s) { /* :1065-1072 */
+static void imp_dec_cfl(orc_imp* s) { /* :1070-1077 */
     if (s->CFL > 0.1) { s->CFL *= 0.75; if (s->CFL < 0.1) s->CFL = 0.1; }
 }
-static void imp_inc_cfl(orc_imp* s) { /* :1074-1081 */
+static void imp_inc_cfl(orc_imp* s) { /* :1079-1086 */
     if (s->CFL < s->p.cfl_max) { s->CFL *= s->p.cfl_scale; if (s->CFL > s->p.cfl_max) s->CFL = s->p.cfl_max; }
 }
 
@@ -1298,7 +1298,7 @@ int orc_imp_create(const orc_mesh* m, const orc_imp_params* prm, int nm, const d
         if (m->c2[e] < 0 && (m->bnd[e] < 0 || m->bnd[e] >= nbnd)) { orc_imp_free(s); return -1; }
     orc_imp_set_state(s, U0);
     s->CFL = prm->cfl;
-    if (!prm->steady) for (int i = 0; i < nc; i++) s->cTau[i] = prm->tau_xml; /* calcTimeStep, :301-307 */
+    if (!prm->steady) for (int i = 0; i < nc; i++) s->cTau[i] = prm->tau_xml; /* calcTimeStep, :296-333 */
     *out = s;
     return 0;
 }
@@ -1332,7 +1332,7 @@ void orc_imp_system(orc_imp* s, double* diag, double* off, double* rhs, double* 
     if (ctau) memcpy(ctau, s->cTau, sizeof(double) * nc);
 }
 
-/* Apply the update of a solved system: :680-708, then remediation and the CFL rules. */
+/* Apply the update of a solved system: :675-692, then remediation and the CFL rules. */
 static void imp_apply(orc_imp* s, const double* dx) {
     const orc_mesh* m = s->m;
     const double GAM = 1.4;
@@ -1358,7 +1358,7 @@ int orc_imp_lim_count(const orc_imp* s) {
     return n;
 }
 
-/* nsteps passes of the loop body of FVM_TVD_IMPLICIT::run, :517-733 */
+/* nsteps passes of the loop body of FVM_TVD_IMPLICIT::run, :527-735 */
 int orc_imp_step(orc_imp* s, int nsteps) {
     s->newton_hit = 0;
     for (int k = 0; k < nsteps; k++) {

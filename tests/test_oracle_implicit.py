@@ -41,7 +41,7 @@ def oracle_of(oracle, g):
 
 def run_to(o, steps, cap=1000):
     """FVM_TVD_IMPLICIT::run's loop: passes until the step counter reaches STEP_MAX (a pass
-    whose solve failed in a steady run does not count, :519-520)."""
+    whose solve failed in a steady run does not count, :532)."""
     for _ in range(cap):
         if o.info()["step"] >= steps:
             return
