@@ -130,6 +130,21 @@ __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
     st4(c.R, e, a.u, a.v, a.cz, a.E + a.p / a.r);  // H of eigenValues' callers, :565
 }
 
+// (s * 0.5) * l as s * (0.5 l): halving is exact for |s| >= 2^-1021 (exponent field >= 2,
+// decided on the integer pipe) and so is 0.5 l, so both round the same real number;
+// a zero gives the same signed zero; smaller nonzero s take the two products (out of line,
+// so that the common path is not evaluated beside them).
+static __device__ __noinline__ double mul_half_l_tiny(double s, double l) { return (s * 0.5) * l; }
+__device__ __forceinline__ double mul_half_l(double s, double hl, double l) {
+    const long long b = __double_as_longlong(s);
+    if (__builtin_expect(((b >> 52) & 0x7ff) >= 2 || (b << 1) == 0, 1)) return s * hl;  // (zeros: +-0 either way)
+    return mul_half_l_tiny(s, l);
+}
+// 0.0 + x: x, with -0 turned into +0 (on the integer pipe)
+__device__ __forceinline__ double plus_zero(double x) {
+    return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
 // One face's 0.5 l R diag(lam+-) L (eigenValues / rightEigenVector / leftEigenVector /
 // calcAP / calcAM, :335-406, scaled by l in run, :572-600) from the Roe state (u, v, c,
 // H), with the normal (nx, ny) of the side being assembled. The reference forms
@@ -138,9 +153,12 @@ __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
 // a zero term never changes such a sum (started from +0 it cannot become -0), so column k
 // contributes to A+ only where lam_k > 0 and to A- only where lam_k < 0, in the
 // reference's order of k: the same bits with half the products.
-// Adds A+ into dg (the cell's diagonal block); returns A- in am.
+// Adds A+ into dg (the cell's diagonal block; first: dg holds nothing yet, the sums start
+// from 0); returns A- in am.
+template <bool FIRST>
 __device__ __forceinline__ void face_jacobians(double u, double v, double c, double H, double GAM, double nx,
                                                double ny, double l, double* dg, double* am) {
+    const double hl = 0.5 * l;
     const double qn = u * nx + v * ny;
     const double q2 = u * u + v * v;
     const double lx = -ny, ly = nx;
@@ -182,8 +200,9 @@ __device__ __forceinline__ void face_jacobians(double u, double v, double c, dou
         }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            dg[4 * i + j] = dg[4 * i + j] + sp[j] * 0.5 * l;
-            am[4 * i + j] = 0.0 + sm[j] * 0.5 * l;
+            const double ap = mul_half_l(sp[j], hl, l);
+            dg[4 * i + j] = FIRST ? plus_zero(ap) : dg[4 * i + j] + ap;
+            am[4 * i + j] = plus_zero(mul_half_l(sm[j], hl, l));
         }
     }
 }
@@ -215,7 +234,8 @@ __global__ void __launch_bounds__(128) k_imp_assemble(const ImpCase c) {
         ld4(c.R, e, a);
         if (c.steady) lam = lam + (sqrt(a[0] * a[0] + a[1] * a[1]) + a[2]) * l;
         double am[16];
-        face_jacobians(a[0], a[1], a[2], a[3], GAM, neg_if(nx, side2), neg_if(ny, side2), l, dg, am);
+        if (k == 0) face_jacobians<true>(a[0], a[1], a[2], a[3], GAM, neg_if(nx, side2), neg_if(ny, side2), l, dg, am);
+        else face_jacobians<false>(a[0], a[1], a[2], a[3], GAM, neg_if(nx, side2), neg_if(ny, side2), l, dg, am);
         const bool inner = e < c.n_int;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
@@ -234,7 +254,7 @@ __global__ void __launch_bounds__(128) k_imp_assemble(const ImpCase c) {
     }
     const double sd = S / tau;
 #pragma unroll
-    for (int m = 0; m < 16; m++) dg[m] = dg[m] + ((m % 5) == 0 ? sd : 0.0);
+    for (int m = 0; m < 16; m++) dg[m] = (m % 5) == 0 ? dg[m] + sd : plus_zero(dg[m]);  // + 0.0 off the diagonal
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         double2* d = reinterpret_cast<double2*>(c.D + dblk(nc, i, 0, q));

@@ -155,3 +155,16 @@ def test_implicit_run_writes_reference_log(capi, tmp_path, monkeypatch):
     assert s.get_info().step == 4
     names = sorted(p for p in os.listdir(tmp_path) if p.endswith(".vtk"))
     assert names == ["res_0000000000.vtk", "res_0000000002.vtk", "res_0000000004.vtk"]
+
+
+@pytest.mark.parametrize("name", implicit_golden_names())
+def test_implicit_run_loop_equals_reference(capi, tmp_path, monkeypatch, name):
+    """cfd2d_run: FVM_TVD_IMPLICIT::run's loop (t < TMAX, step < STEP_MAX, failed steady solves
+    not counted) reaches the reference's final state."""
+    g = load_golden(name)
+    s = gpu_of(capi, tmp_path, g)
+    monkeypatch.chdir(tmp_path)
+    s.run()
+    assert s.get_info().step == int(g["steps"])
+    assert close(s.state(), g["ref_U"]) < RTOL
+    assert np.array_equal(s.flags(), g["ref_flags"])
