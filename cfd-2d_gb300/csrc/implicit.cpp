@@ -311,6 +311,18 @@ int ImplicitSolver::run() {  // FVM_TVD_IMPLICIT::run, :478-738
 void ImplicitSolver::get_state(double* ro, double* ru, double* rv, double* re) {
     use_device();
     const int nc = ic_.nc;
+    HostArrays4 hv;
+    bool direct = true;
+    double* dst4[4] = {ro, ru, rv, re};
+    for (int k = 0; k < 4; k++) {
+        hv.p[k] = dst4[k] ? static_cast<double*>(device_view(dst4[k])) : nullptr;
+        if (dst4[k] && !hv.p[k]) direct = false;
+    }
+    if (direct) {  // one pass: permute and write over the host link
+        launch_scatter_state_host(perm_case(ic_), ic_.A, hv, stream_);
+        CUDA_CHECK(cudaStreamSynchronize(stream_));
+        return;
+    }
     launch_scatter_state(perm_case(ic_), ic_.A, stage_, stream_);
     double* dst[4] = {ro, ru, rv, re};
     for (int k = 0; k < 4; k++)
@@ -324,12 +336,21 @@ void ImplicitSolver::set_state(const double* ro, const double* ru, const double*
     use_device();
     const int nc = ic_.nc;
     const double* src[4] = {ro, ru, rv, re};
+    HostArrays4 hv;
+    bool direct = true;
     for (int k = 0; k < 4; k++) {
         if (!src[k]) throw Error(CFD2D_ERR_INVALID_ARG, "set_state: all four arrays are required");
-        CUDA_CHECK(cudaMemcpyAsync(stage_ + (size_t)k * nc, src[k], sizeof(double) * nc, cudaMemcpyHostToDevice,
-                                   stream_));
+        hv.p[k] = static_cast<double*>(device_view(src[k]));
+        if (!hv.p[k]) direct = false;
     }
-    launch_gather_state(perm_case(ic_), stage_, ic_.A, stream_);
+    if (direct) {
+        launch_gather_state_host(perm_case(ic_), hv, ic_.A, stream_);
+    } else {
+        for (int k = 0; k < 4; k++)
+            CUDA_CHECK(cudaMemcpyAsync(stage_ + (size_t)k * nc, src[k], sizeof(double) * nc, cudaMemcpyHostToDevice,
+                                       stream_));
+        launch_gather_state(perm_case(ic_), stage_, ic_.A, stream_);
+    }
     CUDA_CHECK(cudaStreamSynchronize(stream_));
 }
 

@@ -88,6 +88,28 @@ __global__ void k_scatter_state(const DevCase c, const double* __restrict__ src,
     for (int k = 0; k < 4; k++) dst[(size_t)k * nc + o] = src[(size_t)k * nc + i];
 }
 
+// The state straight from / to four host arrays the device addresses (pinned memory,
+// or pageable memory where the system gives the GPU coherent access to it): one pass
+// over the host link, permuted on the way, no staging copy in HBM.
+__global__ void k_gather_state_host(const DevCase c, HostArrays4 src, double* __restrict__ dst) {
+    const int nc = c.nc;
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nc) return;
+    const int i = c.iperm[o];
+#pragma unroll
+    for (int k = 0; k < 4; k++) dst[(size_t)k * nc + i] = src.p[k][o];
+}
+
+__global__ void k_scatter_state_host(const DevCase c, const double* __restrict__ src, HostArrays4 dst) {
+    const int nc = c.nc;
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nc) return;
+    const int i = c.iperm[o];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (dst.p[k]) dst.p[k][o] = src[(size_t)k * nc + i];
+}
+
 __global__ void k_permute_scalar(const DevCase c, const double* __restrict__ src, double* __restrict__ dst) {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= c.nc) return;
@@ -190,6 +212,12 @@ void launch_gather_state(const DevCase& c, const double* src, double* dst, cudaS
 }
 void launch_scatter_state(const DevCase& c, const double* src, double* dst, cudaStream_t s) {
     k_scatter_state<<<nblk(c.nc, 256), 256, 0, s>>>(c, src, dst);
+}
+void launch_gather_state_host(const DevCase& c, const HostArrays4& src, double* dst, cudaStream_t s) {
+    k_gather_state_host<<<nblk(c.nc, 256), 256, 0, s>>>(c, src, dst);
+}
+void launch_scatter_state_host(const DevCase& c, const double* src, const HostArrays4& dst, cudaStream_t s) {
+    k_scatter_state_host<<<nblk(c.nc, 256), 256, 0, s>>>(c, src, dst);
 }
 void launch_permute_scalar(const DevCase& c, const double* src, double* dst, cudaStream_t s) {
     k_permute_scalar<<<nblk(c.nc, 256), 256, 0, s>>>(c, src, dst);

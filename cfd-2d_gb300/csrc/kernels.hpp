@@ -124,6 +124,11 @@ void launch_fill_cfl(const DevCase& c, double tau, cudaStream_t s);
 // state permutation between caller order (original cells) and storage order
 void launch_gather_state(const DevCase& c, const double* src_orig, double* dst_store, cudaStream_t s);
 void launch_scatter_state(const DevCase& c, const double* src_store, double* dst_orig, cudaStream_t s);
+// the same from / to four device-addressable host arrays (see device_view in solver.cpp)
+struct HostArrays4 { double* p[4]; };
+void launch_gather_state_host(const DevCase& c, const HostArrays4& src_orig, double* dst_store, cudaStream_t s);
+void launch_scatter_state_host(const DevCase& c, const double* src_store, const HostArrays4& dst_orig,
+                               cudaStream_t s);
 void launch_permute_scalar(const DevCase& c, const double* src_store, double* dst_orig, cudaStream_t s);
 void launch_permute_flags(const DevCase& c, const unsigned* src_store, unsigned* dst_orig, cudaStream_t s);
 // residual of one stage (the reference's ro_int..re_int) in storage order

@@ -399,9 +399,47 @@ int Solver::run() {  // FVM_TVD::run, src/methods/fvm_tvd.cpp:303-462
     return s != CFD2D_OK ? s : status;
 }
 
+void* device_view(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if ((a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged) && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeUnregistered) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && v)
+            return const_cast<void*>(p);
+    }
+    return nullptr;
+}
+
+// all four arrays as device views, or false (any array missing or not addressable)
+static bool host_views(const double* const a[4], HostArrays4& v, bool all_required) {
+    for (int k = 0; k < 4; k++) {
+        if (!a[k]) {
+            if (all_required) return false;
+            v.p[k] = nullptr;
+            continue;
+        }
+        v.p[k] = static_cast<double*>(device_view(a[k]));
+        if (!v.p[k]) return false;
+    }
+    return true;
+}
+
 void Solver::get_state(double* ro, double* ru, double* rv, double* re) {
     use_device();
     const int nc = dc_.nc;
+    const double* dst4[4] = {ro, ru, rv, re};
+    HostArrays4 hv;
+    if (host_views(dst4, hv, false)) {  // one pass: permute and write over the host link
+        launch_scatter_state_host(dc_, dc_.A, hv, stream_);
+        CUDA_CHECK(cudaStreamSynchronize(stream_));
+        return;
+    }
     launch_scatter_state(dc_, dc_.A, stage_, stream_);
     double* dst[4] = {ro, ru, rv, re};
     for (int k = 0; k < 4; k++)
@@ -415,12 +453,17 @@ void Solver::set_state(const double* ro, const double* ru, const double* rv, con
     use_device();
     const int nc = dc_.nc;
     const double* src[4] = {ro, ru, rv, re};
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 4; k++)
         if (!src[k]) throw Error(CFD2D_ERR_INVALID_ARG, "set_state: all four arrays are required");
-        CUDA_CHECK(cudaMemcpyAsync(stage_ + (size_t)k * nc, src[k], sizeof(double) * nc, cudaMemcpyHostToDevice,
-                                   stream_));
+    HostArrays4 hv;
+    if (host_views(src, hv, true)) {  // one pass: read over the host link and permute
+        launch_gather_state_host(dc_, hv, dc_.A, stream_);
+    } else {
+        for (int k = 0; k < 4; k++)
+            CUDA_CHECK(cudaMemcpyAsync(stage_ + (size_t)k * nc, src[k], sizeof(double) * nc, cudaMemcpyHostToDevice,
+                                       stream_));
+        launch_gather_state(dc_, stage_, dc_.A, stream_);
     }
-    launch_gather_state(dc_, stage_, dc_.A, stream_);
     launch_prims(dc_, task_.precision, stream_);
     if (reset_tau) {
         tau_ = task_.tau;
