@@ -449,6 +449,68 @@ void ImplicitSolver::profile_steps(int n, double ms[4], int launches[4]) {
     for (auto& e : ev) cudaEventDestroy(e);
 }
 
+// Binary restart file of an implicit handle: "CFD2DIM1", cell count, step counter and the
+// last solve's status (int64), time and CFL number, then the conserved state (4 x nc,
+// cell order of the mesh files), cTau (nc) and the flag words (nc).
+namespace {
+constexpr char kImpStateMagic[8] = {'C', 'F', 'D', '2', 'D', 'I', 'M', '1'};
+}
+
+void ImplicitSolver::save_state(const char* path) {
+    use_device();
+    const int nc = ic_.nc;
+    std::vector<double> U(4 * (size_t)nc), ct(nc);
+    std::vector<unsigned> fl(nc);
+    get_state(U.data(), U.data() + nc, U.data() + 2 * (size_t)nc, U.data() + 3 * (size_t)nc);
+    get_ctau(ct.data());
+    get_flags(fl.data());
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' opening error.");
+    const int64_t hdr[3] = {nc, steps_, solver_err_};
+    const double hd[2] = {t_, cfl_};
+    bool ok = std::fwrite(kImpStateMagic, 1, 8, fp) == 8 && std::fwrite(hdr, sizeof hdr, 1, fp) == 1 &&
+              std::fwrite(hd, sizeof hd, 1, fp) == 1 &&
+              std::fwrite(U.data(), sizeof(double), U.size(), fp) == U.size() &&
+              std::fwrite(ct.data(), sizeof(double), ct.size(), fp) == ct.size() &&
+              std::fwrite(fl.data(), sizeof(unsigned), fl.size(), fp) == fl.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' write error.");
+}
+
+void ImplicitSolver::load_state(const char* path) {
+    use_device();
+    const int nc = ic_.nc;
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' opening error.");
+    char magic[8];
+    int64_t hdr[3];
+    double hd[2];
+    std::vector<double> U(4 * (size_t)nc), ct(nc);
+    std::vector<unsigned> fl(nc);
+    bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, kImpStateMagic, 8) == 0 &&
+              std::fread(hdr, sizeof hdr, 1, fp) == 1 && hdr[0] == nc && std::fread(hd, sizeof hd, 1, fp) == 1 &&
+              std::fread(U.data(), sizeof(double), U.size(), fp) == U.size() &&
+              std::fread(ct.data(), sizeof(double), ct.size(), fp) == ct.size() &&
+              std::fread(fl.data(), sizeof(unsigned), fl.size(), fp) == fl.size();
+    std::fclose(fp);
+    if (!ok) throw Error(CFD2D_ERR_MESH_FORMAT, std::string("File '") + path + "' is not a state of this mesh.");
+    set_state(U.data(), U.data() + nc, U.data() + 2 * (size_t)nc, U.data() + 3 * (size_t)nc);
+    steps_ = (int)hdr[1];
+    solver_err_ = (int)hdr[2];
+    t_ = hd[0];
+    cfl_ = hd[1];
+    std::vector<double> cts(nc);
+    std::vector<unsigned> fls(nc);
+    for (int i = 0; i < nc; i++) {  // storage cell i holds file cell perm[i]
+        cts[i] = ct[lay_.perm[i]];
+        fls[i] = fl[lay_.perm[i]];
+    }
+    CUDA_CHECK(cudaMemcpyAsync(ic_.ctau, cts.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    CUDA_CHECK(cudaMemcpyAsync(ic_.flags, fls.data(), sizeof(unsigned) * nc, cudaMemcpyHostToDevice, stream_));
+    CUDA_CHECK(cudaMemcpyAsync(ic_.cfl, &cfl_, sizeof(double), cudaMemcpyHostToDevice, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+}
+
 double ImplicitSolver::timed_steps(int n) {
     use_device();
     cudaEvent_t a, b;

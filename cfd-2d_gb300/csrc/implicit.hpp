@@ -134,6 +134,9 @@ public:
     // the block system of the current state (reference cell order, faces in Cell::edgesInd order)
     void system(double* diag, double* off, double* rhs, double* ctau);
     void save_vtk(int step);
+    // restart files: state, cTau, flags, step counter, time, CFL number, solver status
+    void save_state(const char* path);
+    void load_state(const char* path);
     double timed_steps(int n);
     // n steps launched phase by phase with CUDA events around each phase: ms and launch
     // counts of 0 primitives + gradients, 1 Gauss-point fluxes + Roe states, 2 block-row

@@ -120,8 +120,9 @@ int cfd2d_conservation(cfd2d_t* h, double sums[4]);
 int cfd2d_save_vtk(cfd2d_t* h, int step);
 /* Restart files (no counterpart in the reference, which cannot restart): the
  * conserved state, cTau, the cell flags, the step count and the time, in the
- * mesh files' cell order. cfd2d_load_state into a handle made from the same task
- * and mesh continues the run exactly as if it had not stopped. */
+ * mesh files' cell order (an FVM_TVD_IMPLICIT handle also keeps its CFL number and
+ * last solve status). cfd2d_load_state into a handle made from the same task and
+ * mesh continues the run exactly as if it had not stopped. */
 int cfd2d_save_state(cfd2d_t* h, const char* path);
 int cfd2d_load_state(cfd2d_t* h, const char* path);
 

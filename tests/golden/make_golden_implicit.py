@@ -30,14 +30,16 @@ from cfd2d import meshgen as mg  # noqa: E402
 from oracle import pyoracle as po  # noqa: E402
 
 
-def case(n, *, seed, kinds=("BOUND_INLET",), vortex=True, two_regions=False, **task_kw):
+def case(n, *, seed, kinds=("BOUND_INLET",), vortex=True, two_regions=False, two_materials=False, **task_kw):
     m = mg.jittered_square(n, 0.0, 10.0, 0.0, 10.0, 0.1, seed)
     m.bseg_bnd = (m.bseg_side % len(kinds)).astype(np.int32)
     bnds = [mg.ImplicitBoundary(edge_type=k + 1, kind=kd, T=1.0, p=1.0, u=1.0, v=0.0) for k, kd in enumerate(kinds)]
+    if two_materials:  # the right half is a second gas (Cp 4.0: gamma 1.2625)
+        task_kw["materials"] = [("gas", 8.314472, 3.5, 0.0, 0.0), ("heavy", 8.314472, 4.0, 0.0, 0.0)]
     if two_regions:
         m.cell_region = (m.centroids()[:, 0] > 5.0).astype(np.int32)
         regs = [mg.ImplicitRegion(cell_type=3, u=0.0, v=0.0, T=1.0, p=1.0),
-                mg.ImplicitRegion(cell_type=7, u=0.0, v=0.0, T=1.0, p=0.6)]
+                mg.ImplicitRegion(cell_type=7, u=0.0, v=0.0, T=1.0, p=0.6, mat=1 if two_materials else 0)]
     else:
         regs = [mg.ImplicitRegion(cell_type=0, u=1.0, v=0.0, T=1.0, p=1.0)]
     t = mg.ImplicitTask(regions=regs, boundaries=bnds, **task_kw)
@@ -55,6 +57,8 @@ CASES = {
                             limits=(0.85, 1.0e8, 1.0e-8, 1.0e8, 1.0e8)),
     "implicit_steady_limits_godunov": dict(n=8, seed=25, steady=1, step_max=6, flux="GODUNOV",
                                            cfl=(2.0, 1.5, 10.0, 2, 3.0), limits=(0.85, 1.0e8, 1.0e-8, 1.0e8, 1.3)),
+    "implicit_two_materials": dict(n=10, seed=27, tau=0.05, step_max=4, flux="LAX", vortex=False, two_regions=True,
+                                   two_materials=True, kinds=("BOUND_WALL", "BOUND_OUTLET")),
     "implicit_two_region_wall": dict(n=10, seed=26, steady=1, step_max=5, flux="GODUNOV", vortex=False,
                                      two_regions=True, kinds=("BOUND_WALL",), cfl=(1.0, 1.2, 4.0, 1, 1.0e9)),
 }
@@ -64,7 +68,8 @@ def main():
     for name, kw in CASES.items():
         kw = dict(kw)
         m, t, U0 = case(kw.pop("n"), seed=kw.pop("seed"), kinds=kw.pop("kinds", ("BOUND_INLET",)),
-                        vortex=kw.pop("vortex", True), two_regions=kw.pop("two_regions", False), **kw)
+                        vortex=kw.pop("vortex", True), two_regions=kw.pop("two_regions", False),
+                        two_materials=kw.pop("two_materials", False), **kw)
         xml = mg.write_implicit_task_xml(t)
         files = mg.write_triangle(m, [b.edge_type for b in t.boundaries], [r.cell_type for r in t.regions])
         ref = po.run_reference_implicit(xml, files, U0=U0)

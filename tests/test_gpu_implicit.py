@@ -168,3 +168,22 @@ def test_implicit_run_loop_equals_reference(capi, tmp_path, monkeypatch, name):
     assert s.get_info().step == int(g["steps"])
     assert close(s.state(), g["ref_U"]) < RTOL
     assert np.array_equal(s.flags(), g["ref_flags"])
+
+
+def test_implicit_restart_is_bit_exact(capi, tmp_path):
+    """cfd2d_save_state / cfd2d_load_state on an implicit handle (steady: the CFL number and the
+    solve status travel with the state): the resumed run equals the uninterrupted one bit for bit."""
+    m, t, U0, path = make_case(tmp_path, n=16, flux="LAX", steady=1, step_max=8,
+                               cfl=(3.0, 1.5, 20.0, 1, 1.0e9), kinds=("BOUND_INLET", "BOUND_OUTLET"))
+    a = capi.Solver(path)
+    a.set_state(U0)
+    a.step(3)
+    a.save_state(str(tmp_path / "r.bin"))
+    a.step(3)
+    b = capi.Solver(path)
+    b.load_state(str(tmp_path / "r.bin"))
+    b.step(3)
+    assert np.array_equal(a.state(), b.state())
+    assert np.array_equal(a.time_step(), b.time_step())
+    assert a.get_info().step == b.get_info().step
+    assert a.implicit_stats()["cfl"] == b.implicit_stats()["cfl"]
