@@ -354,6 +354,7 @@ class ImplicitTask:
     mesh_name: str = "mesh"
     precision: str | None = None       # GPU option: FP64 (default)
     reorder: str | None = None
+    gmres: tuple | None = None         # (krylov, max_iter, tolerance); None: the reference's (30, 20, 1e-7)
 
 
 def write_implicit_task_xml(t: ImplicitTask) -> str:
@@ -370,6 +371,9 @@ def write_implicit_task_xml(t: ImplicitTask) -> str:
     for tag, val in (("PRECISION", t.precision), ("REORDER", t.reorder)):
         if val is not None:
             L.append(f'    <{tag} value="{val}" />')
+    if t.gmres is not None:
+        k, it, tol = t.gmres
+        L.append(f'    <GMRES krylov="{int(k)}" max_iter="{int(it)}" tolerance="{_v(tol)}" />')
     L += ["  </control>", "  <smoothing>", f'    <using value="{int(t.smoothing[0])}" />',
           f'    <coefficient value="{_v(t.smoothing[1])}" />', "  </smoothing>",
           "  <limits>", f'    <ro min="{_v(rmin)}" max="{_v(rmax)}" />',

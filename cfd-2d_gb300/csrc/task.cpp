@@ -87,6 +87,15 @@ void parse_implicit(TaskConfig& t, const XmlNode* task) {
     t.precision = pick(ctl, "PRECISION", {{"FP64", PREC_FP64}}, PREC_FP64);
     t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}, {"HILBERT", 2}}, -1);
     if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = std::max(1, attr_i(n, "value"));
+    // the matrix solver's parameters (an extension; absent: the reference's, run() and
+    // SolverHypreGmres.h: Krylov dimension 30, 20 iterations, relative tolerance 1e-7)
+    if (const XmlNode* g = ctl->child("GMRES")) {
+        if (g->attr("krylov")) t.gmres_kdim = attr_i(g, "krylov");
+        if (g->attr("max_iter")) t.gmres_maxit = attr_i(g, "max_iter");
+        if (g->attr("tolerance")) t.gmres_eps = attr_d(g, "tolerance");
+        if (t.gmres_kdim < 1 || t.gmres_maxit < 1 || !(t.gmres_eps > 0))
+            throw Error(CFD2D_ERR_TASK, "task.xml: <GMRES> needs krylov >= 1, max_iter >= 1, tolerance > 0");
+    }
     if (t.steady) {
         const XmlNode* c = need(ctl, "CFL", "control");
         t.cfl = attr_d(need(c, "start", "CFL"), "value");

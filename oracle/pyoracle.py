@@ -261,6 +261,9 @@ def implicit_from_task(task, mesh, omesh: OracleMesh | None = None, U0=None, **o
     bp = np.asarray([[b.T, b.p, b.u, b.v] for b in task.boundaries], np.float64).reshape(-1, 4)
     kw = dict(flux=task.flux, steady=task.steady, tau=task.tau, cfl=task.cfl, smoothing=task.smoothing,
               limits=task.limits, materials=mats, cell_mat=cell_mat, bnd_kind=bk, bnd_par=bp, U0=U0)
+    if getattr(task, "gmres", None) is not None:
+        k, it, tol = task.gmres
+        kw["gmres"] = (float(tol), int(it), int(k))
     kw.update(over)
     return OracleImplicit(omesh, **kw)
 

@@ -187,3 +187,24 @@ def test_implicit_restart_is_bit_exact(capi, tmp_path):
     assert np.array_equal(a.time_step(), b.time_step())
     assert a.get_info().step == b.get_info().step
     assert a.implicit_stats()["cfl"] == b.implicit_stats()["cfl"]
+
+
+@pytest.mark.parametrize("gm", [(3, 40, 1e-7), (4, 40, 1e-7), (2, 60, 1e-8), (5, 12, 1e-9)],
+                         ids=["k3", "k4", "k2", "k5_iteration_limit"])
+def test_implicit_restarted_gmres_matches_oracle(capi, oracle, tmp_path, gm):
+    """<GMRES krylov max_iter tolerance> (an extension; the reference fixes 30, 20, 1e-7): a small
+    Krylov dimension makes the solver restart from the true residual, on the device (the
+    restart graph) and in the oracle alike."""
+    m, t, U0, path = make_case(tmp_path, n=16, flux="LAX", tau=0.1, step_max=3, gmres=gm)
+    s = capi.Solver(path)
+    s.set_state(U0)
+    o = oracle.implicit_from_task(t, m, U0=U0)
+    for _ in range(t.step_max):
+        s.step(1)
+        o.step(1)
+        st, oi = s.implicit_stats(), o.info()
+        assert (st["iters"], st["status"]) == (oi["iters"], oi["status"])
+        assert st["rel"] == pytest.approx(oi["rel"], rel=1e-3, abs=1e-14)
+    assert st["iters"] > gm[0]  # at least one restart happened
+    U, ct, fl = o.state()
+    assert close(s.state(), U) < RTOL
