@@ -262,9 +262,17 @@ int ImplicitSolver::step(int n) {
             if (inc_cfl(cfl_, task_))
                 CUDA_CHECK(cudaMemcpyAsync(ic_.cfl, &cfl_, sizeof(double), cudaMemcpyHostToDevice, stream_));
     }
+    return read_status();
+}
+
+// The device error word since the last read (cleared): the Newton cap of the exact Riemann
+// solver, or a non-positive / NaN density or pressure seen by the step.
+int ImplicitSolver::read_status() {
     unsigned e = 0;
     CUDA_CHECK(cudaMemcpyAsync(&e, ic_.err, sizeof e, cudaMemcpyDeviceToHost, stream_));
+    CUDA_CHECK(cudaMemsetAsync(ic_.err, 0, sizeof(unsigned), stream_));
     CUDA_CHECK(cudaStreamSynchronize(stream_));
+    if (e & ERRBIT_NONPHYSICAL) return CFD2D_ERR_NONPHYSICAL;
     if (e & ERRBIT_NEWTON_CAP) return CFD2D_ERR_NEWTON_CAP;
     return CFD2D_OK;
 }
@@ -301,11 +309,8 @@ int ImplicitSolver::run() {  // FVM_TVD_IMPLICIT::run, :478-738
                     CUDA_CHECK(cudaMemcpyAsync(ic_.cfl, &cfl_, sizeof(double), cudaMemcpyHostToDevice, stream_));
         }
     }
-    unsigned e = 0;
-    CUDA_CHECK(cudaMemcpyAsync(&e, ic_.err, sizeof e, cudaMemcpyDeviceToHost, stream_));
-    CUDA_CHECK(cudaStreamSynchronize(stream_));
-    if (e & ERRBIT_NEWTON_CAP) status = CFD2D_ERR_NEWTON_CAP;
-    return status;
+    const int s = read_status();
+    return s != CFD2D_OK ? s : status;
 }
 
 void ImplicitSolver::get_state(double* ro, double* ru, double* rv, double* re) {

@@ -34,7 +34,9 @@ __global__ void __launch_bounds__(256) k_imp_prims(const ImpCase c) {
     if (i >= c.nc) return;
     const int nc = c.nc;
     // convertConsToPar, :1058-1068 (URS(0): p = r e (gam - 1))
-    store_prim(c.W, i, cons2prim<double>(c.A[i], c.A[nc + i], c.A[2 * nc + i], c.A[3 * nc + i], imat(c, i).gm1));
+    const Prim<double> q = cons2prim<double>(c.A[i], c.A[nc + i], c.A[2 * nc + i], c.A[3 * nc + i], imat(c, i).gm1);
+    store_prim(c.W, i, q);
+    if (!(q.r > 0.0) || !(q.p > 0.0)) atomicOr(c.err, ERRBIT_NONPHYSICAL);  // non-positive or NaN: reported, not fixed
 }
 
 // calcGrad, :186-252: per cell over its faces in ascending edge order, the

@@ -161,6 +161,7 @@ private:
     void build_graphs();
     void assemble_only();
     void one_step();
+    int read_status();
     void use_device() const { cudaSetDevice(dev_); }
 
     TaskConfig task_;

@@ -208,3 +208,18 @@ def test_implicit_restarted_gmres_matches_oracle(capi, oracle, tmp_path, gm):
     assert st["iters"] > gm[0]  # at least one restart happened
     U, ct, fl = o.state()
     assert close(s.state(), U) < RTOL
+
+
+@pytest.mark.parametrize("bad", ["nan", "negative_density"])
+def test_implicit_nonphysical_state_is_reported(capi, tmp_path, bad):
+    """A NaN or negative density in the state makes the step return CFD2D_ERR_NONPHYSICAL; the
+    handle stays usable and a good state then steps cleanly."""
+    m, t, U0, path = make_case(tmp_path, n=8, flux="LAX", tau=0.05, step_max=2)
+    s = capi.Solver(path)
+    U = U0.copy()
+    U[0, 5] = np.nan if bad == "nan" else -1.0
+    s.set_state(U)
+    assert s.step(1, allow_warnings=True) == capi.ERR_NONPHYSICAL
+    s.set_state(U0)
+    assert s.step(1) == capi.OK
+    assert np.all(np.isfinite(s.state()))
