@@ -223,3 +223,22 @@ def test_implicit_nonphysical_state_is_reported(capi, tmp_path, bad):
     s.set_state(U0)
     assert s.step(1) == capi.OK
     assert np.all(np.isfinite(s.state()))
+
+
+def test_implicit_full_size_step_matches_oracle(capi, oracle, tmp_path):
+    """The bench workload itself (2,097,152 triangles, LAX, TAU 0.002): the assembled system equals
+    the oracle's bit for bit and one step agrees within 1e-10 with the same GMRES iteration count."""
+    from cfd2d import cases
+    t, m, U0 = cases.vortex_implicit(1024, flux="LAX", tau=0.002)
+    s = capi.Solver(cases.write_implicit_task(t, m, str(tmp_path)), mesh=m)
+    s.set_state(U0)
+    o = oracle.implicit_from_task(t, m, U0=U0)
+    D, O, b, ct = s.implicit_system()
+    D2, O2, b2, ct2 = o.system()
+    assert np.array_equal(D, D2) and np.array_equal(O, O2)
+    assert np.array_equal(b.view(np.int64), b2.view(np.int64))
+    del D, O, D2, O2
+    s.step(1)
+    o.step(1)
+    assert s.implicit_stats()["iters"] == o.info()["iters"]
+    assert close(s.state(), o.state()[0]) < RTOL
