@@ -6,8 +6,9 @@
 // orthogonalises with classical Gram-Schmidt: all inner products <w, v_i> in one pass
 // over the basis, then w -= sum h_i v_i in a second, instead of modified Gram-Schmidt's
 // j + 1 dependent passes (which the oracle and HYPRE use); in exact arithmetic both
-// give the same Krylov iterate, and the basis here is as long as 20 vectors, so the
-// results agree with the oracle's to rounding.
+// give the same Krylov iterate, and with the reference's at most 20 basis vectors the
+// results agree with the oracle's to rounding. Krylov vectors are kept unscaled with
+// their factors 1/|w|, so no normalisation pass runs.
 //
 // One solve is a fixed sequence of kernels (captured in the step's CUDA graph): every
 // kernel first reads the control block and returns at once when the Arnoldi loop has

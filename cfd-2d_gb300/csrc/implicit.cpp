@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 
 #include "cfd2d.h"
 #include "solver.hpp"
@@ -82,7 +83,6 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
         std::vector<double> is(nc);
         for (int i = 0; i < nc; i++) is[i] = 1.0 / lay_.S[i];
         c.invS = upload(is);
-        c.rem_nb = upload(lay_.rem_nb);
         {  // the matrix-vector product's neighbours; a boundary face's block is zero, so it reads the cell itself
             std::vector<int> nb(3 * (size_t)nc);
             for (int k = 0; k < 3; k++)
@@ -221,24 +221,20 @@ void ImplicitSolver::one_step() {
     last_ = *ctl_host_;
     solver_err_ = last_.status;
     const double cfl0 = cfl_;
+    auto dec_cfl = [&] {  // decCFL, :1070-1077
+        if (cfl_ > 0.1) {
+            cfl_ *= 0.75;
+            if (cfl_ < 0.1) cfl_ = 0.1;
+            log_line(" CFL Number has been decreased : %f \n", cfl_);
+        }
+    };
     if (solver_err_ == SOLVE_OK) {
-        if (task_.steady && last_.n_lim >= task_.max_lim_cells) {  // decCFL, :1070-1077
-            if (cfl_ > 0.1) {
-                cfl_ *= 0.75;
-                if (cfl_ < 0.1) cfl_ = 0.1;
-                log_line(" CFL Number has been decreased : %f \n", cfl_);
-            }
-        }
+        failed_in_row_ = 0;
+        if (task_.steady && last_.n_lim >= task_.max_lim_cells) dec_cfl();
     } else {
-        if (task_.steady) {
-            if (cfl_ > 0.1) {
-                cfl_ *= 0.75;
-                if (cfl_ < 0.1) cfl_ = 0.1;
-                log_line(" CFL Number has been decreased : %f \n", cfl_);
-            }
-        } else {
-            solver_err_ = 0;
-        }
+        failed_in_row_++;
+        if (task_.steady) dec_cfl();
+        else solver_err_ = 0;
     }
     if (cfl_ != cfl0) CUDA_CHECK(cudaMemcpyAsync(ic_.cfl, &cfl_, sizeof(double), cudaMemcpyHostToDevice, stream_));
 }
@@ -280,8 +276,7 @@ int ImplicitSolver::read_status() {
 int ImplicitSolver::run() {  // FVM_TVD_IMPLICIT::run, :478-738
     use_device();
     if (steps_ == 0) save_vtk(0);  // init's save(0), :183
-    const int nc = topo_.nc, ne = topo_.ne;
-    (void)nc;
+    const int ne = topo_.ne;
     log_line(task_.steady ? "Steady-State Flow\n" : "Unsteady-State Flow\n");
     log_line("TMAX = %e STEP_MAX = %d\n", task_.tmax, task_.step_max);
     log_line("Flux calculation method: %s\n", task_.flux == FLUX_LAX ? "LAX" : "GODUNOV");
@@ -293,6 +288,11 @@ int ImplicitSolver::run() {  // FVM_TVD_IMPLICIT::run, :478-738
     while (t_ < task_.tmax && (unsigned)steps_ < smax) {
         auto t0 = std::chrono::steady_clock::now();
         one_step();
+        // a steady run whose solves keep failing never advances its step counter (the
+        // reference loops forever there); stop after kMaxFailedSolves passes in a row
+        if (task_.steady && failed_in_row_ >= kMaxFailedSolves)
+            throw Error(CFD2D_ERR_SOLVER, "the linear solver failed " + std::to_string(failed_in_row_) +
+                                              " times in a row at the smallest CFL number");
         if (solver_err_ == SOLVE_OK) {
             auto t1 = std::chrono::steady_clock::now();
             const long ms = (long)std::chrono::duration_cast<std::chrono::milliseconds>(t1 - t0).count();

@@ -78,7 +78,6 @@ struct ImpCase {
     const double* dl;         // 8*ne Gauss-point offsets (gp0: dxL dyL dxR dyR, gp1: ...)
     const double* S;          // nc
     const double* invS;       // nc, RN(1/S)
-    const int* rem_nb;        // 3*nc remediation neighbours
     const int* nbr;           // 3*nc the cell across each face (storage), or the cell itself on the boundary
     const int* iperm;         // original -> storage
     const uint8_t* cmat;      // nc or nullptr
@@ -180,6 +179,8 @@ private:
     double t_ = 0, cfl_ = 0;
     int steps_ = 0;
     int solver_err_ = 0;
+    int failed_in_row_ = 0;                // consecutive failed solves
+    static constexpr int kMaxFailedSolves = 1000;
 };
 
 }  // namespace cfd2d

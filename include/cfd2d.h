@@ -45,6 +45,7 @@ extern "C" {
 #define CFD2D_ERR_NEWTON_CAP 503     /* the exact Riemann solver hit its iteration cap (state still advanced) */
 #define CFD2D_ERR_NONPHYSICAL 504    /* non-positive or NaN density/pressure appeared (state still advanced) */
 #define CFD2D_ERR_CAPACITY 505       /* a size exceeds a fixed capacity of the entry point */
+#define CFD2D_ERR_SOLVER 506         /* FVM_TVD_IMPLICIT: a steady run's linear solves kept failing (run stops) */
 
 /* ---- method selections (task.xml <control> extensions) ------------------ */
 enum { CFD2D_FLUX_GODUNOV = 0, CFD2D_FLUX_LAX = 1, CFD2D_FLUX_ROE = 2, CFD2D_FLUX_HLLC = 3 };

@@ -242,3 +242,17 @@ def test_implicit_full_size_step_matches_oracle(capi, oracle, tmp_path):
     o.step(1)
     assert s.implicit_stats()["iters"] == o.info()["iters"]
     assert close(s.state(), o.state()[0]) < RTOL
+
+
+def test_implicit_steady_run_stops_when_solves_keep_failing(capi, tmp_path, monkeypatch):
+    """A steady run whose every solve fails would loop forever in the reference (the step
+    counter only advances on success); the library stops with CFD2D_ERR_SOLVER."""
+    m, t, U0, path = make_case(tmp_path, n=6, flux="LAX", steady=1, step_max=3, cfl=(2.0, 1.5, 10.0, 1, 1.0e9),
+                               gmres=(30, 1, 1e-14))
+    monkeypatch.chdir(tmp_path)
+    s = capi.Solver(path)
+    with pytest.raises(capi.CfdError) as e:
+        s.run()
+    assert e.value.code == 506
+    st = s.implicit_stats()
+    assert st["status"] != 0 and st["cfl"] == pytest.approx(0.1)
