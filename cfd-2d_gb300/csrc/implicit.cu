@@ -88,6 +88,7 @@ __device__ __forceinline__ Roe roe_average(const Prim<double>& L, const Prim<dou
 // The two Gauss-point fluxes of an edge times l/2 (run's loop, :612-633): interior
 // faces reconstruct linearly from both centres (reconstruct(iFace, pL, pR, p),
 // :444-476), boundary faces take the centre state and its ghost.
+template <int FLUX>
 __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
@@ -110,14 +111,14 @@ __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
             reconstruct<double, RECON_LINEAR>(pL, gL, c.dl[(4 * gp) * ne + e], c.dl[(4 * gp + 1) * ne + e], qL);
             reconstruct<double, RECON_LINEAR>(pR, gR, c.dl[(4 * gp + 2) * ne + e], c.dl[(4 * gp + 3) * ne + e], qR);
             double f[4];
-            if (c.flux == FLUX_LAX) flux_lax(f, pL, pR, nx, ny, GAM, c.ig1_flux);
+            if constexpr (FLUX == FLUX_LAX) flux_lax(f, pL, pR, nx, ny, GAM, c.ig1_flux);
             else hit |= flux_godunov(f, pL, pR, nx, ny, GAM, c.newton_cap);
             fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
         }
     } else {  // both Gauss points see the same centre state and ghost
         const Prim<double> pR = imp_ghost(c.bnds[c.ebnd[e]], qL, nx, ny, imat(c, c1).M);
         double f[4];
-        if (c.flux == FLUX_LAX) flux_lax(f, qL, pR, nx, ny, GAM, c.ig1_flux);
+        if constexpr (FLUX == FLUX_LAX) flux_lax(f, qL, pR, nx, ny, GAM, c.ig1_flux);
         else hit |= flux_godunov(f, qL, pR, nx, ny, GAM, c.newton_cap);
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
@@ -413,7 +414,10 @@ inline int blocks(int n, int t) { return (n + t - 1) / t; }
 
 void imp_launch_prims(const ImpCase& c, cudaStream_t s) { k_imp_prims<<<blocks(c.nc, 256), 256, 0, s>>>(c); }
 void imp_launch_grad(const ImpCase& c, cudaStream_t s) { k_imp_grad<<<blocks(c.nc, 256), 256, 0, s>>>(c); }
-void imp_launch_flux(const ImpCase& c, cudaStream_t s) { k_imp_flux<<<blocks(c.ne, 256), 256, 0, s>>>(c); }
+void imp_launch_flux(const ImpCase& c, cudaStream_t s) {
+    if (c.flux == FLUX_LAX) k_imp_flux<FLUX_LAX><<<blocks(c.ne, 256), 256, 0, s>>>(c);
+    else k_imp_flux<FLUX_GODUNOV><<<blocks(c.ne, 256), 256, 0, s>>>(c);
+}
 void imp_launch_assemble(const ImpCase& c, cudaStream_t s) {
     k_imp_assemble<<<blocks(c.nc, 128), 128, 0, s>>>(c);
 }
