@@ -407,6 +407,10 @@ void* device_view(const void* p) {
         return nullptr;
     }
     if ((a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged) && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeDevice) {  // device memory of the current GPU: used in place
+        int dev = -1;
+        return cudaGetDevice(&dev) == cudaSuccess && dev == a.device ? const_cast<void*>(p) : nullptr;
+    }
     if (a.type == cudaMemoryTypeUnregistered) {
         int dev = 0, v = 0;
         if (cudaGetDevice(&dev) == cudaSuccess &&

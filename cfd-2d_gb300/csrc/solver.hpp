@@ -24,9 +24,10 @@ void log_line(const char* fmt, ...);
 void write_vtk_file(const char* name, const Topo& topo, const std::vector<TaskMaterial>& mats,
                     const std::vector<int>& cell_mat, const double* U, const double* ct, bool implicit_format = false);
 void announce_vtk(const char* name);
-// The address through which kernels on the current device read or write host array p:
-// pinned (or registered) memory, or pageable memory where the device has coherent
-// access to it; nullptr when neither (the caller then stages through a copy).
+// The address through which kernels on the current device read or write array p:
+// pinned (or registered) or managed memory, pageable memory where the device has
+// coherent access to it, or device memory of the current GPU itself; nullptr otherwise
+// (the caller then stages through a copy).
 void* device_view(const void* p);
 void set_verbosity(int v);
 void set_log_file(const char* path);

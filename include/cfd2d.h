@@ -103,7 +103,13 @@ int cfd2d_destroy(cfd2d_t* h);
 
 int cfd2d_get_info(const cfd2d_t* h, cfd2d_info_t* info);
 
-/* Conserved state ro, ru, rv, re (FVM_TVD's arrays, src/methods/fvm_tvd.h:86-89). */
+/* Conserved state ro, ru, rv, re (FVM_TVD's arrays, src/methods/fvm_tvd.h:86-89).
+ * The arrays of get_state / set_state are host memory (pinned or pageable) or device
+ * memory of the handle's GPU; kernels read and write them in place where the GPU can
+ * address them (pinned, managed, device, or pageable on systems with coherent host
+ * access such as Grace), else through a staging copy. Device data must be complete
+ * when the call is made (the library works on its own stream); both calls return
+ * with the transfer done. */
 int cfd2d_get_state(cfd2d_t* h, double* ro, double* ru, double* rv, double* re);
 /* Replace the conserved state. reset_time_step != 0 redoes init's time step
  * (TAU = min(TAU from task.xml, CFL pass), src/methods/fvm_tvd.cpp:211). */

@@ -62,3 +62,27 @@ def test_injected_nonphysical_state_is_a_status(capi, tmp_path, precision, bad):
     assert rc == capi.ERR_NONPHYSICAL
     s.set_state(U0)  # the handle stays usable
     assert s.step(1, allow_warnings=True) == capi.OK
+
+
+def test_state_exchange_with_device_and_pinned_buffers(capi, tmp_path):
+    """cfd2d_set_state / cfd2d_get_state accept device buffers of the handle's GPU and pinned host
+    buffers as well as pageable ones, with identical results."""
+    torch = pytest.importorskip("torch")
+    from cfd2d import cases
+    t, m, U0 = cases.vortex(12, flux="HLLC", recon="MINMOD", scheme="SSPRK3", steps=5)
+    path = cases.write_task(t, m, str(tmp_path))
+    ref = capi.Solver(path, mesh=m)
+    ref.set_state(U0)
+    ref.step(2)
+    want = ref.state()
+    for kind in ("cuda", "pinned"):
+        s = capi.Solver(path, mesh=m)
+        src = torch.from_numpy(U0.copy())
+        src = src.cuda() if kind == "cuda" else src.pin_memory()
+        dst = torch.zeros_like(src)
+        torch.cuda.synchronize()  # device data handed to the library must be ready
+        s.set_state_from([src[k].data_ptr() for k in range(4)])
+        s.step(2)
+        s.state_into([dst[k].data_ptr() for k in range(4)])
+        got = dst.cpu().numpy()
+        assert np.array_equal(got.view(np.int64), want.view(np.int64)), kind
