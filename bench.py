@@ -530,6 +530,94 @@ def implicit_workload(args, capi, cases, world, rank, dist, W, K):
         print(json.dumps(line), flush=True)
 
 
+DG_N = 1024
+
+
+def rkdg_cpu_baseline(n=DG_N, steps=1):
+    """The oracle's FEM_RKDG on one host core: a bounded sample of the same workload
+    (one step of the full mesh, ~10-20 s of CPU work)."""
+    from cfd2d import cases
+    from oracle import pyoracle
+    pyoracle.build()
+    t, m, pm, U0 = cases.rkdg_vortex(n, flux="GODUNOV")
+    o = pyoracle.OracleDG(t, pm)
+    o.set_coeffs(U0)
+    a = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - a
+    return {"value": len(pm.tris) * steps / dt, "unit": UNIT, "cores": 1, "kind": "port", "cpu": cpu_model(),
+            "sample": f"{steps} FEM_RKDG step(s) of the same vortex at {n}x{n}x2 = {len(pm.tris)} triangles on one core"}
+
+
+def rkdg_workload(args, capi, cases, world, rank, dist, W, K):
+    """FEM_RKDG, the reference's explicit P1 discontinuous Galerkin method: isentropic vortex
+    (strength 2) on [0,10]^2, 1024x1024x2 = 2,097,152 jittered triangles (seed 5) as P1
+    coefficients, free-stream inlets, 4-point cell and 3-point edge quadrature, GODUNOV flux
+    (LAX reported beside it), the reference's two stages, unsteady (TAU from the reference's
+    CFL rule). Device time from CUDA events over the step graphs."""
+    n = args.dg_n
+    d = tempfile.mkdtemp(prefix="cfd2d_dg_")
+    out = {}
+    fluxes = ("GODUNOV", "LAX") if args.dg_flux == "both" else (args.dg_flux,)
+    cells = bytes_dev = 0
+    for flux in fluxes:
+        t, m, pm, U0 = cases.rkdg_vortex(n, flux=flux)
+        dk = os.path.join(d, flux)
+        os.makedirs(dk, exist_ok=True)
+        with open(os.path.join(dk, "task.xml"), "w") as f:
+            f.write(cases.mg.write_rkdg_task_xml(t))
+        mesh = cases.mg.Mesh(pm.nodes, pm.tris, m.cell_region, m.bsegs, m.bseg_bnd)
+        s = capi.Solver(os.path.join(dk, "task.xml"), mesh=mesh)
+        s.set_dg_coeffs(U0)
+        s.step(W)
+        barrier(dist)
+        ms = reduce_max(dist, s.timed_steps(K))
+        nc = len(pm.tris)
+        out[flux] = {"ms_per_step": ms / K, "value": world * nc * K / (ms * 1e-3), "tau": s.tau}
+        if not args.no_profile:
+            prof_ms, prof_n = s.profile_steps(2)
+            tot = max(float(prof_ms.sum()), 1e-30)
+            out[flux]["kernels"] = {k: {"ms_per_step": float(prof_ms[i] / 2), "share": float(prof_ms[i] / tot),
+                                        "launches_per_step": int(prof_n[i])}
+                                    for i, k in enumerate(["k_dg_edge", "k_dg_cell", "k_dg_tstep"])}
+        cells, bytes_dev = nc, s.get_info().device_bytes
+        if flux == fluxes[0] and not args.no_e2e:
+            import torch
+            pin_in = torch.empty((nc, 12), dtype=torch.float64).pin_memory()
+            pin_out = torch.empty((nc, 12), dtype=torch.float64).pin_memory()
+            pin_in.copy_(torch.from_numpy(s.dg_coeffs()))
+            Ke = min(K, 10)
+            barrier(dist)
+            a = time.perf_counter()
+            for _ in range(Ke):
+                s.set_dg_coeffs_from(pin_in.data_ptr())
+                s.step(1)
+                s.dg_coeffs_into(pin_out.data_ptr())
+            e2e_s = reduce_max(dist, (time.perf_counter() - a) / Ke)
+            out["e2e"] = {"value": world * nc / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 96 * nc,
+                          "d2h_bytes_per_step": 96 * nc, "steps": Ke,
+                          "path": "cfd2d_dg_set_coeffs + cfd2d_step(1) + cfd2d_dg_get_coeffs, pinned host buffers"}
+        s.close()
+    main_ = out[fluxes[0]]
+    if rank == 0:
+        line = {
+            "metric": "FEM_RKDG cell-updates/s at 2.1M triangles (P1 discontinuous Galerkin, two stages per step)",
+            "value": main_["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": main_["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"isentropic vortex on [0,10]^2, {n}x{n}x2 = {cells} jittered triangles (seed 5), "
+                                   f"P1 coefficients, free-stream inlets, {fluxes[0]} flux, 4-point cell and 3-point edge "
+                                   "quadrature, the reference's Runge-Kutta stages", "cells": cells,
+                       "device_bytes": bytes_dev, "l2": "no flush: a step streams ~3 GB"},
+            "godunov": out.get("GODUNOV"), "lax": out.get("LAX"), "e2e": out.get("e2e"),
+        }
+        if "kernels" in main_:
+            line["gpu_launches"] = K * sum(v["launches_per_step"] for v in main_["kernels"].values())
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = rkdg_cpu_baseline(n)
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -542,12 +630,14 @@ def main():
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--n", type=int, default=N_SIDE, help="squares per side (profiling runs only)")
     ap.add_argument("--workload", default="four_quadrant",
-                    choices=["four_quadrant", "batched", "combined", "adjoint", "implicit"],
+                    choices=["four_quadrant", "batched", "combined", "adjoint", "implicit", "rkdg"],
                     help="four_quadrant: the headline 2.1M-triangle line; batched: 256 uneven vortex instances")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--adj-n", type=int, default=256, help="squares per side of the adjoint-only run's vortex")
     ap.add_argument("--imp-n", type=int, default=IMP_N, help="squares per side of the implicit workload's vortex")
     ap.add_argument("--imp-flux", default="both", choices=["both", "LAX", "GODUNOV"])
+    ap.add_argument("--dg-n", type=int, default=DG_N, help="squares per side of the FEM_RKDG workload's vortex")
+    ap.add_argument("--dg-flux", default="both", choices=["both", "LAX", "GODUNOV"])
     args = ap.parse_args()
     world, rank, local, dist = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -569,6 +659,9 @@ def main():
         return
     if args.workload == "implicit":
         implicit_workload(args, capi, cases, world, rank, dist, W, K)
+        return
+    if args.workload == "rkdg":
+        rkdg_workload(args, capi, cases, world, rank, dist, W, K)
         return
     if args.workload == "adjoint":  # one checkpointed forward + backward of K steps (profiling runs)
         t, m, U0, w, _ = cases.vortex_adjoint(args.adj_n, steps=K)

@@ -38,14 +38,14 @@ def cuda_home() -> str:
 
 
 HOST_SOURCES = ["xml.cpp", "mesh.cpp", "task.cpp", "solver.cpp", "solver_adjoint.cpp", "solver_batch.cpp",
-                "solver_tiles.cpp", "implicit.cpp", "capi.cpp"]
+                "solver_tiles.cpp", "implicit.cpp", "rkdg.cpp", "capi.cpp"]
 # -fmad per translation unit: "false" for the bit-exact FP64 path, "true" for the mixed form
 # (with fast math), "fma" for FMA contraction with IEEE division and square root
 DEVICE_SOURCES = {"kern_fp64.cu": "false", "kern_common.cu": "false", "kern_mixed.cu": "true",
                   "noalloc.cu": "false", "adjoint.cu": "false", "adjoint_mixed.cu": "true",
-                  "implicit.cu": "false", "gmres.cu": "fma"}
+                  "implicit.cu": "false", "gmres.cu": "fma", "rkdg.cu": "false"}
 HEADERS = ["xml.hpp", "mesh.hpp", "task.hpp", "solver.hpp", "kernels.hpp", "kernels.cuh", "kern_inst.cuh",
-           "adjoint.cuh", "adj_inst.cuh", "implicit.hpp"]
+           "adjoint.cuh", "adj_inst.cuh", "implicit.hpp", "rkdg.hpp"]
 
 
 def _stale(out: str, deps) -> bool:

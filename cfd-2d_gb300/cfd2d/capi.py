@@ -77,6 +77,10 @@ SIGNATURES = {
                                           _P, _P, _P],
     "cfd2d_implicit_system": [_P, _D, _D, _D, _D],
     "cfd2d_implicit_stats": [_P, C.POINTER(ImplicitStats)],
+    "cfd2d_dg_get_coeffs": [_P, _D],
+    "cfd2d_dg_set_coeffs": [_P, _D],
+    "cfd2d_dg_set_time_step": [_P, C.c_double],
+    "cfd2d_dg_residuals": [_P, _D],
     "cfd2d_selftest": [_I, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)],
     "cfd2d_set_device": [_I],
     "cfd2d_last_error": [C.c_char_p, C.c_size_t],
@@ -278,6 +282,31 @@ class Solver:
         st = ImplicitStats()
         check(lib().cfd2d_implicit_stats(self.h, C.byref(st)))
         return dict(iters=st.iterations, status=st.status, n_lim=st.n_limited, rel=st.rel_residual, cfl=st.cfl)
+
+    # FEM_RKDG handles: P1 coefficients, 12 per cell (ro[3] ru[3] rv[3] re[3])
+    def dg_coeffs(self, out=None) -> np.ndarray:
+        U = np.empty((self.n, 12)) if out is None else out
+        check(lib().cfd2d_dg_get_coeffs(self.h, _d(U)))
+        return U
+
+    def set_dg_coeffs(self, U):
+        U = np.ascontiguousarray(U, np.float64).reshape(self.n, 12)
+        check(lib().cfd2d_dg_set_coeffs(self.h, _d(U)))
+
+    def dg_coeffs_into(self, ptr):
+        """cfd2d_dg_get_coeffs into a raw pointer (host, pinned or device)."""
+        check(lib().cfd2d_dg_get_coeffs(self.h, C.cast(ptr, C.POINTER(C.c_double))))
+
+    def set_dg_coeffs_from(self, ptr):
+        check(lib().cfd2d_dg_set_coeffs(self.h, C.cast(ptr, C.POINTER(C.c_double))))
+
+    def dg_set_time_step(self, tau: float):
+        check(lib().cfd2d_dg_set_time_step(self.h, float(tau)))
+
+    def dg_residuals(self) -> np.ndarray:
+        r = np.zeros(4)
+        check(lib().cfd2d_dg_residuals(self.h, _d(r)))
+        return r
 
     def state_into(self, ptrs):
         """get_state into four raw host pointers (e.g. pinned buffers)."""

@@ -148,3 +148,92 @@ def write_implicit_task(task, mesh, directory=None, with_mesh_files=False) -> st
             with open(os.path.join(d, task.mesh_name + ext), "w") as f:
                 f.write(txt)
     return path
+
+
+# ---------------------------------------------------------------- FEM_RKDG (P1 discontinuous Galerkin)
+
+MILD_QUADRANTS = {  # (rho, u, v, p): a gentle four-state problem the unlimited P1 method survives
+    "NE": (1.0, 0.1, 0.0, 1.0),
+    "NW": (1.1, 0.0, 0.1, 1.05),
+    "SW": (0.95, 0.1, 0.1, 0.98),
+    "SE": (1.05, -0.1, 0.0, 1.1),
+}
+
+
+def dg_cell_frame(pm):
+    """Cell centres and the basis scales HX, HY of a .proc part the way Grid::readMeshFiles
+    forms them (src/mesh/grid.cpp:306-317)."""
+    p = pm.nodes[pm.tris]
+    cx = (p[:, 0, 0] + p[:, 1, 0] + p[:, 2, 0]) / 3.0
+    cy = (p[:, 0, 1] + p[:, 1, 1] + p[:, 2, 1]) / 3.0
+
+    def h(k):
+        a = np.abs(p[:, 0, k] - p[:, 1, k]); b = np.abs(p[:, 1, k] - p[:, 2, k]); c = np.abs(p[:, 0, k] - p[:, 2, k])
+        return np.maximum(a, np.maximum(b, c))
+    return cx, cy, h(0), h(1)
+
+
+def dg_p1_coeffs(pm, field):
+    """P1 coefficients (nc, 12: ro[3] ru[3] rv[3] re[3]) of a smooth conserved field
+    field(x, y) -> (4, n): the centre value and the centred-difference slopes times HX, HY."""
+    cx, cy, HX, HY = dg_cell_frame(pm)
+    d = 1.0e-6
+    U = field(cx, cy)
+    Ux = (field(cx + d, cy) - field(cx - d, cy)) / (2.0 * d)
+    Uy = (field(cx, cy + d) - field(cx, cy - d)) / (2.0 * d)
+    out = np.empty((len(cx), 12))
+    for v in range(4):
+        out[:, 3 * v] = U[v]
+        out[:, 3 * v + 1] = Ux[v] * HX
+        out[:, 3 * v + 2] = Uy[v] * HY
+    return out
+
+
+def rkdg_vortex(n: int, *, flux="GODUNOV", gp_cell=4, gp_edge=3, tau=2.0e-3, beta=2.0, seed=5, jitter=0.1,
+                steps=10, steady=0, cfl=0.3, rk=None, kinds=("BOUND_INLET",)):
+    """Isentropic vortex (strength beta at (5, 5), free stream rho=u=p=1) on [0,10]^2 for FEM_RKDG:
+    n x n x 2 triangles, P1 coefficients of the exact field at t = 0, free-stream boundaries
+    (or the kinds given, cycled over the four sides). Returns (task, mesh, part, U0)."""
+    m = mg.jittered_square(n, 0.0, 10.0, 0.0, 10.0, jitter, seed)
+    m.bseg_bnd = (m.bseg_side % len(kinds)).astype(np.int32)
+    bnds = [mg.Boundary(f"side{k}", kd, k + 1, 1.0, 0.0, 1.0, 1.0) for k, kd in enumerate(kinds)]
+    t = mg.RkdgTask(regions=[mg.Region("fluid", 1.0, 0.0, 1.0, 1.0)], boundaries=bnds, steady=steady, tau=tau,
+                    tmax=tau * steps, cfl=cfl, gp_cell=gp_cell, gp_edge=gp_edge, flux=flux, rk=rk)
+    pm = mg.proc_mesh(m, [r.name for r in t.regions], [b.name for b in bnds])
+
+    def field(x, y):
+        return mg.isentropic_vortex(np.stack([x, y], axis=1), beta, 5.0, 5.0)
+    return t, m, pm, dg_p1_coeffs(pm, field)
+
+
+def rkdg_quadrants(n: int, *, flux="GODUNOV", gp_cell=4, gp_edge=3, tau=1.0e-3, seed=6, jitter=0.1, steps=10,
+                   steady=0, cfl=0.3, rk=None,
+                   kinds=("BOUND_OUTLET", "BOUND_WALL_SLIP", "BOUND_INLET", "BOUND_WALL_NO_SLIP"), materials=None):
+    """Four gentle quadrant states (MILD_QUADRANTS) on [0,1]^2 set by the task's regions (the
+    reference's own initialisation), one boundary kind per side. Returns (task, mesh, part, None)."""
+    m = mg.jittered_square(n, 0.0, 1.0, 0.0, 1.0, jitter, seed)
+    m.cell_region = mg.quadrant_regions(m.centroids())
+    m.bseg_bnd = (m.bseg_side % len(kinds)).astype(np.int32)
+    regs = []
+    for k, q in enumerate(mg.QUADRANT_ORDER):
+        r, u, v, p = MILD_QUADRANTS[q]
+        regs.append(mg.Region(q, u, v, p / r, p, mat=(k % 2) if materials else 0))
+    bnds = [mg.Boundary(f"b{k}", kd, k + 1, 0.1, 0.05, 1.0, 1.02) for k, kd in enumerate(kinds)]
+    kw = dict(materials=materials) if materials else {}
+    t = mg.RkdgTask(regions=regs, boundaries=bnds, steady=steady, tau=tau, tmax=tau * steps, cfl=cfl,
+                    gp_cell=gp_cell, gp_edge=gp_edge, flux=flux, rk=rk, **kw)
+    pm = mg.proc_mesh(m, [r.name for r in regs], [b.name for b in bnds])
+    return t, m, pm, None
+
+
+def write_rkdg_task(task, pm, directory=None) -> str:
+    """task.xml and mesh/mesh.0000.proc in a directory; returns the task path (the method
+    reads the mesh part relative to the working directory)."""
+    d = directory or tempfile.mkdtemp(prefix="cfd2d_dg_")
+    os.makedirs(os.path.join(d, "mesh"), exist_ok=True)
+    with open(os.path.join(d, "mesh", "mesh.0000.proc"), "w") as f:
+        f.write(mg.write_proc(pm))
+    path = os.path.join(d, "task.xml")
+    with open(path, "w") as f:
+        f.write(mg.write_rkdg_task_xml(task))
+    return path

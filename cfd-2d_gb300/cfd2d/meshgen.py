@@ -399,3 +399,162 @@ def write_implicit_task_xml(t: ImplicitTask) -> str:
         L.append("    </boundCond>")
     L += ["  </boundaries>", "  <mesh>", f'    <name value="{t.mesh_name}" />', "  </mesh>", "</task>", ""]
     return "\n".join(L)
+
+
+# ------------------------------------------------------- FEM_RKDG: .proc mesh parts and task.xml
+
+EDGE_TYPE_NAMED = 0x100  # Edge::TYPE_NAMED, src/mesh/grid.h:70
+
+
+@dataclass
+class ProcMesh:
+    """One mesh part the way the DECOMP method writes it for a single process
+    (src/methods/decomp.cpp:296-331) and Grid::readMeshFiles reads it
+    (src/mesh/grid.cpp:275-420): nodes, triangles with a region name each, and edges
+    as node pairs with a type (0 inside; EDGE_TYPE_NAMED with a boundary name, or a
+    numeric edgeType). Coordinates are what the file holds (printed with %25.15e)."""
+    nodes: np.ndarray          # (nn, 2) float64
+    tris: np.ndarray           # (nc, 3) int32
+    cell_names: list           # (nc,) region name per cell
+    edges: np.ndarray          # (ne, 2) int32
+    edge_type: np.ndarray      # (ne,) int32
+    edge_names: list           # (ne,) boundary name ("" inside)
+
+
+def proc_mesh(mesh: Mesh, region_names, bnd_names=None, bnd_types=None) -> ProcMesh:
+    """The single-process part of a mesh. Edges are numbered in order of first appearance
+    over the cells (cell i, its sides (t0,t1), (t1,t2), (t2,t0)), oriented as first seen.
+    Boundary edges carry the boundary of their segment: by name (bnd_names, the UNV
+    groups' way) or by number (bnd_types, the Triangle markers' way)."""
+    nodes = np.array([[float(f"{x:25.15e}"), float(f"{y:25.15e}")] for x, y in mesh.nodes])
+    tris = mesh.tris.astype(np.int32)
+    a = tris.reshape(-1)
+    b = tris[:, [1, 2, 0]].reshape(-1)
+    key = np.minimum(a, b).astype(np.int64) * (1 << 32) + np.maximum(a, b)
+    uniq, first = np.unique(key, return_index=True)
+    order = np.sort(first)
+    edges = np.stack([a[order], b[order]], axis=1).astype(np.int32)
+    ekey = key[order]
+    bkey = np.minimum(mesh.bsegs[:, 0], mesh.bsegs[:, 1]).astype(np.int64) * (1 << 32) + \
+        np.maximum(mesh.bsegs[:, 0], mesh.bsegs[:, 1])
+    pos = {int(k): i for i, k in enumerate(ekey)}
+    etype = np.zeros(len(edges), np.int32)
+    enames = [""] * len(edges)
+    for s, k in enumerate(bkey):
+        e = pos[int(k)]
+        bi = int(mesh.bseg_bnd[s])
+        if bnd_types is None:
+            etype[e] = EDGE_TYPE_NAMED
+            enames[e] = bnd_names[bi]
+        else:
+            etype[e] = int(bnd_types[bi])
+            enames[e] = str(int(bnd_types[bi]))
+    return ProcMesh(nodes=nodes, tris=tris, cell_names=[region_names[int(r)] for r in mesh.cell_region],
+                    edges=edges, edge_type=etype, edge_names=enames)
+
+
+def write_proc(pm: ProcMesh) -> str:
+    """mesh.0000.proc text of a single-process part (the DECOMP writer's layout)."""
+    out = io.StringIO()
+    w = out.write
+    nn, nc, ne = len(pm.nodes), len(pm.tris), len(pm.edges)
+    w(f"{nn} {nn}\n")
+    for i, (x, y) in enumerate(pm.nodes):
+        w(f"{i:6d} {x:25.15e} {y:25.15e}\n")
+    w(f"\n{nc} {nc}\n")
+    for i, (t, nm) in enumerate(zip(pm.tris, pm.cell_names)):
+        w(f"{i:6d} {t[0]:6d} {t[1]:6d} {t[2]:6d} {nm}\n")
+    w(f"\n{ne} {ne}\n")
+    for i, ((p, q), ty, nm) in enumerate(zip(pm.edges, pm.edge_type, pm.edge_names)):
+        w(f"{i:6d} {p:6d} {q:6d} {int(ty):6d} {nm if ty != 0 else ''}\n")
+    w("\n0\n\n0 0\n")
+    return out.getvalue()
+
+
+def read_proc(text: str) -> ProcMesh:
+    """Parse a single-process .proc part (whitespace-separated, as fscanf reads it)."""
+    tok = text.split()
+    k = 0
+
+    def nxt():
+        nonlocal k
+        k += 1
+        return tok[k - 1]
+    nn, nnx = int(nxt()), int(nxt())
+    nodes = np.empty((nnx, 2))
+    for i in range(nnx):
+        nxt()
+        nodes[i] = float(nxt()), float(nxt())
+    nc, ncx = int(nxt()), int(nxt())
+    tris = np.empty((ncx, 3), np.int32)
+    names = []
+    for i in range(ncx):
+        nxt()
+        tris[i] = int(nxt()), int(nxt()), int(nxt())
+        names.append(nxt())
+    ne, nex = int(nxt()), int(nxt())
+    edges = np.empty((nex, 2), np.int32)
+    et = np.zeros(nex, np.int32)
+    en = [""] * nex
+    for i in range(nex):
+        nxt()
+        edges[i] = int(nxt()), int(nxt())
+        et[i] = int(nxt())
+        if et[i] != 0:
+            en[i] = nxt()
+    return ProcMesh(nodes=nodes, tris=tris, cell_names=names, edges=edges, edge_type=et, edge_names=en)
+
+
+@dataclass
+class RkdgTask:
+    """task.xml of the reference's FEM_RKDG (src/methods/fem_rkdg.cpp:23-380): the mesh is
+    read from mesh/mesh.0000.proc in the working directory; regions are bound by name,
+    boundaries by name (named edges) or edgeType."""
+    regions: list              # Region (name, u, v, T, p, mat)
+    boundaries: list           # Boundary (name, kind, edge_type, u, v, T, p)
+    steady: int = 0
+    tau: float = 1.0e-3
+    tmax: float = 1.0e8
+    cfl: float = 0.5
+    file_output_step: int = 1000000
+    log_output_step: int = 1000000
+    func_count: int = 3
+    gp_cell: int = 4
+    gp_edge: int = 3
+    flux: str = "GODUNOV"      # GODUNOV / LAX (anything else: GODUNOV)
+    materials: list = field(default_factory=lambda: [("gas", 8.314472, 3.5, 0.0, 0.0)])
+    rk: str | None = None      # GPU option RK_MODE: REFERENCE (default) / HEUN
+
+
+def write_rkdg_task_xml(t: RkdgTask) -> str:
+    L = ['<?xml version="1.0" encoding="UTF-8"?>', '<task method="FEM_RKDG">', "  <control>",
+         f'    <STEADY value="{int(t.steady)}" />', f'    <TAU value="{_v(t.tau)}" />',
+         f'    <TMAX value="{_v(t.tmax)}" />', f'    <CFL value="{_v(t.cfl)}" />',
+         f'    <FILE_OUTPUT_STEP value="{int(t.file_output_step)}" />',
+         f'    <LOG_OUTPUT_STEP value="{int(t.log_output_step)}" />',
+         f'    <BASE_FUNC_COUNT value="{int(t.func_count)}" />', f'    <GP_CELL_COUNT value="{int(t.gp_cell)}" />',
+         f'    <GP_EDGE_COUNT value="{int(t.gp_edge)}" />', f'    <FLUX value="{t.flux}" />']
+    if t.rk is not None:
+        L.append(f'    <RK_MODE value="{t.rk}" />')
+    L += ["  </control>", f'  <materials count="{len(t.materials)}">']
+    for k, (name, M, Cp, K, ML) in enumerate(t.materials):
+        L += [f'    <material id="{k}">', f"      <name>{name}</name>", "      <parameters>",
+              f'        <M value="{_v(M)}" />', f'        <Cp value="{_v(Cp)}" />',
+              f'        <K value="{_v(K)}" />', f'        <ML value="{_v(ML)}" />',
+              "      </parameters>", "    </material>"]
+    L += ["  </materials>", f'  <regions count="{len(t.regions)}">']
+    for k, r in enumerate(t.regions):
+        L += [f'    <region id="{k}">', f'      <material id="{r.mat}" />', '      <cell type="3" />',
+              f"      <name>{r.name}</name>", "      <parameters>", f'        <Vx value="{_v(r.u)}" />',
+              f'        <Vy value="{_v(r.v)}" />', f'        <T value="{_v(r.T)}" />',
+              f'        <P value="{_v(r.p)}" />', "      </parameters>", "    </region>"]
+    L += ["  </regions>", "  <boundaries>"]
+    for b in t.boundaries:
+        L += [f'    <boundCond edgeType="{b.edge_type}">', f"      <type>{b.kind}</type>",
+              f"      <name>{b.name}</name>"]
+        if b.kind == "BOUND_INLET":
+            L += ["      <parameters>", f'        <Vx value="{_v(b.u)}" />', f'        <Vy value="{_v(b.v)}" />',
+                  f'        <T value="{_v(b.T)}" />', f'        <P value="{_v(b.p)}" />', "      </parameters>"]
+        L.append("    </boundCond>")
+    L += ["  </boundaries>", "</task>", ""]
+    return "\n".join(L)

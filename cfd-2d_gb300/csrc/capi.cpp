@@ -11,6 +11,7 @@
 
 #include "cfd2d.h"
 #include "implicit.hpp"
+#include "rkdg.hpp"
 #include "mesh.hpp"
 #include "solver.hpp"
 #include "task.hpp"
@@ -19,6 +20,7 @@
 struct cfd2d_solver {
     std::unique_ptr<cfd2d::Solver> s;
     std::unique_ptr<cfd2d::ImplicitSolver> imp;
+    std::unique_ptr<cfd2d::RkdgSolver> dg;
 };
 
 struct cfd2d_mesh {
@@ -150,8 +152,15 @@ std::vector<int> edge_bnd_from_desc(const cfd2d_mesh_desc* m, const cfd2d::Topo&
 // The explicit solver of a handle; entry points of the explicit method only fail on
 // an implicit handle.
 cfd2d::Solver& ex(const cfd2d_t* h) {
-    if (!h->s) throw cfd2d::Error(CFD2D_ERR_INVALID_ARG, "not available for the FVM_TVD_IMPLICIT method");
+    if (!h->s)
+        throw cfd2d::Error(CFD2D_ERR_INVALID_ARG,
+                           h->dg ? "not available for the FEM_RKDG method" : "not available for the FVM_TVD_IMPLICIT method");
     return *h->s;
+}
+
+cfd2d::RkdgSolver& dgs(const cfd2d_t* h) {
+    if (!h->dg) throw cfd2d::Error(CFD2D_ERR_INVALID_ARG, "not a FEM_RKDG handle");
+    return *h->dg;
 }
 
 }  // namespace
@@ -164,11 +173,17 @@ int cfd2d_create(const char* task_xml_path, cfd2d_t** out) {
         if (!task_xml_path || !out) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
         *out = nullptr;
         cfd2d::TaskConfig t = cfd2d::parse_task(task_xml_path);
+        auto h = std::make_unique<cfd2d_solver>();
+        if (t.method == cfd2d::METHOD_FEM_RKDG) {  // Grid::readMeshFiles: mesh/mesh.0000.proc
+            cfd2d::DgMesh m = cfd2d::read_proc_mesh(resolve(t, t.mesh_name, ""));
+            h->dg = std::make_unique<cfd2d::RkdgSolver>(t, std::move(m));
+            *out = h.release();
+            return CFD2D_OK;
+        }
         cfd2d::Topo topo;
         std::vector<int> cr, eb;
         int gp = 2;
         load_task_mesh(t, topo, cr, eb, gp);
-        auto h = std::make_unique<cfd2d_solver>();
         if (t.method == cfd2d::METHOD_FVM_TVD_IMPLICIT)
             h->imp = std::make_unique<cfd2d::ImplicitSolver>(t, std::move(topo), cr, eb);
         else
@@ -186,6 +201,17 @@ int cfd2d_create_with_mesh(const char* task_xml_path, const cfd2d_mesh_desc* mes
         check_desc(mesh);
         if (!mesh->cell_region) return fail(CFD2D_ERR_INVALID_ARG, "cell_region is required");
         cfd2d::TaskConfig t = cfd2d::parse_task(task_xml_path);
+        if (t.method == cfd2d::METHOD_FEM_RKDG) {
+            std::vector<std::string> names;
+            for (auto& r : t.regions) names.push_back(r.name);
+            cfd2d::DgMesh m = cfd2d::dg_mesh_from_arrays(mesh->n_nodes, mesh->xy, mesh->n_cells, mesh->tri,
+                                                         mesh->cell_region, names, mesh->n_bsegs, mesh->bseg,
+                                                         mesh->bseg_bnd, t.bnds);
+            auto h = std::make_unique<cfd2d_solver>();
+            h->dg = std::make_unique<cfd2d::RkdgSolver>(t, std::move(m));
+            *out = h.release();
+            return CFD2D_OK;
+        }
         const bool imp = t.method == cfd2d::METHOD_FVM_TVD_IMPLICIT;
         std::vector<int> tn;
         if (imp) tn = triangle_neigh(mesh->n_cells, mesh->tri);
@@ -292,7 +318,7 @@ int cfd2d_step(cfd2d_t* h, int nsteps) {
     Range r("cfd2d_step");
     return guarded([&] {
         if (!h || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
-        int s = h->imp ? h->imp->step(nsteps) : ex(h).step(nsteps);
+        int s = h->dg ? h->dg->step(nsteps) : h->imp ? h->imp->step(nsteps) : ex(h).step(nsteps);
         if (s != CFD2D_OK) g_err = s == CFD2D_ERR_NEWTON_CAP ? "exact Riemann solver hit its iteration cap"
                                                             : "non-positive or NaN density/pressure";
         return s;
@@ -303,7 +329,7 @@ int cfd2d_run(cfd2d_t* h) {
     Range r("cfd2d_run");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        return h->imp ? h->imp->run() : ex(h).run();
+        return h->dg ? h->dg->run() : h->imp ? h->imp->run() : ex(h).run();
     });
 }
 
@@ -318,6 +344,24 @@ int cfd2d_get_info(const cfd2d_t* h, cfd2d_info_t* info) {
     return guarded([&] {
         if (!h || !info) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
         std::memset(info, 0, sizeof *info);
+        if (h->dg) {
+            const cfd2d::RkdgSolver& m = *h->dg;
+            info->n_cells = m.nc();
+            info->n_edges = m.ne();
+            info->n_boundary_edges = m.n_boundary_edges();
+            info->n_nodes = m.n_nodes();
+            info->step = m.n_steps();
+            info->flux = m.task().flux;
+            info->recon = -1;
+            info->scheme = -1;
+            info->precision = m.task().precision;
+            info->steady = m.task().steady;
+            info->time = m.time();
+            info->tau = m.tau();
+            info->device_bytes = m.device_bytes();
+            info->n_instances = 1;
+            return CFD2D_OK;
+        }
         if (h->imp) {
             const cfd2d::ImplicitSolver& m = *h->imp;
             info->n_cells = m.topo().nc;
@@ -359,7 +403,8 @@ int cfd2d_get_state(cfd2d_t* h, double* ro, double* ru, double* rv, double* re) 
     Range r("cfd2d_get_state");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        if (h->imp) h->imp->get_state(ro, ru, rv, re);
+        if (h->dg) h->dg->get_state(ro, ru, rv, re);
+        else if (h->imp) h->imp->get_state(ro, ru, rv, re);
         else ex(h).get_state(ro, ru, rv, re);
         return CFD2D_OK;
     });
@@ -370,7 +415,8 @@ int cfd2d_set_state(cfd2d_t* h, const double* ro, const double* ru, const double
     Range r("cfd2d_set_state");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        if (h->imp) h->imp->set_state(ro, ru, rv, re);
+        if (h->dg) h->dg->set_state(ro, ru, rv, re);
+        else if (h->imp) h->imp->set_state(ro, ru, rv, re);
         else ex(h).set_state(ro, ru, rv, re, reset_time_step != 0);
         return CFD2D_OK;
     });
@@ -379,7 +425,8 @@ int cfd2d_set_state(cfd2d_t* h, const double* ro, const double* ru, const double
 int cfd2d_get_time_step(cfd2d_t* h, double* ctau) {
     return guarded([&] {
         if (!h || !ctau) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        if (h->imp) h->imp->get_ctau(ctau);
+        if (h->dg) h->dg->get_ctau(ctau);
+        else if (h->imp) h->imp->get_ctau(ctau);
         else ex(h).get_ctau(ctau);
         return CFD2D_OK;
     });
@@ -415,7 +462,8 @@ int cfd2d_save_vtk(cfd2d_t* h, int step) {
     Range r("cfd2d_save_vtk");
     return guarded([&] {
         if (!h) return fail(CFD2D_ERR_INVALID_ARG, "null handle");
-        if (h->imp) h->imp->save_vtk(step);
+        if (h->dg) h->dg->save_vtu(step);
+        else if (h->imp) h->imp->save_vtk(step);
         else ex(h).save_vtk(step);
         return CFD2D_OK;
     });
@@ -480,7 +528,9 @@ int cfd2d_timed_steps(cfd2d_t* h, int nsteps, double* device_ms) {
     Range r("cfd2d_timed_steps");
     return guarded([&] {
         if (!h || !device_ms || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
-        *device_ms = h->imp ? h->imp->timed_steps(nsteps) : ex(h).timed_steps(nsteps);
+        *device_ms = h->dg    ? h->dg->timed_steps(nsteps)
+                     : h->imp ? h->imp->timed_steps(nsteps)
+                              : ex(h).timed_steps(nsteps);
         return CFD2D_OK;
     });
 }
@@ -489,8 +539,15 @@ int cfd2d_profile_steps(cfd2d_t* h, int nsteps, double kernel_ms[4], int kernel_
     Range r("cfd2d_profile_steps");
     return guarded([&] {
         if (!h || !kernel_ms || !kernel_launches || nsteps < 0) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
-        if (h->imp) h->imp->profile_steps(nsteps, kernel_ms, kernel_launches);
-        else ex(h).profile_steps(nsteps, kernel_ms, kernel_launches);
+        if (h->dg) {
+            h->dg->profile_steps(nsteps, kernel_ms, kernel_launches);
+            kernel_ms[3] = 0.0;
+            kernel_launches[3] = 0;
+        } else if (h->imp) {
+            h->imp->profile_steps(nsteps, kernel_ms, kernel_launches);
+        } else {
+            ex(h).profile_steps(nsteps, kernel_ms, kernel_launches);
+        }
         return CFD2D_OK;
     });
 }
@@ -515,6 +572,40 @@ int cfd2d_implicit_stats(const cfd2d_t* h, cfd2d_implicit_stats_t* st) {
         st->n_limited = h->imp->last_n_lim();
         st->rel_residual = h->imp->last_rel();
         st->cfl = h->imp->cfl();
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_dg_get_coeffs(cfd2d_t* h, double* coeffs) {
+    Range r("cfd2d_dg_get_coeffs");
+    return guarded([&] {
+        if (!h || !coeffs) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        dgs(h).get_coeffs(coeffs);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_dg_set_coeffs(cfd2d_t* h, const double* coeffs) {
+    Range r("cfd2d_dg_set_coeffs");
+    return guarded([&] {
+        if (!h || !coeffs) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        dgs(h).set_coeffs(coeffs);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_dg_set_time_step(cfd2d_t* h, double tau) {
+    return guarded([&] {
+        if (!h || !(tau > 0)) return fail(CFD2D_ERR_INVALID_ARG, "bad argument");
+        dgs(h).set_tau(tau);
+        return CFD2D_OK;
+    });
+}
+
+int cfd2d_dg_residuals(cfd2d_t* h, double res[4]) {
+    return guarded([&] {
+        if (!h || !res) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
+        dgs(h).residuals(res);
         return CFD2D_OK;
     });
 }

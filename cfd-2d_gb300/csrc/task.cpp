@@ -70,6 +70,60 @@ int parse_materials(TaskConfig& t, const XmlNode* task) {
     return nm;
 }
 
+// <regions> with names (FVM_TVD::init :71-95, FEM_RKDG::init :80-107)
+void parse_regions(TaskConfig& t, const XmlNode* task, int nm) {
+    const XmlNode* regs = need(task, "regions", "task");
+    int nr = attr_i(regs, "count");
+    auto rlist = regs->children_named("region");
+    if (nr < 1 || nr > (int)rlist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <regions count> does not match");
+    for (int i = 0; i < nr; i++) {
+        TaskRegion r;
+        r.id = attr_i(rlist[i], "id");
+        r.matId = attr_i(need(rlist[i], "material", "region"), "id");
+        r.cellType = attr_i(need(rlist[i], "cell", "region"), "type");
+        r.name = need(rlist[i], "name", "region")->text;
+        const XmlNode* p = need(rlist[i], "parameters", "region");
+        r.u = attr_d(need(p, "Vx", "parameters"), "value");
+        r.v = attr_d(need(p, "Vy", "parameters"), "value");
+        r.T = attr_d(need(p, "T", "parameters"), "value");
+        r.p = attr_d(need(p, "P", "parameters"), "value");
+        if (r.matId < 0 || r.matId >= nm) throw Error(CFD2D_ERR_TASK, "task.xml: region refers to a missing material");
+        t.regions.push_back(r);
+    }
+
+}
+
+// <boundaries>: every <boundCond>, CFDBoundary::create (src/bnd_cond.cpp:10-72)
+void parse_cfd_boundaries(TaskConfig& t, const XmlNode* task) {
+    const XmlNode* bnds = need(task, "boundaries", "task");
+    for (const XmlNode* b : bnds->children_named("boundCond")) {  // CFDBoundary::create, src/bnd_cond.cpp:10-72
+        TaskBound tb;
+        const char* type = need(b, "type", "boundCond")->text.c_str();
+        if (std::strcmp(type, "BOUND_INLET") == 0) {
+            tb.kind = BND_INLET;
+            const XmlNode* p = b->child("parameters");
+            const char* names[4] = {"Vx", "Vy", "T", "P"};
+            for (int k = 0; k < 4; k++) {
+                const XmlNode* n = p ? p->child(names[k]) : nullptr;
+                if (!n) throw Error(CFD2D_ERR_BOUND_NOPAR, std::string("Parameter '") + names[k] +
+                                                               "' isn't specified  for BOUND_INLET.");
+                tb.par[k] = attr_d(n, "value");
+            }
+        } else if (std::strcmp(type, "BOUND_OUTLET") == 0) {
+            tb.kind = BND_OUTLET;
+        } else if (std::strcmp(type, "BOUND_WALL_NO_SLIP") == 0) {
+            tb.kind = BND_WALL_NO_SLIP;
+        } else if (std::strcmp(type, "BOUND_WALL_SLIP") == 0) {
+            tb.kind = BND_WALL_SLIP;
+        } else {
+            throw Error(CFD2D_ERR_BOUND_UNKNOWN, std::string("Unknown boundary type '") + type + "' specified.");
+        }
+        tb.edgeType = attr_i(b, "edgeType");
+        tb.name = need(b, "name", "boundCond")->text;
+        t.bnds.push_back(tb);
+    }
+}
+
 // FVM_TVD_IMPLICIT::init, src/methods/fvm_tvd_implicit.cpp:13-184
 void parse_implicit(TaskConfig& t, const XmlNode* task) {
     t.method = METHOD_FVM_TVD_IMPLICIT;
@@ -158,6 +212,38 @@ void parse_implicit(TaskConfig& t, const XmlNode* task) {
     t.gauss_points = 2;                 // with the midpoint and two Gauss points per edge
 }
 
+// FEM_RKDG::init, src/methods/fem_rkdg.cpp:23-235 (the mesh part is read separately)
+void parse_rkdg(TaskConfig& t, const XmlNode* task) {
+    t.method = METHOD_FEM_RKDG;
+    const XmlNode* ctl = need(task, "control", "task");
+    t.steady = attr_i(need(ctl, "STEADY", "control"), "value") == 0 ? 0 : 1;
+    t.tau = attr_d(need(ctl, "TAU", "control"), "value");
+    t.tmax = attr_d(need(ctl, "TMAX", "control"), "value");
+    t.cfl = attr_d(need(ctl, "CFL", "control"), "value");
+    t.file_step = attr_i(need(ctl, "FILE_OUTPUT_STEP", "control"), "value");
+    t.print_step = attr_i(need(ctl, "LOG_OUTPUT_STEP", "control"), "value");
+    t.dg_func_count = attr_i(need(ctl, "BASE_FUNC_COUNT", "control"), "value");
+    t.dg_gp_cell = attr_i(need(ctl, "GP_CELL_COUNT", "control"), "value");
+    t.dg_gp_edge = attr_i(need(ctl, "GP_EDGE_COUNT", "control"), "value");
+    const char* flx = need(ctl, "FLUX", "control")->attr("value");
+    t.flux = flx && std::strcmp(flx, "LAX") == 0 ? FLUX_LAX : FLUX_GODUNOV;  // anything else: GODUNOV
+    // the reference's mass-matrix inverse is the 3x3 cofactor formula (src/global.cpp:444-470)
+    // and its quadratures exist for these counts only (calcGaussPar, :470-598)
+    if (t.dg_func_count != 3)
+        throw Error(CFD2D_ERR_TASK, "task.xml: BASE_FUNC_COUNT must be 3 (the reference inverts 3x3 mass matrices)");
+    if (t.dg_gp_cell != 3 && t.dg_gp_cell != 4) throw Error(CFD2D_ERR_TASK, "task.xml: GP_CELL_COUNT must be 3 or 4");
+    if (t.dg_gp_edge != 2 && t.dg_gp_edge != 3) throw Error(CFD2D_ERR_TASK, "task.xml: GP_EDGE_COUNT must be 2 or 3");
+    t.dg_rk = pick(ctl, "RK_MODE", {{"REFERENCE", 0}, {"HEUN", 1}}, 0);
+    t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}}, -1);
+    t.precision = pick(ctl, "PRECISION", {{"FP64", PREC_FP64}}, PREC_FP64);
+    if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = std::max(1, attr_i(n, "value"));
+    const int nm = parse_materials(t, task);
+    parse_regions(t, task, nm);
+    parse_cfd_boundaries(t, task);
+    t.mesh_name = "mesh/mesh.0000.proc";  // Grid::readMeshFiles, src/mesh/grid.cpp:279-281 (process 0)
+    t.mesh_type = "proc";
+}
+
 }  // namespace
 
 TaskConfig parse_task(const std::string& path) {
@@ -176,6 +262,10 @@ TaskConfig parse_task(const std::string& path) {
     const char* method = task->attr("method");
     if (method && std::strcmp(method, "FVM_TVD_IMPLICIT") == 0) {
         parse_implicit(t, task);
+        return t;
+    }
+    if (method && std::strcmp(method, "FEM_RKDG") == 0) {
+        parse_rkdg(t, task);
         return t;
     }
     if (method && std::strcmp(method, "FVM_TVD") != 0 && std::strcmp(method, "FVM_TVD_GPU") != 0)
@@ -205,52 +295,8 @@ TaskConfig parse_task(const std::string& path) {
     parse_limits(t, task);
     const int nm = parse_materials(t, task);
 
-    const XmlNode* regs = need(task, "regions", "task");
-    int nr = attr_i(regs, "count");
-    auto rlist = regs->children_named("region");
-    if (nr < 1 || nr > (int)rlist.size()) throw Error(CFD2D_ERR_TASK, "task.xml: <regions count> does not match");
-    for (int i = 0; i < nr; i++) {
-        TaskRegion r;
-        r.id = attr_i(rlist[i], "id");
-        r.matId = attr_i(need(rlist[i], "material", "region"), "id");
-        r.cellType = attr_i(need(rlist[i], "cell", "region"), "type");
-        r.name = need(rlist[i], "name", "region")->text;
-        const XmlNode* p = need(rlist[i], "parameters", "region");
-        r.u = attr_d(need(p, "Vx", "parameters"), "value");
-        r.v = attr_d(need(p, "Vy", "parameters"), "value");
-        r.T = attr_d(need(p, "T", "parameters"), "value");
-        r.p = attr_d(need(p, "P", "parameters"), "value");
-        if (r.matId < 0 || r.matId >= nm) throw Error(CFD2D_ERR_TASK, "task.xml: region refers to a missing material");
-        t.regions.push_back(r);
-    }
-
-    const XmlNode* bnds = need(task, "boundaries", "task");
-    for (const XmlNode* b : bnds->children_named("boundCond")) {  // CFDBoundary::create, src/bnd_cond.cpp:10-72
-        TaskBound tb;
-        const char* type = need(b, "type", "boundCond")->text.c_str();
-        if (std::strcmp(type, "BOUND_INLET") == 0) {
-            tb.kind = BND_INLET;
-            const XmlNode* p = b->child("parameters");
-            const char* names[4] = {"Vx", "Vy", "T", "P"};
-            for (int k = 0; k < 4; k++) {
-                const XmlNode* n = p ? p->child(names[k]) : nullptr;
-                if (!n) throw Error(CFD2D_ERR_BOUND_NOPAR, std::string("Parameter '") + names[k] +
-                                                               "' isn't specified  for BOUND_INLET.");
-                tb.par[k] = attr_d(n, "value");
-            }
-        } else if (std::strcmp(type, "BOUND_OUTLET") == 0) {
-            tb.kind = BND_OUTLET;
-        } else if (std::strcmp(type, "BOUND_WALL_NO_SLIP") == 0) {
-            tb.kind = BND_WALL_NO_SLIP;
-        } else if (std::strcmp(type, "BOUND_WALL_SLIP") == 0) {
-            tb.kind = BND_WALL_SLIP;
-        } else {
-            throw Error(CFD2D_ERR_BOUND_UNKNOWN, std::string("Unknown boundary type '") + type + "' specified.");
-        }
-        tb.edgeType = attr_i(b, "edgeType");
-        tb.name = need(b, "name", "boundCond")->text;
-        t.bnds.push_back(tb);
-    }
+    parse_regions(t, task, nm);
+    parse_cfd_boundaries(t, task);
 
     const XmlNode* mesh = need(task, "mesh", "task");
     const char* mn = need(mesh, "name", "mesh")->attr("value");

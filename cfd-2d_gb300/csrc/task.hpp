@@ -1,4 +1,6 @@
-// task.xml of the FVM_TVD method (src/methods/fvm_tvd.cpp:26-128, src/bnd_cond.cpp:10-72).
+// task.xml of the FVM_TVD method (src/methods/fvm_tvd.cpp:26-128, src/bnd_cond.cpp:10-72),
+// of FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-184) and of FEM_RKDG
+// (src/methods/fem_rkdg.cpp:23-235).
 #pragma once
 #include <string>
 #include <vector>
@@ -12,7 +14,7 @@ struct TaskMaterial { std::string name; int id = 0; double M = 0, Cp = 0, K = 0,
 struct TaskRegion { int id = 0, matId = 0, cellType = 0; std::string name; double u = 0, v = 0, T = 0, p = 0; };
 struct TaskBound { int edgeType = 0; int kind = 0; std::string name; double par[4] = {0, 0, 0, 0}; };
 
-enum MethodKind { METHOD_FVM_TVD = 0, METHOD_FVM_TVD_IMPLICIT = 1 };
+enum MethodKind { METHOD_FVM_TVD = 0, METHOD_FVM_TVD_IMPLICIT = 1, METHOD_FEM_RKDG = 2 };
 
 struct TaskConfig {
     std::string path, dir;
@@ -41,6 +43,9 @@ struct TaskConfig {
     double smoothing_par = 0.0;
     double gmres_eps = 1.0e-7;
     int gmres_maxit = 20, gmres_kdim = 30;
+    // FEM_RKDG (src/methods/fem_rkdg.cpp:23-60): BASE_FUNC_COUNT, GP_CELL_COUNT, GP_EDGE_COUNT;
+    // RK_MODE (an extension): 0 the reference's stages as written, 1 Heun's average with U^n
+    int dg_func_count = 3, dg_gp_cell = 4, dg_gp_edge = 3, dg_rk = 0;
 };
 
 TaskConfig parse_task(const std::string& path);

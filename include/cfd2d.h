@@ -220,6 +220,34 @@ typedef struct {
 int cfd2d_implicit_system(cfd2d_t* h, double* diag, double* off, double* rhs, double* ctau);
 int cfd2d_implicit_stats(const cfd2d_t* h, cfd2d_implicit_stats_t* stats);
 
+/* ---- FEM_RKDG -------------------------------------------------------------- */
+/* A task.xml with <task method="FEM_RKDG"> (src/methods/fem_rkdg.cpp, the reference's
+ * explicit P1 discontinuous Galerkin method; Solver::initMethod, src/methods/solver.cpp:
+ * 49-51) gives a handle of that method: cfd2d_create = FEM_RKDG::init (it reads the mesh
+ * part mesh/mesh.0000.proc that the DECOMP method writes, from the working directory or
+ * the task's folder, Grid::readMeshFiles src/mesh/grid.cpp:275-420; cfd2d_create_with_mesh
+ * takes mesh arrays instead, cell_region and bseg_bnd indexing <regions> and
+ * <boundaries>), cfd2d_run = FEM_RKDG::run (:600-660; a steady task has no end there and
+ * returns CFD2D_ERR_INVALID_ARG), cfd2d_step advances whole steps (both Runge-Kutta
+ * stages), cfd2d_save_vtk writes save()'s res_%010d.pvtu and vtk_data/res_%010d.0000.vtu
+ * (:662-800). cfd2d_get_state gives the polynomials at the cell centres, cfd2d_set_state
+ * sets piecewise constant coefficients (value, 0, 0) as init does from the regions, and
+ * cfd2d_get_time_step cTau. The control element <RK_MODE value="HEUN"/> (no counterpart
+ * in the reference) averages the second stage with U^n instead of the reference's
+ * first-stage result. */
+
+/* The P1 coefficients, 12 per cell in the reference's cell order: ro[3] ru[3] rv[3] re[3]
+ * (FEM_RKDG's VECTOR ro[i], ru[i], rv[i], re[i], basis 1, (x-xc)/HX, (y-yc)/HY). Any host
+ * or device pointer. cfd2d_dg_set_coeffs then recomputes the time step from the task's
+ * TAU as init does (calcTimeStep, :382-447). */
+int cfd2d_dg_get_coeffs(cfd2d_t* h, double* coeffs);
+int cfd2d_dg_set_coeffs(cfd2d_t* h, const double* coeffs);
+/* Impose a time step (every cell's cTau = TAU = tau). */
+int cfd2d_dg_set_time_step(cfd2d_t* h, double tau);
+/* calcResiduals (:1286-1319) of the last step taken by cfd2d_step or cfd2d_run: the
+ * largest |U - ro_old| norm per variable (ro, ru, rv, re). */
+int cfd2d_dg_residuals(cfd2d_t* h, double res[4]);
+
 /* Select the CUDA device that cfd2d_create* places new solvers on (default: the
  * calling thread's current device). A solver keeps its device for life. */
 int cfd2d_set_device(int device);

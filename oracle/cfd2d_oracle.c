@@ -408,6 +408,12 @@ static int riemann_exact(double* RI_, double* EI_, double* PI_, double* UI_, dou
 }
 
 /* Godunov flux, FVM_TVD::calcFlux, src/methods/fvm_tvd.cpp:602-622 */
+/* the exact Riemann solver for the discontinuous Galerkin restatement (cfd2d_oracle_dg.c) */
+int orc_riemann_exact(double* RI, double* EI, double* PI, double* UI, double* VI, double RB, double PB, double UB,
+                      double VB, double RE, double PE, double UE, double VE, double GAM, int cap) {
+    return riemann_exact(RI, EI, PI, UI, VI, RB, PB, UB, VB, RE, PE, UE, VE, GAM, cap);
+}
+
 static int flux_godunov(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM, int cap) {
     double RI, EI, PI, UN, UT;
     double unl = pL->u * nx + pL->v * ny;

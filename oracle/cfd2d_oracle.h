@@ -125,6 +125,38 @@ void orc_imp_free(orc_imp* s);
 int orc_gmres_block(int nc, const int* nbr, const double* diag, const double* off, const double* b, double* x,
                     double eps, int maxit, int kdim, int* iters, double* final_rel);
 
+/* ---------------------------------------------------------------- FEM_RKDG
+ * Restatement of src/methods/fem_rkdg.cpp (cfd2d_oracle_dg.c): P1 discontinuous
+ * Galerkin, two Runge-Kutta stages. The mesh is a .proc part in file order: nodes,
+ * triangles with their region, edges (node pairs) with their boundary index (-1
+ * inside). reg: nreg x (M, Cp, Vx, Vy, T, P) -- the region's material and initial
+ * state; bpar: nbnd x (Vx, Vy, T, P). Coefficients: 12 per cell, ro[3] ru[3] rv[3]
+ * re[3] (the reference's VECTOR ro[i] etc.). */
+enum { ORC_DG_RK_REFERENCE = 0, ORC_DG_RK_HEUN = 1 };
+enum { ORC_ERR_NEWTON_CAP = 1 };
+typedef struct orc_dg orc_dg;
+typedef struct {
+    int steady, flux, gp_cell, gp_edge, rk_mode, newton_cap;
+    double tau, tmax, cfl;
+} orc_dg_params;
+orc_dg* orc_dg_create(const orc_dg_params* p, int nn, const double* xy, int nc, const int* tri,
+                      const int* cell_region, int ne, const int* en, const int* ebnd, int nreg, const double* reg,
+                      int nbnd, const int* bkind, const double* bpar);
+/* coefficients, then the time step as init forms it from the XML TAU */
+void orc_dg_set(orc_dg* d, const double* coeffs);
+void orc_dg_set_tau(orc_dg* d, double tau);
+/* n passes of run()'s loop body; returns ORC_ERR_* bits */
+unsigned orc_dg_step(orc_dg* d, int n);
+/* scal: TAU, t, residuals ro ru rv re, step */
+void orc_dg_get(const orc_dg* d, double* coeffs, double* ctau, double* scal);
+/* cell6: cx cy HX HY S cellJ; invA: 9 per cell (row major); edge4: nx ny l edgeJ */
+void orc_dg_geom(const orc_dg* d, int* cedge, int* c1c2, double* cell6, double* invA, double* edge4);
+/* density, pressure, u, v at each cell centre (the VTU fields) */
+void orc_dg_centre(const orc_dg* d, double* rpuv);
+void orc_dg_free(orc_dg* d);
+int orc_riemann_exact(double* RI, double* EI, double* PI, double* UI, double* VI, double RB, double PB, double UB,
+                      double VB, double RE, double PE, double UE, double VE, double GAM, int cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -379,3 +379,162 @@ def run_reference(task_xml: str, unv_text: str, U0=None, timeout=120, workdir=No
                     init=read_ref_state(os.path.join(d, "out.init.bin")),
                     final=read_ref_state(os.path.join(d, "out.state.bin")),
                     stdout=r.stdout, vtk=vtk)
+
+
+# ------------------------------------------------------------- FEM_RKDG
+
+REF_DG_BIN = os.path.join(HERE, "_ref", "ref_fem_rkdg")
+DG_RK = {"REFERENCE": 0, "HEUN": 1}
+
+
+class DgParams(C.Structure):
+    _fields_ = [("steady", C.c_int), ("flux", C.c_int), ("gp_cell", C.c_int), ("gp_edge", C.c_int),
+                ("rk_mode", C.c_int), ("newton_cap", C.c_int),
+                ("tau", C.c_double), ("tmax", C.c_double), ("cfl", C.c_double)]
+
+
+def _dg_lib():
+    L = lib()
+    if not getattr(L, "_dg_ready", False):
+        P, I, D = C.c_void_p, C.c_int, C.POINTER(C.c_double)
+        IP = C.POINTER(C.c_int)
+        L.orc_dg_create.argtypes = [C.POINTER(DgParams), I, D, I, IP, IP, I, IP, IP, I, D, I, IP, D]
+        L.orc_dg_create.restype = P
+        L.orc_dg_set.argtypes = [P, D]
+        L.orc_dg_set_tau.argtypes = [P, C.c_double]
+        L.orc_dg_step.argtypes = [P, I]; L.orc_dg_step.restype = C.c_uint
+        L.orc_dg_get.argtypes = [P, D, D, D]
+        L.orc_dg_geom.argtypes = [P, IP, IP, D, D, D]
+        L.orc_dg_centre.argtypes = [P, D]
+        L.orc_dg_free.argtypes = [P]
+        L._dg_ready = True
+    return L
+
+
+def dg_binding(task, pm):
+    """Region index per cell (by name, getRegion(typeName)) and boundary index per edge
+    (by name for named edges, else by edgeType; -1 inside), as FEM_RKDG::init binds them
+    (src/methods/fem_rkdg.cpp:196-248, 1382-1401)."""
+    names = {r.name: k for k, r in enumerate(task.regions)}
+    creg = np.array([names[n] for n in pm.cell_names], np.int32)
+    ebnd = np.full(len(pm.edges), -1, np.int32)
+    for e, (ty, nm) in enumerate(zip(pm.edge_type, pm.edge_names)):
+        if ty == 0:
+            continue
+        for k, b in enumerate(task.boundaries):
+            if (ty == 0x100 and b.name == nm) or (ty != 0x100 and ty == b.edge_type):
+                ebnd[e] = k
+                break
+        else:
+            raise ValueError(f"unknown edge type of edge {e}")
+    return creg, ebnd
+
+
+class OracleDG:
+    """The C restatement of FEM_RKDG on one .proc mesh part (see cfd2d_oracle.h)."""
+
+    def __init__(self, task, pm, *, rk=None, newton_cap=100):
+        L = _dg_lib()
+        rk = rk or task.rk or "REFERENCE"
+        p = DgParams(int(task.steady), FLUX.get(task.flux, 0) if task.flux in ("GODUNOV", "LAX") else 0,
+                     int(task.gp_cell), int(task.gp_edge), DG_RK[rk], int(newton_cap),
+                     float(task.tau), float(task.tmax), float(task.cfl))
+        creg, ebnd = dg_binding(task, pm)
+        mats = task.materials
+        reg = np.array([[mats[r.mat][1], mats[r.mat][2], r.u, r.v, r.T, r.p] for r in task.regions], np.float64)
+        bkind = np.array([BND[b.kind] for b in task.boundaries], np.int32)
+        bpar = np.array([[b.u, b.v, b.T, b.p] for b in task.boundaries], np.float64).reshape(-1, 4)
+        self.nodes = np.ascontiguousarray(pm.nodes, np.float64)
+        self.tris = np.ascontiguousarray(pm.tris, np.int32)
+        self.edges = np.ascontiguousarray(pm.edges, np.int32)
+        self._keep = (creg, ebnd, reg, bkind, bpar)
+        self.h = L.orc_dg_create(C.byref(p), len(self.nodes), _d(self.nodes), len(self.tris), _i(self.tris),
+                                 _i(creg), len(self.edges), _i(self.edges), _i(ebnd), len(reg), _d(reg),
+                                 len(bkind), _i(bkind), _d(bpar))
+        if not self.h:
+            raise RuntimeError("orc_dg_create failed")
+        self.nc, self.ne = len(self.tris), len(self.edges)
+
+    def set_coeffs(self, U):
+        U = np.ascontiguousarray(U, np.float64).reshape(self.nc, 12)
+        _dg_lib().orc_dg_set(self.h, _d(U))
+
+    def set_tau(self, tau):
+        _dg_lib().orc_dg_set_tau(self.h, float(tau))
+
+    def step(self, n: int) -> int:
+        return int(_dg_lib().orc_dg_step(self.h, int(n)))
+
+    def state(self) -> dict:
+        U = np.empty((self.nc, 12)); ct = np.empty(self.nc); sc = np.empty(7)
+        _dg_lib().orc_dg_get(self.h, _d(U), _d(ct), _d(sc))
+        return dict(U=U, cTau=ct, tau=float(sc[0]), t=float(sc[1]), res=sc[2:6].copy(), step=int(sc[6]))
+
+    def geom(self) -> dict:
+        ce = np.empty((self.nc, 3), np.int32); cc = np.empty((self.ne, 2), np.int32)
+        c6 = np.empty((self.nc, 6)); ia = np.empty((self.nc, 9)); e4 = np.empty((self.ne, 4))
+        _dg_lib().orc_dg_geom(self.h, _i(ce), _i(cc), _d(c6), _d(ia), _d(e4))
+        return dict(cedge=ce, c1c2=cc, cell6=c6, invA=ia, edge4=e4)
+
+    def centre(self) -> np.ndarray:
+        out = np.empty((self.nc, 4))
+        _dg_lib().orc_dg_centre(self.h, _d(out))
+        return out
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _dg_lib().orc_dg_free(self.h)
+            self.h = None
+
+
+def run_reference_rkdg(task_xml: str, proc_text: str, steps: int, U0=None, tau=None, timeout=300,
+                       workdir=None) -> dict:
+    """Run the reference's own FEM_RKDG (oracle/_ref/ref_fem_rkdg, see oracle/ref/ref_rkdg.cpp)
+    on one case: mesh/mesh.0000.proc = proc_text; U0: (nc, 12) coefficients or None; tau: a
+    time step to impose after init. Returns the dumps, stdout and the VTU/PVTU files."""
+    if not os.path.exists(REF_DG_BIN):
+        raise FileNotFoundError(REF_DG_BIN + " (build with: make -C oracle reference)")
+    with tempfile.TemporaryDirectory(dir=workdir) as d:
+        os.makedirs(os.path.join(d, "mesh"))
+        open(os.path.join(d, "task.xml"), "w").write(task_xml)
+        open(os.path.join(d, "mesh", "mesh.0000.proc"), "w").write(proc_text)
+        args = [REF_DG_BIN, "task.xml", "out", str(int(steps))]
+        if U0 is not None or tau is not None:
+            if U0 is not None:
+                np.ascontiguousarray(U0, np.float64).tofile(os.path.join(d, "init.bin"))
+            args.append("init.bin" if U0 is not None else "-")
+        if tau is not None:
+            args.append(repr(float(tau)))
+        r = subprocess.run(args, cwd=d, capture_output=True, text=True, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError("reference run failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+        out = {}
+        for tag in ("init", "state"):
+            raw = open(os.path.join(d, f"out.{tag}.bin"), "rb").read()
+            nc = int(np.frombuffer(raw[:4], np.int32)[0])
+            sc = np.frombuffer(raw, np.float64, 6, 16)
+            off = 64
+            U = np.frombuffer(raw, np.float64, 12 * nc, off).reshape(nc, 12).copy(); off += 96 * nc
+            ct = np.frombuffer(raw, np.float64, nc, off).copy()
+            out[tag] = dict(U=U, cTau=ct, tau=float(sc[0]), tmax=float(sc[1]), res=sc[2:6].copy())
+        raw = open(os.path.join(d, "out.geom.bin"), "rb").read()
+        nc, ne, nn, gc, ge, fc = (int(x) for x in np.frombuffer(raw[:24], np.int32))
+        off = 32
+        g = {}
+        g["cedge"] = np.frombuffer(raw, np.int32, 3 * nc, off).reshape(nc, 3).copy(); off += 12 * nc
+        g["c1c2"] = np.frombuffer(raw, np.int32, 2 * ne, off).reshape(ne, 2).copy(); off += 8 * ne
+        g["cell6"] = np.frombuffer(raw, np.float64, 6 * nc, off).reshape(nc, 6).copy(); off += 48 * nc
+        g["cgp"] = np.frombuffer(raw, np.float64, 3 * gc * nc, off).reshape(nc, gc, 3).copy(); off += 24 * gc * nc
+        g["invA"] = np.frombuffer(raw, np.float64, 9 * nc, off).reshape(nc, 9).copy(); off += 72 * nc
+        g["edge4"] = np.frombuffer(raw, np.float64, 4 * ne, off).reshape(ne, 4).copy(); off += 32 * ne
+        g["egp"] = np.frombuffer(raw, np.float64, 3 * ge * ne, off).reshape(ne, ge, 3).copy()
+        out["geom"] = g
+        out["stdout"] = r.stdout
+        files = {}
+        for root, _, fs in os.walk(d):
+            for f in fs:
+                if f.endswith(".vtu") or f.endswith(".pvtu"):
+                    full = os.path.join(root, f)
+                    files[os.path.relpath(full, d)] = open(full).read()
+        out["vtu"] = files
+        return out

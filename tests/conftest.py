@@ -22,12 +22,29 @@ def pytest_configure(config):
 def golden_names():
     """Fixtures of the explicit method (reference FVM_TVD runs on UNV meshes)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not p.endswith("berkeley_triangle.npz") and not os.path.basename(p).startswith("implicit_"))
+                  if not p.endswith("berkeley_triangle.npz")
+                  and not os.path.basename(p).startswith(("implicit_", "rkdg_")))
 
 
 def implicit_golden_names():
     """Fixtures of the implicit method (reference FVM_TVD_IMPLICIT runs, make_golden_implicit.py)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "implicit_*.npz")))
+
+
+def rkdg_golden_names():
+    """Fixtures of the discontinuous Galerkin method (reference FEM_RKDG runs, make_golden_rkdg.py)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "rkdg_*.npz")))
+
+
+def rkdg_task(g):
+    """The RkdgTask of a FEM_RKDG fixture."""
+    import json
+    from cfd2d import meshgen as mg
+    d = json.loads(str(g["task_json"]))
+    d["regions"] = [mg.Region(**r) for r in d["regions"]]
+    d["boundaries"] = [mg.Boundary(**b) for b in d["boundaries"]]
+    d["materials"] = [tuple(m) for m in d["materials"]]
+    return mg.RkdgTask(**d)
 
 
 def load_golden(name):
