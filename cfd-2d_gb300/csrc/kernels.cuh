@@ -319,9 +319,8 @@ __device__ __forceinline__ bool riemann_exact(T& RI, T& EI, T& PI, T& UI, T& VI,
             if (!(t_abs(DU - F1 - F2) > eps)) break;
             if (++it >= cap) { hit = true; break; }
         }
-        T PPB = P / PB, PPE = P / PE;
-        T ZFB = CB * t_exp(t_log(PPB) * OGAM);
-        T ZFE = CE * t_exp(t_log(PPE) * OGAM);
+        // the reference forms ZFB and ZFE here for both sides; each is read only on its
+        // rarefaction branch, so it is formed there (same value, no exp/log for a shock)
         if (!(PB > P)) {
             D = UB - t_sqrt((TGAM * P + HGAM * PB) / RB);
             T UBD = UB - D, RUBD = RB * UBD;
@@ -330,6 +329,7 @@ __device__ __forceinline__ bool riemann_exact(T& RI, T& EI, T& PI, T& UI, T& VI,
             EF = P / (AGAM * RF);
             SBL = D; SFL = D;
         } else {
+            const T ZFB = CB * t_exp(t_log(P / PB) * OGAM);
             EF = ZFB * ZFB / SGAM;
             UF = UB + DGAM * (CB - ZFB);
             RF = P / (AGAM * EF);
@@ -344,6 +344,7 @@ __device__ __forceinline__ bool riemann_exact(T& RI, T& EI, T& PI, T& UI, T& VI,
             ES = P / (AGAM * RS);
             SEL = D; SSL = D;
         } else {
+            const T ZFE = CE * t_exp(t_log(P / PE) * OGAM);
             ES = ZFE * ZFE / SGAM;
             US = UE - DGAM * (CE - ZFE);
             RS = P / (AGAM * ES);

@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(128) k_dg_edge(const DgCase c, const double* _
         if (FLUX == FLUX_GODUNOV) hit |= flux_godunov(f, qL, qR, nx, ny, m1.gam, c.newton_cap);
         else flux_lax(f, qL, qR, nx, ny, m1.gam, m1.ig1);
         const double w = c.egw[g];
-        const double w1[3] = {1.0 * w, Fa.x * w, Fa.y * w};  // tmp1 = getF(c1, pt); tmp1 *= w
+        const double w1[3] = {w, GE == 2 ? Fa.x : Fa.x * w, GE == 2 ? Fa.y : Fa.y * w};  // getF(c1, pt) * w (w = 1 for 2 points)
 #pragma unroll
         for (int v = 0; v < 4; v++)
 #pragma unroll
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(128) k_dg_edge(const DgCase c, const double* _
                 i1[3 * v + k] = g == 0 ? pz(t) : i1[3 * v + k] + t;
             }
         if (inner) {
-            const double w2[3] = {1.0 * w, Fb.x * w, Fb.y * w};
+            const double w2[3] = {w, GE == 2 ? Fb.x : Fb.x * w, GE == 2 ? Fb.y : Fb.y * w};
 #pragma unroll
             for (int v = 0; v < 4; v++)
 #pragma unroll
@@ -176,19 +176,39 @@ __global__ void __launch_bounds__(128) k_dg_cell(const DgCase c, int stage, int 
             const double ge = q.v * (q.r * q.E + q.p);
             const double fx[4] = {fr, fu, fv, fe}, gy[4] = {gr, gu, gv, ge};
             const double w = c.cgw[g];
+            // tmpInt = 0; += getDFDX * f = (0, 1/HX, 0) f; += getDFDY * g = (0, 0, 1/HY) g; *= w.
+            // With finite fluxes the products by 0 are +-0 and every sum with them is exact:
+            // component 1 is 0 + f/HX (pz), component 2 is 0 + g/HY, component 0 is +-0 after
+            // the weight, which leaves the running sum as it is (+0 from the first point on,
+            // or the NaN / inf an earlier point left). Non-finite fluxes take the literal form.
+            bool finite = true;
 #pragma unroll
-            for (int v = 0; v < 4; v++) {
-                // tmpInt = 0; += getDFDX * f = (0, 1/HX, 0) f; += getDFDY * g = (0, 0, 1/HY) g; *= w
-                double t0 = 0.0 + 0.0 * fx[v];
-                double t1 = 0.0 + ihx * fx[v];
-                double t2 = 0.0 + 0.0 * fx[v];
-                t0 = t0 + 0.0 * gy[v];
-                t1 = t1 + 0.0 * gy[v];
-                t2 = t2 + ihy * gy[v];
-                t0 = t0 * w; t1 = t1 * w; t2 = t2 * w;
-                in[3 * v] = g == 0 ? pz(t0) : in[3 * v] + t0;
-                in[3 * v + 1] = g == 0 ? pz(t1) : in[3 * v + 1] + t1;
-                in[3 * v + 2] = g == 0 ? pz(t2) : in[3 * v + 2] + t2;
+            for (int v = 0; v < 4; v++)
+                finite = finite && ((__double2hiint(fx[v]) & 0x7ff00000) != 0x7ff00000) &&
+                         ((__double2hiint(gy[v]) & 0x7ff00000) != 0x7ff00000);
+            if (finite) {
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const double t1 = pz(ihx * fx[v]) * w;
+                    const double t2 = pz(ihy * gy[v]) * w;
+                    if (g == 0) in[3 * v] = 0.0;
+                    in[3 * v + 1] = g == 0 ? pz(t1) : in[3 * v + 1] + t1;
+                    in[3 * v + 2] = g == 0 ? pz(t2) : in[3 * v + 2] + t2;
+                }
+            } else {
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    double t0 = 0.0 + 0.0 * fx[v];
+                    double t1 = 0.0 + ihx * fx[v];
+                    double t2 = 0.0 + 0.0 * fx[v];
+                    t0 = t0 + 0.0 * gy[v];
+                    t1 = t1 + 0.0 * gy[v];
+                    t2 = t2 + ihy * gy[v];
+                    t0 = t0 * w; t1 = t1 * w; t2 = t2 * w;
+                    in[3 * v] = g == 0 ? pz(t0) : in[3 * v] + t0;
+                    in[3 * v + 1] = g == 0 ? pz(t1) : in[3 * v + 1] + t1;
+                    in[3 * v + 2] = g == 0 ? pz(t2) : in[3 * v + 2] + t2;
+                }
             }
         }
         const double J = c.cellJ[i];
