@@ -12,6 +12,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include "kernels.hpp"
 
 namespace cfd2d {
@@ -253,46 +255,49 @@ __device__ __forceinline__ T minmod(T a, T b) {
 
 // ------------------------------------------------------------------ fluxes
 
+// a / b: from y = RN(1/b) when RECIP (correctly rounded, the same bits as '/', div_rn),
+// else '/' itself; the FP32 faces always divide outright
+template <bool RECIP>
+__device__ __forceinline__ double div_x(double a, double b, double y) { return RECIP ? div_rn(a, b, y) : a / b; }
+template <bool RECIP>
+__device__ __forceinline__ float div_x(float a, float b, float) { return a / b; }
+
 // Exact Riemann solver rim_orig (src/global.cpp:232-405), structured, with a cap
-// on its Newton loop (the reference has none and can spin forever).
-template <typename T>
+// on its Newton loop (the reference has none and can spin forever). With RECIP the
+// quotients by the side densities (yRB, yRE = their reciprocals), by the side pressures
+// and by the gas constants go through div_rn: the same bits, a third of the FP64 work of
+// a division each.
+template <typename T, bool RECIP = false>
 __device__ __forceinline__ bool riemann_exact(T& RI, T& EI, T& PI, T& UI, T& VI, T RB, T PB, T UB, T VB, T RE,
-                                              T PE, T UE, T VE, T GAM, int cap) {
-    const T AGAM = (GAM - T(1.0));
-    const T DGAM = (T(2.0) / AGAM);
-    const T GGAM = (t_sqrt(GAM * AGAM));
-    const T HGAM = (AGAM / T(2.0));
-    const T FGAM = (T(3.0) * GAM - T(1.0));
-    const T OGAM = (AGAM / (T(2.0) * GAM));
-    const T QGAM = (GAM + T(1.0));
-    const T PGAM = (QGAM / (T(2.0) * GAM));
-    const T RGAM = (T(4.0) * GAM);
-    const T SGAM = (GAM * AGAM);
-    const T TGAM = (QGAM / T(2.0));
+                                              T PE, T UE, T VE, const RimGas<T>& g, int cap, T yRB = T(0),
+                                              T yRE = T(0)) {
+    const T GAM = g.GAM, AGAM = g.AGAM, DGAM = g.DGAM, GGAM = g.GGAM, HGAM = g.HGAM, FGAM = g.FGAM;
+    const T OGAM = g.OGAM, QGAM = g.QGAM, PGAM = g.PGAM, RGAM = g.RGAM, SGAM = g.SGAM, TGAM = g.TGAM;
     T US = T(0.0), UF = T(0.0);
     T RF, RS, EF, ES, SBL, SFL, SSL, SEL, D, P;
     const T eps = T(1.0e-5);
-    T CB = t_sqrt(GAM * PB / RB);
-    T CE = t_sqrt(GAM * PE / RE);
-    T EB = CB * CB / SGAM;
-    T EE = CE * CE / SGAM;
+    T CB = t_sqrt(div_x<RECIP>(GAM * PB, RB, yRB));
+    T CE = t_sqrt(div_x<RECIP>(GAM * PE, RE, yRE));
+    T EB = div_x<RECIP>(CB * CB, SGAM, g.iSGAM);
+    T EE = div_x<RECIP>(CE * CE, SGAM, g.iSGAM);
     T RCB = RB * CB;
     T RCE = RE * CE;
     T DU = UB - UE;
     bool hit = false;
-    if (DU < T(-2.0) * (CB + CE) / AGAM) {  // vacuum
+    if (DU < div_x<RECIP>(T(-2.0) * (CB + CE), AGAM, g.iAGAM)) {  // vacuum
         RF = T(0.0); RS = T(0.0); EF = T(0.0); ES = T(0.0);
         SBL = UB - CB;
-        SFL = UB + T(2.0) * CB / AGAM;
-        SSL = UE - T(2.0) * CE / AGAM;
+        SFL = UB + div_x<RECIP>(T(2.0) * CB, AGAM, g.iAGAM);
+        SSL = UE - div_x<RECIP>(T(2.0) * CE, AGAM, g.iAGAM);
         SEL = UE + CE;
     } else {
         P = (PB * RCE + PE * RCB + DU * RCB * RCE) / (RCB + RCE);
+        const T yPB = RECIP ? T(1) / PB : T(0), yPE = RECIP ? T(1) / PE : T(0);
         int it = 0;
         for (;;) {
             T F1, FS1, F2, FS2;
             if (P < eps) P = eps;
-            T PPB = P / PB;
+            T PPB = div_x<RECIP>(P, PB, yPB);
             if (PB > P) {
                 T ZFB = CB * t_exp(t_log(PPB) * OGAM);
                 F1 = DGAM * (ZFB - CB);
@@ -303,7 +308,7 @@ __device__ __forceinline__ bool riemann_exact(T& RI, T& EI, T& PI, T& UI, T& VI,
                 F1 = (P - PB) / ZNB;
                 FS1 = (QGAM * PPB + FGAM) / (RGAM * ZNB * PKB);
             }
-            T PPE = P / PE;
+            T PPE = div_x<RECIP>(P, PE, yPE);
             if (PE > P) {
                 T ZFE = CE * t_exp(t_log(PPE) * OGAM);
                 F2 = DGAM * (ZFE - CE);
@@ -322,30 +327,30 @@ __device__ __forceinline__ bool riemann_exact(T& RI, T& EI, T& PI, T& UI, T& VI,
         // the reference forms ZFB and ZFE here for both sides; each is read only on its
         // rarefaction branch, so it is formed there (same value, no exp/log for a shock)
         if (!(PB > P)) {
-            D = UB - t_sqrt((TGAM * P + HGAM * PB) / RB);
+            D = UB - t_sqrt(div_x<RECIP>(TGAM * P + HGAM * PB, RB, yRB));
             T UBD = UB - D, RUBD = RB * UBD;
             RF = RUBD * RUBD / (PB - P + RUBD * UBD);
             UF = D + RUBD / RF;
             EF = P / (AGAM * RF);
             SBL = D; SFL = D;
         } else {
-            const T ZFB = CB * t_exp(t_log(P / PB) * OGAM);
-            EF = ZFB * ZFB / SGAM;
+            const T ZFB = CB * t_exp(t_log(div_x<RECIP>(P, PB, yPB)) * OGAM);
+            EF = div_x<RECIP>(ZFB * ZFB, SGAM, g.iSGAM);
             UF = UB + DGAM * (CB - ZFB);
             RF = P / (AGAM * EF);
             SBL = UB - CB;
             SFL = UF - ZFB;
         }
         if (!(PE > P)) {
-            D = UE + t_sqrt((TGAM * P + HGAM * PE) / RE);
+            D = UE + t_sqrt(div_x<RECIP>(TGAM * P + HGAM * PE, RE, yRE));
             T UED = UE - D, RUED = RE * UED;
             RS = RUED * RUED / (PE - P + RUED * UED);
             US = D + RUED / RS;
             ES = P / (AGAM * RS);
             SEL = D; SSL = D;
         } else {
-            const T ZFE = CE * t_exp(t_log(P / PE) * OGAM);
-            ES = ZFE * ZFE / SGAM;
+            const T ZFE = CE * t_exp(t_log(div_x<RECIP>(P, PE, yPE)) * OGAM);
+            ES = div_x<RECIP>(ZFE * ZFE, SGAM, g.iSGAM);
             US = UE - DGAM * (CE - ZFE);
             RS = P / (AGAM * ES);
             SSL = US + ZFE;
@@ -358,29 +363,31 @@ __device__ __forceinline__ bool riemann_exact(T& RI, T& EI, T& PI, T& UI, T& VI,
         if (US >= T(0.0)) { RI = RF; EI = EF; UI = UF; VI = VB; }
         else { RI = RS; EI = ES; UI = US; VI = VE; }
     } else if (SFL > T(0.0)) {
-        UI = (UB + DGAM * GGAM * t_sqrt(EB)) / (T(1) + DGAM);
+        UI = div_x<RECIP>(UB + DGAM * GGAM * t_sqrt(EB), T(1) + DGAM, g.i1DGAM);
         VI = VB;
-        EI = (UI * UI) / SGAM;
-        RI = RB * t_exp(t_log(EI / EB) * (T(1) / AGAM));
+        EI = div_x<RECIP>(UI * UI, SGAM, g.iSGAM);
+        RI = RB * t_exp(t_log(EI / EB) * g.eAGAM);
     } else {
-        UI = (UE - DGAM * GGAM * t_sqrt(EE)) / (T(1) + DGAM);
+        UI = div_x<RECIP>(UE - DGAM * GGAM * t_sqrt(EE), T(1) + DGAM, g.i1DGAM);
         VI = VE;
-        EI = (UI * UI) / SGAM;
-        RI = RE * t_exp(t_log(EI / EE) * (T(1) / AGAM));
+        EI = div_x<RECIP>(UI * UI, SGAM, g.iSGAM);
+        RI = RE * t_exp(t_log(EI / EE) * g.eAGAM);
     }
     PI = AGAM * EI * RI;
     return hit;
 }
 
-// Godunov flux, FVM_TVD::calcFlux, src/methods/fvm_tvd.cpp:602-622
-template <typename T>
-__device__ __forceinline__ bool flux_godunov(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, int cap) {
+// Godunov flux, FVM_TVD::calcFlux, src/methods/fvm_tvd.cpp:602-622 (FEM_RKDG's, :918-937, is
+// the same). With RECIP: a fixed gas and the side densities' reciprocals yL, yR.
+template <typename T, bool RECIP = false>
+__device__ __forceinline__ bool flux_godunov(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny,
+                                             const RimGas<T>& g, int cap, T yL = T(0), T yR = T(0)) {
     T RI, EI, PI, UN, UT;
     T unl = L.u * nx + L.v * ny;
     T unr = R.u * nx + R.v * ny;
     T utl = L.u * ny - L.v * nx;
     T utr = R.u * ny - R.v * nx;
-    bool hit = riemann_exact(RI, EI, PI, UN, UT, L.r, L.p, unl, utl, R.r, R.p, unr, utr, GAM, cap);
+    bool hit = riemann_exact<T, RECIP>(RI, EI, PI, UN, UT, L.r, L.p, unl, utl, R.r, R.p, unr, utr, g, cap, yL, yR);
     T UI = UN * nx + UT * ny;
     T VI = UN * ny - UT * nx;
     f[0] = RI * UN;
@@ -390,12 +397,21 @@ __device__ __forceinline__ bool flux_godunov(T* f, const Prim<T>& L, const Prim<
     return hit;
 }
 
-// Lax-Friedrichs (Rusanov), the reference's template src/methods/fvm_tvd_implicit.cpp:939-960
 template <typename T>
-__device__ __forceinline__ void flux_lax(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
+__device__ __forceinline__ bool flux_godunov(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, int cap) {
+    return flux_godunov<T, false>(f, L, R, nx, ny, rim_gas<T>(GAM), cap);
+}
+
+// Lax-Friedrichs (Rusanov), the reference's template src/methods/fvm_tvd_implicit.cpp:939-960
+// (FEM_RKDG's, :938-958, is the same). With RECIP the quotients by the densities use their
+// reciprocals yL, yR (div_rn: the same bits).
+template <typename T, bool RECIP = false>
+__device__ __forceinline__ void flux_lax(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1,
+                                         T yL = T(0), T yR = T(0)) {
     T unl = L.u * nx + L.v * ny;
     T unr = R.u * nx + R.v * ny;
-    T alpha = t_max(t_abs(unl) + t_sqrt(GAM * L.p / L.r), t_abs(unr) + t_sqrt(GAM * R.p / R.r));
+    T alpha = t_max(t_abs(unl) + t_sqrt(div_x<RECIP>(GAM * L.p, L.r, yL)),
+                    t_abs(unr) + t_sqrt(div_x<RECIP>(GAM * R.p, R.r, yR)));
     T rol = L.r, rul = L.r * L.u, rvl = L.r * L.v;
     T rel = div_by(L.p, GAM - T(1.0), IG1) + T(0.5) * L.r * (L.u * L.u + L.v * L.v);
     T ror = R.r, rur = R.r * R.u, rvr = R.r * R.v;

@@ -13,6 +13,7 @@
 //                centroid (gp0: dxL dyL dxR dyR, gp1: ...), edge flux F[ne][4]
 //                (already multiplied by l/2), boundary index bnd[ne].
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -38,6 +39,38 @@ struct DevBnd {     // one <boundCond>: kind and (Vx, Vy, T, P)
     double u, v, T, p;
 };
 
+// The constants rim_orig derives from GAM (src/global.cpp:240-250), formed as it forms
+// them; a caller with a fixed gas forms them once. iAGAM, iSGAM, i1DGAM are RN(1/AGAM),
+// RN(1/SGAM), RN(1/(1 + DGAM)) for the quotients by them (div_x), eAGAM is 1/AGAM as the
+// reference writes it in the sonic-rarefaction exponent.
+template <typename T> struct RimGas {
+    T GAM, AGAM, DGAM, GGAM, HGAM, FGAM, OGAM, QGAM, PGAM, RGAM, SGAM, TGAM, iAGAM, iSGAM, i1DGAM, eAGAM;
+};
+template <typename T>
+__host__ __device__ __forceinline__ RimGas<T> rim_gas(T GAM) {
+    RimGas<T> g;
+    g.GAM = GAM;
+    g.AGAM = (GAM - T(1.0));
+    g.DGAM = (T(2.0) / g.AGAM);
+#ifdef __CUDA_ARCH__
+    g.GGAM = (::sqrt(GAM * g.AGAM));
+#else
+    g.GGAM = (std::sqrt(GAM * g.AGAM));
+#endif
+    g.HGAM = (g.AGAM / T(2.0));
+    g.FGAM = (T(3.0) * GAM - T(1.0));
+    g.OGAM = (g.AGAM / (T(2.0) * GAM));
+    g.QGAM = (GAM + T(1.0));
+    g.PGAM = (g.QGAM / (T(2.0) * GAM));
+    g.RGAM = (T(4.0) * GAM);
+    g.SGAM = (GAM * g.AGAM);
+    g.TGAM = (g.QGAM / T(2.0));
+    g.iAGAM = T(1) / g.AGAM;
+    g.iSGAM = T(1) / g.SGAM;
+    g.i1DGAM = T(1) / (T(1) + g.DGAM);
+    g.eAGAM = T(1) / g.AGAM;
+    return g;
+}
 // Launch shape of one kernel kind: threads per block and blocks (0 = one
 // thread per item; otherwise a persistent grid that strides over the items).
 // Default: 64-thread blocks, one thread per item (measured best for the single

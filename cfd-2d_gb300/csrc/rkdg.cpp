@@ -483,6 +483,7 @@ RkdgSolver::RkdgSolver(const TaskConfig& t, DgMesh&& mesh) : task_(t), mesh_(std
             d.gm1 = d.gam - 1;
             d.ig1 = 1.0 / (d.gam - 1.0);
             d.iCv = 1.0 / d.Cv;
+            d.rg = rim_gas<double>(d.gam);
             mats_.push_back(d);
         }
         c.mats = upload(mats_);

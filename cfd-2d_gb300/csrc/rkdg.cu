@@ -81,17 +81,20 @@ __global__ void __launch_bounds__(128) k_dg_edge(const DgCase c, const double* _
         const DgPar L = dg_eval(a1, Fa.x, Fa.y, m1.gm1);
         const Prim<double> qL{L.r, L.u, L.v, L.p};
         Prim<double> qR;
+        double yR;
         if (inner) {
             const DgPar R = dg_eval(a2, Fb.x, Fb.y, gm2);
             qR = Prim<double>{R.r, R.u, R.v, R.p};
+            yR = R.y;
         } else {
             // URS(1) of pL (:1428) gives the temperature an outlet or wall ghost carries
             const double Tc = temperature(qL, m1.gm1, m1.Cv);
             qR = ghost_state(c.bnds[c.ebnd[e]], qL, Tc, nx, ny, m1.M);
+            yR = 1.0 / qR.r;
         }
         double f[4];
-        if (FLUX == FLUX_GODUNOV) hit |= flux_godunov(f, qL, qR, nx, ny, m1.gam, c.newton_cap);
-        else flux_lax(f, qL, qR, nx, ny, m1.gam, m1.ig1);
+        if (FLUX == FLUX_GODUNOV) hit |= flux_godunov<double, true>(f, qL, qR, nx, ny, m1.rg, c.newton_cap, L.y, yR);
+        else flux_lax<double, true>(f, qL, qR, nx, ny, m1.gam, m1.ig1, L.y, yR);
         const double w = c.egw[g];
         const double w1[3] = {w, GE == 2 ? Fa.x : Fa.x * w, GE == 2 ? Fa.y : Fa.y * w};  // getF(c1, pt) * w (w = 1 for 2 points)
 #pragma unroll

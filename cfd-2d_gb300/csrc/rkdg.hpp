@@ -35,6 +35,7 @@ enum DgRkMode { DG_RK_REFERENCE = 0, DG_RK_HEUN = 1 };
 // A material with the constants the method derives from it (Material::URS, getGamma).
 struct DgMat {
     double M, Cv, gam, gm1, ig1, iCv;  // ig1 = RN(1/(gam-1)), iCv = RN(1/Cv)
+    RimGas<double> rg;                 // the exact Riemann solver's constants of gam
 };
 
 // Everything the kernels read; passed by value.
