@@ -101,6 +101,19 @@ def ncu_instr():
     return out
 
 
+def ncu_instr_units(name: str):
+    """FP64-unit thread instructions per unit (edge / cell) of a method's kernels, from a
+    committed ncu summary ("instr_per_unit <method> <kernel> <count> <unit>" lines)."""
+    p = os.path.join(ROOT, "profiles", name)
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("instr_per_unit"):
+                _, _, kernel, val, unit = line.split()[:5]
+                out[kernel] = (float(val), unit)
+    return out
+
+
 def cpu_model():
     try:
         r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
@@ -613,6 +626,23 @@ def rkdg_workload(args, capi, cases, world, rank, dist, W, K):
         }
         if "kernels" in main_:
             line["gpu_launches"] = K * sum(v["launches_per_step"] for v in main_["kernels"].values())
+            # the FP64 unit: ncu-counted FP64-unit instructions per edge / cell against GB300's
+            # issue rate (2 per clock and SM at the GPU's maximum SM clock)
+            import torch
+            instr = ncu_instr_units("ncu_instruction_counts_rkdg_vortex_131k.md")
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+            peak = 2.0 * sms * measured_sm_max() * 1e6
+            units = {"edge": (3 * n * n + 2 * n), "cell": cells}
+            fp = {}
+            for kname, key in (("k_dg_edge", "k_dg_edge_godunov"), ("k_dg_cell", "k_dg_cell")):
+                if key in instr and fluxes[0] == "GODUNOV":
+                    cnt, unit = instr[key]
+                    per_launch_ms = main_["kernels"][kname]["ms_per_step"] / 2
+                    ach = cnt * units[unit] / (per_launch_ms * 1e-3)
+                    fp[kname] = {"fp64_instr_per_" + unit: cnt, "achieved_instr_per_s": ach, "frac": ach / peak}
+            if fp:
+                line["fp64_unit"] = {"peak_instr_per_s": peak, "kernels": fp,
+                                     "source": "profiles/ncu_instruction_counts_rkdg_vortex_131k.md"}
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = rkdg_cpu_baseline(n)
         print(json.dumps(line), flush=True)

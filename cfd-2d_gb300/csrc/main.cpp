@@ -1,7 +1,7 @@
 // cfd2d_gpu: the reference's program entry (src/main.cpp:10-39) on the GPU path:
 // read task.xml from the working directory, log to task.log and stdout, run the
-// FVM_TVD loop with its VTK/log cadence, free everything. An optional argument
-// names another task file.
+// task's method (FVM_TVD, FVM_TVD_IMPLICIT or FEM_RKDG) with its file and log
+// cadence, free everything. An optional argument names another task file.
 #include <cstdio>
 
 #include "cfd2d.h"

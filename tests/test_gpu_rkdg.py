@@ -198,3 +198,18 @@ def test_rkdg_half_million_cells_properties(capi, tmp_path):
     C = s.dg_coeffs()
     assert np.isfinite(C).all()
     assert abs(float((J * C[:, 0]).sum()) - m0) <= 1e-12 * abs(m0)
+
+
+def test_rkdg_executable_writes_the_reference_files(capi, tmp_path):
+    """The stand-alone executable (the reference's main) on a FEM_RKDG task: init's step-0
+    files equal the reference's byte for byte, and run() ends with status 0."""
+    import subprocess
+    from conftest import PKG
+    g = load_golden("rkdg_quadrants_lax_3pt")
+    write_dg_case(tmp_path, str(g["task_xml"]), str(g["proc"]))
+    r = subprocess.run([os.path.join(PKG, "lib", "cfd2d_gpu")], cwd=tmp_path, capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert (tmp_path / "res_0000000000.pvtu").read_text() == str(g["ref_pvtu0"])
+    assert (tmp_path / "vtk_data" / "res_0000000000.0000.vtu").read_text() == str(g["ref_vtu0"])
+    assert "UNSTEADY. Proc =    0. Time step TAU = 1.000000e-03." in r.stdout
