@@ -264,6 +264,7 @@ class Task:
     reorder: str | None = None        # NONE / RCM / HILBERT
     fused_stage: str | None = None    # "1" runs the mixed form's stages as one tiled kernel
     adjoint_store: str | None = None  # NONE / PRIMITIVES / ALL: what the adjoint keeps per recorded stage
+    flux_pipeline: str | None = None  # mixed form: ON (default) / OFF, the software-pipelined flux kernel
     method: str = "FVM_TVD"
 
 
@@ -281,7 +282,8 @@ def write_task_xml(t: Task) -> str:
          f'    <LOG_OUTPUT_STEP value="{int(t.log_output_step)}" />']
     for tag, val in (("FLUX", t.flux), ("RECONSTRUCTION", t.reconstruction),
                      ("TIME_SCHEME", t.time_scheme), ("PRECISION", t.precision), ("REORDER", t.reorder),
-                     ("FUSED_STAGE", t.fused_stage), ("ADJOINT_STORE", t.adjoint_store)):
+                     ("FUSED_STAGE", t.fused_stage), ("ADJOINT_STORE", t.adjoint_store),
+                     ("FLUX_PIPELINE", t.flux_pipeline)):
         if val is not None:
             L.append(f'    <{tag} value="{val}" />')
     L += ["  </control>", "  <limits>", f'    <ro min="{_v(rmin)}" max="{_v(rmax)}" />',

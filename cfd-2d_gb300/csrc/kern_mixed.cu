@@ -3,6 +3,7 @@
 // update, limits and time steps in FP64 (kernels.cuh, k_update).
 #define KT float
 #define KFN(name) launch_##name##_mixed
+#define KPIPE 1
 #include "kern_inst.cuh"
 
 namespace cfd2d {

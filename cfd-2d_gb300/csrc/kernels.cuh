@@ -102,6 +102,11 @@ __device__ __forceinline__ void st8(T* __restrict__ p, int i, const T* v) {
     st4(p, 2 * i + 1, v[4], v[5], v[6], v[7]);
 }
 
+// Per-item data a kernel reads once and no later kernel of the stage reads again (edge
+// geometry, face lists) is loaded with the evict-first hint, so the L2 keeps the cell
+// records the neighbour gathers hit.
+template <typename T> __device__ __forceinline__ T ldcs(const T* p) { return __ldcs(p); }
+
 template <typename T>
 __device__ __forceinline__ Prim<T> load_prim(const T* __restrict__ W, int i) {
     T v[4];
@@ -571,8 +576,8 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
     const CellFaces<T> cf = cf_of<T>(c);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const int nb = c.cf_nb[k * nc + i];
-        const T nx = cf.nx[k * nc + i], ny = cf.ny[k * nc + i], l = cf.l[k * nc + i];
+        const int nb = ldcs(c.cf_nb + k * nc + i);
+        const T nx = ldcs(cf.nx + k * nc + i), ny = ldcs(cf.ny + k * nc + i), l = ldcs(cf.l + k * nc + i);
         const bool side2 = nb >= 0 && (nb & 1);
         const Prim<T> o = nb >= 0 ? load_prim(W, nb >> 1) : grad_ghost(c, i, -(nb + 1), q, nx, ny);
         grad_face(g, q, o, nx, ny, l, side2);
@@ -619,13 +624,28 @@ __device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, 
 // Edge flux over the edge's two Gauss points, times l/2 (src/methods/fvm_tvd.cpp:329-352).
 // The edge flux from the two cells' primitives and gradients, both Gauss points,
 // times l/2 (src/methods/fvm_tvd.cpp:329-352): out[4] is what F holds for edge e.
+// An edge's geometry as the flux reads it: normal, length, the Gauss-point offsets
+// (gp0: dxL dyL dxR dyR, gp1: ...; only with reconstruction).
+template <typename T> struct EdgeGeo { T nx, ny, l, dl[8]; };
+template <typename T, int RECON>
+__device__ __forceinline__ EdgeGeo<T> load_geo(const DevCase& c, int e) {
+    EdgeGeo<T> g;
+    g.nx = ldcs(NX_of<T>(c) + e);
+    g.ny = ldcs(NY_of<T>(c) + e);
+    g.l = ldcs(L_of<T>(c) + e);
+    if (RECON != RECON_NONE) {
+        const T* __restrict__ DL = DL_of<T>(c);
+#pragma unroll
+        for (int k = 0; k < 8; k++) g.dl[k] = ldcs(DL + (size_t)k * c.ne + e);
+    }
+    return g;
+}
+
 template <typename T, int FLUX, int RECON>
 __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const Prim<T>& qL, const T* gL,
-                                          const Prim<T>& qR, const T* gR, T* out) {
+                                          const Prim<T>& qR, const T* gR, T* out, const EdgeGeo<T>& geo) {
     // qR: the second cell's primitives on interior edges (e < n_int), qL on boundary edges
-    const int ne = c.ne;
-    const T* __restrict__ DL = DL_of<T>(c);
-    const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
+    const T nx = geo.nx, ny = geo.ny, l = geo.l;
     const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
     const bool inner = e < c.n_int;
     Prim<T> gc = qL;
@@ -657,11 +677,11 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
             dR.r = qL.r - qR.r; dR.u = qL.u - qR.u; dR.v = qL.v - qR.v; dR.p = qL.p - qR.p;
         }
         if (RECON != RECON_NONE)
-            reconstruct<T, RECON>(pL, gL, DL[(4 * gp) * ne + e], DL[(4 * gp + 1) * ne + e], dL);
+            reconstruct<T, RECON>(pL, gL, geo.dl[4 * gp], geo.dl[4 * gp + 1], dL);
         if (inner) {
             pR = qR;
             if (RECON != RECON_NONE)
-                reconstruct<T, RECON>(pR, gR, DL[(4 * gp + 2) * ne + e], DL[(4 * gp + 3) * ne + e], dR);
+                reconstruct<T, RECON>(pR, gR, geo.dl[4 * gp + 2], geo.dl[4 * gp + 3], dR);
         } else {
             pR = ghost_state(b, pL, Tc, nx, ny, M);
         }
@@ -682,20 +702,130 @@ template <typename T, int FLUX, int RECON>
 __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
     const T* __restrict__ W = W_of<T>(c);
     const T* __restrict__ G = G_of<T>(c);
-    const int c1 = c.ec1[e];
+    const int c1 = ldcs(c.ec1 + e);
     const bool inner = e < c.n_int;
     const Prim<T> qL = load_prim(W, c1);
     T gL[8], gR[8];
     if (RECON != RECON_NONE) ld8(G, c1, gL);
     Prim<T> qR = qL;
     if (inner) {
-        const int c2 = c.ec2[e];
+        const int c2 = ldcs(c.ec2 + e);
         qR = load_prim(W, c2);
         if (RECON != RECON_NONE) ld8(G, c2, gR);
     }
     T out[4];
-    flux_core<T, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out);
+    flux_core<T, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e));
     st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
+}
+
+// 16-byte asynchronous global -> shared copies (cp.async, completion tracked per
+// commit group; the waits are hardware waits, no polling).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+// the same, cached in L1 as well (records that neighbouring items read again)
+__device__ __forceinline__ void cp_async16_ca(void* smem_dst, const void* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+// 4-byte asynchronous copy global -> shared, cached in L1 and L2
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+// The mixed form's flux kernel as a persistent, software-pipelined loop. A thread works
+// through edges e, e + S, e + 2S, ... (S = threads in the grid): while it computes one
+// edge, the next edge's inputs -- the two cells' records (W and G, 96 bytes) and the edge's
+// geometry (normal, length, Gauss-point offsets) -- are on their way into its own slots of
+// shared memory (cp.async), and the cell numbers of the edge after that into registers, so
+// no load stalls the arithmetic. Same inputs and arithmetic as k_flux: the same fluxes bit
+// for bit. Dynamic shared memory: 2 stages x (6 float4 + 12 float) per thread.
+constexpr int kPipeStage = 6 * 16 + 12 * 4;  // bytes per thread and stage
+template <int FLUX, int RECON>
+__global__ void __launch_bounds__(256, 3) k_flux_pipe(const DevCase c) {
+    extern __shared__ float4 stg[];
+    const int tid = threadIdx.x, nb = blockDim.x;
+    const float4* __restrict__ W4 = reinterpret_cast<const float4*>(c.W32);
+    const float4* __restrict__ G4 = reinterpret_cast<const float4*>(c.G32);
+    const int stride = gridDim.x * nb;
+    const int ne = c.ne, n_int = c.n_int;
+    // stage k: 6 float4 columns then 12 float columns, each nb wide
+    auto rec = [&](int k) { return reinterpret_cast<float4*>(reinterpret_cast<char*>(stg) + (size_t)k * kPipeStage * nb); };
+    auto geo_col = [&](int k, int j) { return reinterpret_cast<float*>(rec(k) + 6 * nb) + (size_t)j * nb + tid; };
+    int e = blockIdx.x * nb + tid;
+    // cell numbers of the edge whose copies go out next (a, b) and of the one after (a2, b2)
+    int a = 0, b = 0, a2 = 0, b2 = 0;
+    auto cells = [&](int edge, int& x, int& y) {
+        if (edge < ne) {
+            x = ldcs(c.ec1 + edge);
+            y = edge < n_int ? ldcs(c.ec2 + edge) : x;
+        }
+    };
+    auto issue = [&](int k, int edge, int x, int y) {
+        if (edge < ne) {
+            float4* sl = rec(k) + tid;
+            cp_async16_ca(sl, W4 + x);
+            cp_async16_ca(sl + nb, W4 + y);
+            if (RECON != RECON_NONE) {
+                cp_async16_ca(sl + 2 * nb, G4 + 2 * (size_t)x);
+                cp_async16_ca(sl + 3 * nb, G4 + 2 * (size_t)x + 1);
+                cp_async16_ca(sl + 4 * nb, G4 + 2 * (size_t)y);
+                cp_async16_ca(sl + 5 * nb, G4 + 2 * (size_t)y + 1);
+            }
+            cp_async4(geo_col(k, 0), c.nx32 + edge);
+            cp_async4(geo_col(k, 1), c.ny32 + edge);
+            cp_async4(geo_col(k, 2), c.l32 + edge);
+            if (RECON != RECON_NONE)
+#pragma unroll
+                for (int j = 0; j < 8; j++) cp_async4(geo_col(k, 3 + j), c.dl32 + (size_t)j * ne + edge);
+        }
+        cp_async_commit();
+    };
+    cells(e, a, b);
+    issue(0, e, a, b);
+    cells(e + stride, a2, b2);
+    for (int k = 0; e < ne; e += stride, k ^= 1) {
+        const int c1 = a;
+        a = a2; b = b2;
+        issue(k ^ 1, e + stride, a, b);     // the next edge's inputs
+        cells(e + 2 * stride, a2, b2);      // and the cell numbers of the one after
+        cp_async_wait<1>();                 // this edge's inputs (issued one round ago)
+        const float4* sl = rec(k) + tid;
+        const float4 wl = sl[0];
+        const Prim<float> qL{wl.x, wl.y, wl.z, wl.w};
+        Prim<float> qR = qL;
+        float gL[8], gR[8];
+        if (RECON != RECON_NONE) {
+            const float4 x0 = sl[2 * nb], x1 = sl[3 * nb];
+            gL[0] = x0.x; gL[1] = x0.y; gL[2] = x0.z; gL[3] = x0.w; gL[4] = x1.x; gL[5] = x1.y; gL[6] = x1.z; gL[7] = x1.w;
+        }
+        if (e < n_int) {
+            const float4 wr = sl[nb];
+            qR = Prim<float>{wr.x, wr.y, wr.z, wr.w};
+            if (RECON != RECON_NONE) {
+                const float4 y0 = sl[4 * nb], y1 = sl[5 * nb];
+                gR[0] = y0.x; gR[1] = y0.y; gR[2] = y0.z; gR[3] = y0.w; gR[4] = y1.x; gR[5] = y1.y; gR[6] = y1.z; gR[7] = y1.w;
+            }
+        }
+        EdgeGeo<float> geo;
+        geo.nx = *geo_col(k, 0);
+        geo.ny = *geo_col(k, 1);
+        geo.l = *geo_col(k, 2);
+        if (RECON != RECON_NONE)
+#pragma unroll
+            for (int j = 0; j < 8; j++) geo.dl[j] = *geo_col(k, 3 + j);
+        float out[4];
+        flux_core<float, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out, geo);
+        st4(c.F32, e, out[0], out[1], out[2], out[3]);
+    }
+    cp_async_wait<0>();
 }
 
 template <typename T, int FLUX, int RECON, bool STRIDE>
@@ -894,17 +1024,6 @@ __device__ __forceinline__ void update_one(const DevCase& c, int i) {
     update_finish<T, SCHEME, STAGE>(c, i, R, Wm_of<T>(c));
 }
 
-// 16-byte asynchronous global -> shared copies (cp.async, completion tracked per
-// commit group; the waits are hardware waits, no polling).
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // The mixed form's whole Runge-Kutta stage for tiles of cells (persistent CTAs of 256
 // threads, each looping over tiles): a tile's and its two-ring halo's primitives are
 // staged in shared memory (fetched with cp.async while the CTA works on its previous
@@ -985,7 +1104,7 @@ __global__ void __launch_bounds__(256, 5) k_stage_fused(const DevCase c, const D
             }
             float out[4];
             const int c1 = l1 < n_own ? own0 + l1 : tl.halo[h0 + l1 - n_own];
-            flux_core<float, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out);
+            flux_core<float, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out, load_geo<float, RECON>(c, e));
             Fs[k] = make_float4(out[0], out[1], out[2], out[3]);
         }
         __syncthreads();

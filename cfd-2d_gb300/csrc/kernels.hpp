@@ -125,6 +125,7 @@ struct DevCase {
     double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
     int steady;
     int newton_cap;
+    int flux_pipe;         // mixed form: the software-pipelined flux kernel (k_flux_pipe)
     // state
     double* A;             // 4*nc conserved state U^n (and result)
     double* B;             // 4*nc stage state
@@ -145,6 +146,8 @@ struct DevCase {
 // ---- launchers (kern_fp64.cu / kern_mixed.cu / kern_common.cu)
 void launch_grad(const DevCase& c, int precision, cudaStream_t s);
 void launch_flux(const DevCase& c, int precision, int flux, int recon, cudaStream_t s);
+// the mixed form's pipelined flux kernels' launch attributes, set once before any capture
+void launch_flux_prepare_mixed();
 // stage update; reads A (and B for later stages), writes B or A and the next primitives
 void launch_update(const DevCase& c, int precision, int scheme, int stage, cudaStream_t s);
 void launch_remediate(const DevCase& c, int precision, cudaStream_t s);

@@ -149,6 +149,8 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
         c.lim_pmin = task_.lim_pmin; c.lim_pmax = task_.lim_pmax; c.lim_umax = task_.lim_umax;
         c.steady = task_.steady;
         c.newton_cap = task_.newton_cap;
+        c.flux_pipe = mixed && task_.flux_pipe != 0 ? 1 : 0;
+        if (c.flux_pipe) launch_flux_prepare_mixed();
         c.A = dalloc<double>(4 * (size_t)nc);
         c.B = dalloc<double>(4 * (size_t)nc);
         c.cfl = dalloc<double>(nc);

@@ -34,6 +34,7 @@ struct TaskConfig {
     int fused = -1;           // mixed form, SSP-RK3 / Heun: 1 runs one tiled kernel per stage (opt-in)
     int adj_store = -1;       // adjoint segment store: 0 states only, 1 + primitives, 2 + gradients, -1 by memory
     int newton_cap = 100;     // iteration cap of the exact Riemann solver
+    int flux_pipe = 1;        // mixed form: the software-pipelined flux kernel (0: one thread per edge)
     // FVM_TVD_IMPLICIT (src/methods/fvm_tvd_implicit.cpp:13-184): <CFL> start (in cfl),
     // scale, max, step, max_limited_cells; <smoothing>; the matrix solver's parameters
     // (run() hard-codes 20 iterations and 1e-7, SolverHypreGmres.h the Krylov dimension 30)

@@ -84,3 +84,23 @@ def test_fused_with_rcm_order(capi, tmp_path):
     a.step(8)
     b.step(8)
     assert np.array_equal(a.state(), b.state())
+
+
+@pytest.mark.parametrize("flux,recon", [("HLLC", "MINMOD"), ("ROE", "MINMOD"), ("GODUNOV", "LINEAR"),
+                                        ("LAX", "NONE")])
+def test_pipelined_flux_equals_one_thread_per_edge(capi, tmp_path, flux, recon):
+    """The mixed form's default flux kernel (persistent, cp.async-pipelined gathers) against
+    the one-thread-per-edge kernel (FLUX_PIPELINE OFF): the same fluxes, the same bits."""
+    kinds = ("BOUND_INLET", "BOUND_OUTLET", "BOUND_WALL_SLIP", "BOUND_WALL_NO_SLIP")
+    t, m, U0 = cases.vortex(150, flux=flux, recon=recon, scheme="SSPRK3", steps=10, bnd_kinds=kinds)
+    out = []
+    for pipe in ("OFF", "ON"):
+        t.precision = "MIXED"
+        t.flux_pipeline = pipe
+        d = tmp_path / pipe
+        d.mkdir(exist_ok=True)
+        s = capi.Solver(cases.write_task(t, m, str(d)), mesh=m)
+        s.set_state(U0, reset_time_step=True)
+        s.step(10)
+        out.append(s.state())
+    assert np.array_equal(out[0].view(np.int64), out[1].view(np.int64))
