@@ -586,6 +586,28 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
     st8(G_of<T>(c), i, g);
 }
 
+// 16-byte asynchronous global -> shared copies (cp.async, completion tracked per
+// commit group; the waits are hardware waits, no polling).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+// the same, cached in L1 as well (records that neighbouring items read again)
+__device__ __forceinline__ void cp_async16_ca(void* smem_dst, const void* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
+// 4-byte asynchronous copy global -> shared, cached in L1 and L2
+__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+
 template <typename T, bool STRIDE>
 __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -716,28 +738,6 @@ __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
     T out[4];
     flux_core<T, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e));
     st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
-}
-
-// 16-byte asynchronous global -> shared copies (cp.async, completion tracked per
-// commit group; the waits are hardware waits, no polling).
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-// the same, cached in L1 as well (records that neighbouring items read again)
-__device__ __forceinline__ void cp_async16_ca(void* smem_dst, const void* gmem_src) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
-}
-
-// 4-byte asynchronous copy global -> shared, cached in L1 and L2
-__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
 }
 
 // The mixed form's flux kernel as a persistent, software-pipelined loop. A thread works
