@@ -473,7 +473,8 @@ int cfd2d_save_state(cfd2d_t* h, const char* path) {
     Range r("cfd2d_save_state");
     return guarded([&] {
         if (!h || !path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        if (h->imp) h->imp->save_state(path);
+        if (h->dg) h->dg->save_state(path);
+        else if (h->imp) h->imp->save_state(path);
         else ex(h).save_state(path);
         return CFD2D_OK;
     });
@@ -483,7 +484,8 @@ int cfd2d_load_state(cfd2d_t* h, const char* path) {
     Range r("cfd2d_load_state");
     return guarded([&] {
         if (!h || !path) return fail(CFD2D_ERR_INVALID_ARG, "null argument");
-        if (h->imp) h->imp->load_state(path);
+        if (h->dg) h->dg->load_state(path);
+        else if (h->imp) h->imp->load_state(path);
         else ex(h).load_state(path);
         return CFD2D_OK;
     });

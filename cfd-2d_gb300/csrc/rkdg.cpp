@@ -708,6 +708,58 @@ void RkdgSolver::get_ctau(double* out) {
     for (int i = 0; i < c_.nc; i++) out[i] = tmp[iperm_[i]];
 }
 
+namespace {
+const char kDgStateMagic[8] = {'C', 'F', 'D', '2', 'D', 'D', 'G', '1'};
+}
+
+// Restart files (no counterpart in the reference): coefficients (caller order), cTau, the
+// step counter, t and TAU; a resumed run continues bit for bit as the uninterrupted one.
+void RkdgSolver::save_state(const char* path) {
+    use_device();
+    const int nc = c_.nc;
+    std::vector<double> U(12 * (size_t)nc), ct(nc);
+    get_coeffs(U.data());
+    get_ctau(ct.data());
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' opening error.");
+    const int64_t hdr[2] = {nc, steps_};
+    const double hd[2] = {t_, tau_};
+    bool ok = std::fwrite(kDgStateMagic, 1, 8, fp) == 8 && std::fwrite(hdr, sizeof hdr, 1, fp) == 1 &&
+              std::fwrite(hd, sizeof hd, 1, fp) == 1 &&
+              std::fwrite(U.data(), sizeof(double), U.size(), fp) == U.size() &&
+              std::fwrite(ct.data(), sizeof(double), ct.size(), fp) == ct.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    if (!ok) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' write error.");
+}
+
+void RkdgSolver::load_state(const char* path) {
+    use_device();
+    const int nc = c_.nc;
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) throw Error(CFD2D_ERR_FILE_OPENING, std::string("File '") + path + "' opening error.");
+    char magic[8];
+    int64_t hdr[2];
+    double hd[2];
+    std::vector<double> U(12 * (size_t)nc), ct(nc);
+    bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, kDgStateMagic, 8) == 0 &&
+              std::fread(hdr, sizeof hdr, 1, fp) == 1 && hdr[0] == nc && std::fread(hd, sizeof hd, 1, fp) == 1 &&
+              std::fread(U.data(), sizeof(double), U.size(), fp) == U.size() &&
+              std::fread(ct.data(), sizeof(double), ct.size(), fp) == ct.size();
+    std::fclose(fp);
+    if (!ok) throw Error(CFD2D_ERR_MESH_FORMAT, std::string("File '") + path + "' is not a state of this mesh.");
+    const size_t bytes = 12 * (size_t)nc * sizeof(double);
+    CUDA_CHECK(cudaMemcpyAsync(stage_, U.data(), bytes, cudaMemcpyHostToDevice, stream_));
+    dg_launch_gather(c_, stage_, c_.A, stream_);
+    std::vector<double> cts(nc);
+    for (int i = 0; i < nc; i++) cts[iperm_[i]] = ct[i];
+    CUDA_CHECK(cudaMemcpyAsync(c_.ctau, cts.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, stream_));
+    CUDA_CHECK(cudaStreamSynchronize(stream_));
+    steps_ = (int)hdr[1];
+    t_ = hd[0];
+    tau_ = hd[1];
+    res_valid_ = false;
+}
+
 void RkdgSolver::set_tau(double tau) {
     use_device();
     tau_ = tau;

@@ -132,6 +132,9 @@ public:
     void set_tau(double tau);        // impose a time step (every cell)
     void residuals(double out[4]);   // of the last step
     void save_vtu(int step);
+    // restart files: coefficients, cTau, step counter, time and TAU
+    void save_state(const char* path);
+    void load_state(const char* path);
     double timed_steps(int n);      // device ms of n steps (graph replays between CUDA events)
     // n steps launched kernel by kernel with events: ms of 0 edge kernels, 1 cell kernels,
     // 2 time step (steady), launches per step in launches[0..2]

@@ -213,3 +213,22 @@ def test_rkdg_executable_writes_the_reference_files(capi, tmp_path):
     assert (tmp_path / "res_0000000000.pvtu").read_text() == str(g["ref_pvtu0"])
     assert (tmp_path / "vtk_data" / "res_0000000000.0000.vtu").read_text() == str(g["ref_vtu0"])
     assert "UNSTEADY. Proc =    0. Time step TAU = 1.000000e-03." in r.stdout
+
+
+def test_rkdg_restart_resumes_bit_for_bit(capi, tmp_path):
+    """cfd2d_save_state / cfd2d_load_state on a FEM_RKDG handle: 3 steps, save, 3 more; a new
+    handle loading the file and taking 3 steps ends on the same coefficients, time and step."""
+    t, m, pm, U0 = cases.rkdg_vortex(20, flux="GODUNOV", steady=1, cfl=0.05)
+    task = write_dg_case(tmp_path, mg.write_rkdg_task_xml(t), mg.write_proc(pm))
+    a = capi.Solver(task)
+    a.set_dg_coeffs(U0)
+    a.step(3)
+    a.save_state(str(tmp_path / "dg.state"))
+    a.step(3)
+    b = capi.Solver(task)
+    b.load_state(str(tmp_path / "dg.state"))
+    assert b.get_info().step == 3
+    b.step(3)
+    assert np.array_equal(bits(a.dg_coeffs()), bits(b.dg_coeffs()))
+    assert np.array_equal(bits(a.time_step()), bits(b.time_step()))
+    assert b.get_info().step == 6 and b.get_info().time == a.get_info().time
