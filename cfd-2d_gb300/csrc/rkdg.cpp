@@ -609,6 +609,7 @@ int RkdgSolver::read_status() {
     CUDA_CHECK(cudaMemcpyAsync(&e, c_.err, sizeof e, cudaMemcpyDeviceToHost, stream_));
     CUDA_CHECK(cudaMemsetAsync(c_.err, 0, sizeof(unsigned), stream_));
     CUDA_CHECK(cudaStreamSynchronize(stream_));
+    if (e & ERRBIT_NONPHYSICAL) return CFD2D_ERR_NONPHYSICAL;
     if (e & ERRBIT_NEWTON_CAP) return CFD2D_ERR_NEWTON_CAP;
     return CFD2D_OK;
 }

@@ -265,6 +265,11 @@ __global__ void __launch_bounds__(128) k_dg_cell(const DgCase c, int stage, int 
                 res[k] = (out[k] + o) * 0.5;
             }
             store12(c.A, i, res);
+            // a non-positive or NaN cell-mean density or energy is reported (the state is
+            // still advanced, as the reference would): bit tests on the integer pipe
+            const long long br = __double_as_longlong(res[0]), be = __double_as_longlong(res[9]);
+            if (br <= 0 || br >= 0x7ff0000000000000ll || be <= 0 || be >= 0x7ff0000000000000ll)
+                atomicOr(c.err, ERRBIT_NONPHYSICAL);
             if (with_res) {  // calcResiduals, :1286-1319: | U - ro_old |, ro_old the cell's own for shared cells
 #pragma unroll
                 for (int v = 0; v < 4; v++) {

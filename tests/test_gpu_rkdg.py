@@ -232,3 +232,18 @@ def test_rkdg_restart_resumes_bit_for_bit(capi, tmp_path):
     assert np.array_equal(bits(a.dg_coeffs()), bits(b.dg_coeffs()))
     assert np.array_equal(bits(a.time_step()), bits(b.time_step()))
     assert b.get_info().step == 6 and b.get_info().time == a.get_info().time
+
+
+def test_rkdg_reports_a_nonphysical_state(capi, tmp_path):
+    """A negative density injected into the coefficients: the step returns
+    CFD2D_ERR_NONPHYSICAL (the state is still advanced) and the handle stays usable."""
+    t, m, pm, U0 = cases.rkdg_vortex(10, flux="LAX")
+    s = capi.Solver(write_dg_case(tmp_path, mg.write_rkdg_task_xml(t), mg.write_proc(pm)))
+    bad = U0.copy()
+    bad[7, 0] = -1.0
+    s.set_dg_coeffs(bad)
+    rc = s.step(1, allow_warnings=True)
+    assert rc == capi.ERR_NONPHYSICAL
+    s.set_dg_coeffs(U0)
+    assert s.step(2) == 0
+    assert np.isfinite(s.dg_coeffs()).all()
