@@ -69,6 +69,7 @@ ImplicitSolver::ImplicitSolver(const TaskConfig& t, Topo&& topo, const std::vect
         c.tau_xml = task_.tau;
         c.gam_flux = 1.4;  // __GAM, src/methods/fvm_tvd_implicit.cpp:536
         c.ig1_flux = 1.0 / (c.gam_flux - 1.0);
+        c.rg_flux = rim_gas<double>(c.gam_flux);
         c.lim_rmin = task_.lim_rmin; c.lim_rmax = task_.lim_rmax;
         c.lim_pmin = task_.lim_pmin; c.lim_pmax = task_.lim_pmax; c.lim_umax = task_.lim_umax;
         c.face = upload(lay_.face);

@@ -112,14 +112,14 @@ __global__ void __launch_bounds__(256) k_imp_flux(const ImpCase c) {
             reconstruct<double, RECON_LINEAR>(pR, gR, c.dl[(4 * gp + 2) * ne + e], c.dl[(4 * gp + 3) * ne + e], qR);
             double f[4];
             if constexpr (FLUX == FLUX_LAX) flux_lax(f, pL, pR, nx, ny, GAM, c.ig1_flux);
-            else hit |= flux_godunov(f, pL, pR, nx, ny, GAM, c.newton_cap);
+            else hit |= flux_godunov<double, false>(f, pL, pR, nx, ny, c.rg_flux, c.newton_cap);
             fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
         }
     } else {  // both Gauss points see the same centre state and ghost
         const Prim<double> pR = imp_ghost(c.bnds[c.ebnd[e]], qL, nx, ny, imat(c, c1).M);
         double f[4];
         if constexpr (FLUX == FLUX_LAX) flux_lax(f, qL, pR, nx, ny, GAM, c.ig1_flux);
-        else hit |= flux_godunov(f, qL, pR, nx, ny, GAM, c.newton_cap);
+        else hit |= flux_godunov<double, false>(f, qL, pR, nx, ny, c.rg_flux, c.newton_cap);
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
     }

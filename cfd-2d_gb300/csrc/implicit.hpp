@@ -66,6 +66,7 @@ struct ImpCase {
     double smoothing_par;
     double tau_xml;
     double gam_flux, ig1_flux;
+    RimGas<double> rg_flux;   // the exact Riemann solver's constants of gam_flux
     double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
     // geometry (storage order)
     const int* face;          // 3*nc: (edge << 1) | side (side 1: the cell is c2)

@@ -528,6 +528,14 @@ __device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& 
     if (FLUX == FLUX_HLLC) { flux_hllc(f, L, R, nx, ny, GAM, IG1); return false; }
     return flux_godunov(f, L, R, nx, ny, GAM, cap);
 }
+// The same with the FP64 Riemann solver's gas constants formed once (on the host, in the
+// same operations): FP64 faces use them, FP32 faces form their own per call as before.
+template <typename T, int FLUX>
+__device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1,
+                                         int cap, const RimGas<double>& rg) {
+    if constexpr (FLUX == FLUX_GODUNOV && sizeof(T) == 8) return flux_godunov<double, false>(f, L, R, nx, ny, rg, cap);
+    return num_flux<T, FLUX>(f, L, R, nx, ny, GAM, IG1, cap);
+}
 
 // ------------------------------------------------------------------ kernels
 
@@ -708,7 +716,7 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
             pR = ghost_state(b, pL, Tc, nx, ny, M);
         }
         T f[4];
-        hit |= num_flux<T, FLUX>(f, pL, pR, nx, ny, GAM, IG1, c.newton_cap);
+        hit |= num_flux<T, FLUX>(f, pL, pR, nx, ny, GAM, IG1, c.newton_cap, c.rg_flux);
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
         if (RECON == RECON_NONE) {  // both Gauss points see the cell-centre states
             fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];

@@ -121,6 +121,7 @@ struct DevCase {
     const float* invS32;   // nc, 1/S in FP32 (mixed form)
     double gam_flux;
     double ig1_flux;       // RN(1/(gam_flux - 1)), computed on the host
+    RimGas<double> rg_flux;  // the exact Riemann solver's constants of gam_flux
     double cfl_number;
     double lim_rmin, lim_rmax, lim_pmin, lim_pmax, lim_umax;
     int steady;

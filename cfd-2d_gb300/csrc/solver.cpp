@@ -141,6 +141,7 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
         c.gam_flux = 1.4;  // hard-coded in FVM_TVD::run, src/methods/fvm_tvd.cpp:345,398
         c.gam_flux_f = 1.4f;
         c.ig1_flux = 1.0 / (c.gam_flux - 1.0);
+        c.rg_flux = rim_gas<double>(c.gam_flux);
         c.ig1_flux_f = 1.0f / (c.gam_flux_f - 1.0f);
         c.lim_f[0] = (float)task_.lim_rmin; c.lim_f[1] = (float)task_.lim_rmax;
         c.lim_f[2] = (float)task_.lim_pmin; c.lim_f[3] = (float)task_.lim_pmax; c.lim_f[4] = (float)task_.lim_umax;
