@@ -247,3 +247,18 @@ def test_rkdg_reports_a_nonphysical_state(capi, tmp_path):
     s.set_dg_coeffs(U0)
     assert s.step(2) == 0
     assert np.isfinite(s.dg_coeffs()).all()
+
+
+def test_rkdg_full_size_step_equals_oracle(capi, oracle, tmp_path):
+    """The bench workload's mesh (1024 x 1024 x 2 = 2,097,152 triangles, P1 vortex, LAX): one
+    step through cfd2d_create_with_mesh equals the oracle's bit for bit."""
+    t, m, pm, U0 = cases.rkdg_vortex(1024, flux="LAX")
+    (tmp_path / "task.xml").write_text(mg.write_rkdg_task_xml(t))
+    mesh = mg.Mesh(pm.nodes, pm.tris, m.cell_region, m.bsegs, m.bseg_bnd)
+    s = capi.Solver(str(tmp_path / "task.xml"), mesh=mesh)
+    s.set_dg_coeffs(U0)
+    s.step(1)
+    o = oracle.OracleDG(t, pm)
+    o.set_coeffs(U0)
+    o.step(1)
+    assert np.array_equal(bits(s.dg_coeffs()), bits(o.state()["U"]))
