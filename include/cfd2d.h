@@ -73,7 +73,7 @@ typedef struct {
 typedef struct {
     int n_cells, n_edges, n_boundary_edges, n_nodes;
     int step;                /* steps taken */
-    int flux, recon, scheme, precision, steady;
+    int flux, recon, scheme, precision, steady;  /* recon, scheme: -1 on a FEM_RKDG handle */
     double time;             /* t as the reference accumulates it (t += TAU per unsteady step) */
     double tau;              /* global time step TAU (unsteady) */
     size_t device_bytes;     /* device memory held by the handle */
