@@ -262,3 +262,25 @@ def test_rkdg_full_size_step_equals_oracle(capi, oracle, tmp_path):
     o.set_coeffs(U0)
     o.step(1)
     assert np.array_equal(bits(s.dg_coeffs()), bits(o.state()["U"]))
+
+
+def test_rkdg_numeric_edge_types_bind_like_names(capi, oracle, tmp_path):
+    """Boundary edges typed by number (bound to <boundCond edgeType>) and by name (TYPE_NAMED,
+    bound by <name>) give the same run; both equal the oracle."""
+    t, m, pm, U0 = cases.rkdg_vortex(16, flux="LAX",
+                                     kinds=("BOUND_INLET", "BOUND_OUTLET", "BOUND_WALL_SLIP", "BOUND_WALL_NO_SLIP"))
+    pm_num = mg.proc_mesh(m, [r.name for r in t.regions], bnd_types=[b.edge_type for b in t.boundaries])
+    assert set(pm_num.edge_type[pm_num.edge_type != 0]) == {1, 2, 3, 4}
+    out = []
+    for k, part in enumerate((pm, pm_num)):
+        d = tmp_path / str(k)
+        d.mkdir()
+        s = capi.Solver(write_dg_case(d, mg.write_rkdg_task_xml(t), mg.write_proc(part)))
+        s.set_dg_coeffs(U0)
+        s.step(4)
+        out.append(s.dg_coeffs())
+    o = oracle.OracleDG(t, pm_num)
+    o.set_coeffs(U0)
+    o.step(4)
+    assert np.array_equal(bits(out[0]), bits(out[1]))
+    assert np.array_equal(bits(out[1]), bits(o.state()["U"]))

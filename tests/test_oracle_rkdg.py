@@ -108,3 +108,11 @@ def test_oracle_rkdg_reference_mode_differs_from_heun(oracle):
     a = oracle.OracleDG(t, pm, rk="REFERENCE"); a.set_coeffs(U0); a.step(1)
     b = oracle.OracleDG(t, pm, rk="HEUN"); b.set_coeffs(U0); b.step(1)
     assert not np.array_equal(a.state()["U"], b.state()["U"])
+
+
+def test_proc_part_with_numeric_edge_types_round_trip():
+    t, m, pm, _ = cases.rkdg_quadrants(5)
+    pm_num = mg.proc_mesh(m, [r.name for r in t.regions], bnd_types=[b.edge_type for b in t.boundaries])
+    back = mg.read_proc(mg.write_proc(pm_num))
+    assert np.array_equal(back.edge_type, pm_num.edge_type) and back.edge_names == pm_num.edge_names
+    assert set(back.edge_type[back.edge_type != 0]) == {b.edge_type for b in t.boundaries}
