@@ -1,6 +1,6 @@
 /*
  * cfd2d oracle: plain-C restatement of the reference FVM_TVD explicit solver.
- * TEST INFRASTRUCTURE ONLY (see cfd2d_oracle.h): the checker, never the product.
+ * TEST INFRASTRUCTURE ONLY (see cfd2d_oracle.h): a reference to check against, never the product.
  *
  * Structure mirrors the reference on purpose: array-of-edges loops that scatter
  * into cells (src/methods/fvm_tvd.cpp:242-301, 329-365), the same conversions,

@@ -4,7 +4,7 @@
  *
  * TEST INFRASTRUCTURE ONLY. The product (libcfd2d_gpu.so) never links, loads or
  * calls this code; only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg use it, as the checker.
+ * baseline leg use it, to check the GPU results against.
  *
  * Parity: pinned against the reference's own FVM_TVD compiled from its sources
  * (oracle/Makefile, target "reference") on the fixtures in tests/golden/: in the

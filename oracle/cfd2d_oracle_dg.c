@@ -2,7 +2,7 @@
  * CPU restatement of the reference's explicit discontinuous Galerkin method FEM_RKDG
  * (src/methods/fem_rkdg.cpp) -- TEST INFRASTRUCTURE ONLY. The GPU library never links,
  * loads or calls this file; the tests, the smoke check and the CPU baseline of the
- * benchmark use it as the checker. Compiled with -ffp-contract=off so every product
+ * benchmark use it to check the GPU results against. Compiled with -ffp-contract=off so every product
  * and sum rounds on its own, as in the reference's build.
  *
  * Scope: P1 basis (BASE_FUNC_COUNT 3: 1, (x-xc)/HX, (y-yc)/HY, :1441-1452), cell

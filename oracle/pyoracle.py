@@ -1,7 +1,7 @@
 """ctypes binding of the C oracle and a runner for the reference's own FVM_TVD.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, as the checker. The product never imports it.
+CPU-baseline leg of bench.py, to check the GPU results against. The product never imports it.
 """
 from __future__ import annotations
 

@@ -8,7 +8,7 @@ driven by oracle/ref/ref_driver.cpp. Each fixture stores the inputs (task.xml,
 the mesh files and arrays, an optional per-cell initial state) and the
 reference's outputs (its Grid, its TAU, and the state after STEP_MAX steps).
 
-Run in the development container (the reference tree is not on the GPU machine):
+Run where the reference source tree is present (it is needed to build the reference):
     python tests/golden/make_golden.py
 """
 from __future__ import annotations

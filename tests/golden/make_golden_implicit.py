@@ -9,7 +9,7 @@ mesh files and arrays, the task parameters, an optional per-cell initial state) 
 the reference's outputs after STEP_MAX steps (state, cTau, flags, CFL, the last
 solve's iterations and residual) and its step-0 VTK file.
 
-Run in the development container (the reference tree is not on the GPU machine):
+Run where the reference source tree is present (it is needed to build the reference):
     python tests/golden/make_golden_implicit.py
 """
 from __future__ import annotations

@@ -8,7 +8,7 @@ mesh/mesh.0000.proc text, the task parameters, optional initial P1 coefficients 
 imposed time step) and the reference's outputs: the coefficients after init and after the
 steps, cTau, TAU, the residuals, the step-0 VTU and PVTU files and the log.
 
-Run in the development container (the reference tree is not on the GPU machine):
+Run where the reference source tree is present (it is needed to build the reference):
     python tests/golden/make_golden_rkdg.py
 """
 from __future__ import annotations
