@@ -243,9 +243,10 @@ def reference_arm(args, world, rank):
     ctx = mp.get_context("spawn")
     procs = max(1, (os.cpu_count() or 1))
     procs = min(procs, int(os.environ.get("CFD2D_REF_PROCS", 16)))
-    # bounded sample: the CPU step costs seconds, so time at most 3 steps per process
-    steps = max(1, min(args.steps, 3))
-    warm = 0 if args.warmup <= 0 else 1
+    # every process times the same --steps K after --warmup W steps as our arm (each CPU
+    # step of the full mesh costs ~1.5 s on one Grace core, so K=20, W=5 is ~40 s)
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
     q = ctx.Queue()
     ps = [ctx.Process(target=_ref_worker, args=((N_SIDE, warm, steps, q),)) for _ in range(procs)]
     for p in ps:
@@ -267,9 +268,10 @@ def reference_arm(args, world, rank):
             "config": {"workload": WORKLOAD, "cells": cells, "parallelism": f"{procs} host processes, one "
                        "independent instance each"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                             "sample": f"{steps} SSP-RK3 step(s) of the full 2,097,152-triangle workload per "
-                                       f"process, {procs} processes (the reference cannot run HLLC/minmod/SSP-RK3; "
-                                       "the oracle restates it and equals it bit for bit in its own mode)"},
+                             "sample": f"{steps} SSP-RK3 step(s) (after {warm} warm-up steps) of the full "
+                                       f"2,097,152-triangle workload per process, {procs} processes (the reference "
+                                       "cannot run HLLC/minmod/SSP-RK3; the oracle restates it and equals it bit for "
+                                       "bit in its own mode)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

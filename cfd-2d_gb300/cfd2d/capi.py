@@ -75,6 +75,7 @@ SIGNATURES = {
     "cfd2d_load_state": [_P, C.c_char_p],
     "cfd2d_residual_first_order_static": [_I, _I, _P, _P, _P, _P, _P, _I, _IP, _D, C.c_double, C.c_double, _I,
                                           _P, _P, _P],
+    "cfd2d_static_reset": [],
     "cfd2d_implicit_system": [_P, _D, _D, _D, _D],
     "cfd2d_implicit_stats": [_P, C.POINTER(ImplicitStats)],
     "cfd2d_dg_get_coeffs": [_P, _D],

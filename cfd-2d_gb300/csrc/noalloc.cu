@@ -54,8 +54,11 @@ __global__ void __launch_bounds__(256) k_static_edge_flux(const StaticArgs a) {
     if (e >= a.ne) return;
     const int nc = a.nc, ne = a.ne;
     const int c1 = a.c12[2 * e], c2 = a.c12[2 * e + 1];
+    // the boundary index is read and checked on boundary edges only: a mesh without
+    // boundary conditions (n_bnd == 0) is valid as long as no edge needs one
     const int bi = c2 >= 0 ? 0 : (a.bnd ? a.bnd[e] : -1);
-    if (c1 < 0 || c1 >= nc || c2 >= nc || c2 < -1 || bi < 0 || bi >= a.nbnd) {  // inconsistent mesh: NaN, no access
+    const bool bad_bnd = c2 < 0 && (bi < 0 || bi >= a.nbnd);
+    if (c1 < 0 || c1 >= nc || c2 >= nc || c2 < -1 || bad_bnd) {  // inconsistent mesh: NaN, no access
         for (int k = 0; k < 4; k++) a.F[(size_t)k * ne + e] = __longlong_as_double(0x7ff8000000000000ll);
         return;
     }
@@ -98,6 +101,8 @@ __global__ void __launch_bounds__(256) k_static_gather(const StaticArgs a) {
 
 // Device address of the scratch array, looked up once per device with that
 // device current (the host-side symbol is only a stand-in, not a device address).
+// A cudaDeviceReset ends the context that address belongs to; cfd2d_static_reset
+// forgets the cached addresses so that the next call looks them up again.
 std::mutex g_mu;
 void* g_scratch_dev[64] = {nullptr};
 
@@ -114,6 +119,11 @@ extern "C" int cfd2d_residual_first_order_static(int n_cells, int n_edges, const
         (n_bnd > 0 && (!edge_bnd || !bnd_kind || !bnd_par)) || n_bnd < 0 || flux < 0 || flux > 3)
         return CFD2D_ERR_INVALID_ARG;
     if (n_edges > CFD2D_STATIC_MAX_EDGES || n_bnd > kMaxBnd) return CFD2D_ERR_CAPACITY;
+    for (int k = 0; k < n_bnd; k++)
+        if (bnd_kind[k] < BND_INLET || bnd_kind[k] > BND_WALL_NO_SLIP) return CFD2D_ERR_INVALID_ARG;
+    // an error some earlier, unrelated CUDA work left pending is not this call's: it is
+    // reported before anything runs and left pending for its owner
+    if (cudaPeekAtLastError() != cudaSuccess) return CFD2D_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return CFD2D_ERR_NO_DEVICE;
     void* scratch;
@@ -159,6 +169,14 @@ extern "C" int cfd2d_residual_first_order_static(int n_cells, int n_edges, const
     case FLUX_HLLC: k_static_edge_flux<FLUX_HLLC><<<ge, 256, 0, s>>>(a); break;
     default: k_static_edge_flux<FLUX_GODUNOV><<<ge, 256, 0, s>>>(a); break;
     }
+    if (cudaGetLastError() != cudaSuccess) return CFD2D_ERR_CUDA;  // the flux launch
     k_static_gather<<<gc, 256, 0, s>>>(a);
-    return cudaGetLastError() == cudaSuccess ? CFD2D_OK : CFD2D_ERR_CUDA;
+    return cudaGetLastError() == cudaSuccess ? CFD2D_OK : CFD2D_ERR_CUDA;  // the gather launch
+}
+
+extern "C" int cfd2d_static_reset(void) {
+    using namespace cfd2d;
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (void*& p : g_scratch_dev) p = nullptr;
+    return CFD2D_OK;
 }

@@ -271,15 +271,26 @@ int cfd2d_set_device(int device);
  * address (make it before any stream capture). All calls share the array:
  * calls that overlap on the GPU race, so order them on one stream. Returns
  * CFD2D_ERR_CAPACITY when n_edges > CFD2D_STATIC_MAX_EDGES or n_bnd > 16,
- * CFD2D_ERR_INVALID_ARG for a null pointer, a non-positive size or an unknown
- * flux, CFD2D_ERR_CUDA when the array lookup or a launch fails; it leaves the
- * cfd2d_last_error message untouched (setting it could allocate). An index
- * outside the mesh gives NaN in R, never an out-of-bounds access. */
+ * CFD2D_ERR_INVALID_ARG for a null pointer, a non-positive size, an unknown
+ * flux or a bnd_kind outside 1..4 (1 INLET, 2 OUTLET, 3 WALL_SLIP,
+ * 4 WALL_NO_SLIP), CFD2D_ERR_CUDA when the array lookup or a launch fails, or,
+ * before anything runs, when a CUDA error of earlier work is pending on the
+ * thread (it is left pending for its owner); it leaves the cfd2d_last_error
+ * message untouched (setting it could allocate). n_bnd may be 0 when no edge
+ * is a boundary edge. An index outside the mesh, or a boundary edge whose
+ * edge_bnd is not in 0..n_bnd-1, gives NaN in R, never an out-of-bounds
+ * access. The device address of the array is cached per device; after
+ * cudaDeviceReset call cfd2d_static_reset before the next call on that
+ * device. */
 #define CFD2D_STATIC_MAX_EDGES 262144
 int cfd2d_residual_first_order_static(int n_cells, int n_edges, const int* cell_edges, const int* edge_c12,
                                       const double* edge_n, const double* edge_l, const int* edge_bnd, int n_bnd,
                                       const int* bnd_kind, const double* bnd_par, double M, double Cp, int flux,
                                       const double* U, double* R, void* stream);
+/* Forget the device addresses cfd2d_residual_first_order_static cached (needed after
+ * a cudaDeviceReset, which ends the context they belong to). No counterpart in the
+ * reference. */
+int cfd2d_static_reset(void);
 
 /* Message of the last failed call on this thread. */
 int cfd2d_last_error(char* buf, size_t n);

@@ -272,7 +272,7 @@ def run_reference_implicit(task_xml: str, tri_files: dict, U0=None, timeout=300,
     """Run the reference's own FVM_TVD_IMPLICIT (oracle/_ref/ref_fvm_tvd_implicit) on one case;
     tri_files: extension -> text of mesh.node/.ele/.neigh/.poly."""
     if not os.path.exists(REF_IMP_BIN):
-        raise FileNotFoundError(REF_IMP_BIN + " (build with: make -C oracle reference)")
+        raise FileNotFoundError(REF_IMP_BIN + " (build with: make -C oracle reference REF=<reference checkout>)")
     with tempfile.TemporaryDirectory(dir=workdir) as d:
         open(os.path.join(d, "task.xml"), "w").write(task_xml)
         for ext, text in tri_files.items():
@@ -363,7 +363,7 @@ def read_ref_state(path) -> dict:
 def run_reference(task_xml: str, unv_text: str, U0=None, timeout=120, workdir=None) -> dict:
     """Run the reference's own FVM_TVD (oracle/_ref/ref_fvm_tvd) on one case."""
     if not os.path.exists(REF_BIN):
-        raise FileNotFoundError(REF_BIN + " (build with: make -C oracle reference)")
+        raise FileNotFoundError(REF_BIN + " (build with: make -C oracle reference REF=<reference checkout>)")
     with tempfile.TemporaryDirectory(dir=workdir) as d:
         open(os.path.join(d, "task.xml"), "w").write(task_xml)
         open(os.path.join(d, "mesh.unv"), "w").write(unv_text)
@@ -493,7 +493,7 @@ def run_reference_rkdg(task_xml: str, proc_text: str, steps: int, U0=None, tau=N
     on one case: mesh/mesh.0000.proc = proc_text; U0: (nc, 12) coefficients or None; tau: a
     time step to impose after init. Returns the dumps, stdout and the VTU/PVTU files."""
     if not os.path.exists(REF_DG_BIN):
-        raise FileNotFoundError(REF_DG_BIN + " (build with: make -C oracle reference)")
+        raise FileNotFoundError(REF_DG_BIN + " (build with: make -C oracle reference REF=<reference checkout>)")
     with tempfile.TemporaryDirectory(dir=workdir) as d:
         os.makedirs(os.path.join(d, "mesh"))
         open(os.path.join(d, "task.xml"), "w").write(task_xml)

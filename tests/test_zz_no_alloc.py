@@ -67,6 +67,54 @@ def test_static_residual_matches_handle_residual_twice(capi, tmp_path, flux):
             assert np.array_equal(R.view(np.int64), R_ref.view(np.int64))
 
 
+def test_static_residual_without_boundary_conditions(capi, tmp_path):
+    """n_bnd == 0 is a valid call: every cell whose three edges are interior gets the
+    handle's residual bit for bit; cells on a boundary edge (which would need a
+    boundary condition) get NaN, and nothing reads outside the arrays."""
+    import torch
+    t, m, U0 = cases.vortex(20, flux="HLLC", recon="NONE", scheme="EULER", bnd_kinds=KINDS, seed=22)
+    s = capi.Solver(cases.write_task(t, m, str(tmp_path)), mesh=m)
+    mesh = capi.Mesh(nodes=m.nodes, tris=m.tris, bsegs=m.bsegs, bseg_bnd=m.bseg_bnd).export()
+    cuda = torch.device("cuda:0")
+    ce = mesh["cell_edges"].reshape(-1, 3)
+    c12 = mesh["edge_c12"].reshape(-1, 2)
+    interior = np.all(c12[ce][:, :, 1] >= 0, axis=1)
+    assert interior.sum() > 0 and (~interior).sum() > 0
+    dev = {k: torch.from_numpy(np.ascontiguousarray(mesh[v]).ravel()).to(cuda)
+           for k, v in (("cell_edges", "cell_edges"), ("c12", "edge_c12"), ("n", "edge_n"), ("l", "edge_l"),
+                        ("bnd", "edge_bnd"))}
+    s.set_state(U0)
+    R_ref = s.residual()
+    U_dev = torch.from_numpy(np.ascontiguousarray(U0)).to(cuda)
+    R_dev = torch.zeros((4, m.n_cells), dtype=torch.float64, device=cuda)
+    p = lambda x: C.c_void_p(x.data_ptr())
+    rc = capi.lib().cfd2d_residual_first_order_static(
+        m.n_cells, len(mesh["edge_l"]), p(dev["cell_edges"]), p(dev["c12"]), p(dev["n"]), p(dev["l"]),
+        p(dev["bnd"]), 0, None, None, t.materials[0][1], t.materials[0][2], 3, p(U_dev), p(R_dev),
+        C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert rc == capi.OK
+    R = R_dev.cpu().numpy()
+    assert np.array_equal(R[:, interior].view(np.int64), R_ref[:, interior].view(np.int64))
+    assert np.all(np.isnan(R[:, ~interior]))
+
+
+def test_static_residual_rejects_unknown_boundary_kind(capi):
+    import torch
+    cuda = torch.device("cuda:0")
+    buf = torch.zeros(16, dtype=torch.float64, device=cuda)
+    ibuf = torch.zeros(16, dtype=torch.int32, device=cuda)
+    p = lambda x: C.c_void_p(x.data_ptr())
+    par = np.zeros(8)
+    for bad in (0, 5, -1):
+        kinds = np.array([2, bad], np.int32)
+        rc = capi.lib().cfd2d_residual_first_order_static(
+            4, 4, p(ibuf), p(ibuf), p(buf), p(buf), p(ibuf), 2,
+            kinds.ctypes.data_as(C.POINTER(C.c_int)), par.ctypes.data_as(C.POINTER(C.c_double)),
+            8.314472, 3.5, 3, p(buf), p(buf), None)
+        assert rc == 6  # CFD2D_ERR_INVALID_ARG, before anything is launched
+
+
 def test_static_residual_rejects_oversized_mesh(capi):
     import torch
     cuda = torch.device("cuda:0")
