@@ -297,13 +297,35 @@ def cpu_baseline_single(seconds: float = 12.0):
             "sample": f"{k} SSP-RK3 step(s) of the full 2,097,152-triangle workload on one core"}
 
 
-def adjoint_measure(capi, cases, d):
+def fd_check(s, U0, g, ndir, steps=200, every=20, eps=1e-6, seed=4):
+    """The FP64 gradient against central finite differences of the FP64 forward (eps 1e-6)
+    in ndir seeded unit directions of the 4 N-dimensional initial state; the error of a
+    direction is |g.d - fd| / max(|fd|, 1e-3 |g|) (|g| / sqrt(4 N) is the typical size of a
+    directional derivative, so the floor keeps near-zero directions from dividing by noise)."""
+    rng = np.random.default_rng(seed)
+    gn = float(np.linalg.norm(g))
+    errs = []
+    for _ in range(ndir):
+        dvec = rng.standard_normal(U0.shape)
+        dvec /= np.linalg.norm(dvec)
+        s.set_state(U0 + eps * dvec)
+        jp = s.forward(steps, every)
+        s.set_state(U0 - eps * dvec)
+        jm = s.forward(steps, every)
+        fd = (jp - jm) / (2 * eps)
+        errs.append(abs(float(np.sum(g * dvec)) - fd) / max(abs(fd), 1e-3 * gn))
+    return {"directions": ndir, "eps": eps, "seed": seed, "max_rel_err": max(errs),
+            "median_rel_err": float(np.median(errs)), "rel_err": [float("%.3g" % e) for e in errs]}
+
+
+def adjoint_measure(capi, cases, d, fd_dirs=64):
     """Differentiation workload: 256x256x2 = 131,072-triangle vortex, HLLC + minmod +
     SSP-RK3, 200 steps, J = sum over the box [6,8]x[4,6] of S (p-1)^2, checkpoint
     every 20 steps. For the FP64 form and for the mixed form (FP32 faces in the
     forward and in the adjoint's face work), times a plain 200-step forward, the
     checkpointed forward and the backward sweep (wall clock; each call ends
-    synchronised); the mixed gradient is compared with the FP64 one."""
+    synchronised); the mixed gradient is compared with the FP64 one, the FP64 gradient
+    with central finite differences in fd_dirs seeded directions."""
     t, m, U0, w, _ = cases.vortex_adjoint(256, steps=200)
     out, grads = {}, {}
     for form in ("fp64", "mixed"):
@@ -322,11 +344,13 @@ def adjoint_measure(capi, cases, d):
         b = time.perf_counter()
         g, gb = s.backward()
         c = time.perf_counter()
-        s.close()
         grads[form] = g
         out[form] = {"J": J, "grad_norm": float(np.linalg.norm(g)), "forward_ms": fw * 1e3,
                      "forward_checkpointed_ms": (b - a) * 1e3, "backward_ms": (c - b) * 1e3,
                      "ratio_backward_over_forward": (c - b) / fw, "ratio_gradient_over_forward": (c - a) / fw}
+        if form == "fp64" and fd_dirs > 0:
+            out[form]["fd_check"] = fd_check(s, U0, g, fd_dirs)
+        s.close()
     t.precision = None
     out["mixed"]["grad_rel_diff_vs_fp64"] = float(np.linalg.norm(grads["mixed"] - grads["fp64"]) /
                                                   np.linalg.norm(grads["fp64"]))
@@ -337,22 +361,30 @@ def adjoint_measure(capi, cases, d):
     return res
 
 
-def combined_workload(args, capi, cases, world, rank, dist, W, K, n_side=4096, steps=300, every=30):
+COMBINED_N = 4096
+ADJOINT_MEMORY = 180e9  # bytes (180 GB, decimal): the combined configuration's device-memory budget
+
+
+def combined_measure(capi, cases, W, n_side=COMBINED_N, steps=300, every=30, err_steps=30):
     """Scale + mixed precision + adjoint: 4096x4096x2 = 33,554,432 triangles, four-quadrant
-    Riemann problem (seed 5, +-0.05h), HLLC + minmod + SSP-RK3, CFL 0.4, 300 steps with FP32
-    faces / FP64 accumulation, discrete adjoint (FP32 face work, FP64 per-cell sums) of J = sum
-    over cells with centroid in
-    [1/4, 3/4]^2 of S rho^2, checkpoint every 30 steps. The error is measured against the FP64
-    solver run on the same mesh and steps (the FP64 path equals the CPU oracle bit for bit)."""
+    Riemann problem (seed 5, +-0.05h), HLLC + minmod + SSP-RK3, CFL 0.4. The mixed form
+    (FP32 faces / FP64 accumulation) runs `steps` steps timed on the device, then the
+    checkpointed forward (every `every` steps) and the discrete adjoint (FP32 face work,
+    FP64 per-cell sums) of J = sum over cells with centroid in [1/4, 3/4]^2 of S rho^2, with
+    the handle's device memory capped at ADJOINT_MEMORY (the store keeps what fits the
+    budget). The error is measured after `err_steps` steps against the FP64 solver on the
+    same mesh (the FP64 path equals the CPU oracle bit for bit)."""
     d = tempfile.mkdtemp(prefix="cfd2d_comb_")
     a0 = time.perf_counter()
     t, m, _ = cases.four_quadrant(n_side, seed=5, steps=steps, precision="MIXED")
+    t.adjoint_memory = ADJOINT_MEMORY
     xy = m.centroids()
     p = m.nodes[m.tris]
     S = 0.5 * np.abs((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) -
                      (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
     del p
     w = np.where((xy[:, 0] >= 0.25) & (xy[:, 0] <= 0.75) & (xy[:, 1] >= 0.25) & (xy[:, 1] <= 0.75), S, 0.0)
+    del xy, S
     s = capi.Solver(cases.write_task(t, m, d), mesh=m)
     nc = s.n
     s.set_objective(1, w, 0.0)
@@ -368,38 +400,52 @@ def combined_workload(args, capi, cases, world, rank, dist, W, K, n_side=4096, s
     g, _ = s.backward()
     c = time.perf_counter()
     dev_bytes = s.get_info().device_bytes
+    s.set_state(U0)
+    s.step(err_steps)
     Umx = s.state()
     s.close()
     t.precision = None
+    t.adjoint_memory = None
     r = capi.Solver(cases.write_task(t, m, d), mesh=m)
-    ms64 = r.timed_steps(steps)
+    ms64 = r.timed_steps(err_steps)
     U64 = r.state()
     r.close()
     l1 = lambda x, y: float(np.sum(np.abs(x - y)) / np.sum(np.abs(y)))
     linf = lambda x, y: float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
     hbm, peak_kind = measured_peaks()
     rate = nc * steps / (ms_fw * 1e-3)
+    return {
+        "workload": f"four-quadrant Riemann problem, {n_side}x{n_side}x2 = {nc:,} triangles (seed 5, +-0.05h), "
+                    f"HLLC + minmod + SSP-RK3, CFL 0.4, {steps} steps; J = sum_{{[1/4,3/4]^2}} S rho^2, "
+                    f"checkpoint every {every}",
+        "cells": nc, "steps": steps, "checkpoint_every": every,
+        "value": rate, "unit": UNIT, "ms_per_step": ms_fw / steps, "dtype": "f32 faces / f64 accumulate",
+        "roofline_step": {"achieved": rate * STEP_BYTES["mixed"] / 1e9,
+                          "frac": rate * STEP_BYTES["mixed"] / 1e9 / hbm, "peak": hbm, "peak_kind": peak_kind,
+                          "bytes_per_cell_update": STEP_BYTES["mixed"]},
+        "fp64": {"value": nc * err_steps / (ms64 * 1e-3), "ms_per_step": ms64 / err_steps},
+        "error_vs_fp64": {"steps": err_steps, "l1_rho": l1(Umx[0], U64[0]), "l1_rhoE": l1(Umx[3], U64[3]),
+                          "linf_rho": linf(Umx[0], U64[0]), "linf_rhoE": linf(Umx[3], U64[3])},
+        "adjoint": {"J": J, "grad_norm": float(np.linalg.norm(g)), "finite": bool(np.all(np.isfinite(g))),
+                    "forward_checkpointed_ms": (b - a) * 1e3, "backward_ms": (c - b) * 1e3,
+                    "ratio_backward_over_mixed_forward": (c - b) * 1e3 / ms_fw,
+                    "ratio_gradient_over_mixed_forward": (c - a) * 1e3 / ms_fw},
+        "device_bytes_with_adjoint": dev_bytes, "device_budget_bytes": ADJOINT_MEMORY,
+        "within_budget": bool(dev_bytes <= ADJOINT_MEMORY), "setup_s": setup_s}
+
+
+def combined_workload(args, capi, cases, world, rank, dist, W, K):
+    """The combined configuration on its own line, the FP64 comparison at its full 300 steps."""
+    res = combined_measure(capi, cases, W, err_steps=300)
     if rank == 0:
-        print(json.dumps({
-            "metric": "cell-updates/s, 33.5M triangles, mixed forward + mixed discrete adjoint",
-            "value": rate, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": W,
-            "ms_per_step": ms_fw / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 faces / f64 accumulate", "data": "synthetic",
-            "config": {"workload": "four-quadrant Riemann problem, 4096x4096x2 = 33,554,432 triangles (seed 5, "
-                                   "+-0.05h), HLLC + minmod + SSP-RK3, CFL 0.4, 300 steps; J = sum_{[1/4,3/4]^2} "
-                                   "S rho^2, checkpoint every 30", "cells": nc,
-                       "l2": "no flush: working set far above the 129 MB L2"},
-            "roofline_step": {"achieved": rate * STEP_BYTES["mixed"] / 1e9,
-                              "frac": rate * STEP_BYTES["mixed"] / 1e9 / hbm, "peak": hbm, "peak_kind": peak_kind,
-                              "bytes_per_cell_update": STEP_BYTES["mixed"]},
-            "fp64": {"value": nc * steps / (ms64 * 1e-3), "ms_per_step": ms64 / steps},
-            "error_vs_fp64": {"l1_rho": l1(Umx[0], U64[0]), "l1_rhoE": l1(Umx[3], U64[3]),
-                              "linf_rho": linf(Umx[0], U64[0]), "linf_rhoE": linf(Umx[3], U64[3])},
-            "adjoint": {"J": J, "grad_norm": float(np.linalg.norm(g)), "finite": bool(np.all(np.isfinite(g))),
-                        "forward_checkpointed_ms": (b - a) * 1e3, "backward_ms": (c - b) * 1e3,
-                        "ratio_backward_over_mixed_forward": (c - b) * 1e3 / ms_fw,
-                        "ratio_backward_over_fp64_forward": (c - b) * 1e3 / ms64},
-            "device_bytes_with_adjoint": dev_bytes, "setup_s": setup_s}), flush=True)
+        line = {"metric": "cell-updates/s, 33.5M triangles, mixed forward + mixed discrete adjoint",
+                "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": res["steps"], "warmup": W,
+                "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": res["dtype"], "data": "synthetic",
+                "config": {"workload": res["workload"], "cells": res["cells"],
+                           "l2": "no flush: working set far above the 129 MB L2"}}
+        line.update({k: v for k, v in res.items() if k not in line and k not in ("workload", "cells")})
+        print(json.dumps(line), flush=True)
 
 
 def batched_workload(args, capi, cases, world, rank, dist, W, K):
@@ -660,6 +706,7 @@ def main():
     ap.add_argument("--forms", default="fp64,mixed", help="comma list of fp64, mixed (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--no-combined", action="store_true", help="leave out the 33.5M-triangle combined key")
     ap.add_argument("--n", type=int, default=N_SIDE, help="squares per side (profiling runs only)")
     ap.add_argument("--workload", default="four_quadrant",
                     choices=["four_quadrant", "batched", "combined", "adjoint", "implicit", "rkdg"],
@@ -804,6 +851,9 @@ def main():
     e2e_s = reduce_max(dist, (time.perf_counter() - a) / Ke)
 
     adj = adjoint_measure(capi, cases, d)
+    s64.close()
+    smx.close()
+    comb = combined_measure(capi, cases, W) if not args.no_combined else None
 
     hbm, peak_kind = measured_peaks()
     traffic = ncu_traffic()
@@ -866,12 +916,12 @@ def main():
         "gpu_launches": K * (3 * 3 + 1),
         "clocks": clocks,
     }
+    if comb is not None:
+        line["combined"] = comb
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_single()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    s64.close()
-    smx.close()
     if dist is not None:
         dist.destroy_process_group()
 

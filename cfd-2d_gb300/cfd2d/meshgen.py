@@ -264,6 +264,7 @@ class Task:
     reorder: str | None = None        # NONE / RCM / HILBERT
     fused_stage: str | None = None    # "1" runs the mixed form's stages as one tiled kernel
     adjoint_store: str | None = None  # NONE / PRIMITIVES / ALL: what the adjoint keeps per recorded stage
+    adjoint_memory: float | None = None  # device-memory budget of the handle for the adjoint, bytes
     flux_pipeline: str | None = None  # mixed form: ON (default) / OFF, the software-pipelined flux kernel
     method: str = "FVM_TVD"
 
@@ -283,6 +284,7 @@ def write_task_xml(t: Task) -> str:
     for tag, val in (("FLUX", t.flux), ("RECONSTRUCTION", t.reconstruction),
                      ("TIME_SCHEME", t.time_scheme), ("PRECISION", t.precision), ("REORDER", t.reorder),
                      ("FUSED_STAGE", t.fused_stage), ("ADJOINT_STORE", t.adjoint_store),
+                     ("ADJOINT_MEMORY", None if t.adjoint_memory is None else _v(t.adjoint_memory)),
                      ("FLUX_PIPELINE", t.flux_pipeline)):
         if val is not None:
             L.append(f'    <{tag} value="{val}" />')

@@ -96,7 +96,9 @@ double Solver::forward(int nsteps, int k, int* status) {
     // only the stage's primitives W and gradients G (face precision), so the first
     // choice is W and G, then W alone (G re-derived per stage); the FP64 stage states
     // (from which both are re-derived) only when W does not fit either. "Fits": within
-    // 80% of the free device memory beyond what is allocated already.
+    // 80% of the free device memory beyond what is allocated already and, with an
+    // ADJOINT_MEMORY budget, with the handle's device bytes (solver, adjoint arrays,
+    // checkpoints and this store) at most the budget.
     store_wg_ = false;
     store_g_ = false;
     {
@@ -108,7 +110,14 @@ double Solver::forward(int nsteps, int k, int* status) {
         size_t free_b = 0, total_b = 0;
         CUDA_CHECK(cudaMemGetInfo(&free_b, &total_b));
         const size_t have = wg_slots_ * dbl + seg_slots_ * 4 * nc * dbl;  // reusable if released
-        auto fits = [&](size_t doubles) { return doubles <= wg_slots_ || doubles * dbl <= (free_b + have) / 10 * 8; };
+        const size_t base = bytes_ - std::min(bytes_, have);             // everything but the store
+        const double budget = task_.adj_memory;
+        auto in_budget = [&](size_t bytes) { return budget <= 0.0 || (double)(base + bytes) <= budget; };
+        auto fits = [&](size_t doubles) {
+            return (doubles <= wg_slots_ || doubles * dbl <= (free_b + have) / 10 * 8) && in_budget(doubles * dbl);
+        };
+        if (!in_budget(std::min(need_w, need_x) * dbl))
+            throw Error(CFD2D_ERR_CAPACITY, "the adjoint's smallest segment store exceeds ADJOINT_MEMORY");
         const int mode = task_.adj_store;
         if (mode == 2 || (mode < 0 && fits(need))) {
             store_wg_ = store_g_ = true;

@@ -289,6 +289,8 @@ TaskConfig parse_task(const std::string& path) {
     t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}, {"HILBERT", 2}}, -1);
     t.fused = pick(ctl, "FUSED_STAGE", {{"0", 0}, {"1", 1}, {"OFF", 0}, {"ON", 1}}, -1);
     t.adj_store = pick(ctl, "ADJOINT_STORE", {{"AUTO", -1}, {"NONE", 0}, {"PRIMITIVES", 1}, {"ALL", 2}}, -1);
+    if (const XmlNode* n = ctl->child("ADJOINT_MEMORY")) t.adj_memory = attr_d(n, "value");
+    if (!(t.adj_memory >= 0.0)) throw Error(CFD2D_ERR_TASK, "ERROR: ADJOINT_MEMORY must be a byte count >= 0.");
     t.flux_pipe = pick(ctl, "FLUX_PIPELINE", {{"0", 0}, {"1", 1}, {"OFF", 0}, {"ON", 1}}, 1);
     if (const XmlNode* n = ctl->child("NEWTON_CAP")) t.newton_cap = attr_i(n, "value");
     if (t.newton_cap < 1) t.newton_cap = 1;

@@ -126,7 +126,10 @@ def test_adjoint_of_mixed_forward_tracks_fp64(capi, tmp_path):
 
 def test_full_size_adjoint_64_directions(capi, tmp_path):
     """131,072 triangles (256 x 256 x 2), HLLC + minmod + SSP-RK3, 200 steps,
-    checkpoint every 20: 64 seeded directions against central FD."""
+    checkpoint every 20: every one of 64 seeded directions within 1e-5 of central FD at
+    eps = 1e-6. A direction's error is |g.d - fd| / max(|fd|, 1e-3 |g|); |g| / sqrt(4 N)
+    is the typical directional derivative, so the floor only keeps near-zero directions
+    from dividing by FD round-off. The errors of all directions are printed."""
     t, m, U0, w, _ = cases.vortex_adjoint(256, steps=200)
     s = _solver(capi, tmp_path, t, m, w)
     s.set_state(U0)
@@ -139,8 +142,63 @@ def test_full_size_adjoint_64_directions(capi, tmp_path):
         fd = (_J(s, U0 + 1e-6 * d, 200, 20) - _J(s, U0 - 1e-6 * d, 200, 20)) / 2e-6
         errs.append(abs(float(np.sum(g * d)) - fd) / max(abs(fd), 1e-3 * np.linalg.norm(g)))
     errs = np.array(errs)
-    # a direction may straddle a minmod or wave-pattern switch; none may exceed 10x the bar
-    assert np.median(errs) <= TOL and errs.max() <= 10 * TOL, errs
+    print("per-direction relative FD error:", " ".join("%.2e" % e for e in errs))
+    print("max %.3e median %.3e" % (errs.max(), np.median(errs)))
+    assert errs.max() <= TOL, errs
+
+
+def test_combined_mixed_adjoint_within_memory_budget(capi, tmp_path):
+    """The combined configuration's path at reduced size: four-quadrant Riemann problem,
+    FP32 faces / FP64 accumulation, HLLC + minmod + SSP-RK3, J = sum over the central
+    quarter of S rho^2, checkpointed forward and mixed adjoint with an ADJOINT_MEMORY
+    budget that the full store (primitives and gradients) would exceed. The handle stays
+    within the budget, its gradient equals the unconstrained run's bit for bit (the store
+    modes re-derive what they do not keep), and it tracks the FP64 gradient, which in turn
+    agrees with central FD."""
+    t, m, _ = cases.four_quadrant(48, seed=5, steps=12)
+    U0 = None  # the task's own initial state (four regions), read from the first handle
+    xy = m.centroids()
+    p = m.nodes[m.tris]
+    S = 0.5 * np.abs((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) -
+                     (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
+    w = np.where((xy[:, 0] >= 0.25) & (xy[:, 0] <= 0.75) & (xy[:, 1] >= 0.25) & (xy[:, 1] <= 0.75), S, 0.0)
+    t.precision = "MIXED"
+    runs = {}
+    for name, budget in (("free", None), ("budget", "probe")):
+        d = tmp_path / name
+        d.mkdir()
+        if budget == "probe":  # the unconstrained handle's bytes less half of its full store
+            nst, k, nc = 3, 4, m.n_cells
+            full_store = k * nst * 12 * nc * 4
+            t.adjoint_memory = float(runs["free"][2] - full_store // 2)
+        s = capi.Solver(cases.write_task(t, m, str(d)), mesh=m)
+        s.set_objective(1, w, 0.0)
+        if U0 is None:
+            U0 = s.state()
+        s.set_state(U0)
+        J = s.forward(12, 4)
+        g, _ = s.backward()
+        runs[name] = (J, g, s.get_info().device_bytes)
+        s.close()
+    assert runs["budget"][2] <= t.adjoint_memory < runs["free"][2]
+    assert runs["budget"][0] == runs["free"][0] and np.array_equal(runs["budget"][1], runs["free"][1])
+    t.precision = None
+    t.adjoint_memory = None
+    d = tmp_path / "fp64"
+    d.mkdir()
+    s = capi.Solver(cases.write_task(t, m, str(d)), mesh=m)
+    s.set_objective(1, w, 0.0)
+    s.set_state(U0)
+    s.forward(12, 4)
+    g64, _ = s.backward()
+    gmx = runs["free"][1]
+    assert np.all(np.isfinite(gmx))
+    assert np.linalg.norm(gmx - g64) <= 1e-3 * np.linalg.norm(g64)
+    rng = np.random.default_rng(5)
+    for _ in range(3):
+        dv = rng.standard_normal(U0.shape); dv /= np.linalg.norm(dv)
+        fd = (_J(s, U0 + 1e-6 * dv, 12, 4) - _J(s, U0 - 1e-6 * dv, 12, 4)) / 2e-6
+        assert abs(float(np.sum(g64 * dv)) - fd) <= TOL * max(abs(fd), 1e-3 * np.linalg.norm(g64))
 
 
 @pytest.mark.parametrize("precision", [None, "MIXED"])
