@@ -194,12 +194,12 @@ __device__ __forceinline__ void vjp_lax(const Prim<T>& L, const Prim<T>& R, T nx
     Lb.u += unlb * nx; Lb.v += unlb * ny; Rb.u += unrb * nx; Rb.v += unrb * ny;
 }
 
-// Ss = num / den with the reciprocal iden = 1/den also returned: FP64 through the
-// correctly rounded reciprocal form (the forward's quotient bit for bit), FP32 as
-// the forward divides.
+// Ss = num / den as the forward forms it (hllc_quot: the forward's quotient bit for bit),
+// with an approximation of 1/den for the derivatives (the Newton reciprocal hllc_quot
+// starts from; FP32: a division)
 __device__ __forceinline__ double star_speed(double num, double den, double& iden) {
-    iden = 1.0 / den;
-    return div_rn(num, den, iden);
+    iden = hllc_in_range(den) ? hllc_rcp1(den) : 1.0 / den;
+    return hllc_quot(num, den);
 }
 __device__ __forceinline__ float star_speed(float num, float den, float& iden) {
     iden = 1.0f / den;
@@ -210,8 +210,7 @@ __device__ __forceinline__ float star_speed(float num, float den, float& iden) {
 template <typename T>
 __device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
                                          Prim<T>& Lb, Prim<T>& Rb) {
-    const T aL = GAM * L.p / L.r, aR = GAM * R.p / R.r;
-    const T cL = t_sqrt(aL), cR = t_sqrt(aR);
+    const T cL = hllc_sound(GAM * L.p, L.r), cR = hllc_sound(GAM * R.p, R.r);  // the forward's values
     const T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     const T EL = energy(L.r, L.u, L.v, L.p, IG1);
     const T ER = energy(R.r, R.u, R.v, R.p, IG1);
@@ -234,7 +233,7 @@ __device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T n
         T FK[4];
         phys_flux(FK, K.r, K.u, K.v, K.p, EK, unK, nx, ny);
         const T ps = t_fma(mK, Ss - unK, K.p);
-        const T inv = T(1.0) / (SK - Ss);
+        const T inv = hllc_recip(SK - Ss);
         const T sp = SK * ps;
         // A_k and h_k only feed the derivatives: fused freely
         const T A0 = madd(-FK[0], SK, K.r), A1 = madd(-FK[1], SK, K.r * K.u), A2 = madd(-FK[2], SK, K.r * K.v),
@@ -297,9 +296,15 @@ __device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T n
     // un = u nx + v ny
     Lb.u = madd(Lb.u, unLb, nx); Lb.v = madd(Lb.v, unLb, ny);
     Rb.u = madd(Rb.u, unRb, nx); Rb.v = madd(Rb.v, unRb, ny);
-    // c = sqrt(GAM p / r): dc = (GAM dp - a dr) / (2 c r)
-    if (cLb != T(0.0)) { const T ab = T(0.5) * cLb / (cL * L.r); Lb.p = madd(Lb.p, ab, GAM); Lb.r = madd(Lb.r, -ab, aL); }
-    if (cRb != T(0.0)) { const T ab = T(0.5) * cRb / (cR * R.r); Rb.p = madd(Rb.p, ab, GAM); Rb.r = madd(Rb.r, -ab, aR); }
+    // c = sqrt(GAM p / r) = sqrt(a): dc = (GAM dp - a dr) / (2 c r), a = c^2
+    if (cLb != T(0.0)) {
+        const T ab = hllc_quot(T(0.5) * cLb, cL * L.r);
+        Lb.p = madd(Lb.p, ab, GAM); Lb.r = madd(Lb.r, -ab, cL * cL);
+    }
+    if (cRb != T(0.0)) {
+        const T ab = hllc_quot(T(0.5) * cRb, cR * R.r);
+        Rb.p = madd(Rb.p, ab, GAM); Rb.r = madd(Rb.r, -ab, cR * cR);
+    }
 }
 
 template <int FLUX, typename T>

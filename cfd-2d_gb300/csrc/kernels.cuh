@@ -175,6 +175,34 @@ __device__ __forceinline__ float neg_if(float x, bool s) { return __int_as_float
 __device__ __forceinline__ double div_by(double a, double b, double y) { return div_rn(a, b, y); }
 __device__ __forceinline__ float div_by(float a, float, float y) { return a * y; }
 
+// FP32 <-> FP64 conversions on the integer pipe. GB300's FP64 unit issues ~2
+// instructions per clock and SM, and the hardware conversions run there; these
+// bit-level versions keep the mixed form's update kernel off that unit.
+// Widening is exact for zero, normal, infinite and NaN floats (the mixed kernels
+// run with FTZ, so no subnormal float reaches it; one would read as zero).
+__device__ __forceinline__ double widen(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned ex = (b >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
+    if (ex == 0) return __longlong_as_double((long long)sgn);
+    const unsigned long long e64 = ex == 0xffu ? 0x7ffull : (unsigned long long)(ex + (1023 - 127));
+    return __longlong_as_double((long long)(sgn | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// Narrowing rounds to nearest (ties away from zero), flushes below FLT_MIN to
+// zero, saturates to infinity and keeps NaN a NaN.
+__device__ __forceinline__ float narrow(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ffull);
+    if (e == 0x7ff) return __uint_as_float(sgn | ((b & 0xfffffffffffffull) ? 0x7fc00000u : 0x7f800000u));
+    const int ef = e - 1023 + 127;
+    if (ef <= 0) return __uint_as_float(sgn);
+    if (ef >= 0xff) return __uint_as_float(sgn | 0x7f800000u);
+    const unsigned m = (unsigned)(b >> 29) & 0x7fffffu;
+    const unsigned rnd = (unsigned)(b >> 28) & 1u;
+    return __uint_as_float((sgn | ((unsigned)ef << 23) | m) + rnd);  // a carry moves into the exponent
+}
+
 // convertConsToPar + Material::URS(0), src/methods/fvm_tvd.cpp:803-813, src/global.cpp:15-18
 template <typename T>
 __device__ __forceinline__ Prim<T> cons2prim(T ro, T ru, T rv, T re, T gm1) {
@@ -443,13 +471,76 @@ template <typename T> __device__ __forceinline__ T energy(T r, T u, T v, T p, T 
     return t_fma(p, IG1, (T(0.5) * r) * t_fma(u, u, v * v));
 }
 
+// Newton-refined quotient, reciprocal and sound speed of the FP64 HLLC flux. HLLC has no
+// counterpart in the reference, so its arithmetic is this project's definition and the
+// oracle performs the very same operations (same bits): a binary32 seed, then FP64 Newton
+// steps with fused multiply-adds (Newton-Raphson for 1/b and for sqrt(a/r), the final
+// quotient corrected as in Markstein, "IA-64 and Elementary Functions", 2000). The seed
+// is x truncated to binary32 (sign, rebiased exponent, top 23 fraction bits: integer
+// operations) and the binary32 operations are correctly rounded (IEEE), so every step is
+// defined bit for bit. Within |x| in [2^-60, 2^60) every binary32 value stays normal and
+// every result is within about one ulp of the exact one; other operands take the IEEE
+// expression. Each costs 4-6 FP64 instructions where a division or square root costs ~9.
+__device__ __forceinline__ bool hllc_in_range(double x) {  // 2^-60 <= |x| < 2^60
+    const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+    return e >= 1023 - 60 && e < 1023 + 60;
+}
+__device__ __forceinline__ float hllc_seed(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    const unsigned ex = (unsigned)((b >> 52) & 0x7ff) - (1023u - 127u);
+    return __uint_as_float(sgn | (ex << 23) | ((unsigned)(b >> 29) & 0x7fffffu));
+}
+// 1/b to ~2^-46 (one Newton step from the binary32 reciprocal of the seed)
+__device__ __forceinline__ double hllc_rcp1(double b) {
+    const double y0 = widen(__frcp_rn(hllc_seed(b)));
+    return fma(y0, fma(-b, y0, 1.0), y0);
+}
+// a / b: one Newton step for 1/b, then q = a y corrected once (|a|, |b| in range; a = 0
+// gives the IEEE signed zero)
+__device__ __forceinline__ double hllc_quot(double a, double b) {
+    if (hllc_in_range(b)) {
+        if (hllc_in_range(a)) {
+            const double y = hllc_rcp1(b);
+            const double q = a * y;
+            return fma(fma(-q, b, a), y, q);
+        }
+        const long long ia = __double_as_longlong(a);
+        if ((ia & 0x7fffffffffffffffll) == 0)
+            return __longlong_as_double((ia ^ __double_as_longlong(b)) & (long long)0x8000000000000000ull);
+    }
+    return a / b;
+}
+__device__ __forceinline__ float hllc_quot(float a, float b) { return a / b; }
+// 1/b: two Newton steps
+__device__ __forceinline__ double hllc_recip(double b) {
+    if (!hllc_in_range(b)) return 1.0 / b;
+    const double y = hllc_rcp1(b);
+    return fma(y, fma(-b, y, 1.0), y);
+}
+__device__ __forceinline__ float hllc_recip(float b) { return 1.0f / b; }
+// sqrt(a / r) for a = GAMMA p, r the density (both positive and in range): s0 and
+// h = 1/(2 r s0) from binary32, then two steps s <- s + (a - (r s) s) h
+__device__ __forceinline__ double hllc_sound(double a, double r) {
+    if (!(a > 0.0) || !(r > 0.0) || !hllc_in_range(a) || !hllc_in_range(r)) return sqrt(a / r);
+    const float af = hllc_seed(a), rf = hllc_seed(r);
+    const float sf = __fsqrt_rn(__fdiv_rn(af, rf));
+    const double h = widen(__fdiv_rn(0.5f, __fmul_rn(rf, sf)));
+    double s = widen(sf);
+    s = fma(fma(-(r * s), s, a), h, s);
+    s = fma(fma(-(r * s), s, a), h, s);
+    return s;
+}
+__device__ __forceinline__ float hllc_sound(float a, float r) { return t_sqrt(a / r); }
+
 // HLLC (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, sec. 10.4-10.6),
 // Davis wave speeds S_L = min(unL-cL, unR-cR), S_R = max(unL+cL, unR+cR), star flux
 // F*_K = [S*(S_K U_K - F_K) + S_K p* D*] / (S_K - S*), D* = (0, nx, ny, S*),
 // p* = p_K + rho_K (S_K - un_K)(S* - un_K): one division instead of Toro's star state.
+// FP64: c = hllc_sound(GAMMA p, rho), S* = hllc_quot, 1/(S_K - S*) = hllc_recip.
 template <typename T>
 __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
-    T cL = t_sqrt(GAM * L.p / L.r), cR = t_sqrt(GAM * R.p / R.r);
+    T cL = hllc_sound(GAM * L.p, L.r), cR = hllc_sound(GAM * R.p, R.r);
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     T EL = energy(L.r, L.u, L.v, L.p, IG1);
     T ER = energy(R.r, R.u, R.v, R.p, IG1);
@@ -457,14 +548,14 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
     if (SL >= T(0.0)) { phys_flux(f, L.r, L.u, L.v, L.p, EL, unL, nx, ny); return; }
     if (SR <= T(0.0)) { phys_flux(f, R.r, R.u, R.v, R.p, ER, unR, nx, ny); return; }
     T mL = L.r * (SL - unL), mR = R.r * (SR - unR);
-    T Ss = t_fma(-mR, unR, t_fma(mL, unL, R.p - L.p)) / (mL - mR);
+    T Ss = hllc_quot(t_fma(-mR, unR, t_fma(mL, unL, R.p - L.p)), mL - mR);
     const bool left = Ss >= T(0.0);
     const Prim<T>& K = left ? L : R;
     T SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
     T FK[4];
     phys_flux(FK, K.r, K.u, K.v, K.p, EK, unK, nx, ny);
     T ps = t_fma(mK, Ss - unK, K.p);
-    T inv = T(1.0) / (SK - Ss);
+    T inv = hllc_recip(SK - Ss);
     T sp = SK * ps;
     f[0] = (Ss * t_fma(SK, K.r, -FK[0])) * inv;
     f[1] = t_fma(Ss, t_fma(SK, K.r * K.u, -FK[1]), sp * nx) * inv;
@@ -844,34 +935,6 @@ __global__ void __launch_bounds__(256) k_flux(const DevCase c) {
     } else {
         for (int e = e0; e < c.ne; e += gridDim.x * blockDim.x) flux_one<T, FLUX, RECON>(c, e);  // persistent grid
     }
-}
-
-// FP32 <-> FP64 conversions on the integer pipe. GB300's FP64 unit issues ~2
-// instructions per clock and SM, and the hardware conversions run there; these
-// bit-level versions keep the mixed form's update kernel off that unit.
-// Widening is exact for zero, normal, infinite and NaN floats (the mixed kernels
-// run with FTZ, so no subnormal float reaches it; one would read as zero).
-__device__ __forceinline__ double widen(float x) {
-    const unsigned b = __float_as_uint(x);
-    const unsigned ex = (b >> 23) & 0xffu;
-    const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
-    if (ex == 0) return __longlong_as_double((long long)sgn);
-    const unsigned long long e64 = ex == 0xffu ? 0x7ffull : (unsigned long long)(ex + (1023 - 127));
-    return __longlong_as_double((long long)(sgn | (e64 << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
-}
-// Narrowing rounds to nearest (ties away from zero), flushes below FLT_MIN to
-// zero, saturates to infinity and keeps NaN a NaN.
-__device__ __forceinline__ float narrow(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
-    const int e = (int)((b >> 52) & 0x7ffull);
-    if (e == 0x7ff) return __uint_as_float(sgn | ((b & 0xfffffffffffffull) ? 0x7fc00000u : 0x7f800000u));
-    const int ef = e - 1023 + 127;
-    if (ef <= 0) return __uint_as_float(sgn);
-    if (ef >= 0xff) return __uint_as_float(sgn | 0x7f800000u);
-    const unsigned m = (unsigned)(b >> 29) & 0x7fffffu;
-    const unsigned rnd = (unsigned)(b >> 28) & 1u;
-    return __uint_as_float((sgn | ((unsigned)ef << 23) | m) + rnd);  // a carry moves into the exponent
 }
 
 // Knuth's TwoSum: s + e == a + b exactly (round to nearest, no reassociation).

@@ -10,6 +10,7 @@
 #include "cfd2d_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -466,6 +467,62 @@ static double energy(double r, double u, double v, double p, double IG1) {
     return fma(p, IG1, (0.5 * r) * fma(u, u, v * v));
 }
 
+/* Newton-refined quotient, reciprocal and sound speed of the FP64 HLLC flux: this
+ * project's definition of that flux's arithmetic, the same operations as the GPU
+ * (hllc_quot / hllc_recip / hllc_sound in the library's kernels). A binary32 seed
+ * (x truncated: sign, rebiased exponent, top 23 fraction bits), correctly rounded
+ * binary32 operations, then FP64 Newton steps with fma (Newton-Raphson for 1/b and
+ * sqrt(a/r); the quotient corrected as in Markstein, "IA-64 and Elementary
+ * Functions", 2000). Within |x| in [2^-60, 2^60) every binary32 value is normal;
+ * other operands take the IEEE expression. */
+static int hllc_in_range(double x) {
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    int e = (int)((b >> 52) & 0x7ff);
+    return e >= 1023 - 60 && e < 1023 + 60;
+}
+static float hllc_seed(double x) {
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    uint32_t sgn = (uint32_t)(b >> 32) & 0x80000000u;
+    uint32_t ex = (uint32_t)((b >> 52) & 0x7ff) - (1023u - 127u);
+    uint32_t f = sgn | (ex << 23) | ((uint32_t)(b >> 29) & 0x7fffffu);
+    float r;
+    memcpy(&r, &f, 4);
+    return r;
+}
+static double hllc_rcp1(double b) {
+    double y0 = (double)(1.0f / hllc_seed(b));  /* a correctly rounded binary32 division */
+    return fma(y0, fma(-b, y0, 1.0), y0);
+}
+static double hllc_quot(double a, double b) {
+    if (hllc_in_range(b)) {
+        if (hllc_in_range(a)) {
+            double y = hllc_rcp1(b), q = a * y;
+            return fma(fma(-q, b, a), y, q);
+        }
+        if (a == 0.0) return copysign(0.0, a) * copysign(1.0, b);
+    }
+    return a / b;
+}
+static double hllc_recip(double b) {
+    if (!hllc_in_range(b)) return 1.0 / b;
+    double y = hllc_rcp1(b);
+    return fma(y, fma(-b, y, 1.0), y);
+}
+static double hllc_sound(double a, double r) {
+    if (!(a > 0.0) || !(r > 0.0) || !hllc_in_range(a) || !hllc_in_range(r)) return sqrt(a / r);
+    float af = hllc_seed(a), rf = hllc_seed(r);
+    float qf = af / rf;
+    float sf = sqrtf(qf);
+    float tf = rf * sf;
+    float hf = 0.5f / tf;
+    double h = (double)hf, s = (double)sf;
+    s = fma(fma(-(r * s), s, a), h, s);
+    s = fma(fma(-(r * s), s, a), h, s);
+    return s;
+}
+
 /* HLLC flux (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics,
  * 3rd ed., sec. 10.4-10.6) with Davis wave-speed estimates
  * S_L = min(un_L - c_L, un_R - c_R), S_R = max(un_L + c_L, un_R + c_R), and the
@@ -473,10 +530,11 @@ static double energy(double r, double u, double v, double p, double IG1) {
  *   F*_K = [S*(S_K U_K - F_K) + S_K p* D*] / (S_K - S*),  D* = (0, nx, ny, S*),
  *   p* = p_K + rho_K (S_K - un_K)(S* - un_K),
  * which equals F_K + S_K (U*_K - U_K) for Toro's star state U*_K. Energies use
- * p/(gamma-1) as p * (1/(gamma-1)). */
+ * p/(gamma-1) as p * (1/(gamma-1)). c = hllc_sound(GAMMA p, rho), S* = hllc_quot,
+ * 1/(S_K - S*) = hllc_recip. */
 static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
     double IG1 = 1.0 / (GAM - 1.0);
-    double cL = sqrt(GAM * pL->p / pL->r), cR = sqrt(GAM * pR->p / pR->r);
+    double cL = hllc_sound(GAM * pL->p, pL->r), cR = hllc_sound(GAM * pR->p, pR->r);
     double unL = dot2(pL->u, nx, pL->v, ny), unR = dot2(pR->u, nx, pR->v, ny);
     double EL = energy(pL->r, pL->u, pL->v, pL->p, IG1);
     double ER = energy(pR->r, pR->u, pR->v, pR->p, IG1);
@@ -484,14 +542,14 @@ static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double
     if (SL >= 0.0) { phys_flux(f, pL->r, pL->u, pL->v, pL->p, EL, unL, nx, ny); return; }
     if (SR <= 0.0) { phys_flux(f, pR->r, pR->u, pR->v, pR->p, ER, unR, nx, ny); return; }
     double mL = pL->r * (SL - unL), mR = pR->r * (SR - unR);
-    double Ss = fma(-mR, unR, fma(mL, unL, pR->p - pL->p)) / (mL - mR);
+    double Ss = hllc_quot(fma(-mR, unR, fma(mL, unL, pR->p - pL->p)), mL - mR);
     const Par* K; double SK, unK, EK, mK;
     if (Ss >= 0.0) { K = pL; SK = SL; unK = unL; EK = EL; mK = mL; }
     else { K = pR; SK = SR; unK = unR; EK = ER; mK = mR; }
     double FK[4];
     phys_flux(FK, K->r, K->u, K->v, K->p, EK, unK, nx, ny);
     double ps = fma(mK, Ss - unK, K->p);
-    double inv = 1.0 / (SK - Ss);
+    double inv = hllc_recip(SK - Ss);
     double sp = SK * ps;
     f[0] = (Ss * fma(SK, K->r, -FK[0])) * inv;
     f[1] = fma(Ss, fma(SK, K->r * K->u, -FK[1]), sp * nx) * inv;
