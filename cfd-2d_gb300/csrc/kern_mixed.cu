@@ -39,6 +39,44 @@ void fused_by_recon(const DevCase& c, const DevTiles& t, int recon, int scheme, 
 }
 }  // namespace
 
+namespace {
+template <int FLUX, int RECON, int SCHEME>
+void fu_by_stage(const DevCase& c, const DevTiles& t, int stage, float* wo, cudaStream_t s) {
+    const size_t smem = 16 * (size_t)t.max_edges;
+    auto go = [&](auto kern) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<t.n_tiles, t.tile, smem, s>>>(c, t, wo);
+    };
+    if (stage == 0) go(k_flux_update<FLUX, RECON, SCHEME, 0>);
+    else if (stage == 1) go(k_flux_update<FLUX, RECON, SCHEME, 1>);
+    else if (SCHEME == TIME_SSPRK3) go(k_flux_update<FLUX, RECON, TIME_SSPRK3, 2>);
+}
+template <int FLUX, int RECON>
+void fu_by_scheme(const DevCase& c, const DevTiles& t, int scheme, int stage, float* wo, cudaStream_t s) {
+    if (scheme == TIME_SSPRK3) fu_by_stage<FLUX, RECON, TIME_SSPRK3>(c, t, stage, wo, s);
+    else if (scheme == TIME_HEUN) fu_by_stage<FLUX, RECON, TIME_HEUN>(c, t, stage, wo, s);
+    else fu_by_stage<FLUX, RECON, TIME_EULER>(c, t, stage, wo, s);
+}
+template <int FLUX>
+void fu_by_recon(const DevCase& c, const DevTiles& t, int recon, int scheme, int stage, float* wo, cudaStream_t s) {
+    if (recon == RECON_NONE) fu_by_scheme<FLUX, RECON_NONE>(c, t, scheme, stage, wo, s);
+    else if (recon == RECON_LINEAR) fu_by_scheme<FLUX, RECON_LINEAR>(c, t, scheme, stage, wo, s);
+    else fu_by_scheme<FLUX, RECON_MINMOD>(c, t, scheme, stage, wo, s);
+}
+}  // namespace
+
+// The mixed form's flux and update of one stage per tile (k_flux_update); the stage's
+// primitives are c.W32, its gradients c.G32, the new primitives go to w_out.
+void launch_flux_update_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,
+                              float* w_out, cudaStream_t s) {
+    switch (flux) {
+    case FLUX_LAX: fu_by_recon<FLUX_LAX>(c, t, recon, scheme, stage, w_out, s); break;
+    case FLUX_ROE: fu_by_recon<FLUX_ROE>(c, t, recon, scheme, stage, w_out, s); break;
+    case FLUX_HLLC: fu_by_recon<FLUX_HLLC>(c, t, recon, scheme, stage, w_out, s); break;
+    default: fu_by_recon<FLUX_GODUNOV>(c, t, recon, scheme, stage, w_out, s); break;
+    }
+}
+
 // One fused stage of the mixed form (SSP-RK3 or Heun): gradients, fluxes and update per tile.
 void launch_stage_fused_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,
                               const float* w_in, float* w_out, cudaStream_t s) {

@@ -171,6 +171,17 @@ __device__ __forceinline__ double neg_if(double x, bool s) {
     return __hiloint2double(__double2hiint(x) ^ (s ? (int)0x80000000 : 0), __double2loint(x));
 }
 __device__ __forceinline__ float neg_if(float x, bool s) { return __int_as_float(__float_as_int(x) ^ (s ? (int)0x80000000 : 0)); }
+// x * 0.5 (exact halving, the correctly rounded x / 2): for normal x above the smallest
+// binade a decrement of the exponent field on the integer pipe, zeros unchanged; the rest
+// (subnormal results, inf, NaN) through the FP64 multiply. Bit for bit x * 0.5.
+__device__ __forceinline__ double half_exact(double x) {
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e > 1 && e < 0x7ff) return __longlong_as_double(b - (1ll << 52));
+    if ((b & 0x7fffffffffffffffll) == 0) return x;
+    return x * 0.5;
+}
+__device__ __forceinline__ float half_exact(float x) { return x * 0.5f; }
 // a / b given y = RN(1/b): the correctly rounded quotient in FP64, a * y in the FP32 faces.
 __device__ __forceinline__ double div_by(double a, double b, double y) { return div_rn(a, b, y); }
 __device__ __forceinline__ float div_by(float a, float, float y) { return a * y; }
@@ -468,7 +479,7 @@ __device__ __forceinline__ void phys_flux(T* f, T r, T u, T v, T p, T E, T un, T
 }
 template <typename T> __device__ __forceinline__ T dot2(T a, T x, T b, T y) { return t_fma(a, x, b * y); }
 template <typename T> __device__ __forceinline__ T energy(T r, T u, T v, T p, T IG1) {
-    return t_fma(p, IG1, (T(0.5) * r) * t_fma(u, u, v * v));
+    return t_fma(p, IG1, half_exact(r) * t_fma(u, u, v * v));
 }
 
 // Newton-refined quotient, reciprocal and sound speed of the FP64 HLLC flux. HLLC has no
@@ -637,8 +648,8 @@ __device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& 
 template <typename T>
 __device__ __forceinline__ void grad_face(T* g, const Prim<T>& q, const Prim<T>& o, T nx, T ny, T l, bool side2) {
     // x * 0.5 is the correctly rounded x / 2 (exact halving), without a division
-    const T hr = (q.r + o.r) * T(0.5), hp = (q.p + o.p) * T(0.5);
-    const T hu = (q.u + o.u) * T(0.5), hv = (q.v + o.v) * T(0.5);
+    const T hr = half_exact(q.r + o.r), hp = half_exact(q.p + o.p);
+    const T hu = half_exact(q.u + o.u), hv = half_exact(q.v + o.v);
     const T v[8] = {hr * nx * l, hr * ny * l, hp * nx * l, hp * ny * l,
                     hu * nx * l, hu * ny * l, hv * nx * l, hv * ny * l};
 #pragma unroll
@@ -819,8 +830,9 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
     out[0] = fs[0] * lh; out[1] = fs[1] * lh; out[2] = fs[2] * lh; out[3] = fs[3] * lh;
 }
 
+// The flux of edge e (what F holds for it) from the stage's W and G.
 template <typename T, int FLUX, int RECON>
-__device__ __forceinline__ void flux_one(const DevCase& c, int e) {
+__device__ __forceinline__ void flux_edge(const DevCase& c, int e, T* out) {
     const T* __restrict__ W = W_of<T>(c);
     const T* __restrict__ G = G_of<T>(c);
     const int c1 = ldcs(c.ec1 + e);
@@ -834,8 +846,13 @@ __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
         qR = load_prim(W, c2);
         if (RECON != RECON_NONE) ld8(G, c2, gR);
     }
-    T out[4];
     flux_core<T, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e));
+}
+
+template <typename T, int FLUX, int RECON>
+__device__ __forceinline__ void flux_one(const DevCase& c, int e) {
+    T out[4];
+    flux_edge<T, FLUX, RECON>(c, e, out);
     st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
 }
 
@@ -1201,6 +1218,49 @@ __global__ void __launch_bounds__(256, 5) k_stage_fused(const DevCase c, const D
         __syncthreads();  // shared buffers are free for the next round
     }
     cp_async_wait<0>();
+}
+
+// The mixed form's flux and update of one stage per tile of cells (one CTA of 256 threads
+// per tile): the fluxes of every edge of the tile's own cells (from the stage's W in
+// c.W32 and the gradients k_grad left in c.G32, read through the caches) go into shared
+// memory, then each own cell gathers its three and updates, writing its new primitives
+// to w_out (another buffer: the neighbouring tiles still read the old ones). An edge on
+// the tile border is evaluated by both tiles with the same inputs and the same code as
+// k_flux, and the cell sums are those of k_update: the per-kernel path's results bit for
+// bit, without the edge fluxes' round trip through memory, and with the update's FP64
+// work overlapping other tiles' gathers.
+template <int FLUX, int RECON, int SCHEME, int STAGE>
+__global__ void __launch_bounds__(256) k_flux_update(const DevCase c, const DevTiles tl, float* __restrict__ w_out) {
+    extern __shared__ float4 Fs[];
+    const int t = blockIdx.x;
+    const int own0 = t * tl.tile, n_own = min(tl.tile, c.nc - own0);
+    const int e0 = tl.edge_off[t], nE = tl.edge_off[t + 1] - e0;
+    for (int k = threadIdx.x; k < nE; k += blockDim.x) {
+        float out[4];
+        flux_edge<float, FLUX, RECON>(c, tl.tedge[e0 + k].x, out);
+        Fs[k] = make_float4(out[0], out[1], out[2], out[3]);
+    }
+    __syncthreads();
+    const int k = threadIdx.x;
+    if (k >= n_own) return;
+    const int i = own0 + k;
+    if (!update_begin<SCHEME, STAGE>(c, i)) {  // frozen cell: its primitives do not change
+        reinterpret_cast<float4*>(w_out)[i] = reinterpret_cast<const float4*>(c.W32)[i];
+        return;
+    }
+    const int2* __restrict__ gf = tl.gface + 3 * ((size_t)tl.gface_off[t] + k);
+    float tv[3][4];
+#pragma unroll
+    for (int f = 0; f < 3; f++) {
+        const int2 fr = gf[f];
+        const float4 v = Fs[(unsigned)fr.y >> 16];
+        const bool add = (fr.x & 1) != 0;  // c2 adds the edge flux, c1 subtracts it
+        tv[f][0] = neg_if(v.x, !add); tv[f][1] = neg_if(v.y, !add);
+        tv[f][2] = neg_if(v.z, !add); tv[f][3] = neg_if(v.w, !add);
+    }
+    double R[4];
+    residual_pair_sum(tv, R);
+    update_finish<float, SCHEME, STAGE>(c, i, R, w_out);
 }
 
 template <typename T, int SCHEME, int STAGE, bool STRIDE>

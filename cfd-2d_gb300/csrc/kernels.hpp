@@ -188,6 +188,8 @@ struct DevTiles {
     const int2* gface = nullptr;     // per gradient cell and face: x = (edge << 1) | side,
                                      // y = local neighbour (0xffff: boundary) | local flux edge << 16 (own cells)
 };
+void launch_flux_update_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,
+                              float* w_out, cudaStream_t s);
 void launch_stage_fused_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,
                               const float* w_in, float* w_out, cudaStream_t s);
 

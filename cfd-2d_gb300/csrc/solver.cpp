@@ -68,7 +68,7 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
     const int nc = topo_.nc;
     cell_mat_.resize(nc);
     for (int i = 0; i < nc; i++) cell_mat_[i] = task_.regions[cell_region[i]].matId;
-    const int order = task_.reorder >= 0 ? task_.reorder : (task_.fused == 1 ? ORDER_HILBERT : ORDER_RCM);
+    const int order = task_.reorder >= 0 ? task_.reorder : (task_.fused >= 1 ? ORDER_HILBERT : ORDER_RCM);
     lay_ = make_layout(topo_, cell_mat_, edge_bnd, order);
     const int ne = lay_.ne;
     CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
@@ -265,7 +265,26 @@ void Solver::enqueue_step(cudaEvent_t* ev, int* kinds, int* nev) {
         if (begin) kinds[*nev / 2] = kind;
         CUDA_CHECK(cudaEventRecord(ev[(*nev)++], stream_));
     };
-    if (fused_ && gauss_points_ != 0) {  // one tiled kernel per stage, primitives rotated through wrot_
+    if (fused_ == 2 && gauss_points_ != 0) {  // gradients, then one tiled flux-and-update kernel per stage
+        for (int st = 0; st < nst; st++) {
+            DevCase cs = dc_;  // the stage's primitives, rotated through wrot_
+            cs.W32 = wrot_[st];
+            if (task_.recon != RECON_NONE) {
+                mark(0, true);
+                launch_grad(cs, p, stream_);
+                mark(0, false);
+            }
+            mark(1, true);
+            launch_flux_update_mixed(cs, tiles_, task_.flux, task_.recon, task_.scheme, st, wrot_[(st + 1) % nst],
+                                     stream_);
+            mark(1, false);
+        }
+        mark(3, true);
+        launch_remediate(dc_, p, stream_);
+        mark(3, false);
+        return;
+    }
+    if (fused_ == 1 && gauss_points_ != 0) {  // one tiled kernel per stage, primitives rotated through wrot_
         for (int st = 0; st < nst; st++) {
             mark(1, true);
             launch_stage_fused_mixed(dc_, tiles_, task_.flux, task_.recon, task_.scheme, st, wrot_[st],

@@ -28,10 +28,11 @@ struct TileLists {
 }  // namespace
 
 void Solver::build_tiles() {
-    fused_ = false;
-    const bool applies = task_.precision == PREC_MIXED && task_.fused == 1 && gauss_points_ != 0 &&
+    fused_ = 0;
+    const bool applies = task_.precision == PREC_MIXED && task_.fused >= 1 && gauss_points_ != 0 &&
                          (task_.scheme == TIME_SSPRK3 || task_.scheme == TIME_HEUN);
     if (!applies) return;
+    const int mode = task_.fused;
     const int nc = dc_.nc;
     const int nt = (nc + kTile - 1) / kTile;
     const Layout& L = lay_;
@@ -118,7 +119,8 @@ void Solver::build_tiles() {
         max_grad = std::max(max_grad, n_own + tl[t].nh1);
         max_edges = std::max(max_edges, (int)tl[t].tedge.size());
     }
-    const size_t smem = 16 * (2 * (size_t)max_cells + 2 * (size_t)max_grad + (size_t)max_edges);
+    const size_t smem = mode == 1 ? 16 * (2 * (size_t)max_cells + 2 * (size_t)max_grad + (size_t)max_edges)
+                                  : 16 * (size_t)max_edges;  // flux-and-update: the tile's edge fluxes only
     if (smem > kMaxSmem) return;
     std::vector<int> halo;
     std::vector<int2> tedge, gface;
@@ -150,7 +152,7 @@ void Solver::build_tiles() {
     const int nst = task_.scheme == TIME_SSPRK3 ? 3 : 2;
     wrot_[0] = dc_.W32;
     for (int k = 1; k < nst; k++) wrot_[k] = dalloc<float>(4 * (size_t)nc);
-    fused_ = true;
+    fused_ = mode;
 }
 
 }  // namespace cfd2d

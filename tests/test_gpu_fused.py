@@ -1,6 +1,8 @@
-"""The mixed form's opt-in fused stage kernel (gradients, fluxes and update of a
-tile of cells in one launch, from shared memory) against the same form on its
-per-kernel path: identical inputs and identical arithmetic, so identical bits."""
+"""The mixed form's tiled stage kernels against the same form on its per-kernel path:
+FUSED_STAGE 1 (gradients, fluxes and update of a tile of cells in one launch, from
+shared memory) and FUSED_STAGE 2 (the per-kernel gradients, then the fluxes of a tile's
+edges in shared memory and its cells' update in one launch). Identical inputs and
+identical arithmetic, so identical bits."""
 import numpy as np
 import pytest
 
@@ -9,10 +11,13 @@ from cfd2d import cases
 pytestmark = pytest.mark.gpu
 
 
-def _pair(capi, tmp_path, t, m, U0=None, **kw):
+MODES = ("1", "2")
+
+
+def _pair(capi, tmp_path, t, m, U0=None, mode="1", **kw):
     out = []
     kw.setdefault("reorder", "HILBERT")
-    for fused in ("0", "1"):
+    for fused in ("0", mode):
         t.precision = "MIXED"
         t.fused_stage = fused
         for k, v in kw.items():
@@ -26,40 +31,44 @@ def _pair(capi, tmp_path, t, m, U0=None, **kw):
     return out
 
 
-def _is_fused(s):
-    """Profile one step (it is taken): the fused path launches no separate gradient or update kernels."""
+def _is_fused(s, mode="1"):
+    """Profile one step (it is taken): the tiled paths launch no separate update kernel, FUSED_STAGE 1
+    no separate gradient kernel either."""
     ms, cnt = s.profile_steps(1)
-    return cnt[0] == 0 and cnt[2] == 0 and cnt[1] > 0
+    return (cnt[0] == 0 or mode == "2") and cnt[2] == 0 and cnt[1] > 0
 
 
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("flux,recon,scheme", [("HLLC", "MINMOD", "SSPRK3"), ("ROE", "MINMOD", "HEUN"),
                                                ("LAX", "LINEAR", "SSPRK3"), ("HLLC", "NONE", "HEUN"),
                                                ("GODUNOV", "LINEAR", "SSPRK3")])
-def test_fused_equals_per_kernel_vortex(capi, tmp_path, flux, recon, scheme):
+def test_fused_equals_per_kernel_vortex(capi, tmp_path, flux, recon, scheme, mode):
     kinds = ("BOUND_INLET", "BOUND_OUTLET", "BOUND_WALL_SLIP", "BOUND_WALL_NO_SLIP")
     t, m, U0 = cases.vortex(96, flux=flux, recon=recon, scheme=scheme, steps=12, bnd_kinds=kinds)
-    a, b = _pair(capi, tmp_path, t, m, U0)
-    assert not _is_fused(a) and _is_fused(b)
+    a, b = _pair(capi, tmp_path, t, m, U0, mode=mode)
+    assert not _is_fused(a, mode) and _is_fused(b, mode)
     a.step(12)
     b.step(12)
     assert np.array_equal(a.state(), b.state())
     assert np.array_equal(a.time_step(), b.time_step())
 
 
-def test_fused_equals_per_kernel_local_time_step(capi, tmp_path):
+@pytest.mark.parametrize("mode", MODES)
+def test_fused_equals_per_kernel_local_time_step(capi, tmp_path, mode):
     t, m, U0 = cases.vortex(80, flux="HLLC", recon="MINMOD", scheme="SSPRK3", steps=10, steady=1)
-    a, b = _pair(capi, tmp_path, t, m, U0)
+    a, b = _pair(capi, tmp_path, t, m, U0, mode=mode)
     a.step(10)
     b.step(10)
     assert np.array_equal(a.state(), b.state())
     assert np.array_equal(a.time_step(), b.time_step())
 
 
-def test_fused_equals_per_kernel_limits_and_remediation(capi, tmp_path):
+@pytest.mark.parametrize("mode", MODES)
+def test_fused_equals_per_kernel_limits_and_remediation(capi, tmp_path, mode):
     """A |u| limit below the vortex peak flags cells (frozen, then remediated)."""
     t, m, U0 = cases.vortex(64, flux="HLLC", recon="MINMOD", scheme="SSPRK3", steps=30)
     t.limits = (1e-8, 1e8, 1e-8, 1e8, 1.55)
-    a, b = _pair(capi, tmp_path, t, m, U0)
+    a, b = _pair(capi, tmp_path, t, m, U0, mode=mode)
     a.step(30)
     b.step(30)
     assert np.array_equal(a.flags(), b.flags())
@@ -67,20 +76,22 @@ def test_fused_equals_per_kernel_limits_and_remediation(capi, tmp_path):
     assert np.array_equal(a.state(), b.state())
 
 
-def test_fused_four_quadrant_full_size(capi, tmp_path):
+@pytest.mark.parametrize("mode", MODES)
+def test_fused_four_quadrant_full_size(capi, tmp_path, mode):
     """2,097,152 triangles, HLLC + minmod + SSP-RK3, 5 steps: the bench workload."""
     t, m, _ = cases.four_quadrant(1024, steps=5)
-    a, b = _pair(capi, tmp_path, t, m)
+    a, b = _pair(capi, tmp_path, t, m, mode=mode)
     a.step(5)
     b.step(5)
     assert np.array_equal(a.state(), b.state())
 
 
-def test_fused_with_rcm_order(capi, tmp_path):
+@pytest.mark.parametrize("mode", MODES)
+def test_fused_with_rcm_order(capi, tmp_path, mode):
     """Long thin tiles (RCM order) still fit and still give the per-kernel bits."""
     t, m, U0 = cases.vortex(64, flux="HLLC", recon="MINMOD", scheme="SSPRK3", steps=8)
-    a, b = _pair(capi, tmp_path, t, m, U0, reorder="RCM")
-    assert not _is_fused(a) and _is_fused(b)
+    a, b = _pair(capi, tmp_path, t, m, U0, mode=mode, reorder="RCM")
+    assert not _is_fused(a, mode) and _is_fused(b, mode)
     a.step(8)
     b.step(8)
     assert np.array_equal(a.state(), b.state())
