@@ -448,53 +448,66 @@ def combined_workload(args, capi, cases, world, rank, dist, W, K):
         print(json.dumps(line), flush=True)
 
 
-def batched_workload(args, capi, cases, world, rank, dist, W, K):
+def batched_measure(capi, cases, W, K, instances=256, forms=("fp64", "mixed"), dist=None):
     """256 isentropic-vortex instances, triangle counts log-uniform in [10k, 400k]
-    (seed 3), Mach uniform in [0.1, 0.8], strength uniform in [1, 5], Roe +
-    minmod + SSP-RK3, CFL 0.5, FP64: one batched solver (autotuned launch
-    shapes, one CUDA graph per step) against the same instances solved one
-    after another, K steps each; device time from CUDA events."""
+    (seed 3), Mach uniform in [0.1, 0.8], strength uniform in [1, 5], Roe + minmod +
+    SSP-RK3, CFL 0.5: per form (FP64, and FP32 faces / FP64 accumulation) one batched
+    solver (autotuned launch shapes, one CUDA graph per step) against the same instances
+    solved one after another, K steps each; device time from CUDA events."""
     d = tempfile.mkdtemp(prefix="cfd2d_batch_")
-    insts = cases.batched_vortices(args.instances, steps=K)
-    paths = []
-    for k, (t, m, _) in enumerate(insts):
-        dk = os.path.join(d, f"i{k}")
-        os.makedirs(dk)
-        paths.append(cases.write_task(t, m, dk))
-    a = time.perf_counter()
-    b = capi.Batch(paths, meshes=[m for _, m, _ in insts])
-    b.set_state(np.concatenate([U0 for _, _, U0 in insts], axis=1), reset_time_step=True)
-    create_s = time.perf_counter() - a
-    tune_json = os.path.join(d, "tuning.json")
-    b.autotune(tune_json)
-    tuning = json.load(open(tune_json))
-    nc = b.n
-    b.step(W)
-    ms_b = reduce_max(dist, b.timed_steps(K))
-    b.close()
-    seq_ms = 0.0
-    for k, (t, m, U0) in enumerate(insts):
-        s = capi.Solver(paths[k], mesh=m)
-        s.set_state(U0, reset_time_step=True)
-        s.step(W)
-        seq_ms += s.timed_steps(K)
-        s.close()
-    seq_ms = reduce_max(dist, seq_ms)
-    rate_b = world * nc * K / (ms_b * 1e-3)
-    rate_s = world * nc * K / (seq_ms * 1e-3)
+    insts = cases.batched_vortices(instances, steps=K)
+    out = {}
+    for form in forms:
+        paths = []
+        for k, (t, m, _) in enumerate(insts):
+            t.precision = "MIXED" if form == "mixed" else None
+            dk = os.path.join(d, f"{form}_{k}")
+            os.makedirs(dk)
+            paths.append(cases.write_task(t, m, dk))
+        a = time.perf_counter()
+        b = capi.Batch(paths, meshes=[m for _, m, _ in insts])
+        b.set_state(np.concatenate([U0 for _, _, U0 in insts], axis=1), reset_time_step=True)
+        create_s = time.perf_counter() - a
+        tune_json = os.path.join(d, f"tuning_{form}.json")
+        b.autotune(tune_json)
+        tuning = json.load(open(tune_json))
+        nc = b.n
+        b.step(W)
+        ms_b = reduce_max(dist, b.timed_steps(K))
+        b.close()
+        seq_ms = 0.0
+        for k, (t, m, U0) in enumerate(insts):
+            s = capi.Solver(paths[k], mesh=m)
+            s.set_state(U0, reset_time_step=True)
+            s.step(W)
+            seq_ms += s.timed_steps(K)
+            s.close()
+        seq_ms = reduce_max(dist, seq_ms)
+        out[form] = {"value": nc * K / (ms_b * 1e-3), "ms_per_step": ms_b / K,
+                     "sequential": {"value": nc * K / (seq_ms * 1e-3), "ms_per_step_all_instances": seq_ms / K},
+                     "speedup_vs_sequential": seq_ms / ms_b, "autotune": tuning, "create_s": create_s}
+    out["cells"] = nc
+    out["instances"] = instances
+    out["steps"] = K
+    out["workload"] = (f"{instances} isentropic-vortex instances on [0,10]^2, triangles log-uniform in [10k, 400k] "
+                       "(seed 3), Mach U[0.1,0.8], strength U[1,5], Roe + minmod + SSP-RK3, CFL 0.5")
+    return out
+
+
+def batched_workload(args, capi, cases, world, rank, dist, W, K):
+    """The batched configuration on its own line (FP64 headline, the mixed form beside it)."""
+    res = batched_measure(capi, cases, W, K, args.instances, dist=dist)
     if rank == 0:
+        f = res["fp64"]
         print(json.dumps({
             "metric": "aggregate cell-updates/s, 256 uneven vortex instances, batched vs sequential",
-            "value": rate_b, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": ms_b / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "value": world * f["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{args.instances} isentropic-vortex instances on [0,10]^2, triangles log-uniform "
-                                   "in [10k, 400k] (seed 3), Mach U[0.1,0.8], strength U[1,5], Roe + minmod + "
-                                   "SSP-RK3, CFL 0.5", "cells": nc, "instances": args.instances,
+            "config": {"workload": res["workload"], "cells": res["cells"], "instances": res["instances"],
                        "l2": "no flush: the batch's working set (~12 GB) exceeds the 129 MB L2"},
-            "sequential": {"value": rate_s, "ms_per_step_all_instances": seq_ms / K},
-            "speedup_vs_sequential": seq_ms / ms_b,
-            "autotune": tuning, "create_s": create_s,
+            "sequential": f["sequential"], "speedup_vs_sequential": f["speedup_vs_sequential"],
+            "autotune": f["autotune"], "create_s": f["create_s"], "mixed": res.get("mixed"),
             "gpu_launches": K * (3 * 3 + 1)}), flush=True)
 
 
@@ -707,6 +720,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-combined", action="store_true", help="leave out the 33.5M-triangle combined key")
+    ap.add_argument("--no-batched", action="store_true", help="leave out the 256-instance batched key")
     ap.add_argument("--n", type=int, default=N_SIDE, help="squares per side (profiling runs only)")
     ap.add_argument("--workload", default="four_quadrant",
                     choices=["four_quadrant", "batched", "combined", "adjoint", "implicit", "rkdg"],
@@ -854,6 +868,7 @@ def main():
     s64.close()
     smx.close()
     comb = combined_measure(capi, cases, W) if not args.no_combined else None
+    batch = batched_measure(capi, cases, W, min(K, 20), dist=dist) if not args.no_batched else None
 
     hbm, peak_kind = measured_peaks()
     traffic = ncu_traffic()
@@ -918,6 +933,8 @@ def main():
     }
     if comb is not None:
         line["combined"] = comb
+    if batch is not None:
+        line["batched"] = batch
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_single()
     if rank == 0:

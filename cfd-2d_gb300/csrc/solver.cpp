@@ -224,6 +224,7 @@ Solver::~Solver() {
         if (snap_host_[k]) cudaFreeHost(snap_host_[k]);
         if (snap_ev_[k]) cudaEventDestroy(snap_ev_[k]);
     }
+    drop_record_graphs();
     if (gexec_) cudaGraphExecDestroy(gexec_);
     if (graph_) cudaGraphDestroy(graph_);
     if (stream_) cudaStreamSynchronize(stream_);

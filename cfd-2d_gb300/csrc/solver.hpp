@@ -120,6 +120,10 @@ private:
     void release(void* p, size_t bytes);
     void adjoint_setup();
     void record_step(double* store, void* wg);
+    void record_segment(int n);
+    void drop_record_graphs();
+    // captured recording segments: (n, (graph, store kind 0 states / 1 W / 2 W and G))
+    std::vector<std::pair<int, std::pair<cudaGraphExec_t, int>>> rec_graphs_;
     DevCase adj_dc_{};
     bool adj_ready_ = false;
     int obj_kind_ = -1;
@@ -145,6 +149,7 @@ private:
     bool store_g_ = false;        // ... and their G
     size_t ckpt_slots_ = 0, seg_slots_ = 0;
     int fw_steps_ = 0, fw_k_ = 0;
+    bool last_recorded_ = false;  // forward() left the last segment's stages in the store
     template <typename T> T* upload(const std::vector<T>& v);
     struct VtkJob { int step = 0, buf = 0; };
     void vtk_writer();

@@ -125,6 +125,8 @@ double Solver::forward(int nsteps, int k, int* status) {
             store_wg_ = true;
         }
         const size_t want = store_g_ ? need : (store_wg_ ? need_w : 0);
+        if ((store_wg_ && segstore_) || want > wg_slots_ || (!store_wg_ && (size_t)k * nst > seg_slots_))
+            drop_record_graphs();  // the store moves: graphs captured on it are stale
         if (store_wg_ && segstore_) {  // the states are not kept: give their memory back first
             release(segstore_, seg_slots_ * 4 * nc * dbl);
             segstore_ = nullptr;
@@ -142,10 +144,22 @@ double Solver::forward(int nsteps, int k, int* status) {
         }
     }
     CUDA_CHECK(cudaMemsetAsync(dc_.flags, 0, sizeof(unsigned) * nc, stream_));
+    last_recorded_ = false;
     for (size_t s = 0; s < nseg; s++) {
         CUDA_CHECK(cudaMemcpyAsync(ckpt_ + s * 4 * nc, dc_.A, sizeof(double) * 4 * nc, cudaMemcpyDeviceToDevice,
                                    stream_));
         const int n = std::min<int>(k, nsteps - (int)s * k);
+        if (s + 1 == nseg) {
+            // the last segment is the first the backward sweep walks: its stages are recorded
+            // now (the step's own kernels, so the same bits) instead of being recomputed there
+            record_segment(n);
+            for (int j = 0; j < n; j++) {
+                if (!task_.steady) t_ += tau_;
+                steps_++;
+            }
+            last_recorded_ = true;
+            continue;
+        }
         for (int j = 0; j < n; j++) {
             if (!task_.steady) t_ += tau_;
             CUDA_CHECK(cudaGraphLaunch(gexec_, stream_));
@@ -162,6 +176,42 @@ double Solver::forward(int nsteps, int k, int* status) {
     double J = 0.0;
     for (double v : h) J += v;
     return J;
+}
+
+void Solver::drop_record_graphs() {
+    for (auto& g : rec_graphs_) cudaGraphExecDestroy(g.second.first);
+    rec_graphs_.clear();
+}
+
+// n forward steps that keep every stage in the segment store (what the backward sweep
+// reads), captured once per n into a CUDA graph and replayed.
+void Solver::record_segment(int n) {
+    const size_t nc = dc_.nc;
+    const int nst = n_stages(task_.scheme);
+    const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
+    const size_t per_stage = (store_g_ ? 12 : 4) * nc * fsize;
+    cudaGraphExec_t exec = nullptr;
+    for (auto& g : rec_graphs_)
+        if (g.first == n && g.second.second == (store_wg_ ? (store_g_ ? 2 : 1) : 0)) exec = g.second.first;
+    if (!exec) {
+        cudaGraph_t graph = nullptr;
+        CUDA_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int j = 0; j < n; j++)
+                record_step(store_wg_ ? nullptr : segstore_ + (size_t)j * nst * 4 * nc,
+                            store_wg_ ? reinterpret_cast<char*>(wgstore_) + (size_t)j * nst * per_stage : nullptr);
+        } catch (...) {
+            cudaStreamEndCapture(stream_, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        CUDA_CHECK(cudaStreamEndCapture(stream_, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CUDA_CHECK(e);
+        rec_graphs_.push_back({n, {exec, store_wg_ ? (store_g_ ? 2 : 1) : 0}});
+    }
+    CUDA_CHECK(cudaGraphLaunch(exec, stream_));
 }
 
 // One forward step that keeps, when given, every stage's input state in
@@ -229,11 +279,14 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
     // One segment after its checkpoint is restored: recompute its n steps, recording the
     // stages, then walk them backwards. Captured once per segment length into a CUDA
     // graph and replayed, so the host issues one launch per segment.
-    auto segment = [&](int n, bool first_step) {  // first_step: the forward's last step, started from dJ/dU
-        launch_prims(dc_, task_.precision, stream_);
-        for (int j = 0; j < n; j++)
-            record_step(store_wg_ ? nullptr : segstore_ + (size_t)j * nst * 4 * nc,
-                        store_wg_ ? wg_at(j * nst) : nullptr);
+    // recorded: the segment's stages are in the store already (the forward's last segment)
+    auto segment = [&](int n, bool first_step, bool recorded) {  // first_step: the forward's last step
+        if (!recorded) {
+            launch_prims(dc_, task_.precision, stream_);
+            for (int j = 0; j < n; j++)
+                record_step(store_wg_ ? nullptr : segstore_ + (size_t)j * nst * 4 * nc,
+                            store_wg_ ? wg_at(j * nst) : nullptr);
+        }
         for (int j = n - 1; j >= 0; j--) {
             // every later step is started by the stage-0 kernel of the step after it
             if (first_step && j == n - 1) launch_adj_step_start(adj_dc_, a, ct_f, ca_f, stream_);
@@ -262,7 +315,7 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
             }
         }
     };
-    std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // key: 2 n + (first step)
+    std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // key: 4 n + 2 (recorded) + (first step)
     auto release = [&]() {
         for (auto& g : graphs) cudaGraphExecDestroy(g.second);
         graphs.clear();
@@ -270,10 +323,12 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
     try {
         for (int seg = nseg - 1; seg >= 0; seg--) {
             const int n = std::min(fw_k_, fw_steps_ - seg * fw_k_);
-            CUDA_CHECK(cudaMemcpyAsync(dc_.A, ckpt_ + (size_t)seg * 4 * nc, sizeof(double) * 4 * nc,
-                                       cudaMemcpyDeviceToDevice, stream_));
             const bool first = seg == nseg - 1;
-            const int key = 2 * n + (first ? 1 : 0);
+            const bool recorded = first && last_recorded_;
+            if (!recorded)
+                CUDA_CHECK(cudaMemcpyAsync(dc_.A, ckpt_ + (size_t)seg * 4 * nc, sizeof(double) * 4 * nc,
+                                           cudaMemcpyDeviceToDevice, stream_));
+            const int key = 4 * n + (recorded ? 2 : 0) + (first ? 1 : 0);
             cudaGraphExec_t exec = nullptr;
             for (auto& g : graphs)
                 if (g.first == key) exec = g.second;
@@ -281,7 +336,7 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
                 cudaGraph_t graph = nullptr;
                 CUDA_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
                 try {
-                    segment(n, first);
+                    segment(n, first, recorded);
                 } catch (...) {
                     cudaStreamEndCapture(stream_, &graph);
                     if (graph) cudaGraphDestroy(graph);
