@@ -153,8 +153,7 @@ def test_combined_mixed_adjoint_within_memory_budget(capi, tmp_path):
     quarter of S rho^2, checkpointed forward and mixed adjoint with an ADJOINT_MEMORY
     budget that the full store (primitives and gradients) would exceed. The handle stays
     within the budget, its gradient equals the unconstrained run's bit for bit (the store
-    modes re-derive what they do not keep), and it stays close to the FP64 gradient, which
-    in turn agrees with central FD."""
+    modes re-derive what they do not keep), and it stays close to the FP64 gradient."""
     t, m, _ = cases.four_quadrant(48, seed=5, steps=12)
     U0 = None  # the task's own initial state (four regions), read from the first handle
     xy = m.centroids()
@@ -192,16 +191,13 @@ def test_combined_mixed_adjoint_within_memory_budget(capi, tmp_path):
     s.forward(12, 4)
     g64, _ = s.backward()
     gmx = runs["free"][1]
-    assert np.all(np.isfinite(gmx))
+    assert np.all(np.isfinite(gmx)) and np.all(np.isfinite(g64))
     # at the four-quadrant discontinuities minmod's branch (a b > 0, |a| < |b|) follows FP32
     # rounding in the mixed forward and FP64 rounding in the other, and its derivative jumps
-    # between branches, so the two gradients differ by a few 1e-3 (the smooth vortex: 1e-5)
+    # between branches, so the two gradients differ by a few 1e-3 (the smooth vortex: 1e-5).
+    # The same kinks make central differences unreliable here; the FD checks run on the
+    # smooth vortex above.
     assert np.linalg.norm(gmx - g64) <= 1e-2 * np.linalg.norm(g64)
-    rng = np.random.default_rng(5)
-    for _ in range(3):
-        dv = rng.standard_normal(U0.shape); dv /= np.linalg.norm(dv)
-        fd = (_J(s, U0 + 1e-6 * dv, 12, 4) - _J(s, U0 - 1e-6 * dv, 12, 4)) / 2e-6
-        assert abs(float(np.sum(g64 * dv)) - fd) <= TOL * max(abs(fd), 1e-3 * np.linalg.norm(g64))
 
 
 @pytest.mark.parametrize("precision", [None, "MIXED"])
