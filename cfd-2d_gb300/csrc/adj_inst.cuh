@@ -116,6 +116,97 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 0) k_adj_flux(const 
     st8(o + 16, 0, g2b);
 }
 
+// The forward flux kernel of a recomputed stage that also keeps the evaluation's record
+// (FluxRec: face states, sound speeds, minmod's branches) for k_adj_flux_rec. Compiled with
+// the forward kernels' flags and the same code, so F is the forward's bit for bit.
+template <typename T, int RECON>
+__global__ void __launch_bounds__(256) k_flux_rec(const DevCase c, const FluxRec r) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= c.ne) return;
+    T out[4];
+    flux_edge<T, FLUX_HLLC, RECON, true>(c, e, out, r);
+    st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
+}
+
+// k_adj_flux (HLLC) reading the forward's record of each Gauss point instead of
+// recomputing the reconstruction, the ghost state, the sound speeds and minmod's
+// branches: the same reverse operations on the same values, so the same bits.
+template <typename T, int RECON>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 0) k_adj_flux_rec(const DevCase c, const AdjCase a,
+                                                                              const FluxRec r) {
+    const int ne = c.ne;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const T* DL = DL_of<T>(c);
+    const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
+    const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
+    const int c1 = c.ec1[e];
+    const bool inner = e < c.n_int;
+    const int c2 = inner ? c.ec2[e] : -1;
+    Prim<T> qL{};
+    DevBnd b{};
+    T Tc = T(0), M = T(0), gm1 = T(0), Cv = T(0);
+    T fb[4];
+    {
+        double m1[4], m2[4] = {0, 0, 0, 0};
+        ld4(a.mu, c1, m1);
+        if (inner) ld4(a.mu, c2, m2);
+        const double lh = to_wide(l) * (RECON == RECON_NONE ? 1.0 : 0.5);
+        for (int k = 0; k < 4; k++) fb[k] = to_face<T>((m2[k] - m1[k]) * lh);
+    }
+    if (!inner) {
+        qL = load_prim(W_of<T>(c), c1);
+        b = c.bnds[c.ebnd[e]];
+        const MatT<T> mt = matT_of<T>(c, c1);
+        gm1 = mt.gm1; Cv = mt.Cv; M = mt.M;
+        Tc = temperature(qL, gm1, Cv);
+    }
+    Prim<T> q1b = zero_prim<T>(), q2b = zero_prim<T>(), gcb = zero_prim<T>();
+    T g1b[8], g2b[8], bp[4];
+#pragma unroll
+    for (int k = 0; k < 8; k++) { g1b[k] = acc0<T>(); g2b[k] = acc0<T>(); }
+#pragma unroll
+    for (int k = 0; k < 4; k++) bp[k] = acc0<T>();
+    T Tcb = acc0<T>();
+    const unsigned bits = RECON == RECON_MINMOD ? r.bits[e] : 0u;
+    const int ngp = RECON == RECON_NONE ? 1 : 2;
+#pragma unroll 1
+    for (int gp = 0; gp < ngp; gp++) {
+        const T* v = static_cast<const T*>(r.v) + (size_t)(10 * gp) * ne + e;
+        const Prim<T> pL{v[0], v[ne], v[2 * (size_t)ne], v[3 * (size_t)ne]};
+        const Prim<T> pR{v[4 * (size_t)ne], v[5 * (size_t)ne], v[6 * (size_t)ne], v[7 * (size_t)ne]};
+        const T cL = v[8 * (size_t)ne], cR = v[9 * (size_t)ne];
+        T dxL = T(0), dyL = T(0), dxR = T(0), dyR = T(0);
+        if (RECON != RECON_NONE) {
+            dxL = DL[(4 * gp) * ne + e]; dyL = DL[(4 * gp + 1) * ne + e];
+            if (inner) { dxR = DL[(4 * gp + 2) * ne + e]; dyR = DL[(4 * gp + 3) * ne + e]; }
+        }
+        Prim<T> pLb = zero_prim<T>(), pRb = zero_prim<T>();
+        vjp_hllc_c(pL, pR, cL, cR, nx, ny, GAM, IG1, fb, pLb, pRb);
+        if (!inner) vjp_ghost(b, pL, Tc, nx, ny, M, pRb, pLb, Tcb, bp);
+        if (RECON == RECON_NONE) {
+            q1b.r += pLb.r; q1b.u += pLb.u; q1b.v += pLb.v; q1b.p += pLb.p;
+            if (inner) { q2b.r += pRb.r; q2b.u += pRb.u; q2b.v += pRb.v; q2b.p += pRb.p; }
+        } else if (inner) {
+            vjp_reconstruct_code<RECON>(bits >> (16 * gp), dxL, dyL, pLb, q1b, g1b, q2b);
+            vjp_reconstruct_code<RECON>(bits >> (16 * gp + 8), dxR, dyR, pRb, q2b, g2b, q1b);
+        } else {
+            vjp_reconstruct_code<RECON>(bits >> (16 * gp), dxL, dyL, pLb, q1b, g1b, gcb);
+        }
+    }
+    if (!inner) {
+        if (RECON == RECON_MINMOD) vjp_ghost(b, qL, Tc, nx, ny, M, gcb, q1b, Tcb, bp);
+        vjp_temperature(qL, gm1, Cv, Tcb, q1b);
+        double* o = a.eb + 4 * (size_t)(e - c.n_int);
+        o[0] += to_wide(bp[0]); o[1] += to_wide(bp[1]); o[2] += to_wide(bp[2]); o[3] += to_wide(bp[3]);
+    }
+    T* o = static_cast<T*>(a.eq) + 24 * (size_t)e;
+    st4(o, 0, q1b.r, q1b.u, q1b.v, q1b.p);
+    st8(o + 4, 0, g1b);
+    st4(o + 12, 0, q2b.r, q2b.u, q2b.v, q2b.p);
+    st8(o + 16, 0, g2b);
+}
+
 // The three faces' contributions summed exactly (SumAcc): the primitive adjoint is
 // rounded once into FP64 (it is summed again in k_adj_cell), the gradient adjoint
 // into the face precision (it only enters products there).
@@ -247,6 +338,18 @@ void adj_flux_by_recon(const DevCase& c, const AdjCase& a, int recon, cudaStream
 void KFN(adj_flux)(const DevCase& c, const AdjCase& a, int flux, int recon, cudaStream_t s) {
     if (flux == FLUX_HLLC) adj_flux_by_recon<FLUX_HLLC>(c, a, recon, s);
     else adj_flux_by_recon<FLUX_LAX>(c, a, recon, s);
+}
+void KFN(flux_rec)(const DevCase& c, int recon, const FluxRec& r, cudaStream_t s) {
+    const int g = adj_nblk(c.ne, 256);
+    if (recon == RECON_NONE) k_flux_rec<KT, RECON_NONE><<<g, 256, 0, s>>>(c, r);
+    else if (recon == RECON_LINEAR) k_flux_rec<KT, RECON_LINEAR><<<g, 256, 0, s>>>(c, r);
+    else k_flux_rec<KT, RECON_MINMOD><<<g, 256, 0, s>>>(c, r);
+}
+void KFN(adj_flux_rec)(const DevCase& c, const AdjCase& a, int recon, const FluxRec& r, cudaStream_t s) {
+    const int g = adj_nblk(c.ne, 128);
+    if (recon == RECON_NONE) k_adj_flux_rec<KT, RECON_NONE><<<g, 128, 0, s>>>(c, a, r);
+    else if (recon == RECON_LINEAR) k_adj_flux_rec<KT, RECON_LINEAR><<<g, 128, 0, s>>>(c, a, r);
+    else k_adj_flux_rec<KT, RECON_MINMOD><<<g, 128, 0, s>>>(c, a, r);
 }
 void KFN(adj_gather)(const DevCase& c, const AdjCase& a, cudaStream_t s) {
     k_adj_gather<KT><<<adj_nblk(c.nc, 128), 128, 0, s>>>(c, a);

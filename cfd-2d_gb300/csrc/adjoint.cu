@@ -9,6 +9,8 @@
 namespace cfd2d {
 
 void launch_adj_flux_mixed(const DevCase&, const AdjCase&, int, int, cudaStream_t);
+void launch_flux_rec_mixed(const DevCase&, int, const FluxRec&, cudaStream_t);
+void launch_adj_flux_rec_mixed(const DevCase&, const AdjCase&, int, const FluxRec&, cudaStream_t);
 void launch_adj_gather_mixed(const DevCase&, const AdjCase&, cudaStream_t);
 void launch_adj_cell_mixed(const DevCase&, const AdjCase&, double, double, int, cudaStream_t);
 
@@ -105,6 +107,15 @@ __global__ void __launch_bounds__(256) k_objective_grad(const DevCase c, const A
 void launch_adj_flux(const DevCase& c, const AdjCase& a, int flux, int recon, int precision, cudaStream_t s) {
     if (precision == PREC_MIXED) launch_adj_flux_mixed(c, a, flux, recon, s);
     else launch_adj_flux_fp64(c, a, flux, recon, s);
+}
+void launch_flux_rec(const DevCase& c, int recon, const FluxRec& r, int precision, cudaStream_t s) {
+    if (precision == PREC_MIXED) launch_flux_rec_mixed(c, recon, r, s);
+    else launch_flux_rec_fp64(c, recon, r, s);
+}
+void launch_adj_flux_rec(const DevCase& c, const AdjCase& a, int recon, const FluxRec& r, int precision,
+                         cudaStream_t s) {
+    if (precision == PREC_MIXED) launch_adj_flux_rec_mixed(c, a, recon, r, s);
+    else launch_adj_flux_rec_fp64(c, a, recon, r, s);
 }
 void launch_adj_gather(const DevCase& c, const AdjCase& a, int precision, cudaStream_t s) {
     if (precision == PREC_MIXED) launch_adj_gather_mixed(c, a, s);

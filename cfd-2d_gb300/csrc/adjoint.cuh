@@ -206,11 +206,11 @@ __device__ __forceinline__ float star_speed(float num, float den, float& iden) {
     return num / den;
 }
 
-// HLLC in the single-division star-flux form (flux_hllc in kernels.cuh)
+// HLLC in the single-division star-flux form (flux_hllc in kernels.cuh), with the forward's
+// sound speeds cL, cR given
 template <typename T>
-__device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
-                                         Prim<T>& Lb, Prim<T>& Rb) {
-    const T cL = hllc_sound(GAM * L.p, L.r), cR = hllc_sound(GAM * R.p, R.r);  // the forward's values
+__device__ __forceinline__ void vjp_hllc_c(const Prim<T>& L, const Prim<T>& R, T cL, T cR, T nx, T ny, T GAM, T IG1,
+                                           const T* fb, Prim<T>& Lb, Prim<T>& Rb) {
     const T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     const T EL = energy(L.r, L.u, L.v, L.p, IG1);
     const T ER = energy(R.r, R.u, R.v, R.p, IG1);
@@ -307,6 +307,13 @@ __device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T n
     }
 }
 
+template <typename T>
+__device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
+                                         Prim<T>& Lb, Prim<T>& Rb) {
+    const T cL = hllc_sound(GAM * L.p, L.r), cR = hllc_sound(GAM * R.p, R.r);  // the forward's values
+    vjp_hllc_c(L, R, cL, cR, nx, ny, GAM, IG1, fb, Lb, Rb);
+}
+
 template <int FLUX, typename T>
 __device__ __forceinline__ void vjp_flux(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
                                          Prim<T>& Lb, Prim<T>& Rb) {
@@ -338,6 +345,26 @@ __device__ __forceinline__ void vjp_reconstruct_a(const Prim<T>& q, const T* a, 
             if (mm_first(a[k], b)) { gb[2 * k] = madd(gb[2 * k], db, dx); gb[2 * k + 1] = madd(gb[2 * k + 1], db, dy); }
             else { nbv[k] += db; qbv[k] -= db; }
         }
+    }
+    qb.r += qbv[0]; qb.p += qbv[1]; qb.u += qbv[2]; qb.v += qbv[3];
+    nbb.r += nbv[0]; nbb.p += nbv[1]; nbb.u += nbv[2]; nbb.v += nbv[3];
+}
+
+// The same VJP with minmod's branches read from the forward's record (code: 2 bits per
+// variable r, p, u, v; 1 the projection, 2 the neighbour difference, 0 neither) instead
+// of being recomputed: the same operations on the same values.
+template <int RECON, typename T>
+__device__ __forceinline__ void vjp_reconstruct_code(unsigned code, T dx, T dy, const Prim<T>& pb, Prim<T>& qb,
+                                                     T* gb, Prim<T>& nbb) {
+    const T pv[4] = {pb.r, pb.p, pb.u, pb.v};
+    T qbv[4] = {acc0<T>(), acc0<T>(), acc0<T>(), acc0<T>()}, nbv[4] = {acc0<T>(), acc0<T>(), acc0<T>(), acc0<T>()};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const T db = pv[k];
+        qbv[k] += db;
+        const unsigned br = RECON == RECON_LINEAR ? 1u : (code >> (2 * k)) & 3u;
+        if (br == 1u) { gb[2 * k] = madd(gb[2 * k], db, dx); gb[2 * k + 1] = madd(gb[2 * k + 1], db, dy); }
+        else if (br == 2u) { nbv[k] += db; qbv[k] -= db; }
     }
     qb.r += qbv[0]; qb.p += qbv[1]; qb.u += qbv[2]; qb.v += qbv[3];
     nbb.r += nbv[0]; nbb.p += nbv[1]; nbb.u += nbv[2]; nbb.v += nbv[3];

@@ -550,8 +550,7 @@ __device__ __forceinline__ float hllc_sound(float a, float r) { return t_sqrt(a 
 // p* = p_K + rho_K (S_K - un_K)(S* - un_K): one division instead of Toro's star state.
 // FP64: c = hllc_sound(GAMMA p, rho), S* = hllc_quot, 1/(S_K - S*) = hllc_recip.
 template <typename T>
-__device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
-    T cL = hllc_sound(GAM * L.p, L.r), cR = hllc_sound(GAM * R.p, R.r);
+__device__ __forceinline__ void flux_hllc_c(T* f, const Prim<T>& L, const Prim<T>& R, T cL, T cR, T nx, T ny, T IG1) {
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     T EL = energy(L.r, L.u, L.v, L.p, IG1);
     T ER = energy(R.r, R.u, R.v, R.p, IG1);
@@ -572,6 +571,11 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
     f[1] = t_fma(Ss, t_fma(SK, K.r * K.u, -FK[1]), sp * nx) * inv;
     f[2] = t_fma(Ss, t_fma(SK, K.r * K.v, -FK[2]), sp * ny) * inv;
     f[3] = t_fma(Ss, t_fma(SK, EK, -FK[3]), sp * Ss) * inv;
+}
+template <typename T>
+__device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
+    const T cL = hllc_sound(GAM * L.p, L.r), cR = hllc_sound(GAM * R.p, R.r);
+    flux_hllc_c(f, L, R, cL, cR, nx, ny, IG1);
 }
 
 // Roe flux (Roe 1981) in the face-normal frame with the Harten-Hyman entropy fix
@@ -738,19 +742,29 @@ __device__ __forceinline__ T proj(T gx, T gy, T dx, T dy) {
 
 // dq = neighbour value minus own centre value per variable (minmod only; formed
 // once per edge: the two sides' differences are exact negatives of each other).
+// minmod's branch as a 2-bit code: 0 zero (the signs differ), 1 the projection, 2 the difference
+template <typename T>
+__device__ __forceinline__ unsigned mm_code(T a, T b) {
+    return mm_pos(a, b) ? (mm_first(a, b) ? 1u : 2u) : 0u;
+}
+// Returns minmod's branches for r, p, u, v (2 bits each, in that order; 0 without minmod),
+// which the adjoint's recorded path reads instead of recomputing them.
 template <typename T, int RECON>
-__device__ __forceinline__ void reconstruct(Prim<T>& q, const T* g, T dx, T dy, const Prim<T>& dq) {
+__device__ __forceinline__ unsigned reconstruct(Prim<T>& q, const T* g, T dx, T dy, const Prim<T>& dq) {
     T dr = proj<T, RECON>(g[0], g[1], dx, dy);
     T dp = proj<T, RECON>(g[2], g[3], dx, dy);
     T du = proj<T, RECON>(g[4], g[5], dx, dy);
     T dv = proj<T, RECON>(g[6], g[7], dx, dy);
+    unsigned code = 0;
     if (RECON == RECON_MINMOD) {
+        code = mm_code(dr, dq.r) | mm_code(dp, dq.p) << 2 | mm_code(du, dq.u) << 4 | mm_code(dv, dq.v) << 6;
         dr = minmod(dr, dq.r);
         dp = minmod(dp, dq.p);
         du = minmod(du, dq.u);
         dv = minmod(dv, dq.v);
     }
     q.r += dr; q.p += dp; q.u += du; q.v += dv;
+    return code;
 }
 
 // Edge flux over the edge's two Gauss points, times l/2 (src/methods/fvm_tvd.cpp:329-352).
@@ -773,9 +787,13 @@ __device__ __forceinline__ EdgeGeo<T> load_geo(const DevCase& c, int e) {
     return g;
 }
 
-template <typename T, int FLUX, int RECON>
+// With REC (HLLC only) the evaluation also leaves what the adjoint's recorded path reads
+// (FluxRec): per Gauss point the two face states and sound speeds, and minmod's branches.
+template <typename T, int FLUX, int RECON, bool REC = false>
 __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const Prim<T>& qL, const T* gL,
-                                          const Prim<T>& qR, const T* gR, T* out, const EdgeGeo<T>& geo) {
+                                          const Prim<T>& qR, const T* gR, T* out, const EdgeGeo<T>& geo,
+                                          const FluxRec& rec = FluxRec{}) {
+    static_assert(!REC || FLUX == FLUX_HLLC, "flux records are kept for HLLC");
     // qR: the second cell's primitives on interior edges (e < n_int), qL on boundary edges
     const T nx = geo.nx, ny = geo.ny, l = geo.l;
     const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
@@ -800,6 +818,7 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
     }
     T fs[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
     bool hit = false;
+    unsigned codes = 0;
 #pragma unroll
     for (int gp = 0; gp < 2; gp++) {
         Prim<T> pL = qL, pR;
@@ -809,30 +828,41 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
             dR.r = qL.r - qR.r; dR.u = qL.u - qR.u; dR.v = qL.v - qR.v; dR.p = qL.p - qR.p;
         }
         if (RECON != RECON_NONE)
-            reconstruct<T, RECON>(pL, gL, geo.dl[4 * gp], geo.dl[4 * gp + 1], dL);
+            codes |= reconstruct<T, RECON>(pL, gL, geo.dl[4 * gp], geo.dl[4 * gp + 1], dL) << (16 * gp);
         if (inner) {
             pR = qR;
             if (RECON != RECON_NONE)
-                reconstruct<T, RECON>(pR, gR, geo.dl[4 * gp + 2], geo.dl[4 * gp + 3], dR);
+                codes |= reconstruct<T, RECON>(pR, gR, geo.dl[4 * gp + 2], geo.dl[4 * gp + 3], dR) << (16 * gp + 8);
         } else {
             pR = ghost_state(b, pL, Tc, nx, ny, M);
         }
         T f[4];
-        hit |= num_flux<T, FLUX>(f, pL, pR, nx, ny, GAM, IG1, c.newton_cap, c.rg_flux);
+        if constexpr (REC) {
+            const T cL = hllc_sound(GAM * pL.p, pL.r), cR = hllc_sound(GAM * pR.p, pR.r);
+            T* v = static_cast<T*>(rec.v) + (size_t)(10 * gp) * c.ne + e;
+            const size_t ne = c.ne;
+            v[0] = pL.r; v[ne] = pL.u; v[2 * ne] = pL.v; v[3 * ne] = pL.p;
+            v[4 * ne] = pR.r; v[5 * ne] = pR.u; v[6 * ne] = pR.v; v[7 * ne] = pR.p;
+            v[8 * ne] = cL; v[9 * ne] = cR;
+            flux_hllc_c(f, pL, pR, cL, cR, nx, ny, IG1);
+        } else {
+            hit |= num_flux<T, FLUX>(f, pL, pR, nx, ny, GAM, IG1, c.newton_cap, c.rg_flux);
+        }
         fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
         if (RECON == RECON_NONE) {  // both Gauss points see the cell-centre states
             fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
             break;
         }
     }
+    if constexpr (REC) rec.bits[e] = codes;
     if (hit) atomicOr(c.err, ERRBIT_NEWTON_CAP);
     const T lh = l * T(0.5);
     out[0] = fs[0] * lh; out[1] = fs[1] * lh; out[2] = fs[2] * lh; out[3] = fs[3] * lh;
 }
 
-// The flux of edge e (what F holds for it) from the stage's W and G.
-template <typename T, int FLUX, int RECON>
-__device__ __forceinline__ void flux_edge(const DevCase& c, int e, T* out) {
+// The flux of edge e (what F holds for it) from the stage's W and G (with REC: and its record).
+template <typename T, int FLUX, int RECON, bool REC = false>
+__device__ __forceinline__ void flux_edge(const DevCase& c, int e, T* out, const FluxRec& rec = FluxRec{}) {
     const T* __restrict__ W = W_of<T>(c);
     const T* __restrict__ G = G_of<T>(c);
     const int c1 = ldcs(c.ec1 + e);
@@ -846,7 +876,7 @@ __device__ __forceinline__ void flux_edge(const DevCase& c, int e, T* out) {
         qR = load_prim(W, c2);
         if (RECON != RECON_NONE) ld8(G, c2, gR);
     }
-    flux_core<T, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e));
+    flux_core<T, FLUX, RECON, REC>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e), rec);
 }
 
 template <typename T, int FLUX, int RECON>

@@ -75,6 +75,15 @@ __host__ __device__ __forceinline__ RimGas<T> rim_gas(T GAM) {
 // thread per item; otherwise a persistent grid that strides over the items).
 // Default: 64-thread blocks, one thread per item (measured best for the single
 // four-quadrant workload in both precisions; the autotuner can override it).
+// What a forward HLLC flux evaluation leaves for the adjoint's recorded path, per edge (SoA,
+// face precision): v[(10 g + j) ne + e] for Gauss point g, j 0-3 the left face state (r, u,
+// v, p), 4-7 the right one, 8-9 the left and right sound speeds; bits[e] minmod's branches
+// (2 bits per variable r, p, u, v; 8 bits per side, left then right; 16 per Gauss point).
+struct FluxRec {
+    void* v = nullptr;
+    unsigned* bits = nullptr;
+};
+
 struct LaunchShape { int block = 64, grid = 0; };
 enum { KIND_GRAD = 0, KIND_FLUX = 1, KIND_UPDATE = 2, N_TUNED_KINDS = 3 };
 
@@ -210,6 +219,10 @@ struct AdjCase {
 
 // precision: PREC_FP64 (FP64 faces) or PREC_MIXED (FP32 faces, FP64 per-cell sums)
 void launch_adj_flux(const DevCase& c, const AdjCase& a, int flux, int recon, int precision, cudaStream_t s);
+// HLLC only: the forward flux of a recomputed stage with its record, and the flux VJP reading it
+void launch_flux_rec(const DevCase& c, int recon, const FluxRec& r, int precision, cudaStream_t s);
+void launch_adj_flux_rec(const DevCase& c, const AdjCase& a, int recon, const FluxRec& r, int precision,
+                         cudaStream_t s);
 void launch_adj_gather(const DevCase& c, const AdjCase& a, int precision, cudaStream_t s);
 void launch_adj_cell(const DevCase& c, const AdjCase& a, double coef_t, double coef_acc, int first, int precision,
                      cudaStream_t s);

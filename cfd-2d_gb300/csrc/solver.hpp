@@ -119,7 +119,7 @@ private:
     // free one dalloc'd buffer (after the stream is idle) and forget it
     void release(void* p, size_t bytes);
     void adjoint_setup();
-    void record_step(double* store, void* wg);
+    void record_step(double* store, void* wg, int rec_slot = -1);
     void record_segment(int n);
     void drop_record_graphs();
     // captured recording segments: (n, (graph, store kind 0 states / 1 W / 2 W and G))
@@ -147,6 +147,11 @@ private:
     size_t wg_slots_ = 0;         // doubles allocated in wgstore_
     bool store_wg_ = false;       // the recorded stages' W are kept
     bool store_g_ = false;        // ... and their G
+    bool store_rec_ = false;      // ... and their HLLC flux records (FluxRec per stage)
+    char* recstore_ = nullptr;    // per recorded stage: rec_stage_bytes() bytes
+    size_t rec_bytes_ = 0;        // bytes allocated in recstore_
+    size_t rec_stage_bytes() const;
+    FluxRec rec_at(size_t slot) const;
     size_t ckpt_slots_ = 0, seg_slots_ = 0;
     int fw_steps_ = 0, fw_k_ = 0;
     bool last_recorded_ = false;  // forward() left the last segment's stages in the store

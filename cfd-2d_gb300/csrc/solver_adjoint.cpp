@@ -101,32 +101,49 @@ double Solver::forward(int nsteps, int k, int* status) {
     // checkpoints and this store) at most the budget.
     store_wg_ = false;
     store_g_ = false;
+    store_rec_ = false;
     {
         const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
         const size_t dbl = sizeof(double);
         const size_t need = ((size_t)k * nst * 12 * nc * fsize + dbl - 1) / dbl;   // W and G, in doubles
         const size_t need_w = ((size_t)k * nst * 4 * nc * fsize + dbl - 1) / dbl;  // W
         const size_t need_x = (size_t)k * nst * 4 * nc;                            // FP64 states
+        const size_t need_rec = (size_t)k * nst * rec_stage_bytes();              // HLLC flux records, bytes
         size_t free_b = 0, total_b = 0;
         CUDA_CHECK(cudaMemGetInfo(&free_b, &total_b));
-        const size_t have = wg_slots_ * dbl + seg_slots_ * 4 * nc * dbl;  // reusable if released
-        const size_t base = bytes_ - std::min(bytes_, have);             // everything but the store
+        const size_t have = wg_slots_ * dbl + seg_slots_ * 4 * nc * dbl + rec_bytes_;  // reusable if released
+        const size_t base = bytes_ - std::min(bytes_, have);                        // everything but the store
         const double budget = task_.adj_memory;
         auto in_budget = [&](size_t bytes) { return budget <= 0.0 || (double)(base + bytes) <= budget; };
+        auto fits_bytes = [&](size_t bytes) { return bytes <= (free_b + have) / 10 * 8 && in_budget(bytes); };
         auto fits = [&](size_t doubles) {
             return (doubles <= wg_slots_ || doubles * dbl <= (free_b + have) / 10 * 8) && in_budget(doubles * dbl);
         };
         if (!in_budget(std::min(need_w, need_x) * dbl))
             throw Error(CFD2D_ERR_CAPACITY, "the adjoint's smallest segment store exceeds ADJOINT_MEMORY");
         const int mode = task_.adj_store;
-        if (mode == 2 || (mode < 0 && fits(need))) {
+        const bool rec_ok = task_.flux == FLUX_HLLC;
+        if (rec_ok && (mode == 3 || (mode < 0 && fits_bytes(need * dbl + need_rec)))) {
+            store_wg_ = store_g_ = store_rec_ = true;
+        } else if (mode >= 2 || (mode < 0 && fits(need))) {
             store_wg_ = store_g_ = true;
         } else if (mode == 1 || (mode < 0 && fits(need_w))) {
             store_wg_ = true;
         }
         const size_t want = store_g_ ? need : (store_wg_ ? need_w : 0);
-        if ((store_wg_ && segstore_) || want > wg_slots_ || (!store_wg_ && (size_t)k * nst > seg_slots_))
+        const size_t want_rec = store_rec_ ? need_rec : 0;
+        if ((store_wg_ && segstore_) || want > wg_slots_ || (!store_wg_ && (size_t)k * nst > seg_slots_) ||
+            want_rec > rec_bytes_ || (!store_rec_ && recstore_))
             drop_record_graphs();  // the store moves: graphs captured on it are stale
+        if (recstore_ && (!store_rec_ || want_rec > rec_bytes_)) {
+            release(recstore_, rec_bytes_);
+            recstore_ = nullptr;
+            rec_bytes_ = 0;
+        }
+        if (store_rec_ && !recstore_) {
+            recstore_ = dalloc<char>(want_rec);
+            rec_bytes_ = want_rec;
+        }
         if (store_wg_ && segstore_) {  // the states are not kept: give their memory back first
             release(segstore_, seg_slots_ * 4 * nc * dbl);
             segstore_ = nullptr;
@@ -185,21 +202,38 @@ void Solver::drop_record_graphs() {
 
 // n forward steps that keep every stage in the segment store (what the backward sweep
 // reads), captured once per n into a CUDA graph and replayed.
+size_t Solver::rec_stage_bytes() const {
+    const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
+    const size_t b = (size_t)dc_.ne * (20 * fsize + sizeof(unsigned));
+    return (b + 255) / 256 * 256;
+}
+
+FluxRec Solver::rec_at(size_t slot) const {
+    const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
+    FluxRec r;
+    char* v = recstore_ + slot * rec_stage_bytes();
+    r.v = v;
+    r.bits = reinterpret_cast<unsigned*>(v + (size_t)dc_.ne * 20 * fsize);
+    return r;
+}
+
 void Solver::record_segment(int n) {
     const size_t nc = dc_.nc;
     const int nst = n_stages(task_.scheme);
     const size_t fsize = task_.precision == PREC_MIXED ? sizeof(float) : sizeof(double);
     const size_t per_stage = (store_g_ ? 12 : 4) * nc * fsize;
+    const int kind = store_rec_ ? 3 : (store_wg_ ? (store_g_ ? 2 : 1) : 0);
     cudaGraphExec_t exec = nullptr;
     for (auto& g : rec_graphs_)
-        if (g.first == n && g.second.second == (store_wg_ ? (store_g_ ? 2 : 1) : 0)) exec = g.second.first;
+        if (g.first == n && g.second.second == kind) exec = g.second.first;
     if (!exec) {
         cudaGraph_t graph = nullptr;
         CUDA_CHECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
         try {
             for (int j = 0; j < n; j++)
                 record_step(store_wg_ ? nullptr : segstore_ + (size_t)j * nst * 4 * nc,
-                            store_wg_ ? reinterpret_cast<char*>(wgstore_) + (size_t)j * nst * per_stage : nullptr);
+                            store_wg_ ? reinterpret_cast<char*>(wgstore_) + (size_t)j * nst * per_stage : nullptr,
+                            j * nst);
         } catch (...) {
             cudaStreamEndCapture(stream_, &graph);
             if (graph) cudaGraphDestroy(graph);
@@ -209,15 +243,16 @@ void Solver::record_segment(int n) {
         const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         CUDA_CHECK(e);
-        rec_graphs_.push_back({n, {exec, store_wg_ ? (store_g_ ? 2 : 1) : 0}});
+        rec_graphs_.push_back({n, {exec, kind}});
     }
     CUDA_CHECK(cudaGraphLaunch(exec, stream_));
 }
 
 // One forward step that keeps, when given, every stage's input state in
 // store[stage] or the stage's primitives (and, with store_g_, gradients) in the
-// face precision in wg[stage] (12 or 4 nc values per stage).
-void Solver::record_step(double* store, void* wg) {
+// face precision in wg[stage] (12 or 4 nc values per stage), and with store_rec_ each
+// stage's HLLC flux record in the record slot rec_slot + stage.
+void Solver::record_step(double* store, void* wg, int rec_slot) {
     const size_t nc = dc_.nc;
     const int nst = n_stages(task_.scheme);
     const int p = task_.precision;
@@ -236,7 +271,12 @@ void Solver::record_step(double* store, void* wg) {
                 CUDA_CHECK(cudaMemcpyAsync(w + 4 * nc * fsize, G, fsize * 8 * nc, cudaMemcpyDeviceToDevice,
                                            stream_));
         }
-        launch_flux(dc_, p, task_.flux, task_.recon, stream_);
+        if (store_rec_ && rec_slot >= 0) {
+            const FluxRec r = rec_at((size_t)rec_slot + st);
+            launch_flux_rec(dc_, task_.recon, r, p, stream_);
+        } else {
+            launch_flux(dc_, p, task_.flux, task_.recon, stream_);
+        }
         launch_update(dc_, p, task_.scheme, st, stream_);
     }
     launch_remediate(dc_, p, stream_);
@@ -285,7 +325,7 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
             launch_prims(dc_, task_.precision, stream_);
             for (int j = 0; j < n; j++)
                 record_step(store_wg_ ? nullptr : segstore_ + (size_t)j * nst * 4 * nc,
-                            store_wg_ ? wg_at(j * nst) : nullptr);
+                            store_wg_ ? wg_at(j * nst) : nullptr, j * nst);
         }
         for (int j = n - 1; j >= 0; j--) {
             // every later step is started by the stage-0 kernel of the step after it
@@ -307,7 +347,8 @@ void Solver::backward(double* dJdU0, double* dJdbnd) {
                     launch_prims(cx, p, stream_);
                     if (task_.recon != RECON_NONE) launch_grad(cx, p, stream_);
                 }
-                launch_adj_flux(cx, a, task_.flux, task_.recon, p, stream_);
+                if (store_rec_) launch_adj_flux_rec(cx, a, task_.recon, rec_at((size_t)j * nst + st), p, stream_);
+                else launch_adj_flux(cx, a, task_.flux, task_.recon, p, stream_);
                 launch_adj_gather(cx, a, p, stream_);
                 double ct = ct_f, ca = ca_f;
                 if (st > 0) stage_coefs(task_.scheme, st, ct, ca);

@@ -33,7 +33,8 @@ struct TaskConfig {
     int reorder = -1;         // cell order: 0 file order, 1 RCM, 2 Hilbert; -1: RCM (Hilbert with the fused stage)
     int fused = -1;           // mixed form, SSP-RK3 / Heun: 1 one tiled kernel per stage (gradients, fluxes,
                               // update), 2 gradients then one tiled flux-and-update kernel per stage
-    int adj_store = -1;       // adjoint segment store: 0 states only, 1 + primitives, 2 + gradients, -1 by memory
+    int adj_store = -1;       // adjoint segment store: 0 states only, 1 + primitives, 2 + gradients,
+                              // 3 + HLLC flux records, -1 by memory
     double adj_memory = 0.0;  // device-memory budget of the handle for the adjoint (bytes; 0: 80% of the free memory)
     int newton_cap = 100;     // iteration cap of the exact Riemann solver
     int flux_pipe = 1;        // mixed form: the software-pipelined flux kernel (0: one thread per edge)

@@ -202,13 +202,15 @@ def test_combined_mixed_adjoint_within_memory_budget(capi, tmp_path):
 
 @pytest.mark.parametrize("precision", [None, "MIXED"])
 def test_adjoint_store_modes_give_the_same_gradient(capi, tmp_path, precision):
-    """Recorded stages keep their states only, their primitives too, or primitives and
-    gradients: whatever is not kept is re-derived by the forward's own kernels, so the
-    gradient is the same bit for bit."""
+    """Recorded stages keep their states only, their primitives too, primitives and
+    gradients, or these and the HLLC flux evaluations' records (face states, sound speeds,
+    minmod's branches): whatever is not kept is re-derived by the forward's own kernels,
+    and the recorded values are the ones they re-derive, so the gradient is the same bit
+    for bit."""
     t, m, U0, w, _ = cases.vortex_adjoint(32, steps=9)
     t.precision = precision
     grads = []
-    for mode in ("NONE", "PRIMITIVES", "ALL"):
+    for mode in ("NONE", "PRIMITIVES", "ALL", "FLUXES"):
         t.adjoint_store = mode
         d = tmp_path / mode
         d.mkdir()
