@@ -174,12 +174,17 @@ __device__ __forceinline__ float neg_if(float x, bool s) { return __int_as_float
 // x * 0.5 (exact halving, the correctly rounded x / 2): for normal x above the smallest
 // binade a decrement of the exponent field on the integer pipe, zeros unchanged; the rest
 // (subnormal results, inf, NaN) through the FP64 multiply. Bit for bit x * 0.5.
+// Below the smallest normal binade the magnitude bits halve with round-half-even (one
+// bit is dropped, so a dropped 1 is a tie), which is the IEEE result there too; inf and
+// NaN are returned as they are. Integer operations only.
 __device__ __forceinline__ double half_exact(double x) {
     const long long b = __double_as_longlong(x);
-    const int e = (int)((b >> 52) & 0x7ff);
+    const long long mag = b & 0x7fffffffffffffffll;
+    const int e = (int)(mag >> 52);
     if (e > 1 && e < 0x7ff) return __longlong_as_double(b - (1ll << 52));
-    if ((b & 0x7fffffffffffffffll) == 0) return x;
-    return x * 0.5;
+    if (e == 0x7ff) return x;
+    const long long m = (mag >> 1) + ((mag & 1) & ((mag >> 1) & 1));
+    return __longlong_as_double((b & (long long)0x8000000000000000ull) | m);
 }
 __device__ __forceinline__ float half_exact(float x) { return x * 0.5f; }
 // a / b given y = RN(1/b): the correctly rounded quotient in FP64, a * y in the FP32 faces.
@@ -272,14 +277,15 @@ __device__ __forceinline__ Prim<T> ghost_state(const DevBnd& b, const Prim<T>& q
 // the sign of its bits (positive, non-NaN doubles are exactly the patterns in
 // (0, 0x7ff0...0]). mm_first is |a| < |b| on magnitude bits, which orders non-NaN
 // values like fabs does. Bit for bit the reference's result.
+static __device__ __noinline__ double mul_outright(double a, double b) { return a * b; }
 __device__ __forceinline__ bool mm_pos(double a, double b) {
     const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
     const long long ma = ia & 0x7fffffffffffffffll, mb = ib & 0x7fffffffffffffffll;
     if (ma == 0 || mb == 0) return false;
     const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
-    if (ea >= 1 && eb >= 1 && ea + eb >= 972)
+    if (__builtin_expect(ea >= 1 && eb >= 1 && ea + eb >= 972, 1))
         return (ia ^ ib) >= 0 && ma <= 0x7ff0000000000000ll && mb <= 0x7ff0000000000000ll;
-    const long long pb = __double_as_longlong(a * b);
+    const long long pb = __double_as_longlong(mul_outright(a, b));  // a branch, not a predicated multiply
     return pb > 0 && pb <= 0x7ff0000000000000ll;
 }
 __device__ __forceinline__ bool mm_first(double a, double b) {
@@ -509,9 +515,13 @@ __device__ __forceinline__ double hllc_rcp1(double b) {
 }
 // a / b: one Newton step for 1/b, then q = a y corrected once (|a|, |b| in range; a = 0
 // gives the IEEE signed zero)
+// (the IEEE fallbacks sit in functions of their own so that the compiler branches to them
+// instead of issuing them, predicated off, beside the common path)
+static __device__ __noinline__ double recip_outright(double b) { return 1.0 / b; }
+static __device__ __noinline__ double sound_outright(double a, double r) { return sqrt(a / r); }
 __device__ __forceinline__ double hllc_quot(double a, double b) {
     if (hllc_in_range(b)) {
-        if (hllc_in_range(a)) {
+        if (__builtin_expect(hllc_in_range(a), 1)) {
             const double y = hllc_rcp1(b);
             const double q = a * y;
             return fma(fma(-q, b, a), y, q);
@@ -520,12 +530,12 @@ __device__ __forceinline__ double hllc_quot(double a, double b) {
         if ((ia & 0x7fffffffffffffffll) == 0)
             return __longlong_as_double((ia ^ __double_as_longlong(b)) & (long long)0x8000000000000000ull);
     }
-    return a / b;
+    return div_outright(a, b);
 }
 __device__ __forceinline__ float hllc_quot(float a, float b) { return a / b; }
 // 1/b: two Newton steps
 __device__ __forceinline__ double hllc_recip(double b) {
-    if (!hllc_in_range(b)) return 1.0 / b;
+    if (__builtin_expect(!hllc_in_range(b), 0)) return recip_outright(b);
     const double y = hllc_rcp1(b);
     return fma(y, fma(-b, y, 1.0), y);
 }
@@ -533,7 +543,8 @@ __device__ __forceinline__ float hllc_recip(float b) { return 1.0f / b; }
 // sqrt(a / r) for a = GAMMA p, r the density (both positive and in range): s0 and
 // h = 1/(2 r s0) from binary32, then two steps s <- s + (a - (r s) s) h
 __device__ __forceinline__ double hllc_sound(double a, double r) {
-    if (!(a > 0.0) || !(r > 0.0) || !hllc_in_range(a) || !hllc_in_range(r)) return sqrt(a / r);
+    const long long ia = __double_as_longlong(a), ir = __double_as_longlong(r);
+    if (__builtin_expect(ia < 0 || ir < 0 || !hllc_in_range(a) || !hllc_in_range(r), 0)) return sound_outright(a, r);
     const float af = hllc_seed(a), rf = hllc_seed(r);
     const float sf = __fsqrt_rn(__fdiv_rn(af, rf));
     const double h = widen(__fdiv_rn(0.5f, __fmul_rn(rf, sf)));
