@@ -65,6 +65,18 @@ void fu_by_recon(const DevCase& c, const DevTiles& t, int recon, int scheme, int
 }
 }  // namespace
 
+void launch_flux_grad_mixed(const DevCase& c, int flux, int recon, cudaStream_t s) {
+    const int g = (c.ne + 255) / 256;
+    auto go = [&](auto kern) { kern<<<g, 256, 0, s>>>(c); };
+    const bool mm = recon == RECON_MINMOD;
+    switch (flux) {
+    case FLUX_LAX: mm ? go(k_flux_grad<FLUX_LAX, RECON_MINMOD>) : go(k_flux_grad<FLUX_LAX, RECON_LINEAR>); break;
+    case FLUX_ROE: mm ? go(k_flux_grad<FLUX_ROE, RECON_MINMOD>) : go(k_flux_grad<FLUX_ROE, RECON_LINEAR>); break;
+    case FLUX_HLLC: mm ? go(k_flux_grad<FLUX_HLLC, RECON_MINMOD>) : go(k_flux_grad<FLUX_HLLC, RECON_LINEAR>); break;
+    default: mm ? go(k_flux_grad<FLUX_GODUNOV, RECON_MINMOD>) : go(k_flux_grad<FLUX_GODUNOV, RECON_LINEAR>); break;
+    }
+}
+
 // The mixed form's flux and update of one stage per tile (k_flux_update); the stage's
 // primitives are c.W32, its gradients c.G32, the new primitives go to w_out.
 void launch_flux_update_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,

@@ -1261,6 +1261,50 @@ __global__ void __launch_bounds__(256, 5) k_stage_fused(const DevCase c, const D
     cp_async_wait<0>();
 }
 
+// Gradient of cell i (FP32 faces) from its three 16-byte face records: the operations of
+// grad_one on the same values.
+__device__ __forceinline__ void grad_of_cell(const DevCase& c, int i, const Prim<float>& q, float* g) {
+    const float4* __restrict__ rec = c.cfrec32 + 3 * (size_t)i;
+    const float* __restrict__ W = c.W32;
+#pragma unroll
+    for (int m = 0; m < 8; m++) g[m] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float4 r = __ldg(rec + k);
+        const int nb = __float_as_int(r.x);
+        const float nx = r.y, ny = r.z, l = r.w;
+        const bool side2 = nb >= 0 && (nb & 1);
+        const Prim<float> o = nb >= 0 ? load_prim(W, nb >> 1) : grad_ghost(c, i, -(nb + 1), q, nx, ny);
+        grad_face(g, q, o, nx, ny, l, side2);
+    }
+    grad_finish(c, i, g);
+}
+
+// The mixed form's edge flux with the two cells' Green-Gauss gradients formed in the
+// kernel (each cell's once per edge it borders, from the stage's W and the cells' face
+// records) instead of read from G: no gradient array written and read back, no gradient
+// launch. The same operations on the same values as k_grad + k_flux, so the same fluxes.
+template <int FLUX, int RECON>
+__global__ void __launch_bounds__(256) k_flux_grad(const DevCase c) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= c.ne) return;
+    const float* __restrict__ W = c.W32;
+    const int c1 = ldcs(c.ec1 + e);
+    const bool inner = e < c.n_int;
+    const Prim<float> qL = load_prim(W, c1);
+    float gL[8], gR[8];
+    grad_of_cell(c, c1, qL, gL);
+    Prim<float> qR = qL;
+    if (inner) {
+        const int c2 = ldcs(c.ec2 + e);
+        qR = load_prim(W, c2);
+        grad_of_cell(c, c2, qR, gR);
+    }
+    float out[4];
+    flux_core<float, FLUX, RECON>(c, e, c1, qL, gL, qR, gR, out, load_geo<float, RECON>(c, e));
+    st4(c.F32, e, out[0], out[1], out[2], out[3]);
+}
+
 // The mixed form's flux and update of one stage per tile of cells (one CTA of 256 threads
 // per tile): the fluxes of every edge of the tile's own cells (from the stage's W in
 // c.W32 and the gradients k_grad left in c.G32, read through the caches) go into shared

@@ -128,6 +128,7 @@ struct DevCase {
     float ig1_flux_f;      // 1/(gam_flux - 1) in FP32
     float lim_f[5];        // limits in FP32 (mixed form)
     const float* invS32;   // nc, 1/S in FP32 (mixed form)
+    const float4* cfrec32; // 3*nc (mixed form): per cell and face {cf_nb bits, nx, ny, l} in one 16-byte record
     double gam_flux;
     double ig1_flux;       // RN(1/(gam_flux - 1)), computed on the host
     RimGas<double> rg_flux;  // the exact Riemann solver's constants of gam_flux
@@ -197,6 +198,8 @@ struct DevTiles {
     const int2* gface = nullptr;     // per gradient cell and face: x = (edge << 1) | side,
                                      // y = local neighbour (0xffff: boundary) | local flux edge << 16 (own cells)
 };
+// the mixed form's flux kernel that forms its two cells' gradients itself (no G array)
+void launch_flux_grad_mixed(const DevCase& c, int flux, int recon, cudaStream_t s);
 void launch_flux_update_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,
                               float* w_out, cudaStream_t s);
 void launch_stage_fused_mixed(const DevCase& c, const DevTiles& t, int flux, int recon, int scheme, int stage,

@@ -68,7 +68,8 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
     const int nc = topo_.nc;
     cell_mat_.resize(nc);
     for (int i = 0; i < nc; i++) cell_mat_[i] = task_.regions[cell_region[i]].matId;
-    const int order = task_.reorder >= 0 ? task_.reorder : (task_.fused >= 1 ? ORDER_HILBERT : ORDER_RCM);
+    const int order = task_.reorder >= 0 ? task_.reorder
+                                         : (task_.fused == 1 || task_.fused == 2 ? ORDER_HILBERT : ORDER_RCM);
     lay_ = make_layout(topo_, cell_mat_, edge_bnd, order);
     const int ne = lay_.ne;
     CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
@@ -95,6 +96,15 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
             c.cf_nb = upload(nb);
             if (mixed) {
                 c.cf_nx32 = upload(to_f32(fx)); c.cf_ny32 = upload(to_f32(fy)); c.cf_l32 = upload(to_f32(fl));
+                std::vector<float4> rec(3 * (size_t)nc);
+                for (int i = 0; i < nc; i++)
+                    for (int k = 0; k < 3; k++) {
+                        const size_t q = (size_t)k * nc + i;
+                        float nbf;
+                        std::memcpy(&nbf, &nb[q], sizeof nbf);
+                        rec[3 * (size_t)i + k] = make_float4(nbf, (float)fx[q], (float)fy[q], (float)fl[q]);
+                    }
+                c.cfrec32 = upload(rec);
             } else {
                 c.cf_nx = upload(fx); c.cf_ny = upload(fy); c.cf_l = upload(fl);
             }
@@ -298,7 +308,11 @@ void Solver::enqueue_step(cudaEvent_t* ev, int* kinds, int* nev) {
         return;
     }
     for (int st = 0; st < nst; st++) {
-        if (gauss_points_ == 0) {  // 1-point edges: the Gauss-point loop is empty, no flux
+        if (fused_ == 3) {  // the flux kernel forms the gradients it needs
+            mark(1, true);
+            launch_flux_grad_mixed(dc_, task_.flux, task_.recon, stream_);
+            mark(1, false);
+        } else if (gauss_points_ == 0) {  // 1-point edges: the Gauss-point loop is empty, no flux
             size_t b = 4 * (size_t)dc_.ne * (p == PREC_MIXED ? sizeof(float) : sizeof(double));
             CUDA_CHECK(cudaMemsetAsync(p == PREC_MIXED ? (void*)dc_.F32 : (void*)dc_.F64, 0, b, stream_));
         } else {

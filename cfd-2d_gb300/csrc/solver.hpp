@@ -170,7 +170,8 @@ private:
     // mixed form, SSP-RK3 / Heun: tiles for the fused stage kernel (solver_tiles.cpp)
     void build_tiles();
     DevTiles tiles_{};
-    int fused_ = 0;  // 0 per-kernel stages, 1 one tiled kernel per stage, 2 gradients + tiled flux-and-update
+    int fused_ = 0;  // 0 per-kernel stages, 1 one tiled kernel per stage, 2 gradients + tiled flux-and-update,
+                     // 3 per-kernel stages whose flux kernel forms the gradients
     float* wrot_[3] = {nullptr, nullptr, nullptr};  // primitives rotated through the stages; wrot_[0] == dc_.W32
     void compute_tau();
     void enqueue_step(cudaEvent_t* ev = nullptr, int* kinds = nullptr, int* nev = nullptr);

@@ -29,6 +29,10 @@ struct TileLists {
 
 void Solver::build_tiles() {
     fused_ = 0;
+    if (task_.precision == PREC_MIXED && task_.fused == 3 && gauss_points_ != 0 && task_.recon != RECON_NONE) {
+        fused_ = 3;  // gradients formed in the flux kernel: no tiles
+        return;
+    }
     const bool applies = task_.precision == PREC_MIXED && task_.fused >= 1 && gauss_points_ != 0 &&
                          (task_.scheme == TIME_SSPRK3 || task_.scheme == TIME_HEUN);
     if (!applies) return;

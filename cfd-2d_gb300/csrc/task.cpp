@@ -287,7 +287,8 @@ TaskConfig parse_task(const std::string& path) {
     t.scheme = pick(ctl, "TIME_SCHEME", {{"EULER", TIME_EULER}, {"HEUN", TIME_HEUN}, {"SSPRK3", TIME_SSPRK3}}, TIME_HEUN);
     t.precision = pick(ctl, "PRECISION", {{"FP64", PREC_FP64}, {"MIXED", PREC_MIXED}}, PREC_FP64);
     t.reorder = pick(ctl, "REORDER", {{"NONE", 0}, {"RCM", 1}, {"HILBERT", 2}}, -1);
-    t.fused = pick(ctl, "FUSED_STAGE", {{"0", 0}, {"1", 1}, {"2", 2}, {"OFF", 0}, {"ON", 1}, {"FLUX_UPDATE", 2}}, -1);
+    t.fused = pick(ctl, "FUSED_STAGE", {{"0", 0}, {"1", 1}, {"2", 2}, {"3", 3}, {"OFF", 0}, {"ON", 1},
+                                        {"FLUX_UPDATE", 2}, {"GRAD_IN_FLUX", 3}}, -1);
     t.adj_store = pick(ctl, "ADJOINT_STORE",
                        {{"AUTO", -1}, {"NONE", 0}, {"PRIMITIVES", 1}, {"ALL", 2}, {"FLUXES", 3}}, -1);
     if (const XmlNode* n = ctl->child("ADJOINT_MEMORY")) t.adj_memory = attr_d(n, "value");

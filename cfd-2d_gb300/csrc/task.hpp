@@ -32,7 +32,8 @@ struct TaskConfig {
     int flux = FLUX_GODUNOV, recon = RECON_LINEAR, scheme = TIME_HEUN, precision = PREC_FP64;
     int reorder = -1;         // cell order: 0 file order, 1 RCM, 2 Hilbert; -1: RCM (Hilbert with the fused stage)
     int fused = -1;           // mixed form, SSP-RK3 / Heun: 1 one tiled kernel per stage (gradients, fluxes,
-                              // update), 2 gradients then one tiled flux-and-update kernel per stage
+                              // update), 2 gradients then one tiled flux-and-update kernel per stage,
+                              // 3 the flux kernel forms the two cells' gradients (no gradient kernel)
     int adj_store = -1;       // adjoint segment store: 0 states only, 1 + primitives, 2 + gradients,
                               // 3 + HLLC flux records, -1 by memory
     double adj_memory = 0.0;  // device-memory budget of the handle for the adjoint (bytes; 0: 80% of the free memory)

@@ -1,7 +1,8 @@
 """The mixed form's tiled stage kernels against the same form on its per-kernel path:
 FUSED_STAGE 1 (gradients, fluxes and update of a tile of cells in one launch, from
-shared memory) and FUSED_STAGE 2 (the per-kernel gradients, then the fluxes of a tile's
-edges in shared memory and its cells' update in one launch). Identical inputs and
+shared memory), FUSED_STAGE 2 (the per-kernel gradients, then the fluxes of a tile's
+edges in shared memory and its cells' update in one launch) and FUSED_STAGE 3 (the flux
+kernel forms its two cells' gradients; no gradient kernel). Identical inputs and
 identical arithmetic, so identical bits."""
 import numpy as np
 import pytest
@@ -11,7 +12,7 @@ from cfd2d import cases
 pytestmark = pytest.mark.gpu
 
 
-MODES = ("1", "2")
+MODES = ("1", "2", "3")
 
 
 def _pair(capi, tmp_path, t, m, U0=None, mode="1", **kw):
@@ -33,8 +34,10 @@ def _pair(capi, tmp_path, t, m, U0=None, mode="1", **kw):
 
 def _is_fused(s, mode="1"):
     """Profile one step (it is taken): the tiled paths launch no separate update kernel, FUSED_STAGE 1
-    no separate gradient kernel either."""
+    no separate gradient kernel either; FUSED_STAGE 3 no gradient kernel but its update kernel."""
     ms, cnt = s.profile_steps(1)
+    if mode == "3":
+        return cnt[0] == 0 and cnt[1] > 0 and cnt[2] > 0
     return (cnt[0] == 0 or mode == "2") and cnt[2] == 0 and cnt[1] > 0
 
 
@@ -46,7 +49,8 @@ def test_fused_equals_per_kernel_vortex(capi, tmp_path, flux, recon, scheme, mod
     kinds = ("BOUND_INLET", "BOUND_OUTLET", "BOUND_WALL_SLIP", "BOUND_WALL_NO_SLIP")
     t, m, U0 = cases.vortex(96, flux=flux, recon=recon, scheme=scheme, steps=12, bnd_kinds=kinds)
     a, b = _pair(capi, tmp_path, t, m, U0, mode=mode)
-    assert not _is_fused(a, mode) and _is_fused(b, mode)
+    # without reconstruction there are no gradients to form: FUSED_STAGE 3 keeps the per-kernel path
+    assert _is_fused(b, mode) != (mode == "3" and recon == "NONE")
     a.step(12)
     b.step(12)
     assert np.array_equal(a.state(), b.state())
