@@ -171,22 +171,6 @@ __device__ __forceinline__ double neg_if(double x, bool s) {
     return __hiloint2double(__double2hiint(x) ^ (s ? (int)0x80000000 : 0), __double2loint(x));
 }
 __device__ __forceinline__ float neg_if(float x, bool s) { return __int_as_float(__float_as_int(x) ^ (s ? (int)0x80000000 : 0)); }
-// x * 0.5 (exact halving, the correctly rounded x / 2): for normal x above the smallest
-// binade a decrement of the exponent field on the integer pipe, zeros unchanged; the rest
-// (subnormal results, inf, NaN) through the FP64 multiply. Bit for bit x * 0.5.
-// Below the smallest normal binade the magnitude bits halve with round-half-even (one
-// bit is dropped, so a dropped 1 is a tie), which is the IEEE result there too; inf and
-// NaN are returned as they are. Integer operations only.
-__device__ __forceinline__ double half_exact(double x) {
-    const long long b = __double_as_longlong(x);
-    const long long mag = b & 0x7fffffffffffffffll;
-    const int e = (int)(mag >> 52);
-    if (e > 1 && e < 0x7ff) return __longlong_as_double(b - (1ll << 52));
-    if (e == 0x7ff) return x;
-    const long long m = (mag >> 1) + ((mag & 1) & ((mag >> 1) & 1));
-    return __longlong_as_double((b & (long long)0x8000000000000000ull) | m);
-}
-__device__ __forceinline__ float half_exact(float x) { return x * 0.5f; }
 // a / b given y = RN(1/b): the correctly rounded quotient in FP64, a * y in the FP32 faces.
 __device__ __forceinline__ double div_by(double a, double b, double y) { return div_rn(a, b, y); }
 __device__ __forceinline__ float div_by(float a, float, float y) { return a * y; }
@@ -485,7 +469,7 @@ __device__ __forceinline__ void phys_flux(T* f, T r, T u, T v, T p, T E, T un, T
 }
 template <typename T> __device__ __forceinline__ T dot2(T a, T x, T b, T y) { return t_fma(a, x, b * y); }
 template <typename T> __device__ __forceinline__ T energy(T r, T u, T v, T p, T IG1) {
-    return t_fma(p, IG1, half_exact(r) * t_fma(u, u, v * v));
+    return t_fma(p, IG1, (T(0.5) * r) * t_fma(u, u, v * v));
 }
 
 // Newton-refined quotient, reciprocal and sound speed of the FP64 HLLC flux. HLLC has no
@@ -663,8 +647,8 @@ __device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& 
 template <typename T>
 __device__ __forceinline__ void grad_face(T* g, const Prim<T>& q, const Prim<T>& o, T nx, T ny, T l, bool side2) {
     // x * 0.5 is the correctly rounded x / 2 (exact halving), without a division
-    const T hr = half_exact(q.r + o.r), hp = half_exact(q.p + o.p);
-    const T hu = half_exact(q.u + o.u), hv = half_exact(q.v + o.v);
+    const T hr = (q.r + o.r) * T(0.5), hp = (q.p + o.p) * T(0.5);
+    const T hu = (q.u + o.u) * T(0.5), hv = (q.v + o.v) * T(0.5);
     const T v[8] = {hr * nx * l, hr * ny * l, hp * nx * l, hp * ny * l,
                     hu * nx * l, hu * ny * l, hv * nx * l, hv * ny * l};
 #pragma unroll
