@@ -49,7 +49,9 @@ def test_fused_equals_per_kernel_vortex(capi, tmp_path, flux, recon, scheme, mod
     kinds = ("BOUND_INLET", "BOUND_OUTLET", "BOUND_WALL_SLIP", "BOUND_WALL_NO_SLIP")
     t, m, U0 = cases.vortex(96, flux=flux, recon=recon, scheme=scheme, steps=12, bnd_kinds=kinds)
     a, b = _pair(capi, tmp_path, t, m, U0, mode=mode)
-    # without reconstruction there are no gradients to form: FUSED_STAGE 3 keeps the per-kernel path
+    # (each check takes one step on its solver.) Without reconstruction there are no
+    # gradients to form: FUSED_STAGE 3 keeps the per-kernel path
+    assert not _is_fused(a, mode)
     assert _is_fused(b, mode) != (mode == "3" and recon == "NONE")
     a.step(12)
     b.step(12)
