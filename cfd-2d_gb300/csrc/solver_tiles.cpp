@@ -33,7 +33,7 @@ void Solver::build_tiles() {
         fused_ = 3;  // gradients formed in the flux kernel: no tiles
         return;
     }
-    const bool applies = task_.precision == PREC_MIXED && task_.fused >= 1 && gauss_points_ != 0 &&
+    const bool applies = task_.precision == PREC_MIXED && (task_.fused == 1 || task_.fused == 2) && gauss_points_ != 0 &&
                          (task_.scheme == TIME_SSPRK3 || task_.scheme == TIME_HEUN);
     if (!applies) return;
     const int mode = task_.fused;
