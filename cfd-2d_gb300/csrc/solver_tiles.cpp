@@ -29,7 +29,10 @@ struct TileLists {
 
 void Solver::build_tiles() {
     fused_ = 0;
-    if (task_.precision == PREC_MIXED && task_.fused == 3 && gauss_points_ != 0 && task_.recon != RECON_NONE) {
+    // the mixed form's default (FUSED_STAGE absent): gradients formed in the flux kernel
+    // (measured 0.554 against 0.574 ms per step of the 2.1M-triangle four-quadrant case)
+    const int want = task_.fused < 0 ? 3 : task_.fused;
+    if (task_.precision == PREC_MIXED && want == 3 && gauss_points_ != 0 && task_.recon != RECON_NONE) {
         fused_ = 3;  // gradients formed in the flux kernel: no tiles
         return;
     }

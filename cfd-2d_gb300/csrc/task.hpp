@@ -31,7 +31,7 @@ struct TaskConfig {
     // method selections; absent elements give the reference's method
     int flux = FLUX_GODUNOV, recon = RECON_LINEAR, scheme = TIME_HEUN, precision = PREC_FP64;
     int reorder = -1;         // cell order: 0 file order, 1 RCM, 2 Hilbert; -1: RCM (Hilbert with the fused stage)
-    int fused = -1;           // mixed form, SSP-RK3 / Heun: 1 one tiled kernel per stage (gradients, fluxes,
+    int fused = -1;           // mixed form (-1: 3), 0 per-kernel stages; SSP-RK3 / Heun: 1 one tiled kernel per stage (gradients, fluxes,
                               // update), 2 gradients then one tiled flux-and-update kernel per stage,
                               // 3 the flux kernel forms the two cells' gradients (no gradient kernel)
     int adj_store = -1;       // adjoint segment store: 0 states only, 1 + primitives, 2 + gradients,

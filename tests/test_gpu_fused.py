@@ -112,6 +112,7 @@ def test_pipelined_flux_equals_one_thread_per_edge(capi, tmp_path, flux, recon):
     out = []
     for pipe in ("OFF", "ON"):
         t.precision = "MIXED"
+        t.fused_stage = "0"  # the per-kernel path, whose flux kernel the option selects
         t.flux_pipeline = pipe
         d = tmp_path / pipe
         d.mkdir(exist_ok=True)
