@@ -29,9 +29,11 @@ struct TileLists {
 
 void Solver::build_tiles() {
     fused_ = 0;
-    // the mixed form's default (FUSED_STAGE absent): gradients formed in the flux kernel
-    // (measured 0.554 against 0.574 ms per step of the 2.1M-triangle four-quadrant case)
-    const int want = task_.fused < 0 ? 3 : task_.fused;
+    // the mixed form's default (FUSED_STAGE absent) for a single instance: gradients formed in
+    // the flux kernel (0.554 against 0.574 ms per step of the 2.1M-triangle four-quadrant case);
+    // a batch keeps the per-kernel path, whose launch shapes the autotuner sets (256 uneven
+    // instances, Roe: 6.8 against 8.5 ms per step)
+    const int want = task_.fused < 0 ? (inst_.empty() ? 3 : 0) : task_.fused;
     if (task_.precision == PREC_MIXED && want == 3 && gauss_points_ != 0 && task_.recon != RECON_NONE) {
         fused_ = 3;  // gradients formed in the flux kernel: no tiles
         return;
