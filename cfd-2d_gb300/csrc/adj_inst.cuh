@@ -25,20 +25,28 @@ namespace {
 
 inline int adj_nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
+template <typename T, int FLUX, int RECON, int SIDE>
+__device__ __forceinline__ void adj_flux_edge(const DevCase& c, const AdjCase& a, int e);
 template <typename T, int FLUX, int RECON>
 // FP32 faces: at most 128 registers (two 256-thread blocks' worth per SM), measured
-// faster than the compiler's unconstrained choice; FP64 faces: unconstrained.
+// faster than the compiler's unconstrained choice; FP64 faces: unconstrained. Interior and
+// boundary edges (stored last) run their own instantiations.
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 0) k_adj_flux(const DevCase c, const AdjCase a) {
-    const int ne = c.ne;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+    if (e >= c.ne) return;
+    if (e < c.n_int) adj_flux_edge<T, FLUX, RECON, EDGE_INNER>(c, a, e);
+    else adj_flux_edge<T, FLUX, RECON, EDGE_BOUNDARY>(c, a, e);
+}
+template <typename T, int FLUX, int RECON, int SIDE>
+__device__ __forceinline__ void adj_flux_edge(const DevCase& c, const AdjCase& a, int e) {
+    const int ne = c.ne;
     const T* W = W_of<T>(c);
     const T* G = G_of<T>(c);
     const T* DL = DL_of<T>(c);
     const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
     const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
     const int c1 = c.ec1[e];
-    const bool inner = e < c.n_int;
+    const bool inner = edge_inner<SIDE>(c, e);
     const int c2 = inner ? c.ec2[e] : -1;
     const Prim<T> qL = load_prim(W, c1);
     Prim<T> qR = qL, gc = qL;
@@ -124,24 +132,32 @@ __global__ void __launch_bounds__(256) k_flux_rec(const DevCase c, const FluxRec
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
     T out[4];
-    flux_edge<T, FLUX_HLLC, RECON, true>(c, e, out, r);
+    if (e < c.n_int) flux_edge<T, FLUX_HLLC, RECON, true, EDGE_INNER>(c, e, out, r);
+    else flux_edge<T, FLUX_HLLC, RECON, true, EDGE_BOUNDARY>(c, e, out, r);
     st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
 }
 
 // k_adj_flux (HLLC) reading the forward's record of each Gauss point instead of
 // recomputing the reconstruction, the ghost state, the sound speeds and minmod's
 // branches: the same reverse operations on the same values, so the same bits.
+template <typename T, int RECON, int SIDE>
+__device__ __forceinline__ void adj_flux_rec_edge(const DevCase& c, const AdjCase& a, const FluxRec& r, int e);
 template <typename T, int RECON>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 0) k_adj_flux_rec(const DevCase c, const AdjCase a,
                                                                               const FluxRec r) {
-    const int ne = c.ne;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
+    if (e >= c.ne) return;
+    if (e < c.n_int) adj_flux_rec_edge<T, RECON, EDGE_INNER>(c, a, r, e);
+    else adj_flux_rec_edge<T, RECON, EDGE_BOUNDARY>(c, a, r, e);
+}
+template <typename T, int RECON, int SIDE>
+__device__ __forceinline__ void adj_flux_rec_edge(const DevCase& c, const AdjCase& a, const FluxRec& r, int e) {
+    const int ne = c.ne;
     const T* DL = DL_of<T>(c);
     const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
     const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
     const int c1 = c.ec1[e];
-    const bool inner = e < c.n_int;
+    const bool inner = edge_inner<SIDE>(c, e);
     const int c2 = inner ? c.ec2[e] : -1;
     Prim<T> qL{};
     DevBnd b{};

@@ -784,7 +784,15 @@ __device__ __forceinline__ EdgeGeo<T> load_geo(const DevCase& c, int e) {
 
 // With REC (HLLC only) the evaluation also leaves what the adjoint's recorded path reads
 // (FluxRec): per Gauss point the two face states and sound speeds, and minmod's branches.
-template <typename T, int FLUX, int RECON, bool REC = false>
+// SIDE: EDGE_ANY (interior or boundary, decided at run time), EDGE_INNER or EDGE_BOUNDARY
+// (known at compile time: the interior instantiation carries no boundary code, which a
+// warp would otherwise issue, predicated off, for every interior edge).
+enum { EDGE_ANY = 0, EDGE_INNER = 1, EDGE_BOUNDARY = 2 };
+template <int SIDE>
+__device__ __forceinline__ bool edge_inner(const DevCase& c, int e) {
+    return SIDE == EDGE_INNER ? true : (SIDE == EDGE_BOUNDARY ? false : e < c.n_int);
+}
+template <typename T, int FLUX, int RECON, bool REC = false, int SIDE = EDGE_ANY>
 __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const Prim<T>& qL, const T* gL,
                                           const Prim<T>& qR, const T* gR, T* out, const EdgeGeo<T>& geo,
                                           const FluxRec& rec = FluxRec{}) {
@@ -792,7 +800,7 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
     // qR: the second cell's primitives on interior edges (e < n_int), qL on boundary edges
     const T nx = geo.nx, ny = geo.ny, l = geo.l;
     const T GAM = gam_of<T>(c), IG1 = ig1_of<T>(c);
-    const bool inner = e < c.n_int;
+    const bool inner = edge_inner<SIDE>(c, e);
     Prim<T> gc = qL;
     DevBnd b{};
     T Tc = T(0), M = T(0);
@@ -856,12 +864,12 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
 }
 
 // The flux of edge e (what F holds for it) from the stage's W and G (with REC: and its record).
-template <typename T, int FLUX, int RECON, bool REC = false>
+template <typename T, int FLUX, int RECON, bool REC = false, int SIDE = EDGE_ANY>
 __device__ __forceinline__ void flux_edge(const DevCase& c, int e, T* out, const FluxRec& rec = FluxRec{}) {
     const T* __restrict__ W = W_of<T>(c);
     const T* __restrict__ G = G_of<T>(c);
     const int c1 = ldcs(c.ec1 + e);
-    const bool inner = e < c.n_int;
+    const bool inner = edge_inner<SIDE>(c, e);
     const Prim<T> qL = load_prim(W, c1);
     T gL[8], gR[8];
     if (RECON != RECON_NONE) ld8(G, c1, gL);
@@ -871,13 +879,16 @@ __device__ __forceinline__ void flux_edge(const DevCase& c, int e, T* out, const
         qR = load_prim(W, c2);
         if (RECON != RECON_NONE) ld8(G, c2, gR);
     }
-    flux_core<T, FLUX, RECON, REC>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e), rec);
+    flux_core<T, FLUX, RECON, REC, SIDE>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e), rec);
 }
 
+// Interior and boundary edges through their own instantiations (boundary edges are stored
+// last, so the branch is uniform in every warp but the one holding the first boundary edge).
 template <typename T, int FLUX, int RECON>
 __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
     T out[4];
-    flux_edge<T, FLUX, RECON>(c, e, out);
+    if (e < c.n_int) flux_edge<T, FLUX, RECON, false, EDGE_INNER>(c, e, out);
+    else flux_edge<T, FLUX, RECON, false, EDGE_BOUNDARY>(c, e, out);
     st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
 }
 
