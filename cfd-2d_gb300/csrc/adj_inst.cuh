@@ -132,8 +132,7 @@ __global__ void __launch_bounds__(256) k_flux_rec(const DevCase c, const FluxRec
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
     T out[4];
-    if (e < c.n_int) flux_edge<T, FLUX_HLLC, RECON, true, EDGE_INNER>(c, e, out, r);
-    else flux_edge<T, FLUX_HLLC, RECON, true, EDGE_BOUNDARY>(c, e, out, r);
+    flux_edge<T, FLUX_HLLC, RECON, true>(c, e, out, r);
     st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
 }
 

@@ -786,7 +786,8 @@ __device__ __forceinline__ EdgeGeo<T> load_geo(const DevCase& c, int e) {
 // (FluxRec): per Gauss point the two face states and sound speeds, and minmod's branches.
 // SIDE: EDGE_ANY (interior or boundary, decided at run time), EDGE_INNER or EDGE_BOUNDARY
 // (known at compile time: the interior instantiation carries no boundary code, which a
-// warp would otherwise issue, predicated off, for every interior edge).
+// warp would otherwise issue, predicated off, for every interior edge; the adjoint's flux
+// kernels use them).
 enum { EDGE_ANY = 0, EDGE_INNER = 1, EDGE_BOUNDARY = 2 };
 template <int SIDE>
 __device__ __forceinline__ bool edge_inner(const DevCase& c, int e) {
@@ -882,13 +883,10 @@ __device__ __forceinline__ void flux_edge(const DevCase& c, int e, T* out, const
     flux_core<T, FLUX, RECON, REC, SIDE>(c, e, c1, qL, gL, qR, gR, out, load_geo<T, RECON>(c, e), rec);
 }
 
-// Interior and boundary edges through their own instantiations (boundary edges are stored
-// last, so the branch is uniform in every warp but the one holding the first boundary edge).
 template <typename T, int FLUX, int RECON>
 __device__ __forceinline__ void flux_one(const DevCase& c, int e) {
     T out[4];
-    if (e < c.n_int) flux_edge<T, FLUX, RECON, false, EDGE_INNER>(c, e, out);
-    else flux_edge<T, FLUX, RECON, false, EDGE_BOUNDARY>(c, e, out);
+    flux_edge<T, FLUX, RECON>(c, e, out);
     st4(F_of<T>(c), e, out[0], out[1], out[2], out[3]);
 }
 
