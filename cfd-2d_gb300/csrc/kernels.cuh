@@ -542,30 +542,32 @@ __device__ __forceinline__ float hllc_sound(float a, float r) { return t_sqrt(a 
 // HLLC (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, sec. 10.4-10.6),
 // Davis wave speeds S_L = min(unL-cL, unR-cR), S_R = max(unL+cL, unR+cR), star flux
 // F*_K = [S*(S_K U_K - F_K) + S_K p* D*] / (S_K - S*), D* = (0, nx, ny, S*),
-// p* = p_K + rho_K (S_K - un_K)(S* - un_K): one division instead of Toro's star state.
-// FP64: c = hllc_sound(GAMMA p, rho), S* = hllc_quot, 1/(S_K - S*) = hllc_recip.
+// p* = p_K + rho_K (S_K - un_K)(S* - un_K): one division instead of Toro's star state;
+// S_K U_K - F_K is formed from m_K = rho_K (S_K - un_K) and only the side that is used
+// forms its energy. FP64: c = hllc_sound(GAMMA p, rho), S* = hllc_quot,
+// 1/(S_K - S*) = hllc_recip.
 template <typename T>
 __device__ __forceinline__ void flux_hllc_c(T* f, const Prim<T>& L, const Prim<T>& R, T cL, T cR, T nx, T ny, T IG1) {
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
-    T EL = energy(L.r, L.u, L.v, L.p, IG1);
-    T ER = energy(R.r, R.u, R.v, R.p, IG1);
     T SL = t_min(unL - cL, unR - cR), SR = t_max(unL + cL, unR + cR);
-    if (SL >= T(0.0)) { phys_flux(f, L.r, L.u, L.v, L.p, EL, unL, nx, ny); return; }
-    if (SR <= T(0.0)) { phys_flux(f, R.r, R.u, R.v, R.p, ER, unR, nx, ny); return; }
-    T mL = L.r * (SL - unL), mR = R.r * (SR - unR);
+    if (SL >= T(0.0)) { phys_flux(f, L.r, L.u, L.v, L.p, energy(L.r, L.u, L.v, L.p, IG1), unL, nx, ny); return; }
+    if (SR <= T(0.0)) { phys_flux(f, R.r, R.u, R.v, R.p, energy(R.r, R.u, R.v, R.p, IG1), unR, nx, ny); return; }
+    T dL = SL - unL, dR = SR - unR;
+    T mL = L.r * dL, mR = R.r * dR;
     T Ss = hllc_quot(t_fma(-mR, unR, t_fma(mL, unL, R.p - L.p)), mL - mR);
     const bool left = Ss >= T(0.0);
     const Prim<T>& K = left ? L : R;
-    T SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
-    T FK[4];
-    phys_flux(FK, K.r, K.u, K.v, K.p, EK, unK, nx, ny);
+    T SK = left ? SL : SR, unK = left ? unL : unR, dK = left ? dL : dR, mK = left ? mL : mR;
+    T EK = energy(K.r, K.u, K.v, K.p, IG1);
+    // S_K U_K - F_K = (m_K, m_K u - p nx, m_K v - p ny, E_K (S_K - un_K) - p un_K)
+    T A1 = t_fma(mK, K.u, -(K.p * nx)), A2 = t_fma(mK, K.v, -(K.p * ny)), A3 = t_fma(EK, dK, -(K.p * unK));
     T ps = t_fma(mK, Ss - unK, K.p);
     T inv = hllc_recip(SK - Ss);
     T sp = SK * ps;
-    f[0] = (Ss * t_fma(SK, K.r, -FK[0])) * inv;
-    f[1] = t_fma(Ss, t_fma(SK, K.r * K.u, -FK[1]), sp * nx) * inv;
-    f[2] = t_fma(Ss, t_fma(SK, K.r * K.v, -FK[2]), sp * ny) * inv;
-    f[3] = t_fma(Ss, t_fma(SK, EK, -FK[3]), sp * Ss) * inv;
+    f[0] = (Ss * mK) * inv;
+    f[1] = t_fma(Ss, A1, sp * nx) * inv;
+    f[2] = t_fma(Ss, A2, sp * ny) * inv;
+    f[3] = t_fma(Ss, A3, sp * Ss) * inv;
 }
 template <typename T>
 __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {

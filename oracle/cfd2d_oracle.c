@@ -529,32 +529,40 @@ static double hllc_sound(double a, double r) {
  * star flux in the form with a single division,
  *   F*_K = [S*(S_K U_K - F_K) + S_K p* D*] / (S_K - S*),  D* = (0, nx, ny, S*),
  *   p* = p_K + rho_K (S_K - un_K)(S* - un_K),
- * which equals F_K + S_K (U*_K - U_K) for Toro's star state U*_K. Energies use
+ * which equals F_K + S_K (U*_K - U_K) for Toro's star state U*_K, with
+ *   S_K U_K - F_K = (m_K, m_K u - p nx, m_K v - p ny, E_K (S_K - un_K) - p un_K),
+ *   m_K = rho_K (S_K - un_K); only the side used forms its energy. Energies use
  * p/(gamma-1) as p * (1/(gamma-1)). c = hllc_sound(GAMMA p, rho), S* = hllc_quot,
  * 1/(S_K - S*) = hllc_recip. */
 static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
     double IG1 = 1.0 / (GAM - 1.0);
     double cL = hllc_sound(GAM * pL->p, pL->r), cR = hllc_sound(GAM * pR->p, pR->r);
     double unL = dot2(pL->u, nx, pL->v, ny), unR = dot2(pR->u, nx, pR->v, ny);
-    double EL = energy(pL->r, pL->u, pL->v, pL->p, IG1);
-    double ER = energy(pR->r, pR->u, pR->v, pR->p, IG1);
     double SL = dmin(unL - cL, unR - cR), SR = dmax(unL + cL, unR + cR);
-    if (SL >= 0.0) { phys_flux(f, pL->r, pL->u, pL->v, pL->p, EL, unL, nx, ny); return; }
-    if (SR <= 0.0) { phys_flux(f, pR->r, pR->u, pR->v, pR->p, ER, unR, nx, ny); return; }
-    double mL = pL->r * (SL - unL), mR = pR->r * (SR - unR);
+    if (SL >= 0.0) {
+        phys_flux(f, pL->r, pL->u, pL->v, pL->p, energy(pL->r, pL->u, pL->v, pL->p, IG1), unL, nx, ny);
+        return;
+    }
+    if (SR <= 0.0) {
+        phys_flux(f, pR->r, pR->u, pR->v, pR->p, energy(pR->r, pR->u, pR->v, pR->p, IG1), unR, nx, ny);
+        return;
+    }
+    double dL = SL - unL, dR = SR - unR;
+    double mL = pL->r * dL, mR = pR->r * dR;
     double Ss = hllc_quot(fma(-mR, unR, fma(mL, unL, pR->p - pL->p)), mL - mR);
-    const Par* K; double SK, unK, EK, mK;
-    if (Ss >= 0.0) { K = pL; SK = SL; unK = unL; EK = EL; mK = mL; }
-    else { K = pR; SK = SR; unK = unR; EK = ER; mK = mR; }
-    double FK[4];
-    phys_flux(FK, K->r, K->u, K->v, K->p, EK, unK, nx, ny);
+    const Par* K; double SK, unK, dK, mK;
+    if (Ss >= 0.0) { K = pL; SK = SL; unK = unL; dK = dL; mK = mL; }
+    else { K = pR; SK = SR; unK = unR; dK = dR; mK = mR; }
+    double EK = energy(K->r, K->u, K->v, K->p, IG1);
+    /* S_K U_K - F_K = (m_K, m_K u - p nx, m_K v - p ny, E_K (S_K - un_K) - p un_K) */
+    double A1 = fma(mK, K->u, -(K->p * nx)), A2 = fma(mK, K->v, -(K->p * ny)), A3 = fma(EK, dK, -(K->p * unK));
     double ps = fma(mK, Ss - unK, K->p);
     double inv = hllc_recip(SK - Ss);
     double sp = SK * ps;
-    f[0] = (Ss * fma(SK, K->r, -FK[0])) * inv;
-    f[1] = fma(Ss, fma(SK, K->r * K->u, -FK[1]), sp * nx) * inv;
-    f[2] = fma(Ss, fma(SK, K->r * K->v, -FK[2]), sp * ny) * inv;
-    f[3] = fma(Ss, fma(SK, EK, -FK[3]), sp * Ss) * inv;
+    f[0] = (Ss * mK) * inv;
+    f[1] = fma(Ss, A1, sp * nx) * inv;
+    f[2] = fma(Ss, A2, sp * ny) * inv;
+    f[3] = fma(Ss, A3, sp * Ss) * inv;
 }
 
 /* Roe flux (Roe, J. Comput. Phys. 43, 1981) in the face-normal frame with the
