@@ -29,13 +29,17 @@ template <typename T, int FLUX, int RECON, int SIDE>
 __device__ __forceinline__ void adj_flux_edge(const DevCase& c, const AdjCase& a, int e);
 template <typename T, int FLUX, int RECON>
 // FP32 faces: at most 128 registers (two 256-thread blocks' worth per SM), measured
-// faster than the compiler's unconstrained choice; FP64 faces: unconstrained. Interior and
-// boundary edges (stored last) run their own instantiations.
+// faster than the compiler's unconstrained choice; FP64 faces: unconstrained. With FP64 faces
+// interior and boundary edges (stored last) run their own instantiations.
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 0) k_adj_flux(const DevCase c, const AdjCase a) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
-    if (e < c.n_int) adj_flux_edge<T, FLUX, RECON, EDGE_INNER>(c, a, e);
-    else adj_flux_edge<T, FLUX, RECON, EDGE_BOUNDARY>(c, a, e);
+    if constexpr (sizeof(T) == 8) {  // FP64 faces: no contraction, the same bits in either instantiation
+        if (e < c.n_int) adj_flux_edge<T, FLUX, RECON, EDGE_INNER>(c, a, e);
+        else adj_flux_edge<T, FLUX, RECON, EDGE_BOUNDARY>(c, a, e);
+    } else {
+        adj_flux_edge<T, FLUX, RECON, EDGE_ANY>(c, a, e);
+    }
 }
 template <typename T, int FLUX, int RECON, int SIDE>
 __device__ __forceinline__ void adj_flux_edge(const DevCase& c, const AdjCase& a, int e) {
@@ -146,8 +150,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 0) k_adj_flux_rec(co
                                                                               const FluxRec r) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
-    if (e < c.n_int) adj_flux_rec_edge<T, RECON, EDGE_INNER>(c, a, r, e);
-    else adj_flux_rec_edge<T, RECON, EDGE_BOUNDARY>(c, a, r, e);
+    if constexpr (sizeof(T) == 8) {
+        if (e < c.n_int) adj_flux_rec_edge<T, RECON, EDGE_INNER>(c, a, r, e);
+        else adj_flux_rec_edge<T, RECON, EDGE_BOUNDARY>(c, a, r, e);
+    } else {
+        adj_flux_rec_edge<T, RECON, EDGE_ANY>(c, a, r, e);
+    }
 }
 template <typename T, int RECON, int SIDE>
 __device__ __forceinline__ void adj_flux_rec_edge(const DevCase& c, const AdjCase& a, const FluxRec& r, int e) {

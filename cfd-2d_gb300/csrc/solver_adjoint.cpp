@@ -122,7 +122,9 @@ double Solver::forward(int nsteps, int k, int* status) {
         if (!in_budget(std::min(need_w, need_x) * dbl))
             throw Error(CFD2D_ERR_CAPACITY, "the adjoint's smallest segment store exceeds ADJOINT_MEMORY");
         const int mode = task_.adj_store;
-        const bool rec_ok = task_.flux == FLUX_HLLC;
+        // flux records with FP64 faces only: FP32 faces are compiled with contraction, which
+        // the compiler may apply differently in the recording kernel than in the forward's
+        const bool rec_ok = task_.flux == FLUX_HLLC && task_.precision != PREC_MIXED;
         if (rec_ok && (mode == 3 || (mode < 0 && fits_bytes(need * dbl + need_rec)))) {
             store_wg_ = store_g_ = store_rec_ = true;
         } else if (mode >= 2 || (mode < 0 && fits(need))) {

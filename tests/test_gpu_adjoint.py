@@ -210,7 +210,8 @@ def test_adjoint_store_modes_give_the_same_gradient(capi, tmp_path, precision):
     t, m, U0, w, _ = cases.vortex_adjoint(32, steps=9)
     t.precision = precision
     grads = []
-    for mode in ("NONE", "PRIMITIVES", "ALL", "FLUXES"):
+    modes = ("NONE", "PRIMITIVES", "ALL") + (("FLUXES",) if precision is None else ())  # records: FP64 faces
+    for mode in modes:
         t.adjoint_store = mode
         d = tmp_path / mode
         d.mkdir()
