@@ -546,6 +546,34 @@ __device__ __forceinline__ float hllc_sound(float a, float r) { return t_sqrt(a 
 // S_K U_K - F_K is formed from m_K = rho_K (S_K - un_K) and only the side that is used
 // forms its energy. FP64: c = hllc_sound(GAMMA p, rho), S* = hllc_quot,
 // 1/(S_K - S*) = hllc_recip.
+// FP32 faces (the mixed form): both energies up front and the star flux from the physical
+// flux F_K; without branches on the energies this measured faster there (124 against
+// 151 us per flux launch at 2.1M triangles).
+__device__ __forceinline__ void flux_hllc_c(float* f, const Prim<float>& L, const Prim<float>& R, float cL, float cR,
+                                            float nx, float ny, float IG1) {
+    float unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
+    float EL = energy(L.r, L.u, L.v, L.p, IG1);
+    float ER = energy(R.r, R.u, R.v, R.p, IG1);
+    float SL = t_min(unL - cL, unR - cR), SR = t_max(unL + cL, unR + cR);
+    if (SL >= 0.0f) { phys_flux(f, L.r, L.u, L.v, L.p, EL, unL, nx, ny); return; }
+    if (SR <= 0.0f) { phys_flux(f, R.r, R.u, R.v, R.p, ER, unR, nx, ny); return; }
+    float mL = L.r * (SL - unL), mR = R.r * (SR - unR);
+    float Ss = hllc_quot(t_fma(-mR, unR, t_fma(mL, unL, R.p - L.p)), mL - mR);
+    const bool left = Ss >= 0.0f;
+    const Prim<float>& K = left ? L : R;
+    float SK = left ? SL : SR, unK = left ? unL : unR, EK = left ? EL : ER, mK = left ? mL : mR;
+    float FK[4];
+    phys_flux(FK, K.r, K.u, K.v, K.p, EK, unK, nx, ny);
+    float ps = t_fma(mK, Ss - unK, K.p);
+    float inv = hllc_recip(SK - Ss);
+    float sp = SK * ps;
+    f[0] = (Ss * t_fma(SK, K.r, -FK[0])) * inv;
+    f[1] = t_fma(Ss, t_fma(SK, K.r * K.u, -FK[1]), sp * nx) * inv;
+    f[2] = t_fma(Ss, t_fma(SK, K.r * K.v, -FK[2]), sp * ny) * inv;
+    f[3] = t_fma(Ss, t_fma(SK, EK, -FK[3]), sp * Ss) * inv;
+}
+// FP64 faces: S_K U_K - F_K from m_K, the used side's energy only (fewer FP64 instructions,
+// the FP64 unit being the bound there)
 template <typename T>
 __device__ __forceinline__ void flux_hllc_c(T* f, const Prim<T>& L, const Prim<T>& R, T cL, T cR, T nx, T ny, T IG1) {
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
