@@ -882,7 +882,13 @@ __device__ __forceinline__ void flux_core(const DevCase& c, int e, int c1, const
         } else {
             hit |= num_flux<T, FLUX>(f, pL, pR, nx, ny, GAM, IG1, c.newton_cap, c.rg_flux);
         }
-        fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
+        // the reference's fluxes sum the Gauss points from +0 (its fSum = 0; fSum += F); this
+        // project's own fluxes (HLLC, Roe) start from the first point's flux
+        if (gp == 0 && (FLUX == FLUX_HLLC || FLUX == FLUX_ROE)) {
+            fs[0] = f[0]; fs[1] = f[1]; fs[2] = f[2]; fs[3] = f[3];
+        } else {
+            fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
+        }
         if (RECON == RECON_NONE) {  // both Gauss points see the cell-centre states
             fs[0] = fs[0] + f[0]; fs[1] = fs[1] + f[1]; fs[2] = fs[2] + f[2]; fs[3] = fs[3] + f[3];
             break;
@@ -1139,16 +1145,23 @@ __device__ __forceinline__ void update_finish(const DevCase& c, int i, const dou
     double u0 = src[i] + cf * R[0], u1 = src[nc + i] + cf * R[1], u2 = src[2 * nc + i] + cf * R[2],
            u3 = src[3 * nc + i] + cf * R[3];
     double* dst = FINAL ? c.A : c.B;
-    if (SCHEME == TIME_HEUN && STAGE == 1) {
+    if (SCHEME == TIME_SSPRK3) {
+        // SSP-RK3 (not in the reference) with fused multiply-adds: X + cf R, then
+        // 3/4 U^n + 1/4 X and 1/3 U^n + 2/3 X (the Euler and Heun stages stay unfused: the
+        // reference's U += cTau/S R)
+        u0 = fma(cf, R[0], src[i]); u1 = fma(cf, R[1], src[nc + i]);
+        u2 = fma(cf, R[2], src[2 * nc + i]); u3 = fma(cf, R[3], src[3 * nc + i]);
+        if (STAGE == 1) {
+            u0 = fma(0.25, u0, 0.75 * c.A[i]); u1 = fma(0.25, u1, 0.75 * c.A[nc + i]);
+            u2 = fma(0.25, u2, 0.75 * c.A[2 * nc + i]); u3 = fma(0.25, u3, 0.75 * c.A[3 * nc + i]);
+        } else if (STAGE == 2) {
+            const double c13 = 1.0 / 3.0, c23 = 2.0 / 3.0;
+            u0 = fma(c23, u0, c13 * c.A[i]); u1 = fma(c23, u1, c13 * c.A[nc + i]);
+            u2 = fma(c23, u2, c13 * c.A[2 * nc + i]); u3 = fma(c23, u3, c13 * c.A[3 * nc + i]);
+        }
+    } else if (SCHEME == TIME_HEUN && STAGE == 1) {
         u0 = 0.5 * (c.A[i] + u0); u1 = 0.5 * (c.A[nc + i] + u1);
         u2 = 0.5 * (c.A[2 * nc + i] + u2); u3 = 0.5 * (c.A[3 * nc + i] + u3);
-    } else if (SCHEME == TIME_SSPRK3 && STAGE == 1) {
-        u0 = 0.75 * c.A[i] + 0.25 * u0; u1 = 0.75 * c.A[nc + i] + 0.25 * u1;
-        u2 = 0.75 * c.A[2 * nc + i] + 0.25 * u2; u3 = 0.75 * c.A[3 * nc + i] + 0.25 * u3;
-    } else if (SCHEME == TIME_SSPRK3 && STAGE == 2) {
-        const double c13 = 1.0 / 3.0, c23 = 2.0 / 3.0;
-        u0 = c13 * c.A[i] + c23 * u0; u1 = c13 * c.A[nc + i] + c23 * u1;
-        u2 = c13 * c.A[2 * nc + i] + c23 * u2; u3 = c13 * c.A[3 * nc + i] + c23 * u3;
     }
     dst[i] = u0; dst[nc + i] = u1; dst[2 * nc + i] = u2; dst[3 * nc + i] = u3;
     const Prim<T> w = prim_face_of<T>(u0, u1, u2, u3, c, i);

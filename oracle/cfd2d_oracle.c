@@ -787,7 +787,12 @@ static void stage_residual(orc_solver* s) {
             Par pL, pR; double f[4];
             face_states(s, e, gp, &pL, &pR);
             s->newton_hit |= calc_flux(s, f, &pL, &pR, nx, ny);
-            fr += f[0]; fu += f[1]; fv += f[2]; fe += f[3];
+            if (gp == 1 && (s->p.flux == ORC_FLUX_HLLC || s->p.flux == ORC_FLUX_ROE)) {
+                /* this project's fluxes start from the first point's flux */
+                fr = f[0]; fu = f[1]; fv = f[2]; fe = f[3];
+            } else {
+                fr += f[0]; fu += f[1]; fv += f[2]; fe += f[3];
+            }
         }
         s->ro_int[c1] -= fr * l; s->ru_int[c1] -= fu * l;
         s->rv_int[c1] -= fv * l; s->re_int[c1] -= fe * l;
@@ -814,8 +819,13 @@ static void stage_update(orc_solver* s) { /* :366-374 */
     for (int i = 0; i < m->nc; i++) {
         if (is_lim(s, i)) continue;
         double cfl = s->cTau[i] / m->S[i];
-        s->ro[i] += cfl * s->ro_int[i]; s->ru[i] += cfl * s->ru_int[i];
-        s->rv[i] += cfl * s->rv_int[i]; s->re[i] += cfl * s->re_int[i];
+        if (s->p.scheme == ORC_TIME_SSPRK3) { /* this project's scheme: fused */
+            s->ro[i] = fma(cfl, s->ro_int[i], s->ro[i]); s->ru[i] = fma(cfl, s->ru_int[i], s->ru[i]);
+            s->rv[i] = fma(cfl, s->rv_int[i], s->rv[i]); s->re[i] = fma(cfl, s->re_int[i], s->re[i]);
+        } else {
+            s->ro[i] += cfl * s->ro_int[i]; s->ru[i] += cfl * s->ru_int[i];
+            s->rv[i] += cfl * s->rv_int[i]; s->re[i] += cfl * s->re_int[i];
+        }
     }
 }
 
@@ -865,10 +875,10 @@ int orc_step(orc_solver* s, int nsteps) {
             if (s->p.scheme == ORC_TIME_SSPRK3 && st == 1)
                 for (int i = 0; i < nc; i++) {
                     if (is_lim(s, i)) continue;
-                    s->ro[i] = 0.75 * s->ro_old[i] + 0.25 * s->ro[i];
-                    s->ru[i] = 0.75 * s->ru_old[i] + 0.25 * s->ru[i];
-                    s->rv[i] = 0.75 * s->rv_old[i] + 0.25 * s->rv[i];
-                    s->re[i] = 0.75 * s->re_old[i] + 0.25 * s->re[i];
+                    s->ro[i] = fma(0.25, s->ro[i], 0.75 * s->ro_old[i]);
+                    s->ru[i] = fma(0.25, s->ru[i], 0.75 * s->ru_old[i]);
+                    s->rv[i] = fma(0.25, s->rv[i], 0.75 * s->rv_old[i]);
+                    s->re[i] = fma(0.25, s->re[i], 0.75 * s->re_old[i]);
                 }
         }
         for (int i = 0; i < nc; i++) {
@@ -876,9 +886,9 @@ int orc_step(orc_solver* s, int nsteps) {
             if (s->p.scheme == ORC_TIME_HEUN) { /* ICASE 97-65 eq. (4.10), :429-437 */
                 s->ro[i] = 0.5 * (s->ro_old[i] + s->ro[i]); s->ru[i] = 0.5 * (s->ru_old[i] + s->ru[i]);
                 s->rv[i] = 0.5 * (s->rv_old[i] + s->rv[i]); s->re[i] = 0.5 * (s->re_old[i] + s->re[i]);
-            } else if (s->p.scheme == ORC_TIME_SSPRK3) { /* Shu-Osher third stage */
-                s->ro[i] = c13 * s->ro_old[i] + c23 * s->ro[i]; s->ru[i] = c13 * s->ru_old[i] + c23 * s->ru[i];
-                s->rv[i] = c13 * s->rv_old[i] + c23 * s->rv[i]; s->re[i] = c13 * s->re_old[i] + c23 * s->re[i];
+            } else if (s->p.scheme == ORC_TIME_SSPRK3) { /* Shu-Osher third stage, fused */
+                s->ro[i] = fma(c23, s->ro[i], c13 * s->ro_old[i]); s->ru[i] = fma(c23, s->ru[i], c13 * s->ru_old[i]);
+                s->rv[i] = fma(c23, s->rv[i], c13 * s->rv_old[i]); s->re[i] = fma(c23, s->re[i], c13 * s->re_old[i]);
             }
             check_limits(s, i);
         }
