@@ -307,6 +307,116 @@ __device__ __forceinline__ void vjp_hllc_c(const Prim<T>& L, const Prim<T>& R, T
     }
 }
 
+// FP64 faces: the VJP of the FP64 forward's arrangement (flux_hllc_c<double> in kernels.cuh:
+// S_K U_K - F_K from m_K = rho_K d_K, d_K = S_K - un_K, and only the used side's energy),
+// recomputing the forward's values and branches with its own expressions.
+__device__ __forceinline__ void vjp_hllc_c(const Prim<double>& L, const Prim<double>& R, double cL, double cR,
+                                           double nx, double ny, double GAM, double IG1, const double* fb,
+                                           Prim<double>& Lb, Prim<double>& Rb) {
+    typedef double T;
+    const T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
+    const T sl1 = unL - cL, sl2 = unR - cR, sr1 = unL + cL, sr2 = unR + cR;
+    const bool l1 = sl1 < sl2, r1 = sr1 > sr2;
+    const T SL = l1 ? sl1 : sl2, SR = r1 ? sr1 : sr2;
+    T unLb = acc0<T>(), unRb = acc0<T>(), SLb = acc0<T>(), SRb = acc0<T>(), cLb = acc0<T>(), cRb = acc0<T>();
+    // E = p IG1 + .5 r (u^2 + v^2): the adjoint Eb of one side's energy into its state
+    auto energy_bar = [&](const Prim<T>& q, T Eb, Prim<T>& qb) {
+        const T e = Eb * q.r;
+        qb.p = madd(qb.p, Eb, IG1); qb.r = madd(qb.r, Eb * T(0.5), t_fma(q.u, q.u, q.v * q.v));
+        qb.u = madd(qb.u, e, q.u); qb.v = madd(qb.v, e, q.v);
+    };
+    if (SL >= T(0.0) || SR <= T(0.0)) {  // supersonic: the upwind side's physical flux
+        T Eb = acc0<T>();
+        if (SL >= T(0.0)) {
+            vjp_phys(L.r, L.u, L.v, L.p, energy(L.r, L.u, L.v, L.p, IG1), unL, nx, ny, fb, Lb.r, Lb.u, Lb.v, Lb.p,
+                     Eb, unLb);
+            energy_bar(L, Eb, Lb);
+        } else {
+            vjp_phys(R.r, R.u, R.v, R.p, energy(R.r, R.u, R.v, R.p, IG1), unR, nx, ny, fb, Rb.r, Rb.u, Rb.v, Rb.p,
+                     Eb, unRb);
+            energy_bar(R, Eb, Rb);
+        }
+    } else {
+        const T dL = SL - unL, dR = SR - unR;
+        const T mL = L.r * dL, mR = R.r * dR;
+        const T num = t_fma(-mR, unR, t_fma(mL, unL, R.p - L.p)), den = mL - mR;
+        T iden;
+        const T Ss = star_speed(num, den, iden);
+        const bool left = Ss >= T(0.0);
+        const Prim<T>& K = left ? L : R;
+        const T SK = left ? SL : SR, unK = left ? unL : unR, dK = left ? dL : dR, mK = left ? mL : mR;
+        const T EK = energy(K.r, K.u, K.v, K.p, IG1);
+        const T A1 = t_fma(mK, K.u, -(K.p * nx)), A2 = t_fma(mK, K.v, -(K.p * ny)), A3 = t_fma(EK, dK, -(K.p * unK));
+        const T ps = t_fma(mK, Ss - unK, K.p);
+        const T inv = hllc_recip(SK - Ss);
+        const T sp = SK * ps;
+        // h0 = Ss mK, h1 = Ss A1 + sp nx, h2 = Ss A2 + sp ny, h3 = Ss A3 + sp Ss; f_k = h_k inv
+        const T h0 = Ss * mK, h1 = madd(Ss * A1, sp, nx), h2 = madd(Ss * A2, sp, ny), h3 = madd(Ss * A3, sp, Ss);
+        const T hb0 = fb[0] * inv, hb1 = fb[1] * inv, hb2 = fb[2] * inv, hb3 = fb[3] * inv;
+        const T invb = madd(madd(madd(fb[0] * h0, fb[1], h1), fb[2], h2), fb[3], h3);
+        T Ssb = madd(madd(madd(hb0 * mK, hb1, A1), hb2, A2), hb3, A3 + sp);
+        T mKb = hb0 * Ss;
+        const T A1b = hb1 * Ss, A2b = hb2 * Ss, A3b = hb3 * Ss;
+        const T spb = madd(madd(hb1 * nx, hb2, ny), hb3, Ss);
+        // inv = 1/(SK - Ss)
+        const T ii = invb * inv * inv;
+        T SKb = -ii;
+        Ssb += ii;
+        // sp = SK ps
+        SKb = madd(SKb, spb, ps);
+        const T psb = spb * SK;
+        // ps = pK + mK (Ss - unK)
+        T Krb = acc0<T>(), Kub = acc0<T>(), Kvb = acc0<T>(), Kpb = psb;
+        T unKb = -psb * mK;
+        mKb = madd(mKb, psb, Ss - unK);
+        Ssb = madd(Ssb, psb, mK);
+        // A1 = mK u - p nx, A2 = mK v - p ny, A3 = EK dK - p unK
+        mKb = madd(madd(mKb, A1b, K.u), A2b, K.v);
+        Kub = madd(Kub, A1b, mK);
+        Kvb = madd(Kvb, A2b, mK);
+        Kpb = madd(madd(madd(Kpb, -A1b, nx), -A2b, ny), -A3b, unK);
+        const T EKb = A3b * dK;
+        T dKb = A3b * EK;
+        unKb = madd(unKb, -A3b, K.p);
+        // Ss = num / den
+        const T numb = Ssb * iden, denb = -Ssb * Ss * iden;
+        Rb.p += numb; Lb.p -= numb;
+        T mLb = madd(denb, numb, unL), mRb = madd(-denb, -numb, unR);
+        unLb = madd(unLb, numb, mL); unRb = madd(unRb, -numb, mR);
+        T dLb = acc0<T>(), dRb = acc0<T>();
+        // route the K side (its m, d, state, energy and speeds) to L or R
+        if (left) {
+            mLb += mKb; dLb += dKb; unLb += unKb; SLb += SKb;
+            Lb.r += Krb; Lb.u += Kub; Lb.v += Kvb; Lb.p += Kpb;
+            energy_bar(L, EKb, Lb);
+        } else {
+            mRb += mKb; dRb += dKb; unRb += unKb; SRb += SKb;
+            Rb.r += Krb; Rb.u += Kub; Rb.v += Kvb; Rb.p += Kpb;
+            energy_bar(R, EKb, Rb);
+        }
+        // mL = rL dL, dL = SL - unL (and R)
+        Lb.r = madd(Lb.r, mLb, dL); dLb = madd(dLb, mLb, L.r);
+        Rb.r = madd(Rb.r, mRb, dR); dRb = madd(dRb, mRb, R.r);
+        SLb += dLb; unLb -= dLb;
+        SRb += dRb; unRb -= dRb;
+        // SL = min(sl1, sl2), SR = max(sr1, sr2)
+        if (l1) { unLb += SLb; cLb -= SLb; } else { unRb += SLb; cRb -= SLb; }
+        if (r1) { unLb += SRb; cLb += SRb; } else { unRb += SRb; cRb += SRb; }
+    }
+    // un = u nx + v ny
+    Lb.u = madd(Lb.u, unLb, nx); Lb.v = madd(Lb.v, unLb, ny);
+    Rb.u = madd(Rb.u, unRb, nx); Rb.v = madd(Rb.v, unRb, ny);
+    // c = sqrt(GAM p / r) = sqrt(a): dc = (GAM dp - a dr) / (2 c r), a = c^2
+    if (cLb != T(0.0)) {
+        const T ab = hllc_quot(T(0.5) * cLb, cL * L.r);
+        Lb.p = madd(Lb.p, ab, GAM); Lb.r = madd(Lb.r, -ab, cL * cL);
+    }
+    if (cRb != T(0.0)) {
+        const T ab = hllc_quot(T(0.5) * cRb, cR * R.r);
+        Rb.p = madd(Rb.p, ab, GAM); Rb.r = madd(Rb.r, -ab, cR * cR);
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void vjp_hllc(const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1, const T* fb,
                                          Prim<T>& Lb, Prim<T>& Rb) {
