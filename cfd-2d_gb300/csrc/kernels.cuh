@@ -603,6 +603,24 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
     flux_hllc_c(f, L, R, cL, cR, nx, ny, IG1);
 }
 
+// The Roe flux's own quotients, reciprocals and square roots: with FP64 faces the
+// Newton-refined sequences of the HLLC flux (this project's definition, the oracle does the
+// same), a / b from a given y ~ 1/b corrected once; FP32 faces as before.
+__device__ __forceinline__ double roe_recip(double x) { return hllc_recip(x); }
+__device__ __forceinline__ float roe_recip(float x) { return 1.0f / x; }
+__device__ __forceinline__ double roe_sqrt(double x) { return hllc_sound(x, 1.0); }
+__device__ __forceinline__ float roe_sqrt(float x) { return t_sqrt(x); }
+__device__ __forceinline__ double roe_quot(double a, double b, double y) {
+    if (__builtin_expect(hllc_in_range(a) && hllc_in_range(b), 1)) {
+        const double q = a * y;
+        return fma(fma(-q, b, a), y, q);
+    }
+    return div_outright(a, b);
+}
+__device__ __forceinline__ float roe_quot(float a, float, float y) { return a * y; }
+__device__ __forceinline__ double roe_sound(double a, double r, double) { return hllc_sound(a, r); }
+__device__ __forceinline__ float roe_sound(float a, float r, float y) { return t_sqrt(div_by(a, r, y)); }
+
 // Roe flux (Roe 1981) in the face-normal frame with the Harten-Hyman entropy fix
 // on the acoustic waves: delta = max(0, lam~ - lam_L, lam_R - lam~), |lam~| -> delta
 // where |lam~| < delta. Roe averages as in roe_orig (src/global.cpp:407-441).
@@ -612,17 +630,17 @@ __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& 
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     T EL = energy(L.r, L.u, L.v, L.p, IG1);
     T ER = energy(R.r, R.u, R.v, R.p, IG1);
-    const T yL = T(1.0) / L.r, yR = T(1.0) / R.r;  // each shared by two quotients below
-    T HL = div_by(EL + L.p, L.r, yL), HR = div_by(ER + R.p, R.r, yR);
-    T sL = t_sqrt(L.r), sR = t_sqrt(R.r);
-    T w = T(1.0) / (sL + sR);
+    const T yL = roe_recip(L.r), yR = roe_recip(R.r);  // each shared by two quotients below
+    T HL = roe_quot(EL + L.p, L.r, yL), HR = roe_quot(ER + R.p, R.r, yR);
+    T sL = roe_sqrt(L.r), sR = roe_sqrt(R.r);
+    T w = roe_recip(sL + sR);
     T ut = (sL * L.u + sR * R.u) * w;
     T vt = (sL * L.v + sR * R.v) * w;
     T Ht = (sL * HL + sR * HR) * w;
     T q2 = ut * ut + vt * vt;
     T c2 = G1 * (Ht - T(0.5) * q2);
-    T c = t_sqrt(c2);
-    T ic2 = T(1.0) / c2;
+    T c = roe_sqrt(c2);
+    T ic2 = roe_recip(c2);
     T unt = ut * nx + vt * ny;
     T rt = sL * sR;
     T dr = R.r - L.r, dp = R.p - L.p, dun = unR - unL;
@@ -631,7 +649,7 @@ __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& 
     T a2 = dr - dp * ic2;
     T a4 = (dp + rt * c * dun) * (T(0.5) * ic2);
     T l1 = unt - c, l4 = unt + c;
-    T cL = t_sqrt(div_by(GAM * L.p, L.r, yL)), cR = t_sqrt(div_by(GAM * R.p, R.r, yR));
+    T cL = roe_sound(GAM * L.p, L.r, yL), cR = roe_sound(GAM * R.p, R.r, yR);
     T d1 = t_max(T(0.0), t_max(l1 - (unL - cL), (unR - cR) - l1));
     T d4 = t_max(T(0.0), t_max(l4 - (unL + cL), (unR + cR) - l4));
     T al1 = t_abs(l1); if (al1 < d1) al1 = d1;

@@ -565,26 +565,38 @@ static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double
     f[3] = fma(Ss, A3, sp * Ss) * inv;
 }
 
+/* The Roe flux's quotients, reciprocals and square roots: the Newton-refined sequences of
+ * the HLLC flux; a / b from y ~ 1/b corrected once (outside [2^-60, 2^60): IEEE). */
+static double roe_quot(double a, double b, double y) {
+    if (hllc_in_range(a) && hllc_in_range(b)) {
+        double q = a * y;
+        return fma(fma(-q, b, a), y, q);
+    }
+    return a / b;
+}
+
 /* Roe flux (Roe, J. Comput. Phys. 43, 1981) in the face-normal frame with the
  * Harten-Hyman entropy fix on the acoustic waves (Harten & Hyman, J. Comput.
  * Phys. 50, 1983): delta = max(0, lam~ - lam_L, lam_R - lam~), |lam~| -> delta
  * where |lam~| < delta. Roe averages as in the reference's roe_orig
- * (src/global.cpp:407-441). */
+ * (src/global.cpp:407-441); quotients, reciprocals and square roots as roe_quot,
+ * hllc_recip and hllc_sound. */
 static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
     double G1 = GAM - 1.0, IG1 = 1.0 / (GAM - 1.0);
     double unL = dot2(pL->u, nx, pL->v, ny), unR = dot2(pR->u, nx, pR->v, ny);
     double EL = energy(pL->r, pL->u, pL->v, pL->p, IG1);
     double ER = energy(pR->r, pR->u, pR->v, pR->p, IG1);
-    double HL = (EL + pL->p) / pL->r, HR = (ER + pR->p) / pR->r;
-    double sL = sqrt(pL->r), sR = sqrt(pR->r);
-    double w = 1.0 / (sL + sR);
+    double yL = hllc_recip(pL->r), yR = hllc_recip(pR->r);
+    double HL = roe_quot(EL + pL->p, pL->r, yL), HR = roe_quot(ER + pR->p, pR->r, yR);
+    double sL = hllc_sound(pL->r, 1.0), sR = hllc_sound(pR->r, 1.0);
+    double w = hllc_recip(sL + sR);
     double ut = (sL * pL->u + sR * pR->u) * w;
     double vt = (sL * pL->v + sR * pR->v) * w;
     double Ht = (sL * HL + sR * HR) * w;
     double q2 = ut * ut + vt * vt;
     double c2 = G1 * (Ht - 0.5 * q2);
-    double c = sqrt(c2);
-    double ic2 = 1.0 / c2;
+    double c = hllc_sound(c2, 1.0);
+    double ic2 = hllc_recip(c2);
     double unt = ut * nx + vt * ny;
     double rt = sL * sR;
     double dr = pR->r - pL->r, dp = pR->p - pL->p, dun = unR - unL;
@@ -593,7 +605,7 @@ static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double 
     double a2 = dr - dp * ic2;
     double a4 = (dp + rt * c * dun) * (0.5 * ic2);
     double l1 = unt - c, l4 = unt + c;
-    double cL = sqrt(GAM * pL->p / pL->r), cR = sqrt(GAM * pR->p / pR->r);
+    double cL = hllc_sound(GAM * pL->p, pL->r), cR = hllc_sound(GAM * pR->p, pR->r);
     double d1 = dmax(0.0, dmax(l1 - (unL - cL), (unR - cR) - l1));
     double d4 = dmax(0.0, dmax(l4 - (unL + cL), (unR + cR) - l4));
     double al1 = fabs(l1); if (al1 < d1) al1 = d1;
