@@ -232,7 +232,7 @@ __device__ __forceinline__ void adj_flux_rec_edge(const DevCase& c, const AdjCas
 
 // The three faces' contributions summed exactly (SumAcc): the primitive adjoint is
 // rounded once into FP64 (it is summed again in k_adj_cell), the gradient adjoint
-// into the face precision (it only enters products there).
+// into the face precision and divided by the cell's area (it only enters products there).
 template <typename T>
 __global__ void __launch_bounds__(256) k_adj_gather(const DevCase c, const AdjCase a) {
     const int nc = c.nc;
@@ -253,9 +253,12 @@ __global__ void __launch_bounds__(256) k_adj_gather(const DevCase c, const AdjCa
         for (int m = 0; m < 8; m++) g[m].add(v[4 + m]);
     }
     st4(a.qbar, i, q[0].value(), q[1].value(), q[2].value(), q[3].value());
+    // kept divided by the cell's area: the Green-Gauss VJP (k_adj_cell) then needs no
+    // per-face weights of its own and no products by 1/S
+    const T iSi = invS_of<T>(c)[i];
     T gv[8];
 #pragma unroll
-    for (int m = 0; m < 8; m++) gv[m] = g[m].face();
+    for (int m = 0; m < 8; m++) gv[m] = g[m].face() * iSi;
     st8(static_cast<T*>(a.gbar), i, gv);
 }
 
@@ -271,14 +274,13 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
     if (i >= nc) return;
     const MatT<T> mt = matT_of<T>(c, i);
     const Prim<T> q = load_prim(W_of<T>(c), i);
-    const T* iS = invS_of<T>(c);
-    const T* gbar = static_cast<const T*>(a.gbar);
-    // the cell's primitive adjoint: the gathered FP64 value plus an exact sum of the
+    // h = the gradient adjoints divided by the area (k_adj_gather)
+    const T* h = static_cast<const T*>(a.gbar);
+    // the cell's primitive adjoint: the gathered FP64 value plus the sum of the
     // Green-Gauss products (r, u, v, p)
     SumAcc<T> qs[4];
-    T gi[8];
-    ld8(gbar, i, gi);
-    const T iSi = iS[i];
+    T hi[8];
+    ld8(h, i, hi);
     T Tcb = acc0<T>();
     Prim<T> qb = zero_prim<T>();  // ghost-path contributions (boundary faces only)
 #pragma unroll
@@ -287,21 +289,22 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
         const int e = f >> 1;
         const bool side2 = f & 1;
         const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
-        const T wi = (side2 ? T(-0.5) : T(0.5)) * l * iSi;
-        // d g_i / d q_i and d g_i / d (neighbour or ghost): the same weight
-        const T s0 = wi * madd(nx * gi[0], ny, gi[1]), s1 = wi * madd(nx * gi[2], ny, gi[3]);
-        const T s2 = wi * madd(nx * gi[4], ny, gi[5]), s3 = wi * madd(nx * gi[6], ny, gi[7]);
-        qs[0].add(s0); qs[3].add(s1); qs[1].add(s2); qs[2].add(s3);
+        // d g_i / d q_i = +-(l/2) n / S_i, the same for the neighbour's or the ghost's value;
+        // the neighbour's gradient takes q_i with the opposite sign and its own 1/S_j
+        const T w = neg_if(T(0.5) * l, side2);
+        const T wx = w * nx, wy = w * ny;
         const int j = side2 ? c.ec1[e] : c.ec2[e];
-        if (j >= 0) {  // the neighbour's gradient uses this cell's value with the opposite orientation
-            T gj[8];
-            ld8(gbar, j, gj);
-            const T wj = (side2 ? T(0.5) : T(-0.5)) * l * iS[j];
-            qs[0].add(wj * madd(nx * gj[0], ny, gj[1]));
-            qs[3].add(wj * madd(nx * gj[2], ny, gj[3]));
-            qs[1].add(wj * madd(nx * gj[4], ny, gj[5]));
-            qs[2].add(wj * madd(nx * gj[6], ny, gj[7]));
+        if (j >= 0) {
+            T hj[8];
+            ld8(h, j, hj);
+            qs[0].add(madd(wx * (hi[0] - hj[0]), wy, hi[1] - hj[1]));
+            qs[3].add(madd(wx * (hi[2] - hj[2]), wy, hi[3] - hj[3]));
+            qs[1].add(madd(wx * (hi[4] - hj[4]), wy, hi[5] - hj[5]));
+            qs[2].add(madd(wx * (hi[6] - hj[6]), wy, hi[7] - hj[7]));
         } else {  // boundary face: the ghost of the unreconstructed centre state
+            const T s0 = madd(wx * hi[0], wy, hi[1]), s1 = madd(wx * hi[2], wy, hi[3]);
+            const T s2 = madd(wx * hi[4], wy, hi[5]), s3 = madd(wx * hi[6], wy, hi[7]);
+            qs[0].add(s0); qs[3].add(s1); qs[1].add(s2); qs[2].add(s3);
             const DevBnd b = c.bnds[c.ebnd[e]];
             const T Tc = temperature(q, mt.gm1, mt.Cv);
             Prim<T> ob;

@@ -82,8 +82,9 @@ __device__ __forceinline__ void vjp_cons2prim(const T* U, T gm1, const Prim<T>& 
 // (E = p/(r gm1) + (u^2 + v^2)/2): no read of the FP64 state.
 template <typename T>
 __device__ __forceinline__ void vjp_cons2prim_q(const Prim<T>& q, T gm1, const Prim<T>& pb, T* Ub) {
-    const T ro = q.r, iro = T(1.0) / ro, u = q.u, v = q.v;
-    const T e = q.p / (ro * gm1);
+    // derivative factors only: Newton-refined reciprocal and quotient (FP64; FP32 divides)
+    const T ro = q.r, iro = hllc_recip(ro), u = q.u, v = q.v;
+    const T e = hllc_quot(q.p, ro * gm1);
     const T E = madd(e, T(0.5), t_fma(u, u, v * v));
     T rb = madd(pb.r, pb.p * e, gm1);
     const T eb = pb.p * ro * gm1;

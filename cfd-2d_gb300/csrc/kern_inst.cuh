@@ -98,6 +98,13 @@ void update_all(const DevCase& c, int scheme, int stage, cudaStream_t s) {
 
 void KFN(grad)(const DevCase& c, cudaStream_t s) {
     const LaunchShape& l = c.shape[KIND_GRAD];
+#ifdef KGRAD_MM
+    if (c.cf_ax) {  // FP64 with minmod: this project's gradient arithmetic
+        if (l.grid > 0) k_grad<KT, true, true><<<l.grid, l.block, 0, s>>>(c);
+        else k_grad<KT, false, true><<<grid_of(l, c.nc), l.block, 0, s>>>(c);
+        return;
+    }
+#endif
     if (l.grid > 0) k_grad<KT, true><<<l.grid, l.block, 0, s>>>(c);
     else k_grad<KT, false><<<grid_of(l, c.nc), l.block, 0, s>>>(c);
 }

@@ -743,6 +743,39 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
     st8(G_of<T>(c), i, g);
 }
 
+// The FP64 gradients that minmod reconstructs from (this project's arithmetic, the oracle's
+// calc_grad_minmod does the same): per face s = q + o and the weights a = RN(RN(n l) / 2)
+// formed on the host, g = (sum over the faces, ascending edge order, of +-s a, the first
+// term taken as it is) * RN(1/S). 52 FP64 operations per cell where grad_one takes ~128:
+// the halving sits in the weights, the division is a product.
+__device__ __forceinline__ void grad_one_mm(const DevCase& c, int i) {
+    const int nc = c.nc;
+    const double* __restrict__ W = c.W64;
+    const Prim<double> q = load_prim(W, i);
+    double g[8];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int nb = ldcs(c.cf_nb + k * nc + i);
+        const double ax = ldcs(c.cf_ax + k * nc + i), ay = ldcs(c.cf_ay + k * nc + i);
+        const bool side2 = nb >= 0 && (nb & 1);
+        Prim<double> o;
+        if (nb >= 0) {
+            o = load_prim(W, nb >> 1);
+        } else {
+            const double nx = ldcs(c.cf_nx + k * nc + i), ny = ldcs(c.cf_ny + k * nc + i);
+            o = grad_ghost(c, i, -(nb + 1), q, nx, ny);
+        }
+        const double sr = q.r + o.r, sp = q.p + o.p, su = q.u + o.u, sv = q.v + o.v;
+        const double v[8] = {sr * ax, sr * ay, sp * ax, sp * ay, su * ax, su * ay, sv * ax, sv * ay};
+#pragma unroll
+        for (int m = 0; m < 8; m++) g[m] = k == 0 ? neg_if(v[m], side2) : g[m] + neg_if(v[m], side2);
+    }
+    const double y = c.invS[i];
+#pragma unroll
+    for (int m = 0; m < 8; m++) g[m] = g[m] * y;
+    st8(c.G64, i, g);
+}
+
 // 16-byte asynchronous global -> shared copies (cp.async, completion tracked per
 // commit group; the waits are hardware waits, no polling).
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
@@ -765,13 +798,21 @@ __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) 
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
 }
 
-template <typename T, bool STRIDE>
+// MM: this project's arithmetic for minmod (FP64 only, grad_one_mm), else the reference's
+template <typename T, bool STRIDE, bool MM = false>
 __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
+    static_assert(!MM || sizeof(T) == 8, "the minmod gradient arithmetic is FP64's");
     const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
     if constexpr (!STRIDE) {  // one thread per item
-        if (i0 < c.nc) grad_one<T>(c, i0);
+        if (i0 < c.nc) {
+            if constexpr (MM) grad_one_mm(c, i0);
+            else grad_one<T>(c, i0);
+        }
     } else {
-        for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) grad_one<T>(c, i);  // persistent grid
+        for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) {  // persistent grid
+            if constexpr (MM) grad_one_mm(c, i);
+            else grad_one<T>(c, i);
+        }
     }
 }
 

@@ -100,6 +100,10 @@ struct DevCase {
     const double* cf_nx;   // 3*nc (FP64 form)
     const double* cf_ny;
     const double* cf_l;
+    // 3*nc (FP64 form with minmod, else nullptr): RN(RN(nx l) / 2), RN(RN(ny l) / 2) per
+    // face, the weights of this project's Green-Gauss arithmetic (grad_one_mm)
+    const double* cf_ax;
+    const double* cf_ay;
     const float* cf_nx32;  // 3*nc (mixed form)
     const float* cf_ny32;
     const float* cf_l32;

@@ -107,6 +107,14 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
                 c.cfrec32 = upload(rec);
             } else {
                 c.cf_nx = upload(fx); c.cf_ny = upload(fy); c.cf_l = upload(fl);
+                if (task_.recon == RECON_MINMOD) {
+                    std::vector<double> ax(3 * (size_t)nc), ay(3 * (size_t)nc);
+                    for (size_t q = 0; q < 3 * (size_t)nc; q++) {
+                        ax[q] = fx[q] * fl[q] * 0.5;
+                        ay[q] = fy[q] * fl[q] * 0.5;
+                    }
+                    c.cf_ax = upload(ax); c.cf_ay = upload(ay);
+                }
             }
         }
         if (mixed) {

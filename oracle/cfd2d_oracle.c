@@ -701,10 +701,49 @@ void orc_get_state(const orc_solver* s, double* U, double* ctau, unsigned* flags
     if (flags) memcpy(flags, s->flag, sizeof(unsigned) * nc);
 }
 
+/* The gradients minmod reconstructs from, in this project's arithmetic (the GPU's
+ * grad_one_mm): per edge s = phi_1 + phi_2 and the weights a = RN(RN(n l) / 2); per cell
+ * g = (sum over its edges in ascending order of +-s a, the first term taken as it is,
+ * c2 subtracting) * RN(1/S). The same Green-Gauss formula as calcGrad's, rounded
+ * differently. */
+static void calc_grad_minmod(orc_solver* s) {
+    const orc_mesh* m = s->m;
+    double* g = s->grad;
+    unsigned char* seen = (unsigned char*)calloc((size_t)m->nc, 1);
+    if (!seen) abort();
+    for (int e = 0; e < m->ne; e++) {
+        int c1 = m->c1[e], c2 = m->c2[e];
+        Par pL, pR;
+        cons2par(s, c1, &pL);
+        if (c2 > -1) cons2par(s, c2, &pR);
+        else boundary_cond(s, e, &pL, &pR);
+        double ax = m->nx[e] * m->l[e] * 0.5, ay = m->ny[e] * m->l[e] * 0.5;
+        double sr = pL.r + pR.r, sp = pL.p + pR.p, su = pL.u + pR.u, sv = pL.v + pR.v;
+        double v[8] = {sr * ax, sr * ay, sp * ax, sp * ay, su * ax, su * ay, sv * ax, sv * ay};
+        double* g1 = g + 8 * (size_t)c1;
+        for (int k = 0; k < 8; k++) g1[k] = seen[c1] ? g1[k] + v[k] : v[k];
+        seen[c1] = 1;
+        if (c2 > -1) {
+            double* g2 = g + 8 * (size_t)c2;
+            for (int k = 0; k < 8; k++) g2[k] = seen[c2] ? g2[k] + (-v[k]) : -v[k];
+            seen[c2] = 1;
+        }
+    }
+    for (int i = 0; i < m->nc; i++) {
+        double y = 1.0 / m->S[i];
+        for (int k = 0; k < 8; k++) g[8 * (size_t)i + k] *= y;
+    }
+    free(seen);
+}
+
 /* calcGrad, src/methods/fvm_tvd.cpp:242-301 */
 static void calc_grad(orc_solver* s) {
     const orc_mesh* m = s->m;
     double* g = s->grad;
+    if (s->p.recon == ORC_RECON_MINMOD) {
+        calc_grad_minmod(s);
+        return;
+    }
     memset(g, 0, sizeof(double) * 8 * (size_t)m->nc);
     for (int e = 0; e < m->ne; e++) {
         int c1 = m->c1[e], c2 = m->c2[e];
