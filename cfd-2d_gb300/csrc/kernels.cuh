@@ -1090,21 +1090,24 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-// The three signed FP32 face fluxes summed exactly as an FP32 pair, rounded once into FP64.
+// The three signed FP32 face fluxes summed as an FP32 pair (TwoSum) and rounded once to
+// FP32: at most half an FP32 ulp of the residual, below the FP32 rounding its fluxes
+// already carry (cancellation among the three costs nothing), and no FP64 addition on
+// the way to the FP64 update.
 __device__ __forceinline__ void residual_pair_sum(const float t[3][4], double* R) {
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         float s1, e1, s2, e2;
         two_sum(t[0][q], t[1][q], s1, e1);
         two_sum(s1, t[2][q], s2, e2);
-        R[q] = widen(s2) + widen(e1 + e2);
+        R[q] = widen(__fadd_rn(s2, __fadd_rn(e1, e2)));
     }
 }
 
 // Residual of cell i: the reference's ro_int..re_int (src/methods/fvm_tvd.cpp:353-363).
 // FP64 faces: 0 -/+ F in ascending original edge order, the reference's own sums.
 // FP32 faces: the three signed fluxes summed exactly as an FP32 pair, then rounded
-// once into FP64 (as accurate as an FP64 sum of the same three values).
+// once to FP32 (residual_pair_sum).
 template <typename T>
 __device__ __forceinline__ void gather_residual(const DevCase& c, int i, double* R) {
     const int nc = c.nc;
