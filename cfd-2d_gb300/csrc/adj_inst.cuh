@@ -279,8 +279,6 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
     // the cell's primitive adjoint: the gathered FP64 value plus the sum of the
     // Green-Gauss products (r, u, v, p)
     SumAcc<T> qs[4];
-    T hi[8];
-    ld8(h, i, hi);
     T Tcb = acc0<T>();
     Prim<T> qb = zero_prim<T>();  // ghost-path contributions (boundary faces only)
 #pragma unroll
@@ -289,22 +287,25 @@ __global__ void __launch_bounds__(256) k_adj_cell(const DevCase c, const AdjCase
         const int e = f >> 1;
         const bool side2 = f & 1;
         const T nx = NX_of<T>(c)[e], ny = NY_of<T>(c)[e], l = L_of<T>(c)[e];
-        // d g_i / d q_i = +-(l/2) n / S_i, the same for the neighbour's or the ghost's value;
-        // the neighbour's gradient takes q_i with the opposite sign and its own 1/S_j
+        // d g_i / d (neighbour or ghost value) = +-(l/2) n / S_i with n outward from c1; the
+        // neighbour's gradient takes q_i with the opposite sign and its own 1/S_j. The own
+        // value's direct terms, (1/S_i) sum_k (l_k/2) n_out,k over the three faces, are the
+        // outward normals of a closed triangle weighted by their lengths: zero, and left out.
         const T w = neg_if(T(0.5) * l, side2);
         const T wx = w * nx, wy = w * ny;
         const int j = side2 ? c.ec1[e] : c.ec2[e];
         if (j >= 0) {
             T hj[8];
             ld8(h, j, hj);
-            qs[0].add(madd(wx * (hi[0] - hj[0]), wy, hi[1] - hj[1]));
-            qs[3].add(madd(wx * (hi[2] - hj[2]), wy, hi[3] - hj[3]));
-            qs[1].add(madd(wx * (hi[4] - hj[4]), wy, hi[5] - hj[5]));
-            qs[2].add(madd(wx * (hi[6] - hj[6]), wy, hi[7] - hj[7]));
+            qs[0].add(-madd(wx * hj[0], wy, hj[1]));
+            qs[3].add(-madd(wx * hj[2], wy, hj[3]));
+            qs[1].add(-madd(wx * hj[4], wy, hj[5]));
+            qs[2].add(-madd(wx * hj[6], wy, hj[7]));
         } else {  // boundary face: the ghost of the unreconstructed centre state
+            T hi[8];
+            ld8(h, i, hi);
             const T s0 = madd(wx * hi[0], wy, hi[1]), s1 = madd(wx * hi[2], wy, hi[3]);
             const T s2 = madd(wx * hi[4], wy, hi[5]), s3 = madd(wx * hi[6], wy, hi[7]);
-            qs[0].add(s0); qs[3].add(s1); qs[1].add(s2); qs[2].add(s3);
             const DevBnd b = c.bnds[c.ebnd[e]];
             const T Tc = temperature(q, mt.gm1, mt.Cv);
             Prim<T> ob;
