@@ -60,9 +60,6 @@ template <typename T> __device__ __forceinline__ CellFaces<T> cf_of(const DevCas
 template <> __device__ __forceinline__ CellFaces<double> cf_of<double>(const DevCase& c) {
     return CellFaces<double>{c.cf_nx, c.cf_ny, c.cf_l};
 }
-template <> __device__ __forceinline__ CellFaces<float> cf_of<float>(const DevCase& c) {
-    return CellFaces<float>{c.cf_nx32, c.cf_ny32, c.cf_l32};
-}
 template <typename T> __device__ __forceinline__ const T* DL_of(const DevCase& c);
 template <> __device__ __forceinline__ const double* DL_of<double>(const DevCase& c) { return c.dl; }
 template <> __device__ __forceinline__ const float* DL_of<float>(const DevCase& c) { return c.dl32; }
@@ -689,8 +686,8 @@ __device__ __forceinline__ bool num_flux(T* f, const Prim<T>& L, const Prim<T>& 
 // ------------------------------------------------------------------ kernels
 
 // Green-Gauss gradients of r, p, u, v (calcGrad, src/methods/fvm_tvd.cpp:242-301),
-// gathered per cell over its faces in ascending original edge order. FP64 divides
-// by S like the reference; the mixed form multiplies by 1/S in FP32.
+// gathered per cell over its faces in ascending original edge order, dividing by S like
+// the reference (FP64; the minmod arithmetic is grad_one_mm, the mixed form's grad_one_w).
 // One face of the Green-Gauss sum: g +-= (q + o)/2 n l (c2 subtracts, c1 adds).
 template <typename T>
 __device__ __forceinline__ void grad_face(T* g, const Prim<T>& q, const Prim<T>& o, T nx, T ny, T l, bool side2) {
@@ -709,19 +706,14 @@ __device__ __forceinline__ Prim<T> grad_ghost(const DevCase& c, int i, int e, co
     const T Tc = temperature(q, mt.gm1, mt.Cv);
     return ghost_state(c.bnds[c.ebnd[e]], q, Tc, nx, ny, mt.M);
 }
-// The sum divided by the area: FP64 through the host-rounded reciprocal (correctly
-// rounded), FP32 as a product with 1/S.
+// The sum divided by the area through the host-rounded reciprocal (correctly rounded, the
+// reference's division); FP64 faces only (the mixed form's gradients are grad_one_w's).
 template <typename T>
 __device__ __forceinline__ void grad_finish(const DevCase& c, int i, T* g) {
-    if constexpr (sizeof(T) == 8) {
-        const double s = c.S[i], y = c.invS[i];  // y = RN(1/S), computed on the host
+    static_assert(sizeof(T) == 8, "the reference's Green-Gauss rounding is kept in FP64");
+    const double s = c.S[i], y = c.invS[i];  // y = RN(1/S), computed on the host
 #pragma unroll
-        for (int m = 0; m < 8; m++) g[m] = div_rn(g[m], s, y);
-    } else {
-        const float is = c.invS32[i];
-#pragma unroll
-        for (int m = 0; m < 8; m++) g[m] = g[m] * is;
-    }
+    for (int m = 0; m < 8; m++) g[m] = div_rn(g[m], s, y);
 }
 
 template <typename T>
@@ -776,6 +768,48 @@ __device__ __forceinline__ void grad_one_mm(const DevCase& c, int i) {
     st8(c.G64, i, g);
 }
 
+// The mixed form's gradients (FP32 faces, every stage path): per face s = q + o and the
+// host-formed weights a = RN32(n l / 2), g = (sum over the faces, ascending edge order, of
+// +-s a, the first term taken as it is) * RN32(1/S): 60 FP32 operations per cell where the
+// reference's expression takes 104. The sign flips run on the integer pipe, so no product
+// is contracted into a sum and every path forms the same bits.
+__device__ __forceinline__ void grad_face_w(float* g, const Prim<float>& q, const Prim<float>& o, float ax, float ay,
+                                            bool side2, bool first) {
+    const float sr = q.r + o.r, sp = q.p + o.p, su = q.u + o.u, sv = q.v + o.v;
+    const float v[8] = {sr * ax, sr * ay, sp * ax, sp * ay, su * ax, su * ay, sv * ax, sv * ay};
+#pragma unroll
+    for (int m = 0; m < 8; m++) g[m] = first ? neg_if(v[m], side2) : g[m] + neg_if(v[m], side2);
+}
+__device__ __forceinline__ void grad_finish_w(const DevCase& c, int i, float* g) {
+    const float is = c.invS32[i];
+#pragma unroll
+    for (int m = 0; m < 8; m++) g[m] = g[m] * is;
+}
+// k_grad's cell for the mixed form: the three faces through the per-cell arrays (the
+// boundary ghosts take the edge's normal)
+__device__ __forceinline__ void grad_one_w(const DevCase& c, int i) {
+    const int nc = c.nc;
+    const float* __restrict__ W = c.W32;
+    const Prim<float> q = load_prim(W, i);
+    float g[8];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int nb = ldcs(c.cf_nb + k * nc + i);
+        const float ax = ldcs(c.cf_ax32 + k * nc + i), ay = ldcs(c.cf_ay32 + k * nc + i);
+        const bool side2 = nb >= 0 && (nb & 1);
+        Prim<float> o;
+        if (nb >= 0) {
+            o = load_prim(W, nb >> 1);
+        } else {
+            const int e = -(nb + 1);
+            o = grad_ghost(c, i, e, q, c.nx32[e], c.ny32[e]);
+        }
+        grad_face_w(g, q, o, ax, ay, side2, k == 0);
+    }
+    grad_finish_w(c, i, g);
+    st8(c.G32, i, g);
+}
+
 // 16-byte asynchronous global -> shared copies (cp.async, completion tracked per
 // commit group; the waits are hardware waits, no polling).
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
@@ -798,7 +832,8 @@ __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gmem_src) 
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src) : "memory");
 }
 
-// MM: this project's arithmetic for minmod (FP64 only, grad_one_mm), else the reference's
+// MM: this project's arithmetic for minmod (FP64 only, grad_one_mm); FP32 faces the mixed
+// form's (grad_one_w); else the reference's
 template <typename T, bool STRIDE, bool MM = false>
 __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
     static_assert(!MM || sizeof(T) == 8, "the minmod gradient arithmetic is FP64's");
@@ -806,11 +841,13 @@ __global__ void __launch_bounds__(256) k_grad(const DevCase c) {
     if constexpr (!STRIDE) {  // one thread per item
         if (i0 < c.nc) {
             if constexpr (MM) grad_one_mm(c, i0);
+            else if constexpr (sizeof(T) == 4) grad_one_w(c, i0);
             else grad_one<T>(c, i0);
         }
     } else {
         for (int i = i0; i < c.nc; i += gridDim.x * blockDim.x) {  // persistent grid
             if constexpr (MM) grad_one_mm(c, i);
+            else if constexpr (sizeof(T) == 4) grad_one_w(c, i);
             else grad_one<T>(c, i);
         }
     }
@@ -1300,16 +1337,15 @@ __global__ void __launch_bounds__(256, 5) k_stage_fused(const DevCase c, const D
             for (int k = threadIdx.x; k < nG; k += blockDim.x) {
                 const int i = k < n_own ? own0 + k : tl.halo[h0 + k - n_own];
                 const Prim<float> q = prim(k);
-                float g[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                float g[8];
 #pragma unroll
                 for (int f = 0; f < 3; f++) {
                     const int2 fr = gf[3 * k + f];
                     const int e = fr.x >> 1, nb = fr.y & 0xffff;
-                    const float nx = c.nx32[e], ny = c.ny32[e], l = c.l32[e];
-                    const Prim<float> o = nb != 0xffff ? prim(nb) : grad_ghost(c, i, e, q, nx, ny);
-                    grad_face(g, q, o, nx, ny, l, (fr.x & 1) != 0);
+                    const Prim<float> o = nb != 0xffff ? prim(nb) : grad_ghost(c, i, e, q, c.nx32[e], c.ny32[e]);
+                    grad_face_w(g, q, o, c.ax32[e], c.ay32[e], (fr.x & 1) != 0, f == 0);
                 }
-                grad_finish(c, i, g);
+                grad_finish_w(c, i, g);
                 Gs[2 * k] = make_float4(g[0], g[1], g[2], g[3]);
                 Gs[2 * k + 1] = make_float4(g[4], g[5], g[6], g[7]);
             }
@@ -1359,23 +1395,26 @@ __global__ void __launch_bounds__(256, 5) k_stage_fused(const DevCase c, const D
     cp_async_wait<0>();
 }
 
-// Gradient of cell i (FP32 faces) from its three 16-byte face records: the operations of
-// grad_one on the same values.
+// Gradient of cell i (FP32 faces) from its three 16-byte face records {neighbour, a_x,
+// a_y, 0}: the operations of grad_one_w on the same values.
 __device__ __forceinline__ void grad_of_cell(const DevCase& c, int i, const Prim<float>& q, float* g) {
     const float4* __restrict__ rec = c.cfrec32 + 3 * (size_t)i;
     const float* __restrict__ W = c.W32;
 #pragma unroll
-    for (int m = 0; m < 8; m++) g[m] = 0.f;
-#pragma unroll
     for (int k = 0; k < 3; k++) {
         const float4 r = __ldg(rec + k);
         const int nb = __float_as_int(r.x);
-        const float nx = r.y, ny = r.z, l = r.w;
         const bool side2 = nb >= 0 && (nb & 1);
-        const Prim<float> o = nb >= 0 ? load_prim(W, nb >> 1) : grad_ghost(c, i, -(nb + 1), q, nx, ny);
-        grad_face(g, q, o, nx, ny, l, side2);
+        Prim<float> o;
+        if (nb >= 0) {
+            o = load_prim(W, nb >> 1);
+        } else {
+            const int e = -(nb + 1);
+            o = grad_ghost(c, i, e, q, c.nx32[e], c.ny32[e]);
+        }
+        grad_face_w(g, q, o, r.y, r.z, side2, k == 0);
     }
-    grad_finish(c, i, g);
+    grad_finish_w(c, i, g);
 }
 
 // The mixed form's edge flux with the two cells' Green-Gauss gradients formed in the
@@ -1383,7 +1422,7 @@ __device__ __forceinline__ void grad_of_cell(const DevCase& c, int i, const Prim
 // records) instead of read from G: no gradient array written and read back, no gradient
 // launch. The same operations on the same values as k_grad + k_flux, so the same fluxes.
 template <int FLUX, int RECON>
-__global__ void __launch_bounds__(256) k_flux_grad(const DevCase c) {
+__global__ void __launch_bounds__(256, 4) k_flux_grad(const DevCase c) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
     const float* __restrict__ W = c.W32;

@@ -104,9 +104,10 @@ struct DevCase {
     // face, the weights of this project's Green-Gauss arithmetic (grad_one_mm)
     const double* cf_ax;
     const double* cf_ay;
-    const float* cf_nx32;  // 3*nc (mixed form)
-    const float* cf_ny32;
-    const float* cf_l32;
+    // 3*nc (mixed form): RN32(nx l / 2), RN32(ny l / 2) per face, the weights of the mixed
+    // form's Green-Gauss arithmetic (grad_one_w)
+    const float* cf_ax32;
+    const float* cf_ay32;
     const int* ec1;        // ne
     const int* ec2;        // ne
     const int* ebnd;       // ne (boundary index, -1 inside)
@@ -117,6 +118,8 @@ struct DevCase {
     const float* nx32;
     const float* ny32;
     const float* l32;
+    const float* ax32;     // ne (mixed form): the per-edge gradient weights, as cf_ax32
+    const float* ay32;
     const float* dl32;
     const double* S;       // nc
     const double* invS;    // nc, RN(1/S) (FP64 form)
@@ -132,7 +135,7 @@ struct DevCase {
     float ig1_flux_f;      // 1/(gam_flux - 1) in FP32
     float lim_f[5];        // limits in FP32 (mixed form)
     const float* invS32;   // nc, 1/S in FP32 (mixed form)
-    const float4* cfrec32; // 3*nc (mixed form): per cell and face {cf_nb bits, nx, ny, l} in one 16-byte record
+    const float4* cfrec32; // 3*nc (mixed form): per cell and face {cf_nb bits, a_x, a_y, 0} in one 16-byte record
     double gam_flux;
     double ig1_flux;       // RN(1/(gam_flux - 1)), computed on the host
     RimGas<double> rg_flux;  // the exact Riemann solver's constants of gam_flux

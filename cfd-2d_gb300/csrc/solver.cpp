@@ -95,14 +95,20 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
             }
             c.cf_nb = upload(nb);
             if (mixed) {
-                c.cf_nx32 = upload(to_f32(fx)); c.cf_ny32 = upload(to_f32(fy)); c.cf_l32 = upload(to_f32(fl));
+                // the mixed form's gradient weights RN32(n l / 2), from the FP64 product
+                std::vector<float> ax(3 * (size_t)nc), ay(3 * (size_t)nc);
+                for (size_t q = 0; q < 3 * (size_t)nc; q++) {
+                    ax[q] = (float)(fx[q] * fl[q] * 0.5);
+                    ay[q] = (float)(fy[q] * fl[q] * 0.5);
+                }
+                c.cf_ax32 = upload(ax); c.cf_ay32 = upload(ay);
                 std::vector<float4> rec(3 * (size_t)nc);
                 for (int i = 0; i < nc; i++)
                     for (int k = 0; k < 3; k++) {
                         const size_t q = (size_t)k * nc + i;
                         float nbf;
                         std::memcpy(&nbf, &nb[q], sizeof nbf);
-                        rec[3 * (size_t)i + k] = make_float4(nbf, (float)fx[q], (float)fy[q], (float)fl[q]);
+                        rec[3 * (size_t)i + k] = make_float4(nbf, ax[q], ay[q], 0.f);
                     }
                 c.cfrec32 = upload(rec);
             } else {
@@ -121,6 +127,12 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
             c.nx32 = upload(to_f32(lay_.nx));
             c.ny32 = upload(to_f32(lay_.ny));
             c.l32 = upload(to_f32(lay_.l));
+            std::vector<float> ex(ne), ey(ne);
+            for (int e = 0; e < ne; e++) {
+                ex[e] = (float)(lay_.nx[e] * lay_.l[e] * 0.5);
+                ey[e] = (float)(lay_.ny[e] * lay_.l[e] * 0.5);
+            }
+            c.ax32 = upload(ex); c.ay32 = upload(ey);
             c.dl32 = upload(to_f32(lay_.dl));
             std::vector<float> is(nc);
             for (int i = 0; i < nc; i++) is[i] = (float)(1.0 / lay_.S[i]);
