@@ -602,7 +602,7 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
 
 // The Roe flux's own quotients, reciprocals and square roots: with FP64 faces the
 // Newton-refined sequences of the HLLC flux (this project's definition, the oracle does the
-// same), a / b from a given y ~ 1/b corrected once; FP32 faces as before.
+// same), a / b from a given y ~ 1/b corrected once; FP32 faces divide and take square roots outright.
 __device__ __forceinline__ double roe_recip(double x) { return hllc_recip(x); }
 __device__ __forceinline__ float roe_recip(float x) { return 1.0f / x; }
 __device__ __forceinline__ double roe_sqrt(double x) { return hllc_sound(x, 1.0); }
@@ -738,7 +738,7 @@ __device__ __forceinline__ void grad_one(const DevCase& c, int i) {
 // The FP64 gradients that minmod reconstructs from (this project's arithmetic, the oracle's
 // calc_grad_minmod does the same): per face s = q + o and the weights a = RN(RN(n l) / 2)
 // formed on the host, g = (sum over the faces, ascending edge order, of +-s a, the first
-// term taken as it is) * RN(1/S). 52 FP64 operations per cell where grad_one takes ~128:
+// term taken as it is) * RN(1/S). 60 FP64 operations per cell where grad_one takes ~128:
 // the halving sits in the weights, the division is a product.
 __device__ __forceinline__ void grad_one_mm(const DevCase& c, int i) {
     const int nc = c.nc;
