@@ -600,44 +600,27 @@ __device__ __forceinline__ void flux_hllc(T* f, const Prim<T>& L, const Prim<T>&
     flux_hllc_c(f, L, R, cL, cR, nx, ny, IG1);
 }
 
-// The Roe flux's own quotients, reciprocals and square roots: with FP64 faces the
-// Newton-refined sequences of the HLLC flux (this project's definition, the oracle does the
-// same), a / b from a given y ~ 1/b corrected once; FP32 faces divide and take square roots outright.
-__device__ __forceinline__ double roe_recip(double x) { return hllc_recip(x); }
-__device__ __forceinline__ float roe_recip(float x) { return 1.0f / x; }
-__device__ __forceinline__ double roe_sqrt(double x) { return hllc_sound(x, 1.0); }
-__device__ __forceinline__ float roe_sqrt(float x) { return t_sqrt(x); }
-__device__ __forceinline__ double roe_quot(double a, double b, double y) {
-    if (__builtin_expect(hllc_in_range(a) && hllc_in_range(b), 1)) {
-        const double q = a * y;
-        return fma(fma(-q, b, a), y, q);
-    }
-    return div_outright(a, b);
-}
-__device__ __forceinline__ float roe_quot(float a, float, float y) { return a * y; }
-__device__ __forceinline__ double roe_sound(double a, double r, double) { return hllc_sound(a, r); }
-__device__ __forceinline__ float roe_sound(float a, float r, float y) { return t_sqrt(div_by(a, r, y)); }
-
 // Roe flux (Roe 1981) in the face-normal frame with the Harten-Hyman entropy fix
 // on the acoustic waves: delta = max(0, lam~ - lam_L, lam_R - lam~), |lam~| -> delta
-// where |lam~| < delta. Roe averages as in roe_orig (src/global.cpp:407-441).
+// where |lam~| < delta. Roe averages as in roe_orig (src/global.cpp:407-441). FP32 faces
+// (the mixed form); the FP64 faces' arithmetic is the overload below.
 template <typename T>
 __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& R, T nx, T ny, T GAM, T IG1) {
     T G1 = GAM - T(1.0);
     T unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
     T EL = energy(L.r, L.u, L.v, L.p, IG1);
     T ER = energy(R.r, R.u, R.v, R.p, IG1);
-    const T yL = roe_recip(L.r), yR = roe_recip(R.r);  // each shared by two quotients below
-    T HL = roe_quot(EL + L.p, L.r, yL), HR = roe_quot(ER + R.p, R.r, yR);
-    T sL = roe_sqrt(L.r), sR = roe_sqrt(R.r);
-    T w = roe_recip(sL + sR);
+    const T yL = T(1.0) / L.r, yR = T(1.0) / R.r;  // each shared by two quotients below
+    T HL = div_by(EL + L.p, L.r, yL), HR = div_by(ER + R.p, R.r, yR);
+    T sL = t_sqrt(L.r), sR = t_sqrt(R.r);
+    T w = T(1.0) / (sL + sR);
     T ut = (sL * L.u + sR * R.u) * w;
     T vt = (sL * L.v + sR * R.v) * w;
     T Ht = (sL * HL + sR * HR) * w;
     T q2 = ut * ut + vt * vt;
     T c2 = G1 * (Ht - T(0.5) * q2);
-    T c = roe_sqrt(c2);
-    T ic2 = roe_recip(c2);
+    T c = t_sqrt(c2);
+    T ic2 = T(1.0) / c2;
     T unt = ut * nx + vt * ny;
     T rt = sL * sR;
     T dr = R.r - L.r, dp = R.p - L.p, dun = unR - unL;
@@ -646,7 +629,7 @@ __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& 
     T a2 = dr - dp * ic2;
     T a4 = (dp + rt * c * dun) * (T(0.5) * ic2);
     T l1 = unt - c, l4 = unt + c;
-    T cL = roe_sound(GAM * L.p, L.r, yL), cR = roe_sound(GAM * R.p, R.r, yR);
+    T cL = t_sqrt(div_by(GAM * L.p, L.r, yL)), cR = t_sqrt(div_by(GAM * R.p, R.r, yR));
     T d1 = t_max(T(0.0), t_max(l1 - (unL - cL), (unR - cR) - l1));
     T d4 = t_max(T(0.0), t_max(l4 - (unL + cL), (unR + cR) - l4));
     T al1 = t_abs(l1); if (al1 < d1) al1 = d1;
@@ -664,6 +647,71 @@ __device__ __forceinline__ void flux_roe(T* f, const Prim<T>& L, const Prim<T>& 
     f[1] = T(0.5) * (FL[1] + FR[1] - D1);
     f[2] = T(0.5) * (FL[2] + FR[2] - D2);
     f[3] = T(0.5) * (FL[3] + FR[3] - D3);
+}
+
+// 1/sqrt(x) for x > 0 in [2^-60, 2^60): t = RN32(1 / RN32(sqrt(x truncated to binary32))),
+// then two Newton steps t <- t + (t/2)(1 - x t t); other operands: IEEE
+static __device__ __noinline__ double rsqrt_outright(double x) { return 1.0 / sqrt(x); }
+__device__ __forceinline__ double roe_rsqrt(double x) {
+    if (__builtin_expect(__double_as_longlong(x) <= 0 || !hllc_in_range(x), 0)) return rsqrt_outright(x);
+    double t = widen(__fdiv_rn(1.0f, __fsqrt_rn(hllc_seed(x))));
+    t = fma(0.5 * t, fma(-(x * t), t, 1.0), t);
+    t = fma(0.5 * t, fma(-(x * t), t, 1.0), t);
+    return t;
+}
+static __device__ __noinline__ double sqrt_outright(double x) { return sqrt(x); }
+
+// The Roe flux with FP64 faces, this project's arithmetic (the oracle's flux_roe does the
+// same): the Roe averages from t = 1/sqrt(rho) (sqrt(rho) = rho t, sqrt(rho) H = (E + p) t),
+// c~ = c~^2 t~ and 1/c~^2 = t~^2 with t~ = 1/sqrt(c~^2), the side sound speeds as HLLC's,
+// 1/(sqrt(rho_L) + sqrt(rho_R)) Newton-refined, and the wave sums fused.
+__device__ __forceinline__ void flux_roe(double* f, const Prim<double>& L, const Prim<double>& R, double nx,
+                                         double ny, double GAM, double IG1) {
+    const double G1 = GAM - 1.0;
+    const double unL = dot2(L.u, nx, L.v, ny), unR = dot2(R.u, nx, R.v, ny);
+    const double EL = energy(L.r, L.u, L.v, L.p, IG1), ER = energy(R.r, R.u, R.v, R.p, IG1);
+    const double tL = roe_rsqrt(L.r), tR = roe_rsqrt(R.r);
+    const double sL = L.r * tL, sR = R.r * tR;
+    const double w = hllc_recip(sL + sR);
+    const double ut = fma(sL, L.u, sR * R.u) * w, vt = fma(sL, L.v, sR * R.v) * w;
+    const double Ht = fma(EL + L.p, tL, (ER + R.p) * tR) * w;
+    const double q2 = fma(ut, ut, vt * vt);
+    const double c2 = G1 * fma(-0.5, q2, Ht);
+    double c, ic2;
+    if (__builtin_expect(c2 > 0.0 && hllc_in_range(c2), 1)) {
+        const double t = roe_rsqrt(c2);
+        c = c2 * t;
+        ic2 = t * t;
+    } else {
+        c = sqrt_outright(c2);
+        ic2 = recip_outright(c2);
+    }
+    const double unt = dot2(ut, nx, vt, ny);
+    const double rt = sL * sR;
+    const double dr = R.r - L.r, dp = R.p - L.p, dun = unR - unL;
+    const double dtx = fma(-dun, nx, R.u - L.u), dty = fma(-dun, ny, R.v - L.v);
+    const double h = 0.5 * ic2, x = (rt * c) * dun;
+    const double a1 = (dp - x) * h, a2 = fma(-dp, ic2, dr), a4 = (dp + x) * h;
+    const double l1 = unt - c, l4 = unt + c;
+    const double cL = hllc_sound(GAM * L.p, L.r), cR = hllc_sound(GAM * R.p, R.r);
+    const double d1 = t_max(0.0, t_max(l1 - (unL - cL), (unR - cR) - l1));
+    const double d4 = t_max(0.0, t_max(l4 - (unL + cL), (unR + cR) - l4));
+    double al1 = t_abs(l1); if (al1 < d1) al1 = d1;
+    double al4 = t_abs(l4); if (al4 < d4) al4 = d4;
+    const double al2 = t_abs(unt);
+    const double w1 = al1 * a1, w2 = al2 * a2, w4 = al4 * a4, ws = al2 * rt;
+    const double cx = c * nx, cy = c * ny, cu = unt * c;
+    const double D0 = (w1 + w2) + w4;
+    const double D1 = fma(w4, ut + cx, fma(w1, ut - cx, fma(w2, ut, ws * dtx)));
+    const double D2 = fma(w4, vt + cy, fma(w1, vt - cy, fma(w2, vt, ws * dty)));
+    const double D3 = fma(w4, Ht + cu, fma(w1, Ht - cu, fma(0.5 * w2, q2, ws * dot2(ut, dtx, vt, dty))));
+    double FL[4], FR[4];
+    phys_flux(FL, L.r, L.u, L.v, L.p, EL, unL, nx, ny);
+    phys_flux(FR, R.r, R.u, R.v, R.p, ER, unR, nx, ny);
+    f[0] = 0.5 * ((FL[0] + FR[0]) - D0);
+    f[1] = 0.5 * ((FL[1] + FR[1]) - D1);
+    f[2] = 0.5 * ((FL[2] + FR[2]) - D2);
+    f[3] = 0.5 * ((FL[3] + FR[3]) - D3);
 }
 
 template <typename T, int FLUX>

@@ -565,45 +565,53 @@ static void flux_hllc(double* f, const Par* pL, const Par* pR, double nx, double
     f[3] = fma(Ss, A3, sp * Ss) * inv;
 }
 
-/* The Roe flux's quotients, reciprocals and square roots: the Newton-refined sequences of
- * the HLLC flux; a / b from y ~ 1/b corrected once (outside [2^-60, 2^60): IEEE). */
-static double roe_quot(double a, double b, double y) {
-    if (hllc_in_range(a) && hllc_in_range(b)) {
-        double q = a * y;
-        return fma(fma(-q, b, a), y, q);
-    }
-    return a / b;
+/* 1/sqrt(x) for x > 0 in [2^-60, 2^60): t = RN32(1 / RN32(sqrt(x truncated to binary32))),
+ * then two Newton steps t <- t + (t/2)(1 - x t t); other operands: IEEE. */
+static double roe_rsqrt(double x) {
+    if (!(x > 0.0) || !hllc_in_range(x)) return 1.0 / sqrt(x);
+    float sf = sqrtf(hllc_seed(x));
+    float tf = 1.0f / sf;
+    double t = (double)tf;
+    t = fma(0.5 * t, fma(-(x * t), t, 1.0), t);
+    t = fma(0.5 * t, fma(-(x * t), t, 1.0), t);
+    return t;
 }
 
 /* Roe flux (Roe, J. Comput. Phys. 43, 1981) in the face-normal frame with the
  * Harten-Hyman entropy fix on the acoustic waves (Harten & Hyman, J. Comput.
  * Phys. 50, 1983): delta = max(0, lam~ - lam_L, lam_R - lam~), |lam~| -> delta
  * where |lam~| < delta. Roe averages as in the reference's roe_orig
- * (src/global.cpp:407-441); quotients, reciprocals and square roots as roe_quot,
- * hllc_recip and hllc_sound. */
+ * (src/global.cpp:407-441). This project's arithmetic: the averages from
+ * t = 1/sqrt(rho) (sqrt(rho) = rho t, sqrt(rho) H = (E + p) t), c~ = c~^2 t~ and
+ * 1/c~^2 = t~^2 with t~ = 1/sqrt(c~^2), the side sound speeds as HLLC's,
+ * 1/(sqrt(rho_L) + sqrt(rho_R)) Newton-refined, the wave sums fused. */
 static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double ny, double GAM) {
     double G1 = GAM - 1.0, IG1 = 1.0 / (GAM - 1.0);
     double unL = dot2(pL->u, nx, pL->v, ny), unR = dot2(pR->u, nx, pR->v, ny);
     double EL = energy(pL->r, pL->u, pL->v, pL->p, IG1);
     double ER = energy(pR->r, pR->u, pR->v, pR->p, IG1);
-    double yL = hllc_recip(pL->r), yR = hllc_recip(pR->r);
-    double HL = roe_quot(EL + pL->p, pL->r, yL), HR = roe_quot(ER + pR->p, pR->r, yR);
-    double sL = hllc_sound(pL->r, 1.0), sR = hllc_sound(pR->r, 1.0);
+    double tL = roe_rsqrt(pL->r), tR = roe_rsqrt(pR->r);
+    double sL = pL->r * tL, sR = pR->r * tR;
     double w = hllc_recip(sL + sR);
-    double ut = (sL * pL->u + sR * pR->u) * w;
-    double vt = (sL * pL->v + sR * pR->v) * w;
-    double Ht = (sL * HL + sR * HR) * w;
-    double q2 = ut * ut + vt * vt;
-    double c2 = G1 * (Ht - 0.5 * q2);
-    double c = hllc_sound(c2, 1.0);
-    double ic2 = hllc_recip(c2);
-    double unt = ut * nx + vt * ny;
+    double ut = fma(sL, pL->u, sR * pR->u) * w, vt = fma(sL, pL->v, sR * pR->v) * w;
+    double Ht = fma(EL + pL->p, tL, (ER + pR->p) * tR) * w;
+    double q2 = fma(ut, ut, vt * vt);
+    double c2 = G1 * fma(-0.5, q2, Ht);
+    double c, ic2;
+    if (c2 > 0.0 && hllc_in_range(c2)) {
+        double t = roe_rsqrt(c2);
+        c = c2 * t;
+        ic2 = t * t;
+    } else {
+        c = sqrt(c2);
+        ic2 = 1.0 / c2;
+    }
+    double unt = dot2(ut, nx, vt, ny);
     double rt = sL * sR;
     double dr = pR->r - pL->r, dp = pR->p - pL->p, dun = unR - unL;
-    double dtx = (pR->u - pL->u) - dun * nx, dty = (pR->v - pL->v) - dun * ny;
-    double a1 = (dp - rt * c * dun) * (0.5 * ic2);
-    double a2 = dr - dp * ic2;
-    double a4 = (dp + rt * c * dun) * (0.5 * ic2);
+    double dtx = fma(-dun, nx, pR->u - pL->u), dty = fma(-dun, ny, pR->v - pL->v);
+    double h = 0.5 * ic2, x = (rt * c) * dun;
+    double a1 = (dp - x) * h, a2 = fma(-dp, ic2, dr), a4 = (dp + x) * h;
     double l1 = unt - c, l4 = unt + c;
     double cL = hllc_sound(GAM * pL->p, pL->r), cR = hllc_sound(GAM * pR->p, pR->r);
     double d1 = dmax(0.0, dmax(l1 - (unL - cL), (unR - cR) - l1));
@@ -612,17 +620,18 @@ static void flux_roe(double* f, const Par* pL, const Par* pR, double nx, double 
     double al4 = fabs(l4); if (al4 < d4) al4 = d4;
     double al2 = fabs(unt);
     double w1 = al1 * a1, w2 = al2 * a2, w4 = al4 * a4, ws = al2 * rt;
-    double D0 = w1 + w2 + w4;
-    double D1 = w1 * (ut - c * nx) + (w2 * ut + ws * dtx) + w4 * (ut + c * nx);
-    double D2 = w1 * (vt - c * ny) + (w2 * vt + ws * dty) + w4 * (vt + c * ny);
-    double D3 = w1 * (Ht - unt * c) + (w2 * (0.5 * q2) + ws * (ut * dtx + vt * dty)) + w4 * (Ht + unt * c);
+    double cx = c * nx, cy = c * ny, cu = unt * c;
+    double D0 = (w1 + w2) + w4;
+    double D1 = fma(w4, ut + cx, fma(w1, ut - cx, fma(w2, ut, ws * dtx)));
+    double D2 = fma(w4, vt + cy, fma(w1, vt - cy, fma(w2, vt, ws * dty)));
+    double D3 = fma(w4, Ht + cu, fma(w1, Ht - cu, fma(0.5 * w2, q2, ws * dot2(ut, dtx, vt, dty))));
     double FL[4], FR[4];
     phys_flux(FL, pL->r, pL->u, pL->v, pL->p, EL, unL, nx, ny);
     phys_flux(FR, pR->r, pR->u, pR->v, pR->p, ER, unR, nx, ny);
-    f[0] = 0.5 * (FL[0] + FR[0] - D0);
-    f[1] = 0.5 * (FL[1] + FR[1] - D1);
-    f[2] = 0.5 * (FL[2] + FR[2] - D2);
-    f[3] = 0.5 * (FL[3] + FR[3] - D3);
+    f[0] = 0.5 * ((FL[0] + FR[0]) - D0);
+    f[1] = 0.5 * ((FL[1] + FR[1]) - D1);
+    f[2] = 0.5 * ((FL[2] + FR[2]) - D2);
+    f[3] = 0.5 * ((FL[3] + FR[3]) - D3);
 }
 
 /* MINMOD, src/methods/LimiterDGCockburn.cpp:110-123 */
