@@ -132,7 +132,7 @@ __device__ __forceinline__ void adj_flux_edge(const DevCase& c, const AdjCase& a
 // (FluxRec: face states, sound speeds, minmod's branches) for k_adj_flux_rec. Compiled with
 // the forward kernels' flags and the same code, so F is the forward's bit for bit.
 template <typename T, int RECON>
-__global__ void __launch_bounds__(256) k_flux_rec(const DevCase c, const FluxRec r) {
+__global__ void __launch_bounds__(128) k_flux_rec(const DevCase c, const FluxRec r) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= c.ne) return;
     T out[4];
@@ -367,10 +367,12 @@ void KFN(adj_flux)(const DevCase& c, const AdjCase& a, int flux, int recon, cuda
     else adj_flux_by_recon<FLUX_LAX>(c, a, recon, s);
 }
 void KFN(flux_rec)(const DevCase& c, int recon, const FluxRec& r, cudaStream_t s) {
-    const int g = adj_nblk(c.ne, 256);
-    if (recon == RECON_NONE) k_flux_rec<KT, RECON_NONE><<<g, 256, 0, s>>>(c, r);
-    else if (recon == RECON_LINEAR) k_flux_rec<KT, RECON_LINEAR><<<g, 256, 0, s>>>(c, r);
-    else k_flux_rec<KT, RECON_MINMOD><<<g, 256, 0, s>>>(c, r);
+    // 128-thread blocks: at ~164 registers a thread, 256-thread blocks leave one block (8
+    // warps) per SM, 128-thread blocks three (12 warps)
+    const int g = adj_nblk(c.ne, 128);
+    if (recon == RECON_NONE) k_flux_rec<KT, RECON_NONE><<<g, 128, 0, s>>>(c, r);
+    else if (recon == RECON_LINEAR) k_flux_rec<KT, RECON_LINEAR><<<g, 128, 0, s>>>(c, r);
+    else k_flux_rec<KT, RECON_MINMOD><<<g, 128, 0, s>>>(c, r);
 }
 void KFN(adj_flux_rec)(const DevCase& c, const AdjCase& a, int recon, const FluxRec& r, cudaStream_t s) {
     const int g = adj_nblk(c.ne, 128);
