@@ -945,13 +945,24 @@ template <typename T> struct EdgeGeo { T nx, ny, l, dl[8]; };
 template <typename T, int RECON>
 __device__ __forceinline__ EdgeGeo<T> load_geo(const DevCase& c, int e) {
     EdgeGeo<T> g;
-    g.nx = ldcs(NX_of<T>(c) + e);
-    g.ny = ldcs(NY_of<T>(c) + e);
-    g.l = ldcs(L_of<T>(c) + e);
-    if (RECON != RECON_NONE) {
-        const T* __restrict__ DL = DL_of<T>(c);
+    if constexpr (sizeof(T) == 4) {  // FP32 faces: the edge's three 16-byte records
+        const float4* __restrict__ r = c.geo32 + 3 * (size_t)e;
+        const float4 a = __ldcs(r);
+        g.nx = a.x; g.ny = a.y; g.l = a.z;
+        if (RECON != RECON_NONE) {
+            const float4 b = __ldcs(r + 1), d = __ldcs(r + 2);
+            g.dl[0] = b.x; g.dl[1] = b.y; g.dl[2] = b.z; g.dl[3] = b.w;
+            g.dl[4] = d.x; g.dl[5] = d.y; g.dl[6] = d.z; g.dl[7] = d.w;
+        }
+    } else {
+        g.nx = ldcs(NX_of<T>(c) + e);
+        g.ny = ldcs(NY_of<T>(c) + e);
+        g.l = ldcs(L_of<T>(c) + e);
+        if (RECON != RECON_NONE) {
+            const T* __restrict__ DL = DL_of<T>(c);
 #pragma unroll
-        for (int k = 0; k < 8; k++) g.dl[k] = ldcs(DL + (size_t)k * c.ne + e);
+            for (int k = 0; k < 8; k++) g.dl[k] = ldcs(DL + (size_t)k * c.ne + e);
+        }
     }
     return g;
 }

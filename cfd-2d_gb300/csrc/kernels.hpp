@@ -120,6 +120,9 @@ struct DevCase {
     const float* l32;
     const float* ax32;     // ne (mixed form): the per-edge gradient weights, as cf_ax32
     const float* ay32;
+    // 3*ne (mixed form): per edge {nx, ny, l, 0} and the two Gauss points' offsets
+    // {dxL, dyL, dxR, dyR}: the flux kernels' geometry in three vector loads
+    const float4* geo32;
     const float* dl32;
     const double* S;       // nc
     const double* invS;    // nc, RN(1/S) (FP64 form)

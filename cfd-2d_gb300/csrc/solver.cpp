@@ -133,6 +133,15 @@ Solver::Solver(const TaskConfig& t, Topo&& topo, const std::vector<int>& cell_re
                 ey[e] = (float)(lay_.ny[e] * lay_.l[e] * 0.5);
             }
             c.ax32 = upload(ex); c.ay32 = upload(ey);
+            std::vector<float4> geo(3 * (size_t)ne);
+            for (int e = 0; e < ne; e++) {
+                const double* d = lay_.dl.data() + e;
+                auto dl = [&](int k) { return (float)d[(size_t)k * ne]; };
+                geo[3 * (size_t)e] = make_float4((float)lay_.nx[e], (float)lay_.ny[e], (float)lay_.l[e], 0.f);
+                geo[3 * (size_t)e + 1] = make_float4(dl(0), dl(1), dl(2), dl(3));
+                geo[3 * (size_t)e + 2] = make_float4(dl(4), dl(5), dl(6), dl(7));
+            }
+            c.geo32 = upload(geo);
             c.dl32 = upload(to_f32(lay_.dl));
             std::vector<float> is(nc);
             for (int i = 0; i < nc; i++) is[i] = (float)(1.0 / lay_.S[i]);
